@@ -1,0 +1,94 @@
+"""Builds libibisgb.so in-tree (ibis_gb300/_build/) for sm_103a.
+
+Host code is compiled without FMA contraction (-ffp-contract=off) so that grid
+preprocessing reproduces the reference's geometry bit for bit on both x86 and
+aarch64 hosts; kernels_exact.cu is compiled with -fmad=false for the
+bitwise-parity FP64 path.  Object files are rebuilt only when a source or
+header changes.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libibisgb.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
+              "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp", "-I", SRC, "-I", INCLUDE] + ARCH
+CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-I", SRC,
+             "-I", INCLUDE]
+
+UNITS = {
+    "mesh.cpp": "cxx",
+    "context.cu": "nvcc",
+    "kernels_common.cu": "nvcc",
+    "kernels_f64.cu": "nvcc",
+    "kernels_mixed.cu": "nvcc",
+    "kernels_exact.cu": "nvcc-nofma",
+}
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libibisgb")
+
+
+def _digest(unit: str, flags: list) -> str:
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(SRC)):
+        if name.endswith((".hpp", ".cuh", ".h")):
+            h.update(open(os.path.join(SRC, name), "rb").read())
+    h.update(open(os.path.join(INCLUDE, "ibisgb.h"), "rb").read())
+    h.update(open(os.path.join(SRC, unit), "rb").read())
+    h.update(" ".join(flags).encode())
+    return h.hexdigest()
+
+
+def _compile(unit: str, kind: str, verbose: bool) -> str:
+    src = os.path.join(SRC, unit)
+    obj = os.path.join(OUT, unit + ".o")
+    if kind == "cxx":
+        cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-c", src, "-o", obj]
+    else:
+        cmd = [_nvcc()] + NVCC_FLAGS + (["-fmad=false"] if kind == "nvcc-nofma" else []) + ["-c", src, "-o", obj]
+    stamp = obj + ".sha"
+    dig = _digest(unit, cmd[1:])
+    if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == dig:
+        return obj
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compiling {unit} failed:\n{r.stdout}\n{r.stderr}")
+    with open(stamp, "w") as f:
+        f.write(dig)
+    return obj
+
+
+def build(verbose: bool = False) -> str:
+    """Compile every unit (in parallel) and link libibisgb.so; returns its path."""
+    os.makedirs(OUT, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
+    newest = max(os.path.getmtime(o) for o in objs)
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        cmd = [_nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-Xcompiler", "-fopenmp", "-lgomp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"linking libibisgb.so failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

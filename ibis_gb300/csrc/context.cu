@@ -1,0 +1,857 @@
+// Host side of libibisgb: the context behind the C ABI (include/ibisgb.h).
+// Reads ibis's config.json, builds the mesh, owns the device memory and one
+// CUDA stream, and drives the residual / Runge-Kutta kernels (one CUDA graph
+// per Runge-Kutta step).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ibisgb.h"
+#include "engine.hpp"
+#include "json_lite.hpp"
+#include "mesh.hpp"
+
+using namespace ibisgb;
+
+namespace {
+
+#define CUDA_OK(x)                                                                          \
+    do {                                                                                    \
+        cudaError_t e_ = (x);                                                               \
+        if (e_ != cudaSuccess)                                                              \
+            throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));               \
+    } while (0)
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct ConfigError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct ArgError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct StateError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// Device allocation owned by the context.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    void alloc(size_t n) {
+        if (p && bytes >= n) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (n == 0) return;
+        CUDA_OK(cudaMalloc(&p, n));
+        bytes = n;
+    }
+    template <class T>
+    T* as() const { return (T*)p; }
+};
+
+template <class T>
+void upload(DBuf& b, const std::vector<T>& v, cudaStream_t s) {
+    b.alloc(v.size() * sizeof(T));
+    if (!v.empty()) CUDA_OK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+// State buffers of one storage type (double for F64 / F64_EXACT, float for MIXED).
+struct StateBufs {
+    DBuf cc, r, face;                              // geometry
+    DBuf prim, vghost, grad, phi, vgrad, flux;     // state and intermediates
+    bool geometry = false;
+    bool prims_current = false;
+};
+
+ActionKind parse_action_kind(const std::string& t) {
+    if (t == "flow_state_copy") return aFlowStateCopy;
+    if (t == "internal_copy") return aInternalCopy;
+    if (t == "internal_copy_reflect_normal") return aReflectNormal;
+    if (t == "internal_vel_copy_reflect") return aVelReflect;
+    if (t == "fix_temperature") return aFixTemperature;
+    if (t == "subsonic_inflow") return aSubsonicInflow;
+    if (t == "subsonic_outflow") return aSubsonicOutflow;
+    if (t == "periodic_copy") return aPeriodicCopy;
+    throw ConfigError("Unknown boundary action " + t);
+}
+
+Action parse_action(const Json& a) {  // build_boundary_action, boundary.cpp:448-479
+    Action out{};
+    out.kind = parse_action_kind(a.at("type").as_string());
+    auto fs = [&](const Json& j) {
+        out.fs[0] = j.at("T").as_double(); out.fs[1] = j.at("p").as_double();
+        out.fs[2] = j.at("rho").as_double(); out.fs[3] = j.at("energy").as_double();
+        out.fs[4] = j.at("vx").as_double(); out.fs[5] = j.at("vy").as_double();
+        out.fs[6] = j.at("vz").as_double();
+    };
+    if (out.kind == aFlowStateCopy || out.kind == aSubsonicInflow) fs(a.at("flow_state"));
+    if (out.kind == aFixTemperature) out.value = a.at("temperature").as_double();
+    if (out.kind == aSubsonicOutflow) out.value = a.at("pressure").as_double();
+    return out;
+}
+
+}  // namespace
+
+struct ibisgb_ctx {
+    std::string err;
+    Json config;
+    FvParams prm{};
+    Mesh mesh;
+    std::vector<BoundDev> bounds_host;
+
+    // Runge-Kutta settings (RungeKutta ctor, runge_kutta.cpp:21-80)
+    bool rk_configured = false;
+    StepCtl ctl_host{};
+    double dt_init = -1.0;
+
+    cudaStream_t stream = nullptr;
+    int device = 0;
+
+    // connectivity and per-cell data shared by all arithmetics
+    DBuf cell_face, cell_nbr, outsign, nfaces, left, right, ghost_src, ghost_face, ghost_bound,
+        bounds, feed_off, feed_ghost, vol;
+    DBuf U, k, vsig, ctl, l2, out, branches;
+    StateBufs s64, s32;
+    std::vector<double> ic_prims;  // host IC primitives (7 x NT), kept until the first update
+    bool have_state = false;
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    double last_l2[6] = {0, 0, 0, 0, 0, 0};
+
+    ~ibisgb_ctx() {
+        for (auto& g : graph)
+            if (g) cudaGraphExecDestroy(g);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int nc() const { return mesh.dim + 2; }
+    int stages() const { return rk_configured ? ctl_host.stages : 1; }
+
+    void parse_config(const std::string& text) {
+        try {
+            config = Json::parse(text);
+        } catch (const std::exception& e) {
+            throw ConfigError(std::string("config.json: ") + e.what());
+        }
+        try {
+            const Json& cf = config.at("convective_flux");  // ConvectiveFlux ctor, convective_flux.cpp:60-82
+            std::string ft = cf.at("flux_calculator").at("type").as_string();
+            if (ft == "hanel") prm.flux = kHanel;
+            else if (ft == "ausmdv") prm.flux = kAusmdv;
+            else if (ft == "ldfss2") { prm.flux = kLdfss2; prm.delta = cf.at("flux_calculator").at("delta").as_double(); }
+            else if (ft == "rusanov") prm.flux = kRusanov;
+            else throw ConfigError("Unknown flux calculator " + ft);
+            prm.order = (int)cf.at("reconstruction_order").as_int();
+            prm.thermo = kRhoU;
+            prm.limiter = 0;
+            prm.eps = 1e-25;
+            if (prm.order > 1) {
+                std::string th = cf.at("thermo_interpolator").as_string();
+                if (th == "rho_p") prm.thermo = kRhoP;
+                else if (th == "rho_T") prm.thermo = kRhoT;
+                else if (th == "rho_u") prm.thermo = kRhoU;
+                else if (th == "p_T") prm.thermo = kPT;
+                else throw ConfigError("Unknown thermo interpolator " + th);
+                std::string lt = cf.at("limiter").at("type").as_string();
+                if (lt == "barth_jespersen") { prm.limiter = 1; prm.eps = cf.at("limiter").at("epsilon").as_double(); }
+                else if (lt == "unlimited") prm.limiter = 0;
+                else throw ConfigError("Unknown limiter " + lt);
+            }
+            if (prm.order != 1 && prm.order != 2) throw ConfigError("Invalid reconstruction order");
+            const Json& vf = config.at("viscous_flux");
+            prm.viscous = vf.at("enabled").as_bool() ? 1 : 0;
+            prm.signal_factor = vf.at("signal_factor").as_double();
+            const Json& gm = config.at("gas_model");  // IdealGas(json), gas_model.h:58-62
+            prm.R = gm.at("R").as_double(); prm.Cv = gm.at("Cv").as_double();
+            prm.Cp = gm.at("Cp").as_double(); prm.gamma = gm.at("gamma").as_double();
+            prm.mu0 = 1.716e-5; prm.T0 = 273.0; prm.Ts = 110.0; prm.Pr = 0.72;
+            if (config.contains("transport_properties")) {  // transport_properties.h:91-109
+                const Json& tp = config.at("transport_properties");
+                const Json& vi = tp.at("viscosity");
+                if (vi.at("type").as_string() != "sutherland") throw ConfigError("Unknown viscosity model");
+                prm.mu0 = vi.at("mu_0").as_double(); prm.T0 = vi.at("T_0").as_double(); prm.Ts = vi.at("T_s").as_double();
+                const Json& kc = tp.at("thermal_conductivity");
+                if (kc.at("type").as_string() != "constant_prandtl_number") throw ConfigError("Unknown thermal conductivity model");
+                prm.Pr = kc.at("Pr").as_double();
+            }
+            const Json& grid = config.at("grid");
+            if (grid.contains("motion") && grid.at("motion").contains("enabled") &&
+                grid.at("motion").at("enabled").as_bool())
+                throw ConfigError("moving grids are not supported");
+            const Json& solver = config.at("solver");
+            if (solver.at("name").as_string() == "runge_kutta") parse_rk(solver);
+        } catch (const ConfigError&) {
+            throw;
+        } catch (const std::exception& e) {
+            throw ConfigError(std::string("config.json: ") + e.what());
+        }
+    }
+
+    void parse_rk(const Json& sc) {
+        StepCtl& c = ctl_host;
+        const Json& bt = sc.at("butcher_tableau");
+        auto b = bt.at("b").as_doubles();
+        if (b.empty() || b.size() > (size_t)kMaxStages) throw ConfigError("unsupported Butcher tableau size");
+        c.stages = (int)b.size();
+        const auto& rows = bt.at("a").elements();
+        for (int i = 1; i < c.stages; i++) {
+            auto row = rows.at(i - 1).as_doubles();
+            for (int j = 0; j < i && j < (int)row.size(); j++) c.a[i][j] = row[j];
+        }
+        for (int i = 0; i < c.stages; i++) c.b[i] = b[i];
+        const Json& cfl = sc.at("cfl");  // make_cfl_schedule, cfl.cpp:157-169
+        std::string ct = cfl.at("type").as_string();
+        if (ct == "constant") {
+            c.cfl = cfl.at("value").as_double();
+        } else if (ct == "linear_interpolate") {
+            auto ts = cfl.at("times").as_doubles(), vs = cfl.at("cfls").as_doubles();
+            if (ts.size() != vs.size() || ts.empty() || ts.size() > 16) throw ConfigError("bad cfl schedule");
+            c.n_cfl = (int)ts.size();
+            for (size_t i = 0; i < ts.size(); i++) { c.cfl_t[i] = ts[i]; c.cfl_v[i] = vs[i]; }
+        } else {
+            throw ConfigError("unsupported CFL schedule for runge_kutta: " + ct);
+        }
+        c.max_time = sc.at("max_time").as_double();
+        c.plot_frequency = sc.at("plot_frequency").as_double();
+        dt_init = sc.at("dt_init").as_double();
+        rk_configured = true;
+    }
+
+    std::vector<BoundarySpec> boundary_specs() {
+        std::vector<BoundarySpec> out;
+        for (const auto& [tag, b] : config.at("grid").at("boundaries").items()) {
+            BoundarySpec s;
+            s.tag = tag;
+            s.ghost_cells = b.at("ghost_cells").as_bool();
+            for (const Json& a : b.at("pre_reconstruction").elements()) {
+                if (a.at("type").as_string() == "periodic_copy") {
+                    s.periodic = true;
+                    s.partner = a.at("partner").as_string();
+                    auto off = a.at("offset").as_doubles();
+                    for (int d = 0; d < 3; d++) s.offset[d] = off.at(d);
+                }
+            }
+            if (!b.at("post_convective_flux").elements().empty())
+                throw ConfigError("post_convective_flux actions (constant_flux) are not supported");
+            out.push_back(s);
+        }
+        return out;
+    }
+
+    void build(const GridInput& in) {
+        if (in.dim != 2 && in.dim != 3) throw ConfigError("grid dimension must be 2 or 3");
+        prm.dim = in.dim;
+        std::vector<BoundarySpec> specs = boundary_specs();
+        build_mesh(in, specs, prm.viscous || prm.order > 1, mesh);
+        const int64_t N = mesh.N, F = mesh.F, G = mesh.G;
+        const int64_t lim = std::numeric_limits<int>::max();
+        if (15 * N >= lim || 5 * F >= lim || 7 * (N + G) >= lim)
+            throw ConfigError("grid too large for 32-bit device indexing");
+        for (const auto& b : mesh.bounds) {  // BoundaryCondition ctor, boundary.cpp:494-515
+            const Json& bj = config.at("grid").at("boundaries").at(b.tag);
+            BoundDev d{};
+            for (const Json& a : bj.at("pre_reconstruction").elements()) {
+                if (d.n_pre == kMaxActions) throw ConfigError("too many boundary actions");
+                d.pre[d.n_pre++] = parse_action(a);
+            }
+            for (const Json& a : bj.at("pre_viscous_grad").elements()) {
+                if (d.n_visc == kMaxActions) throw ConfigError("too many boundary actions");
+                d.visc[d.n_visc++] = parse_action(a);
+            }
+            bounds_host.push_back(d);
+        }
+    }
+
+    // Device buffers are created on the first call that needs the GPU, so that
+    // the host-side numbering and geometry can be inspected without one.
+    bool uploaded = false;
+    void ensure_device() {
+        if (uploaded) return;
+        upload_mesh();
+        uploaded = true;
+    }
+
+    void upload_mesh() {
+        CUDA_OK(cudaGetDevice(&device));
+        CUDA_OK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        const int64_t N = mesh.N, F = mesh.F, G = mesh.G, MF = mesh.MF;
+        std::vector<int> cf(MF * N, -1), nb(MF * N, -1), nfa(N);
+        std::vector<signed char> os(MF * N, 0);
+        for (int64_t c = 0; c < N; c++) {
+            nfa[c] = mesh.nfaces[c];
+            for (int64_t k = 0; k < MF; k++) {
+                cf[k * N + c] = (int)mesh.cell_face[c * MF + k];
+                nb[k * N + c] = (int)mesh.cell_nbr[c * MF + k];
+                os[k * N + c] = mesh.outsign[c * MF + k];
+            }
+        }
+        upload(cell_face, cf, stream); upload(cell_nbr, nb, stream); upload(outsign, os, stream);
+        upload(nfaces, nfa, stream);
+        std::vector<int> l(F), r(F);
+        for (int64_t f = 0; f < F; f++) { l[f] = (int)mesh.left[f]; r[f] = (int)mesh.right[f]; }
+        upload(left, l, stream); upload(right, r, stream);
+        std::vector<int> gs(G), gf(G), gb(G);
+        for (int64_t g = 0; g < G; g++) {
+            gs[g] = (int)mesh.ghost_src[g]; gf[g] = (int)mesh.ghost_face[g]; gb[g] = (int)mesh.ghost_bound[g];
+        }
+        upload(ghost_src, gs, stream); upload(ghost_face, gf, stream); upload(ghost_bound, gb, stream);
+        upload(bounds, bounds_host, stream);
+        // ghosts fed by each valid cell (CSR)
+        std::vector<int> off(N + 1, 0), fg(G);
+        for (int64_t g = 0; g < G; g++) off[gs[g] + 1]++;
+        for (int64_t c = 0; c < N; c++) off[c + 1] += off[c];
+        std::vector<int> cur(off.begin(), off.end() - 1);
+        for (int64_t g = 0; g < G; g++) fg[cur[gs[g]]++] = (int)g;
+        upload(feed_off, off, stream); upload(feed_ghost, fg, stream);
+        std::vector<double> v(mesh.volume.begin(), mesh.volume.begin() + N);
+        upload(vol, v, stream);
+        U.alloc(sizeof(double) * nc() * N);
+        k.alloc(sizeof(double) * nc() * N * stages());
+        vsig.alloc(sizeof(double) * F);
+        CUDA_OK(cudaMemsetAsync(vsig.p, 0, sizeof(double) * F, stream));
+        ctl.alloc(sizeof(StepCtl));
+        l2.alloc(sizeof(double) * (6 + 6 * 304));
+        CUDA_OK(cudaStreamSynchronize(stream));
+    }
+
+    template <class Gm>
+    void upload_geometry(StateBufs& s) {
+        if (s.geometry) return;
+        const int64_t N = mesh.N, NT = mesh.NT(), F = mesh.F;
+        std::vector<Gm> cc(3 * NT), r(6 * N, Gm(0)), fc(13 * F);
+        for (int64_t c = 0; c < NT; c++) { cc[c] = (Gm)mesh.ccx[c]; cc[NT + c] = (Gm)mesh.ccy[c]; cc[2 * NT + c] = (Gm)mesh.ccz[c]; }
+        if (!mesh.r.empty())
+            for (int64_t c = 0; c < N; c++)
+                for (int q = 0; q < 6; q++) r[q * N + c] = (Gm)mesh.r[c * 6 + q];
+        const std::vector<double>* fa[13] = {&mesh.nx, &mesh.ny, &mesh.nz, &mesh.t1x, &mesh.t1y, &mesh.t1z,
+                                             &mesh.t2x, &mesh.t2y, &mesh.t2z, &mesh.fcx, &mesh.fcy, &mesh.fcz, &mesh.area};
+        for (int q = 0; q < 13; q++)
+            for (int64_t f = 0; f < F; f++) fc[q * F + f] = (Gm)(*fa[q])[f];
+        upload(s.cc, cc, stream); upload(s.r, r, stream); upload(s.face, fc, stream);
+        size_t P = sizeof(Gm);
+        s.prim.alloc(P * 7 * NT);
+        s.vghost.alloc(P * 5 * std::max<int64_t>(mesh.G, 1));
+        s.grad.alloc(P * 15 * N);
+        s.phi.alloc(P * 5 * N);
+        s.vgrad.alloc(P * 12 * N);
+        s.flux.alloc(P * nc() * F);
+        s.geometry = true;
+        CUDA_OK(cudaStreamSynchronize(stream));
+    }
+
+    static bool is_mixed(int prec) { return prec == IBISGB_MIXED; }
+    StateBufs& bufs(int prec) { return is_mixed(prec) ? s32 : s64; }
+    KernelOps ops(int prec) const {
+        if (prec == IBISGB_MIXED) return kernels_mixed();
+        if (prec == IBISGB_F64_EXACT) return kernels_f64_exact();
+        return kernels_f64();
+    }
+
+    DevView view(int prec) {
+        StateBufs& s = bufs(prec);
+        DevView v{};
+        v.dim = mesh.dim; v.N = (int)mesh.N; v.G = (int)mesh.G; v.F = (int)mesh.F; v.MF = mesh.MF;
+        v.NT = (int)mesh.NT();
+        v.cell_face = cell_face.as<int>(); v.cell_nbr = cell_nbr.as<int>();
+        v.outsign = outsign.as<signed char>(); v.nfaces = nfaces.as<int>();
+        v.left = left.as<int>(); v.right = right.as<int>();
+        v.ghost_src = ghost_src.as<int>(); v.ghost_face = ghost_face.as<int>();
+        v.ghost_bound = ghost_bound.as<int>(); v.bounds = bounds.as<BoundDev>();
+        v.feed_off = feed_off.as<int>(); v.feed_ghost = feed_ghost.as<int>();
+        v.cc = s.cc.p; v.r = s.r.p; v.face = s.face.p; v.vol = vol.as<double>();
+        v.prim = s.prim.p; v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
+        v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
+        v.U = U.as<double>(); v.k = k.as<double>(); v.ctl = ctl.as<StepCtl>();
+        v.branches = nullptr;
+        return v;
+    }
+
+    // Make the primitives (and ghosts) of arithmetic `prec` reflect the current state.
+    void ensure_prims(int prec) {
+        ensure_device();
+        if (!have_state) throw StateError("no initial condition: call ibisgb_set_primitives first");
+        if (is_mixed(prec)) upload_geometry<float>(s32); else upload_geometry<double>(s64);
+        StateBufs& s = bufs(prec);
+        if (s.prims_current) return;
+        DevView v = view(prec);
+        if (!ic_prims.empty()) {
+            const int64_t NT = mesh.NT();
+            if (is_mixed(prec)) {
+                std::vector<float> f(ic_prims.begin(), ic_prims.end());
+                CUDA_OK(cudaMemcpyAsync(s.prim.p, f.data(), sizeof(float) * 7 * NT, cudaMemcpyHostToDevice, stream));
+                CUDA_OK(cudaStreamSynchronize(stream));
+            } else {
+                CUDA_OK(cudaMemcpyAsync(s.prim.p, ic_prims.data(), sizeof(double) * 7 * NT, cudaMemcpyHostToDevice, stream));
+            }
+            ops(prec).ghost_fill(v, prm, stream);
+        } else {
+            ops(prec).prims_from_U(v, prm, stream);
+        }
+        CUDA_OK(cudaGetLastError());
+        s.prims_current = true;
+    }
+
+    void state_changed(int prec) {
+        ic_prims.clear();
+        s64.prims_current = !is_mixed(prec);
+        s32.prims_current = is_mixed(prec);
+    }
+
+    void set_primitives(const double* T, const double* p, const double* vx, const double* vy, const double* vz) {
+        if (!T || !p || !vx || !vy) throw ArgError("T, p, vx and vy are required");
+        if (mesh.dim == 3 && !vz) throw ArgError("vz is required in 3-D");
+        ensure_device();
+        const int64_t N = mesh.N, NT = mesh.NT();
+        // NativeBinaryInput::read (native.cpp:263-339): update_thermo_from_pT per cell
+        ic_prims.assign(7 * NT, 0.0);
+        std::vector<double> u(nc() * N);
+        for (int64_t i = 0; i < N; i++) {
+            double rho = p[i] / (prm.R * T[i]);
+            double e = prm.Cv * T[i];
+            double w = vz ? vz[i] : 0.0;
+            ic_prims[i] = rho; ic_prims[NT + i] = p[i]; ic_prims[2 * NT + i] = T[i]; ic_prims[3 * NT + i] = e;
+            ic_prims[4 * NT + i] = vx[i]; ic_prims[5 * NT + i] = vy[i]; ic_prims[6 * NT + i] = w;
+            // primatives_to_conserved (primative_conserved_conversion.cpp:31-51)
+            u[i] = rho;
+            u[N + i] = rho * vx[i];
+            u[2 * N + i] = rho * vy[i];
+            if (mesh.dim == 3) u[3 * N + i] = rho * w;
+            double ke = 0.5 * (vx[i] * vx[i] + vy[i] * vy[i] + w * w);
+            u[(mesh.dim + 1) * N + i] = rho * (ke + e);
+        }
+        CUDA_OK(cudaMemcpyAsync(U.p, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+        have_state = true;
+        s64.prims_current = false;
+        s32.prims_current = false;
+        // RungeKutta::initialise: t = 0, dt = dt_init or max (runge_kutta.cpp:82-104)
+        reset_rk();
+    }
+
+    void reset_rk() {
+        StepCtl c = ctl_host;
+        c.t = 0.0;
+        c.time_since_last_plot = 0.0;
+        c.dt = dt_init > 0 ? dt_init : std::numeric_limits<double>::max();
+        c.dt_bits = 0x7FF0000000000000ull;
+        c.bad_cells = 0;
+        c.steps = 0;
+        if (!rk_configured) c.stages = 1;
+        c.halt = 0;
+        c.max_time = rk_configured ? ctl_host.max_time : std::numeric_limits<double>::max();
+        CUDA_OK(cudaMemcpyAsync(ctl.p, &c, sizeof(StepCtl), cudaMemcpyHostToDevice, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+    }
+
+    void residual(int prec, double* out_device, bool record_branches) {
+        ensure_prims(prec);
+        DevView v = view(prec);
+        KernelOps o = ops(prec);
+        // compute_dudt applies the pre-reconstruction actions first (finite_volume.cpp:62)
+        o.ghost_fill(v, prm, stream);
+        if (record_branches && prm.order == 2 && prm.limiter) {
+            branches.alloc(sizeof(unsigned) * 5 * mesh.N);
+            v.branches = branches.as<unsigned>();
+        }
+        bool reco = prm.order == 2;
+        o.recon(v, prm, reco, stream);
+        o.face_flux(v, prm, reco, stream);
+        o.update(v, prm, 0, 0, out_device, stream);
+        CUDA_OK(cudaGetLastError());
+    }
+
+    double estimate_dt(int prec) {
+        ensure_prims(prec);
+        DevView v = view(prec);
+        launch_reset_dt(v.ctl, stream);
+        ops(prec).local_dt(v, prm, stream);
+        CUDA_OK(cudaGetLastError());
+        unsigned long long bits = 0;
+        CUDA_OK(cudaMemcpyAsync(&bits, &((StepCtl*)ctl.p)->dt_bits, sizeof(bits), cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+        double dt;
+        std::memcpy(&dt, &bits, sizeof(dt));
+        return dt;
+    }
+
+    // one Runge-Kutta step (RungeKutta::take_step, runge_kutta.cpp:131-203)
+    void enqueue_step(int prec) {
+        DevView v = view(prec);
+        KernelOps o = ops(prec);
+        const bool reco = prm.order == 2;
+        const int S = ctl_host.stages;
+        o.recon(v, prm, reco, stream);
+        o.face_flux(v, prm, reco, stream);
+        o.update(v, prm, 1, 0, nullptr, stream);
+        o.local_dt(v, prm, stream);
+        launch_dt_finalize(v.ctl, stream);
+        if (S == 1) {
+            o.finalize(v, prm, stream);
+            return;
+        }
+        o.combine(v, prm, 1, stream);
+        for (int s = 1; s < S; s++) {
+            o.recon(v, prm, reco, stream);
+            o.face_flux(v, prm, reco, stream);
+            o.update(v, prm, s == S - 1 ? 3 : 2, s, nullptr, stream);
+        }
+    }
+
+    void rk_run(int prec, int64_t n, ibisgb_rk_status* st) {
+        if (!rk_configured) throw ConfigError("config.json solver is not runge_kutta");
+        ensure_prims(prec);
+        int gi = prec == IBISGB_MIXED ? 1 : (prec == IBISGB_F64_EXACT ? 2 : 0);
+        if (!graph[gi]) {
+            cudaGraph_t g;
+            CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_step(prec);
+            cudaError_t le = cudaGetLastError();
+            CUDA_OK(cudaStreamEndCapture(stream, &g));
+            CUDA_OK(le);
+            CUDA_OK(cudaGraphInstantiate(&graph[gi], g, 0));
+            CUDA_OK(cudaGraphDestroy(g));
+        }
+        for (int64_t i = 0; i < n; i++) CUDA_OK(cudaGraphLaunch(graph[gi], stream));
+        state_changed(prec);
+        StepCtl c;
+        CUDA_OK(cudaMemcpyAsync(&c, ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+        if (st) {
+            st->t = c.t; st->dt = c.dt; st->stable_dt = c.stable_dt; st->steps = c.steps;
+            st->bad_cells = (int64_t)c.bad_cells;
+        }
+        if (c.bad_cells > 0) throw std::runtime_error("bad cells");
+    }
+
+    void get_primitives(double* out7[7]) {
+        if (!have_state) throw StateError("no initial condition");
+        const int64_t N = mesh.N, NT = mesh.NT();
+        if (!ic_prims.empty()) {
+            for (int q = 0; q < 7; q++)
+                if (out7[q]) std::memcpy(out7[q], &ic_prims[q * NT], sizeof(double) * N);
+            return;
+        }
+        if (!s64.prims_current) {
+            upload_geometry<double>(s64);
+            ops(IBISGB_F64).prims_from_U(view(IBISGB_F64), prm, stream);
+            CUDA_OK(cudaGetLastError());
+            s64.prims_current = true;
+        }
+        for (int q = 0; q < 7; q++)
+            if (out7[q])
+                CUDA_OK(cudaMemcpyAsync(out7[q], s64.prim.as<double>() + q * NT, sizeof(double) * N,
+                                        cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+namespace {
+thread_local std::string g_create_error;
+
+template <class F>
+int guarded(ibisgb_ctx* ctx, F&& f) {
+    try {
+        f();
+        return IBISGB_OK;
+    } catch (const ConfigError& e) {
+        if (ctx) ctx->err = e.what();
+        return IBISGB_ERR_CONFIG;
+    } catch (const CudaError& e) {
+        if (ctx) ctx->err = e.what();
+        return IBISGB_ERR_CUDA;
+    } catch (const ArgError& e) {
+        if (ctx) ctx->err = e.what();
+        return IBISGB_ERR_ARG;
+    } catch (const StateError& e) {
+        if (ctx) ctx->err = e.what();
+        return IBISGB_ERR_STATE;
+    } catch (const std::exception& e) {
+        if (ctx) ctx->err = e.what();
+        return std::string(e.what()) == "bad cells" ? IBISGB_ERR_BAD_CELLS : IBISGB_ERR_GRID;
+    }
+}
+
+int create_common(const char* config_json, const GridInput* in_arrays, const char* su2_path,
+                  ibisgb_ctx** out) {
+    if (!out || !config_json) {
+        g_create_error = "null argument";
+        return IBISGB_ERR_ARG;
+    }
+    *out = nullptr;
+    auto ctx = std::make_unique<ibisgb_ctx>();
+    int rc = guarded(ctx.get(), [&] {
+        ctx->parse_config(config_json);
+        if (su2_path) {
+            GridInput in;
+            try {
+                in = read_su2(su2_path);
+            } catch (const std::exception& e) {
+                throw std::runtime_error(std::string("grid: ") + e.what());
+            }
+            ctx->build(in);
+        } else {
+            ctx->build(*in_arrays);
+        }
+    });
+    if (rc != IBISGB_OK) {
+        g_create_error = ctx->err;
+        return rc;
+    }
+    *out = ctx.release();
+    return IBISGB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int ibisgb_create(const char* config_json, const char* su2_path, ibisgb_ctx** out) {
+    if (!su2_path) {
+        g_create_error = "su2_path is null";
+        return IBISGB_ERR_ARG;
+    }
+    return create_common(config_json, nullptr, su2_path, out);
+}
+
+int ibisgb_create_from_arrays(const char* config_json, int32_t dim, int64_t num_vertices,
+                              const double* xyz, int64_t num_cells, const int32_t* cell_types,
+                              const int64_t* cell_offsets, const int64_t* cell_vertices,
+                              int32_t num_markers, const char* marker_names,
+                              const int64_t* marker_offsets, const int32_t* element_types,
+                              const int64_t* element_offsets, const int64_t* element_vertices,
+                              ibisgb_ctx** out) {
+    GridInput in;
+    try {
+        if (!xyz || !cell_types || !cell_offsets || !cell_vertices || num_vertices < 0 || num_cells < 0)
+            throw ArgError("null or negative grid argument");
+        in.dim = dim;
+        in.xyz.assign(xyz, xyz + 3 * num_vertices);
+        for (int64_t c = 0; c < num_cells; c++) {
+            ElemKind k = elem_kind_from_vtk(cell_types[c]);
+            int64_t n = cell_offsets[c + 1] - cell_offsets[c];
+            if (n != vertices_per_elem(k)) throw ArgError("cell vertex count does not match its type");
+            in.cells.push(k, cell_vertices + cell_offsets[c], (int)n);
+        }
+        std::string names = marker_names ? marker_names : "";
+        size_t pos = 0;
+        for (int32_t m = 0; m < num_markers; m++) {
+            size_t nl = names.find('\n', pos);
+            std::string tag = names.substr(pos, nl == std::string::npos ? std::string::npos : nl - pos);
+            pos = nl == std::string::npos ? names.size() : nl + 1;
+            ElemList& dst = in.markers[tag];
+            for (int64_t e = marker_offsets[m]; e < marker_offsets[m + 1]; e++) {
+                ElemKind k = elem_kind_from_vtk(element_types[e]);
+                int64_t n = element_offsets[e + 1] - element_offsets[e];
+                dst.push(k, element_vertices + element_offsets[e], (int)n);
+            }
+        }
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return IBISGB_ERR_ARG;
+    }
+    return create_common(config_json, &in, nullptr, out);
+}
+
+void ibisgb_destroy(ibisgb_ctx* ctx) { delete ctx; }
+
+const char* ibisgb_last_error(const ibisgb_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+int ibisgb_get_sizes(const ibisgb_ctx* ctx, ibisgb_sizes* out) {
+    if (!ctx || !out) return IBISGB_ERR_ARG;
+    out->num_cells = ctx->mesh.N;
+    out->num_ghost_cells = ctx->mesh.G;
+    out->num_faces = ctx->mesh.F;
+    out->dim = ctx->mesh.dim;
+    out->max_faces_per_cell = ctx->mesh.MF;
+    out->n_conserved = ctx->mesh.dim + 2;
+    out->num_boundaries = (int32_t)ctx->mesh.bounds.size();
+    return IBISGB_OK;
+}
+
+int ibisgb_set_primitives(ibisgb_ctx* ctx, const double* T, const double* p, const double* vx,
+                          const double* vy, const double* vz) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->set_primitives(T, p, vx, vy, vz); });
+}
+
+int ibisgb_get_primitives(ibisgb_ctx* ctx, double* rho, double* p, double* T, double* e, double* vx,
+                          double* vy, double* vz) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        double* o[7] = {rho, p, T, e, vx, vy, vz};
+        ctx->get_primitives(o);
+    });
+}
+
+int ibisgb_get_conserved(ibisgb_ctx* ctx, double* out) {
+    if (!ctx || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (!ctx->have_state) throw StateError("no initial condition");
+        ctx->ensure_device();
+        const int64_t N = ctx->mesh.N;
+        const int nc = ctx->nc();
+        std::vector<double> soa(nc * N);
+        CUDA_OK(cudaMemcpyAsync(soa.data(), ctx->U.p, sizeof(double) * nc * N, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        for (int64_t i = 0; i < N; i++)
+            for (int q = 0; q < nc; q++) out[i * nc + q] = soa[q * N + i];
+    });
+}
+
+int ibisgb_residual_device(ibisgb_ctx* ctx, int32_t precision, double* dudt_device, void* stream) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        cudaStream_t user = (cudaStream_t)stream;
+        if (user && user != ctx->stream) {  // order the context stream after the caller's work
+            cudaEvent_t ev;
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+            ctx->residual(precision, dudt_device, true);
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        } else {
+            ctx->residual(precision, dudt_device, true);
+        }
+    });
+}
+
+int ibisgb_residual(ibisgb_ctx* ctx, int32_t precision, double* dudt) {
+    if (!ctx || !dudt) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        const size_t bytes = sizeof(double) * ctx->nc() * ctx->mesh.N;
+        ctx->out.alloc(bytes);
+        ctx->residual(precision, ctx->out.as<double>(), true);
+        CUDA_OK(cudaMemcpyAsync(dudt, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ibisgb_estimate_dt(ibisgb_ctx* ctx, double* dt) {
+    if (!ctx || !dt) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { *dt = ctx->estimate_dt(IBISGB_F64); });
+}
+
+int ibisgb_count_bad_cells(ibisgb_ctx* ctx, int64_t* n) {
+    if (!ctx || !n) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        const int64_t N = ctx->mesh.N;
+        std::vector<double> rho(N), T(N);
+        double* o[7] = {rho.data(), nullptr, T.data(), nullptr, nullptr, nullptr, nullptr};
+        ctx->get_primitives(o);
+        int64_t bad = 0;  // count_bad_cells, finite_volume.cpp:257-270
+        for (int64_t i = 0; i < N; i++)
+            if (T[i] < 0.0 || rho[i] < 0.0 || std::isnan(rho[i]) || std::isinf(rho[i])) bad++;
+        *n = bad;
+    });
+}
+
+int ibisgb_rk_run(ibisgb_ctx* ctx, int32_t precision, int64_t n_steps, ibisgb_rk_status* status) {
+    if (!ctx || n_steps < 0) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        ctx->rk_run(precision, n_steps, status);
+    });
+}
+
+int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]) {
+    if (!ctx || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (!ctx->have_state) throw StateError("no initial condition");
+        launch_l2_norms(ctx->k.as<double>(), (int)ctx->mesh.N, ctx->nc(), ctx->l2.as<double>(), ctx->stream);
+        CUDA_OK(cudaGetLastError());
+        CUDA_OK(cudaMemcpyAsync(out, ctx->l2.p, sizeof(double) * 6, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
+    if (!ctx || !buf) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        const Mesh& m = ctx->mesh;
+        const int64_t N = m.N, F = m.F, G = m.G, MF = m.MF, NT = m.NT();
+        auto put = [&](const void* src, size_t n) {
+            if ((int64_t)n > bytes) throw ArgError("dump buffer too small");
+            std::memcpy(buf, src, n);
+        };
+        auto dev = [&](const void* src, size_t n) {
+            if ((int64_t)n > bytes) throw ArgError("dump buffer too small");
+            if (!src) throw StateError("nothing to dump yet");
+            CUDA_OK(cudaMemcpyAsync(buf, src, n, cudaMemcpyDeviceToHost, ctx->stream));
+            CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        };
+        switch (which) {
+            case 0: put(m.left.data(), sizeof(int64_t) * F); break;
+            case 1: put(m.right.data(), sizeof(int64_t) * F); break;
+            case 2: put(m.cell_face.data(), sizeof(int64_t) * N * MF); break;
+            case 3: {
+                std::vector<int32_t> o(m.outsign.begin(), m.outsign.end());
+                put(o.data(), sizeof(int32_t) * N * MF);
+                break;
+            }
+            case 4: put(m.cell_nbr.data(), sizeof(int64_t) * N * MF); break;
+            case 5: put(m.ghost_src.data(), sizeof(int64_t) * G); break;
+            case 6: {
+                std::vector<double> o;
+                for (auto* a : {&m.nx, &m.ny, &m.nz, &m.t1x, &m.t1y, &m.t1z, &m.t2x, &m.t2y, &m.t2z,
+                                &m.fcx, &m.fcy, &m.fcz, &m.area})
+                    o.insert(o.end(), a->begin(), a->end());
+                put(o.data(), sizeof(double) * 13 * F);
+                break;
+            }
+            case 7: {
+                std::vector<double> o;
+                for (auto* a : {&m.ccx, &m.ccy, &m.ccz, &m.volume}) o.insert(o.end(), a->begin(), a->end());
+                put(o.data(), sizeof(double) * 4 * NT);
+                break;
+            }
+            case 8: dev(ctx->branches.p, sizeof(unsigned) * 5 * N); break;
+            case 9: {
+                if (!ctx->s64.prims_current && !ctx->s32.prims_current) throw StateError("nothing to dump yet");
+                dev(ctx->s64.phi.p, sizeof(double) * 5 * N);
+                break;
+            }
+            case 10: {
+                std::vector<double> soa(ctx->nc() * F);
+                dev(ctx->s64.flux.p, 0);
+                CUDA_OK(cudaMemcpyAsync(soa.data(), ctx->s64.flux.p, sizeof(double) * soa.size(),
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+                CUDA_OK(cudaStreamSynchronize(ctx->stream));
+                std::vector<double> o(soa.size());
+                for (int64_t f = 0; f < F; f++)
+                    for (int q = 0; q < ctx->nc(); q++) o[f * ctx->nc() + q] = soa[q * F + f];
+                put(o.data(), sizeof(double) * o.size());
+                break;
+            }
+            default: throw ArgError("unknown dump");
+        }
+    });
+}
+
+int ibisgb_synchronize(ibisgb_ctx* ctx) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (ctx->stream) CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// Types shared by the host context and the device kernels of the residual engine.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace ibisgb {
+
+enum FluxKind : int { kHanel = 0, kAusmdv = 1, kLdfss2 = 2, kRusanov = 3 };
+enum ThermoKind : int { kRhoP = 0, kRhoT = 1, kRhoU = 2, kPT = 3 };
+
+// Ghost-cell actions (src/finite_volume/finite_volume/boundaries/boundary.cpp)
+enum ActionKind : int {
+    aFlowStateCopy = 0,
+    aInternalCopy = 1,
+    aReflectNormal = 2,  // internal_copy_reflect_normal
+    aVelReflect = 3,     // internal_vel_copy_reflect
+    aFixTemperature = 4,
+    aSubsonicInflow = 5,
+    aSubsonicOutflow = 6,
+    aPeriodicCopy = 7,   // extension: copy of the periodic donor cell
+};
+
+constexpr int kMaxActions = 4;
+constexpr int kMaxStages = 8;
+
+struct Action {
+    int kind;
+    double fs[7];  // T, p, rho, energy, vx, vy, vz
+    double value;  // fix_temperature temperature / subsonic_outflow pressure
+};
+
+// The ghost-cell actions of one boundary tag.
+struct BoundDev {
+    int n_pre, n_visc;
+    Action pre[kMaxActions];   // pre_reconstruction
+    Action visc[kMaxActions];  // pre_viscous_grad
+};
+
+// Gas, transport and finite-volume settings (FiniteVolume ctor, finite_volume.cpp:13-54).
+struct FvParams {
+    int dim;
+    int flux;     // FluxKind
+    int thermo;   // ThermoKind
+    int order;    // reconstruction order 1 or 2
+    int limiter;  // 1: Barth-Jespersen, 0: unlimited
+    int viscous;
+    double eps;            // Barth-Jespersen epsilon
+    double delta;          // LDFSS2 delta
+    double signal_factor;  // viscous dt signal factor
+    double R, Cv, Cp, gamma;
+    double mu0, T0, Ts, Pr;
+};
+
+// Device-side control block of the explicit Runge-Kutta step
+// (RungeKutta::estimate_dt / take_step, runge_kutta.cpp:108-203).
+struct StepCtl {
+    double t, dt, stable_dt, time_since_last_plot;
+    double cfl, max_time, plot_frequency;
+    int n_cfl;  // linear CFL schedule points (0: constant cfl)
+    double cfl_t[16], cfl_v[16];
+    int stages;
+    double a[kMaxStages][kMaxStages];  // tableau a(i, j), row i = stage i (>= 1)
+    double b[kMaxStages];
+    double ca[kMaxStages][kMaxStages];  // a(i, j) * dt of the current step
+    double cb[kMaxStages];              // b(i) * dt
+    unsigned long long dt_bits;         // min over cells of the local dt (bits of a positive double)
+    unsigned long long bad_cells;       // bad cells left by the last solution update
+    long long steps;
+    int halt;  // set when a step left bad cells or t >= max_time (Solver::solve, solver.cpp:38-49)
+};
+
+// Raw device pointers of one context for one arithmetic (P = primitive
+// storage type, Gm = geometry type, both double or float; see layouts below).
+struct DevView {
+    int dim, N, G, F, MF, NT;
+    // connectivity, slot-major: slot k of cell c at [k * N + c]
+    const int* cell_face;
+    const int* cell_nbr;
+    const signed char* outsign;
+    const int* nfaces;
+    const int* left;
+    const int* right;
+    // ghosts (index g = ghost id - N)
+    const int* ghost_src;
+    const int* ghost_face;
+    const int* ghost_bound;
+    const BoundDev* bounds;
+    // ghosts fed by each valid cell (CSR over valid cells)
+    const int* feed_off;
+    const int* feed_ghost;
+    // geometry (type Gm): cc[3][NT], r[6][N], face[13][F] = n, t1, t2, centre, area
+    const void* cc;
+    const void* r;
+    const void* face;
+    const double* vol;  // N
+    // state (type P)
+    void* prim;    // [7][NT]: rho, p, T, e, vx, vy, vz
+    void* vghost;  // [5][G]: p, T, vx, vy, vz after the pre-viscous-gradient actions
+    void* grad;    // [5*3][N]: gradients of the 5 reconstructed variables
+    void* phi;     // [5][N]: their limiter values
+    void* vgrad;   // [4*3][N]: gradients of T, vx, vy, vz for the viscous flux
+    void* flux;    // [nc][F]
+    double* vsig;  // [F]: viscous time-step signal (gamma/rho)(mu/Pr) per face
+    double* U;     // [nc][N]
+    double* k;     // [stages][nc][N]
+    StepCtl* ctl;
+    unsigned* branches;  // optional [N][5] limiter branch codes
+};
+
+// Launch entry points of one kernel build (one arithmetic).
+struct KernelOps {
+    // ghosts from their source cells (pre-reconstruction and pre-viscous actions)
+    void (*ghost_fill)(const DevView&, const FvParams&, cudaStream_t);
+    // gradients + limiters (+ viscous gradients) of every valid cell
+    void (*recon)(const DevView&, const FvParams&, bool reconstruct, cudaStream_t);
+    // face fluxes (convective + viscous)
+    void (*face_flux)(const DevView&, const FvParams&, bool reconstruct, cudaStream_t);
+    // surface integral into stage `stage`; mode: 0 residual only (writes k[stage]),
+    // 1 stage 0 of a step (+ local dt min), 2 intermediate stage (+ next stage state),
+    // 3 last stage (+ solution update). out_rowmajor: optional N x nc output of dU/dt.
+    void (*update)(const DevView&, const FvParams&, int mode, int stage, double* out_rowmajor,
+                   cudaStream_t);
+    // stage-1 state U + a(1,0) dt k0 -> primitives and ghosts (after dt is known)
+    void (*combine)(const DevView&, const FvParams&, int stage, cudaStream_t);
+    // primitives (and ghosts) from U
+    void (*prims_from_U)(const DevView&, const FvParams&, cudaStream_t);
+    // local CFL dt of every valid cell reduced into ctl->dt_bits (face signal of the last flux)
+    void (*local_dt)(const DevView&, const FvParams&, cudaStream_t);
+    // U += sum_j b(j) dt k_j, primitives and ghosts (single-stage tableaus)
+    void (*finalize)(const DevView&, const FvParams&, cudaStream_t);
+};
+
+KernelOps kernels_f64();
+KernelOps kernels_f64_exact();
+KernelOps kernels_mixed();
+
+// precision-independent kernels (kernels_common.cu)
+void launch_dt_finalize(StepCtl* ctl, cudaStream_t s);
+void launch_reset_dt(StepCtl* ctl, cudaStream_t s);
+void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s);
+void launch_count_bad(const void* prim, bool is_float, int N, int NT, unsigned long long* out,
+                      cudaStream_t s);
+
+}  // namespace ibisgb

@@ -1,0 +1,700 @@
+// Residual and Runge-Kutta kernels for sm_103a, templated on
+//   R  arithmetic of reconstruction, limiting and fluxes (double or float),
+//   P  storage type of primitives and per-cell/face intermediates,
+//   Gm storage type of geometry,
+//   DIM 2 or 3, EXACT (reference operation order, pow in Sutherland, used by the
+//   no-FMA build that reproduces ibis bit for bit).
+// One translation unit instantiates one (R, P, Gm, EXACT) family; see kernels_*.cu.
+//
+// Pipeline of one residual evaluation (FiniteVolume::compute_dudt,
+// finite_volume.cpp:56-85), all cell arrays SoA and slot-major:
+//   k_recon   per valid cell: least-squares gradients of the reconstructed
+//             variables and Barth-Jespersen limiters in one pass over the
+//             neighbours (+ the viscous gradients of T, v with the
+//             pre-viscous ghost values)              [gradient.h, limiter.cpp]
+//   k_face    per face: MUSCL reconstruction of both sides, thermo closure,
+//             rotation to the face frame, flux calculator, rotation back,
+//             viscous stress / heat flux             [convective_flux.cpp, viscous_flux.cpp]
+//   k_update  per valid cell: surface integral in double, then the Runge-Kutta
+//             stage combination, conserved->primitive inversion and the
+//             ghost cells this cell feeds (the next evaluation's
+//             pre-reconstruction boundary actions)    [finite_volume.cpp:220-255,
+//                                                      runge_kutta.cpp:131-203]
+#pragma once
+
+#include "numerics.cuh"
+
+namespace ibisgb {
+namespace IBISGB_KNS {
+
+constexpr int kBlock = 256;
+
+inline unsigned blocks_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+// thermo variable pair in the reference's call order (compute_convective_gradient,
+// convective_flux.cpp:180-209): prim indices 0 rho, 1 p, 2 T, 3 e
+IBISGB_HD void thermo_vars(int kind, int& a, int& b) {
+    switch (kind) {
+        case kRhoP: a = 1; b = 0; break;
+        case kRhoU: a = 0; b = 3; break;
+        case kRhoT: a = 0; b = 2; break;
+        default: a = 1; b = 2; break;  // p_T
+    }
+}
+
+struct State64 {
+    double rho, p, T, e, vx, vy, vz;
+};
+
+// primitive index of viscous variable q (0 T, 1 vx, 2 vy, 3 vz)
+IBISGB_HD int visc_prim(int q) { return q == 0 ? 2 : 3 + q; }
+
+// ---------------------------------------------------------------------------
+// Ghost-cell actions on one ghost (boundary.cpp:9-400), in double.
+// ---------------------------------------------------------------------------
+template <class Gm>
+__device__ void apply_actions(const Action* acts, int n, State64& gh, const State64& src,
+                              const Gm* face, int F, int f, const FvParams& prm) {
+    for (int a = 0; a < n; a++) {
+        const Action& A = acts[a];
+        switch (A.kind) {
+            case aFlowStateCopy:
+                gh.T = A.fs[0]; gh.p = A.fs[1]; gh.rho = A.fs[2]; gh.e = A.fs[3];
+                gh.vx = A.fs[4]; gh.vy = A.fs[5]; gh.vz = A.fs[6];
+                break;
+            case aInternalCopy:
+            case aPeriodicCopy:
+                gh = src;
+                break;
+            case aReflectNormal: {
+                gh.T = src.T; gh.p = src.p; gh.rho = src.rho; gh.e = src.e;
+                double x = src.vx, y = src.vy, z = src.vz;
+                double nx = face[f], ny = face[F + f], nz = face[2 * F + f];
+                double t1x = face[3 * F + f], t1y = face[4 * F + f], t1z = face[5 * F + f];
+                double t2x = face[6 * F + f], t2y = face[7 * F + f], t2z = face[8 * F + f];
+                double xs = -(x * nx + y * ny + z * nz);
+                double ys = x * t1x + y * t1y + z * t1z;
+                double zs = x * t2x + y * t2y + z * t2z;
+                gh.vx = xs * nx + ys * t1x + zs * t2x;
+                gh.vy = xs * ny + ys * t1y + zs * t2y;
+                gh.vz = xs * nz + ys * t1z + zs * t2z;
+                break;
+            }
+            case aVelReflect:
+                gh.vx = -src.vx; gh.vy = -src.vy; gh.vz = -src.vz;
+                break;
+            case aFixTemperature:
+                gh.T = 2 * A.value - src.T;
+                break;
+            case aSubsonicInflow: {
+                double nx = face[f], ny = face[F + f], nz = face[2 * F + f];
+                double vc = nx * (A.fs[4] - src.vx) + ny * (A.fs[5] - src.vy) + nz * (A.fs[6] - src.vz);
+                double sos = sqrt(prm.gamma * prm.R * src.T);
+                double rho_ref = src.rho;
+                double p_in = A.fs[1];
+                double p_face = 0.5 * (p_in + src.p - rho_ref * sos * vc);
+                double rho_face = A.fs[2] + (p_face - p_in) / sos / sos;
+                double vxf = A.fs[4] - nx * (p_in - p_face) / (rho_ref * sos);
+                double vyf = A.fs[5] - ny * (p_in - p_face) / (rho_ref * sos);
+                double vzf = A.fs[6] - nz * (p_in - p_face) / (rho_ref * sos);
+                gh.p = 2 * p_face - src.p;
+                gh.rho = 2 * rho_face - src.rho;
+                gh.T = gh.p / (gh.rho * prm.R);
+                gh.e = prm.Cv * gh.T;
+                gh.vx = 2 * vxf - src.vx; gh.vy = 2 * vyf - src.vy; gh.vz = 2 * vzf - src.vz;
+                break;
+            }
+            case aSubsonicOutflow: {
+                double nx = face[f], ny = face[F + f], nz = face[2 * F + f];
+                double p_face = A.value;
+                double rho_ref = src.rho, p_ref = src.p;
+                double sos = sqrt(prm.gamma * prm.R * src.T);
+                double rho_face = src.rho + (p_face - p_ref) / sos / sos;
+                double vxf = src.vx + nx * (p_ref - p_face) / (rho_ref * sos);
+                double vyf = src.vy + ny * (p_ref - p_face) / (rho_ref * sos);
+                double vzf = src.vz + nz * (p_ref - p_face) / (rho_ref * sos);
+                gh.p = 2 * p_face - src.p;
+                gh.rho = 2 * rho_face - src.rho;
+                gh.T = gh.p / (gh.rho * prm.R);
+                gh.e = prm.Cv * gh.T;
+                gh.vx = 2 * vxf - src.vx; gh.vy = 2 * vyf - src.vy; gh.vz = 2 * vzf - src.vz;
+                break;
+            }
+        }
+    }
+}
+
+// Fill ghost g from the state of its source cell: pre-reconstruction actions
+// into the primitive arrays, then the pre-viscous-gradient actions on top of
+// them into the viscous ghost arrays (p, T, vx, vy, vz).
+template <class P, class Gm>
+__device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const State64& src) {
+    const BoundDev& B = v.bounds[v.ghost_bound[g]];
+    const Gm* face = (const Gm*)v.face;
+    int f = v.ghost_face[g];
+    State64 gh = src;
+    apply_actions<Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm);
+    P* pr = (P*)v.prim;
+    const int NT = v.NT, id = v.N + g;
+    pr[id] = (P)gh.rho; pr[NT + id] = (P)gh.p; pr[2 * NT + id] = (P)gh.T; pr[3 * NT + id] = (P)gh.e;
+    pr[4 * NT + id] = (P)gh.vx; pr[5 * NT + id] = (P)gh.vy; pr[6 * NT + id] = (P)gh.vz;
+    if (prm.viscous) {
+        apply_actions<Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm);
+        P* vg = (P*)v.vghost;
+        vg[g] = (P)gh.p; vg[v.G + g] = (P)gh.T; vg[2 * v.G + g] = (P)gh.vx;
+        vg[3 * v.G + g] = (P)gh.vy; vg[4 * v.G + g] = (P)gh.vz;
+    }
+}
+
+template <class P>
+__device__ State64 load_state64(const DevView& v, int c) {
+    const P* pr = (const P*)v.prim;
+    const int NT = v.NT;
+    return State64{(double)pr[c], (double)pr[NT + c], (double)pr[2 * NT + c], (double)pr[3 * NT + c],
+                   (double)pr[4 * NT + c], (double)pr[5 * NT + c], (double)pr[6 * NT + c]};
+}
+
+template <class P, class Gm>
+__global__ void __launch_bounds__(kBlock) k_ghost_fill(DevView v, FvParams prm) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= v.G) return;
+    fill_ghost<P, Gm>(v, prm, g, load_state64<P>(v, v.ghost_src[g]));
+}
+
+// ---------------------------------------------------------------------------
+// k_recon: gradients (WLSGradient::compute_gradients, gradient.h:65-116) and
+// Barth-Jespersen limiters (limiter.cpp:119-159) of every valid cell.
+// ---------------------------------------------------------------------------
+template <class R, class P, class Gm, int DIM, bool EXACT>
+__global__ void __launch_bounds__(kBlock) k_recon(DevView v, FvParams prm, int reconstruct) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    constexpr int NV = DIM == 3 ? 5 : 4;  // reconstructed variables (vz only in 3-D)
+    const int N = v.N, NT = v.NT, G = v.G, F = v.F;
+    const Gm* cc = (const Gm*)v.cc;
+    const Gm* rr = (const Gm*)v.r;
+    const Gm* fcen = (const Gm*)v.face + 9 * F;
+    const P* pr = (const P*)v.prim;
+    const P* vg = (const P*)v.vghost;
+    int ia, ib;
+    thermo_vars(prm.thermo, ia, ib);
+    const int vidx[5] = {ia, ib, 4, 5, 6};
+    const bool visc = prm.viscous != 0;
+    const bool lim = reconstruct && prm.limiter;
+
+    R xi = (R)cc[i], yi = (R)cc[NT + i], zi = DIM == 3 ? (R)cc[2 * NT + i] : R(0.0);
+    R r11 = (R)rr[i], r12 = (R)rr[N + i], r22 = (R)rr[2 * N + i];
+    R r13 = R(0.0), r23 = R(0.0), r33 = R(0.0);
+    if (DIM == 3) { r13 = (R)rr[3 * N + i]; r23 = (R)rr[4 * N + i]; r33 = (R)rr[5 * N + i]; }
+    R beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+
+    R ui[NV], gx[NV], gy[NV], gz[NV], umin[NV], umax[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        ui[q] = (R)pr[vidx[q] * NT + i];
+        gx[q] = R(0.0); gy[q] = R(0.0); gz[q] = R(0.0);
+        umin[q] = ui[q]; umax[q] = ui[q];
+    }
+    constexpr int NW = DIM == 3 ? 4 : 3;  // viscous: T, vx, vy[, vz]
+    R wi[NW], hx[NW], hy[NW], hz[NW];
+#pragma unroll
+    for (int q = 0; q < NW; q++) {
+        wi[q] = (R)pr[visc_prim(q) * NT + i];
+        hx[q] = R(0.0); hy[q] = R(0.0); hz[q] = R(0.0);
+    }
+
+    const int nf = v.nfaces[i];
+    for (int s = 0; s < nf; s++) {
+        const int nb = v.cell_nbr[s * N + i];
+        R dx = (R)cc[nb] - xi, dy = (R)cc[NT + nb] - yi;
+        R dz = DIM == 3 ? (R)cc[2 * NT + nb] - zi : R(0.0);
+        R a1 = dx / (r11 * r11);
+        R a2 = R(1.0) / (r22 * r22) * (dy - r12 / r11 * dx);
+        R a3 = R(0.0);
+        if (DIM == 3) a3 = R(1.0) / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx);
+        R w1 = a1 - r12 / r11 * a2 + beta * a3;
+        R w2 = a2 - r23 / r22 * a3;
+        R w3 = a3;
+        if (reconstruct) {
+#pragma unroll
+            for (int q = 0; q < NV; q++) {
+                R un = (R)pr[vidx[q] * NT + nb];
+                R du = un - ui[q];
+                gx[q] += w1 * du; gy[q] += w2 * du;
+                if (DIM == 3) gz[q] += w3 * du;
+                umin[q] = d_min(umin[q], un);
+                umax[q] = d_max(umax[q], un);
+            }
+        }
+        if (visc) {
+            const bool ghost = nb >= N;
+#pragma unroll
+            for (int q = 0; q < NW; q++) {
+                R un = ghost ? (R)vg[(1 + q) * G + (nb - N)] : (R)pr[visc_prim(q) * NT + nb];
+                R du = un - wi[q];
+                hx[q] += w1 * du; hy[q] += w2 * du;
+                if (DIM == 3) hz[q] += w3 * du;
+            }
+        }
+    }
+
+    if (reconstruct) {
+        P* gout = (P*)v.grad;
+        R phi[NV];
+        unsigned code[NV];
+#pragma unroll
+        for (int q = 0; q < NV; q++) { phi[q] = R(1.0); code[q] = 0u; }
+        if (lim) {
+            const R eps = (R)prm.eps;
+            for (int s = 0; s < nf; s++) {
+                const int f = v.cell_face[s * N + i];
+                R dx = (R)fcen[f] - xi, dy = (R)fcen[F + f] - yi;
+                R dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+#pragma unroll
+                for (int q = 0; q < NV; q++) {
+                    R d2 = DIM == 3 ? gx[q] * dx + gy[q] * dy + gz[q] * dz : gx[q] * dx + gy[q] * dy;
+                    int sg = (d2 > R(0.0)) - (d2 < R(0.0));
+                    d2 = (R)sg * (d_abs(d2) + eps);
+                    if (sg != 0) {
+                        R ratio = sg > 0 ? (umax[q] - ui[q]) / d2 : (umin[q] - ui[q]) / d2;
+                        code[q] |= (unsigned)(sg > 0 ? 1 : 2) << (2 * s);
+                        if (!(phi[q] < ratio)) code[q] = (code[q] & 0xFFFFu) | ((unsigned)(s + 1) << 16);
+                        phi[q] = d_min(phi[q], ratio);
+                    }
+                }
+            }
+            P* pout = (P*)v.phi;
+#pragma unroll
+            for (int q = 0; q < NV; q++) pout[q * N + i] = (P)phi[q];
+            if (v.branches) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) v.branches[i * 5 + q] = q < NV ? code[q] : 0u;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            gout[(3 * q) * N + i] = (P)gx[q];
+            gout[(3 * q + 1) * N + i] = (P)gy[q];
+            gout[(3 * q + 2) * N + i] = (P)gz[q];
+        }
+    }
+    if (visc) {
+        P* hout = (P*)v.vgrad;
+#pragma unroll
+        for (int q = 0; q < NW; q++) {
+            hout[(3 * q) * N + i] = (P)hx[q];
+            hout[(3 * q + 1) * N + i] = (P)hy[q];
+            hout[(3 * q + 2) * N + i] = (P)hz[q];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_face: reconstruction + flux + viscous flux of every face.
+// ---------------------------------------------------------------------------
+template <class R, class P, int DIM>
+IBISGB_HD R lin_interp(R value, R lim, const P* g, int N, int q, int c, R dx, R dy, R dz) {
+    // value + limiter * (grad . d)   (linear_interpolate, convective_flux.cpp:242-255)
+    R s = DIM == 3 ? (R)g[(3 * q) * N + c] * dx + (R)g[(3 * q + 1) * N + c] * dy + (R)g[(3 * q + 2) * N + c] * dz
+                   : (R)g[(3 * q) * N + c] * dx + (R)g[(3 * q + 1) * N + c] * dy;
+    return value + lim * s;
+}
+
+template <class R, class P, class Gm, int DIM, bool EXACT>
+__global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int reconstruct) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.F) return;
+    const int N = v.N, NT = v.NT, F = v.F, G = v.G;
+    const Gm* fg = (const Gm*)v.face;
+    const Gm* cc = (const Gm*)v.cc;
+    const P* pr = (const P*)v.prim;
+    const P* gr = (const P*)v.grad;
+    const P* ph = (const P*)v.phi;
+    const Gas<R> gm(prm);
+    const R nx = (R)fg[f], ny = (R)fg[F + f], nz = DIM == 3 ? (R)fg[2 * F + f] : R(0.0);
+    const R t1x = (R)fg[3 * F + f], t1y = (R)fg[4 * F + f], t1z = DIM == 3 ? (R)fg[5 * F + f] : R(0.0);
+    const R t2x = DIM == 3 ? (R)fg[6 * F + f] : R(0.0), t2y = DIM == 3 ? (R)fg[7 * F + f] : R(0.0);
+    const R t2z = (R)fg[8 * F + f];
+    const R fx = (R)fg[9 * F + f], fy = (R)fg[10 * F + f], fz = DIM == 3 ? (R)fg[11 * F + f] : R(0.0);
+    int ia, ib;
+    thermo_vars(prm.thermo, ia, ib);
+    const int cells[2] = {v.left[f], v.right[f]};
+    FaceSide<R> S[2];
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const int c = cells[side];
+        R q[7];
+#pragma unroll
+        for (int k = 0; k < 7; k++) q[k] = (DIM == 2 && k == 6) ? R(0.0) : (R)pr[k * NT + c];
+        if (reconstruct && c < N) {
+            R dx = fx - (R)cc[c], dy = fy - (R)cc[NT + c], dz = DIM == 3 ? fz - (R)cc[2 * NT + c] : R(0.0);
+            const bool lim = prm.limiter != 0;
+            auto L = [&](int k) { return lim ? (R)ph[k * N + c] : R(1.0); };
+            q[ia] = lin_interp<R, P, DIM>(q[ia], L(0), gr, N, 0, c, dx, dy, dz);
+            q[ib] = lin_interp<R, P, DIM>(q[ib], L(1), gr, N, 1, c, dx, dy, dz);
+            thermo_close<R>(prm.thermo, gm, q[0], q[1], q[2], q[3]);
+            q[4] = lin_interp<R, P, DIM>(q[4], L(2), gr, N, 2, c, dx, dy, dz);
+            q[5] = lin_interp<R, P, DIM>(q[5], L(3), gr, N, 3, c, dx, dy, dz);
+            if (DIM == 3) q[6] = lin_interp<R, P, DIM>(q[6], L(4), gr, N, 4, c, dx, dy, dz);
+        } else if (reconstruct) {
+            // ghost side: first-order copy, then the same thermo closure
+            thermo_close<R>(prm.thermo, gm, q[0], q[1], q[2], q[3]);
+        }
+        S[side].r = q[0]; S[side].p = q[1]; S[side].T = q[2];
+        // transform_to_local_frame (vector3.cpp:141-153)
+        if (DIM == 3) {
+            S[side].u = q[4] * nx + q[5] * ny + q[6] * nz;
+            S[side].v = q[4] * t1x + q[5] * t1y + q[6] * t1z;
+            S[side].w = q[4] * t2x + q[5] * t2y + q[6] * t2z;
+        } else if (EXACT) {
+            S[side].u = q[4] * nx + q[5] * ny + q[6] * nz;
+            S[side].v = q[4] * t1x + q[5] * t1y + q[6] * t1z;
+            S[side].w = R(0.0);
+        } else {
+            S[side].u = q[4] * nx + q[5] * ny;
+            S[side].v = q[4] * t1x + q[5] * t1y;
+            S[side].w = R(0.0);
+        }
+    }
+    R Fl[5];
+    switch (prm.flux) {
+        case kHanel: flux_hanel<R, DIM>(S[0], S[1], gm, Fl); break;
+        case kAusmdv: flux_ausmdv<R, DIM>(S[0], S[1], gm, Fl); break;
+        case kLdfss2: flux_ldfss2<R, DIM>(S[0], S[1], gm, (R)prm.delta, Fl); break;
+        default: flux_rusanov<R, DIM>(S[0], S[1], gm, Fl); break;
+    }
+    // transform_to_global (convective_flux.cpp:145-177)
+    R px = Fl[1], py = Fl[2], pz = DIM == 3 ? Fl[3] : R(0.0);
+    R mx, my, mz = R(0.0);
+    if (DIM == 3 || EXACT) {
+        mx = px * nx + py * t1x + pz * t2x;
+        my = px * ny + py * t1y + pz * t2y;
+        if (DIM == 3) mz = px * nz + py * t1z + pz * t2z;
+    } else {
+        mx = px * nx + py * t1x;
+        my = px * ny + py * t1y;
+    }
+    R en = Fl[4];
+
+    if (prm.viscous) {
+        // viscous_flux.cpp:130-232
+        const int l = cells[0], r = cells[1];
+        const bool lv = l < N, rv = r < N;
+        const P* vgd = (const P*)v.vgrad;
+        const P* vgh = (const P*)v.vghost;
+        constexpr int NW = DIM == 3 ? 4 : 3;
+        R g[4][3];
+        // visc states of both sides (ghost: pre-viscous values)
+        auto vstate = [&](int c, int k) -> R {  // k: 0 p, 1 T, 2 vx, 3 vy, 4 vz
+            if (c >= N) return (R)vgh[k * G + (c - N)];
+            return (R)pr[(k == 0 ? 1 : visc_prim(k - 1)) * NT + c];
+        };
+        if (!lv || !rv) {
+            const int in = lv ? l : r;
+#pragma unroll
+            for (int q = 0; q < NW; q++)
+                for (int d = 0; d < 3; d++) g[q][d] = (R)vgd[(3 * q + d) * N + in];
+        } else {
+            R ex = (R)cc[r] - (R)cc[l], ey = (R)cc[NT + r] - (R)cc[NT + l];
+            R ez = DIM == 3 ? (R)cc[2 * NT + r] - (R)cc[2 * NT + l] : R(0.0);
+            R len_e = d_sqrt(ex * ex + ey * ey + ez * ez);
+            R ehx = ex / len_e, ehy = ey / len_e, ehz = ez / len_e;
+            R edn = ehx * nx + ehy * ny + ehz * nz;
+            // hasselbacher_average_ (viscous_flux.cpp:84-98), variable order vx, vy, vz, T
+#pragma unroll
+            for (int q = 0; q < NW; q++) {
+                R ax = R(0.5) * ((R)vgd[(3 * q) * N + l] + (R)vgd[(3 * q) * N + r]);
+                R ay = R(0.5) * ((R)vgd[(3 * q + 1) * N + l] + (R)vgd[(3 * q + 1) * N + r]);
+                R az = R(0.5) * ((R)vgd[(3 * q + 2) * N + l] + (R)vgd[(3 * q + 2) * N + r]);
+                R ade = ax * ehx + ay * ehy + az * ehz;
+                R corr = ade - ((R)pr[visc_prim(q) * NT + r] - (R)pr[visc_prim(q) * NT + l]) / len_e;
+                g[q][0] = ax - corr * nx / edn;
+                g[q][1] = ay - corr * ny / edn;
+                g[q][2] = az - corr * nz / edn;
+            }
+        }
+        if (DIM == 2) { g[3][0] = R(0.0); g[3][1] = R(0.0); g[3][2] = R(0.0); }
+        // face state: average of p, T, v (average_pT, gas_state.h:219-225) + update_thermo_from_pT
+        R p = R(0.5) * (vstate(l, 0) + vstate(r, 0));
+        R T = R(0.5) * (vstate(l, 1) + vstate(r, 1));
+        R rho = p / (gm.R_ * T);
+        R vx = R(0.5) * (vstate(l, 2) + vstate(r, 2));
+        R vy = R(0.5) * (vstate(l, 3) + vstate(r, 3));
+        R vz = DIM == 3 ? R(0.5) * (vstate(l, 4) + vstate(r, 4)) : R(0.0);
+        R mu = sutherland<R, EXACT>(T, (R)prm.mu0, (R)prm.T0, (R)prm.Ts);
+        R k = gm.Cp * mu / (R)prm.Pr;
+        R lambda = R(-2.0 / 3.0) * mu;
+        const R *gT = g[0], *gx = g[1], *gy = g[2], *gz = g[3];
+        R bulk = lambda * (gx[0] + gy[1] + gz[2]);
+        R txx = R(2.0) * mu * gx[0] + bulk;
+        R tyy = R(2.0) * mu * gy[1] + bulk;
+        R tzz = R(2.0) * mu * gz[2] + bulk;
+        R txy = mu * (gx[1] + gy[0]);
+        R txz = mu * (gx[2] + gz[0]);
+        R tyz = mu * (gy[2] + gz[1]);
+        R thx = vx * txx + vy * txy + vz * txz + k * gT[0];
+        R thy = vx * txy + vy * tyy + vz * tyz + k * gT[1];
+        R thz = vx * txz + vy * tyz + vz * tzz + k * gT[2];
+        mx -= nx * txx + ny * txy + nz * txz;
+        my -= nx * txy + ny * tyy + nz * tyz;
+        if (DIM == 3) mz -= nx * txz + ny * tyz + nz * tzz;
+        en -= nx * thx + ny * thy + nz * thz;
+        // time-step signal (estimate_dt, finite_volume.cpp:167-175), in double
+        double mud = (double)mu, kd = (double)k;
+        double Prf = mud * prm.Cp / kd;
+        v.vsig[f] = (prm.gamma / (double)rho) * (mud / Prf);
+    }
+    P* fo = (P*)v.flux;
+    fo[f] = (P)Fl[0];
+    fo[F + f] = (P)mx;
+    fo[2 * F + f] = (P)my;
+    if (DIM == 3) fo[3 * F + f] = (P)mz;
+    fo[(DIM + 1) * F + f] = (P)en;
+}
+
+// ---------------------------------------------------------------------------
+// k_update: surface integral (flux_surface_integral, finite_volume.cpp:220-255)
+// in double, then (mode 2) the next stage state or (mode 3) the solution
+// update, conserved->primitive inversion (primative_conserved_conversion.cpp:4-23)
+// and the ghost cells fed by this cell.
+// ---------------------------------------------------------------------------
+template <class P, class Gm, int DIM>
+__device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, const double* u) {
+    // conserved_to_primatives in double
+    double rho = u[0];
+    double vx = u[1] / rho;
+    double vy = u[2] / rho;
+    double vz = DIM == 3 ? u[3] / rho : 0.0;
+    double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
+    double e = u[DIM + 1] / rho - ke;
+    double T = e / prm.Cv;
+    double p = rho * prm.R * T;
+    P* pr = (P*)v.prim;
+    const int NT = v.NT;
+    pr[i] = (P)rho; pr[NT + i] = (P)p; pr[2 * NT + i] = (P)T; pr[3 * NT + i] = (P)e;
+    pr[4 * NT + i] = (P)vx; pr[5 * NT + i] = (P)vy; pr[6 * NT + i] = (P)vz;
+    const State64 s{rho, p, T, e, vx, vy, vz};
+    for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
+    return s;
+}
+
+// count_bad_cells (finite_volume.cpp:257-270)
+IBISGB_HD void count_bad(StepCtl* ctl, const State64& s) {
+    if (s.T < 0.0 || s.rho < 0.0 || isnan(s.rho) || isinf(s.rho)) atomicAdd(&ctl->bad_cells, 1ull);
+}
+
+template <class P, class Gm, int DIM>
+__global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int mode, int stage,
+                                                   double* out_rm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    constexpr int NC = DIM + 2;
+    const int N = v.N, F = v.F;
+    const Gm* area = (const Gm*)v.face + 12 * F;
+    const P* fl = (const P*)v.flux;
+    double acc[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) acc[q] = 0.0;
+    const int nf = v.nfaces[i];
+    for (int s = 0; s < nf; s++) {
+        const int f = v.cell_face[s * N + i];
+        const double a = -(double)area[f] * (double)v.outsign[s * N + i];
+#pragma unroll
+        for (int q = 0; q < NC; q++) acc[q] += (double)fl[q * F + f] * a;
+    }
+    const double vol = v.vol[i];
+    double ks[NC];
+    double* kk = v.k + (size_t)stage * NC * N;
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        ks[q] = acc[q] / vol;
+        kk[q * N + i] = ks[q];
+        if (out_rm) out_rm[(size_t)i * NC + q] = ks[q];
+    }
+    if (mode < 2) return;
+    const StepCtl* ctl = v.ctl;
+    if (ctl->halt) return;
+    double u[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) u[q] = v.U[q * N + i];
+    if (mode == 2) {
+        // state of stage s+1 (runge_kutta.cpp:151-181)
+        const int ns = stage + 1;
+#pragma unroll
+        for (int q = 0; q < NC; q++) u[q] = u[q] + v.k[q * N + i] * ctl->ca[ns][0];
+        for (int j = 1; j < ns; j++) {
+            if (ctl->a[ns][j] < 1e-14) continue;
+            const double c = ctl->ca[ns][j];
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
+                u[q] += kj * c;
+            }
+        }
+        commit_state<P, Gm, DIM>(v, prm, i, u);
+    } else {
+        // solution update (runge_kutta.cpp:185-193)
+        for (int j = 0; j < ctl->stages; j++) {
+            const double c = ctl->cb[j];
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
+                u[q] += kj * c;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
+        count_bad(v.ctl, commit_state<P, Gm, DIM>(v, prm, i, u));
+    }
+}
+
+// Solution update from stored stage derivatives (single-stage tableaus, where
+// dt is only known after the one residual evaluation).
+template <class P, class Gm, int DIM>
+__global__ void __launch_bounds__(kBlock) k_finalize(DevView v, FvParams prm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N || v.ctl->halt) return;
+    constexpr int NC = DIM + 2;
+    const int N = v.N;
+    double u[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) u[q] = v.U[q * N + i];
+    for (int j = 0; j < v.ctl->stages; j++) {
+        const double c = v.ctl->cb[j];
+#pragma unroll
+        for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
+    }
+#pragma unroll
+    for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
+    count_bad(v.ctl, commit_state<P, Gm, DIM>(v, prm, i, u));
+}
+
+// State of stage `stage` from U and k_0..k_{stage-1} (after dt is known), then primitives and ghosts.
+template <class P, class Gm, int DIM>
+__global__ void __launch_bounds__(kBlock) k_combine(DevView v, FvParams prm, int stage) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N || v.ctl->halt) return;
+    constexpr int NC = DIM + 2;
+    const int N = v.N;
+    const StepCtl* ctl = v.ctl;
+    double u[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) u[q] = v.U[q * N + i] + v.k[q * N + i] * ctl->ca[stage][0];
+    for (int j = 1; j < stage; j++) {
+        if (ctl->a[stage][j] < 1e-14) continue;
+        const double c = ctl->ca[stage][j];
+#pragma unroll
+        for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
+    }
+    commit_state<P, Gm, DIM>(v, prm, i, u);
+}
+
+template <class P, class Gm, int DIM>
+__global__ void __launch_bounds__(kBlock) k_prims_from_U(DevView v, FvParams prm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    constexpr int NC = DIM + 2;
+    double u[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) u[q] = v.U[q * v.N + i];
+    commit_state<P, Gm, DIM>(v, prm, i, u);
+}
+
+// Local CFL time step of each valid cell, min-reduced into ctl->dt_bits
+// (FiniteVolume::estimate_dt, finite_volume.cpp:130-184).
+template <class P, class Gm, int DIM, bool FROM_U>
+__global__ void __launch_bounds__(kBlock) k_local_dt(DevView v, FvParams prm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double local = 1.0e308 * 10.0;
+    if (i < v.N) {
+        const int N = v.N, F = v.F, NT = v.NT;
+        const Gm* fg = (const Gm*)v.face;
+        double vx, vy, vz, T;
+        if (FROM_U) {
+            double rho = v.U[i];
+            vx = v.U[N + i] / rho;
+            vy = v.U[2 * N + i] / rho;
+            vz = DIM == 3 ? v.U[3 * N + i] / rho : 0.0;
+            double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
+            T = (v.U[(DIM + 1) * N + i] / rho - ke) / prm.Cv;
+        } else {
+            const P* pr = (const P*)v.prim;
+            vx = (double)pr[4 * NT + i]; vy = (double)pr[5 * NT + i]; vz = (double)pr[6 * NT + i];
+            T = (double)pr[2 * NT + i];
+        }
+        const double a = sqrt(prm.gamma * prm.R * T);
+        const double vol = v.vol[i];
+        double src = 0.0, srv = 0.0;
+        const int nf = v.nfaces[i];
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const double A = (double)fg[12 * F + f];
+            const double dot = vx * (double)fg[f] + vy * (double)fg[F + f] + vz * (double)fg[2 * F + f];
+            src += (fabs(dot) + a) * A;
+            if (prm.viscous) {
+                double tmp = v.vsig[f] * A * A;
+                srv += tmp / vol;
+            }
+        }
+        local = vol / (src + prm.signal_factor * srv);
+        if (!(local > 0.0)) local = 1.0e308 * 10.0;
+    }
+    // warp-shuffle + block min, one atomic per block
+    for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_down_sync(0xffffffffu, local, o));
+    __shared__ double wmin[kBlock / 32];
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double m = threadIdx.x < kBlock / 32 ? wmin[threadIdx.x] : 1.0e308 * 10.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) atomicMin(&v.ctl->dt_bits, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+template <class R, class P, class Gm, bool EXACT>
+struct Launch {
+    static void ghost_fill(const DevView& v, const FvParams& p, cudaStream_t s) {
+        if (v.G > 0) k_ghost_fill<P, Gm><<<blocks_for(v.G), kBlock, 0, s>>>(v, p);
+    }
+    static void recon(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {
+        if (!reco && !p.viscous) return;
+        if (v.dim == 3) k_recon<R, P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, reco);
+        else k_recon<R, P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, reco);
+    }
+    static void face_flux(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {
+        if (v.dim == 3) k_face<R, P, Gm, 3, EXACT><<<blocks_for(v.F), kBlock, 0, s>>>(v, p, reco);
+        else k_face<R, P, Gm, 2, EXACT><<<blocks_for(v.F), kBlock, 0, s>>>(v, p, reco);
+    }
+    static void update(const DevView& v, const FvParams& p, int mode, int stage, double* out,
+                       cudaStream_t s) {
+        if (v.dim == 3) k_update<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
+        else k_update<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
+    }
+    static void combine(const DevView& v, const FvParams& p, int stage, cudaStream_t s) {
+        if (v.dim == 3) k_combine<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
+        else k_combine<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
+    }
+    static void prims_from_U(const DevView& v, const FvParams& p, cudaStream_t s) {
+        if (v.dim == 3) k_prims_from_U<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        else k_prims_from_U<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+    }
+    static void local_dt(const DevView& v, const FvParams& p, cudaStream_t s) {
+        constexpr bool FROM_U = sizeof(P) < sizeof(double);
+        if (v.dim == 3) k_local_dt<P, Gm, 3, FROM_U><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        else k_local_dt<P, Gm, 2, FROM_U><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+    }
+    static void finalize(const DevView& v, const FvParams& p, cudaStream_t s) {
+        if (v.dim == 3) k_finalize<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        else k_finalize<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+    }
+    static KernelOps ops() {
+        return KernelOps{&ghost_fill, &recon, &face_flux, &update, &combine, &prims_from_U, &local_dt,
+                         &finalize};
+    }
+};
+
+}  // namespace IBISGB_KNS
+}  // namespace ibisgb

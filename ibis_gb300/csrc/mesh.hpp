@@ -1,0 +1,91 @@
+// Host-side grid preprocessing for the GB300 residual engine.
+//
+// Turns an SU2 element list into the face/cell connectivity, geometry, ghost
+// cells and least-squares factors the device kernels consume.  Numbering and
+// geometry reproduce ibis's GridBlock exactly (src/grid/grid/grid.h:89-167):
+// faces are numbered by first appearance while scanning cells in file order and
+// their VTK faces in order; a face is identified by its vertex set; ghost cells
+// get ids N.. while iterating boundary tags in sorted order, marker faces in
+// file order.  Floating-point formulas keep the reference's operation order and
+// are compiled without FMA contraction, so connectivity, left/right assignment
+// and outsigns are bit-identical to the reference's.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace ibisgb {
+
+enum ElemKind : int8_t { kLine = 0, kTri, kTetra, kQuad, kHex, kWedge, kPyramid };
+
+ElemKind elem_kind_from_vtk(int code);  // grid_io.cpp:28-48
+int vertices_per_elem(ElemKind k);      // grid_io.cpp:72-91
+
+// One list of elements (cells or the faces of one marker), CSR connectivity.
+struct ElemList {
+    std::vector<int8_t> kind;
+    std::vector<int64_t> off{0};
+    std::vector<int64_t> vtx;
+    size_t size() const { return kind.size(); }
+    void push(ElemKind k, const int64_t* ids, int n) {
+        kind.push_back(k);
+        vtx.insert(vtx.end(), ids, ids + n);
+        off.push_back((int64_t)vtx.size());
+    }
+};
+
+struct GridInput {
+    int dim = 0;
+    std::vector<double> xyz;  // 3 per vertex (z = 0 in 2-D)
+    ElemList cells;
+    std::map<std::string, ElemList> markers;  // repeated tags are appended
+    int64_t num_vertices() const { return (int64_t)xyz.size() / 3; }
+};
+
+// SU2 reader (reference: GridIO::read_su2_grid, grid_io.cpp:218-268).
+GridInput read_su2(const std::string& path);
+
+struct BoundarySpec {
+    std::string tag;
+    bool ghost_cells = true;
+    bool periodic = false;       // extension: ghost copies the matching cell across the domain
+    std::string partner;         // periodic partner tag
+    double offset[3] = {0, 0, 0};  // partner face centre = this face centre + offset
+};
+
+struct Mesh {
+    int dim = 0;
+    int64_t N = 0, G = 0, F = 0;
+    int MF = 0;  // max faces per cell
+    int64_t NT() const { return N + G; }
+
+    // faces
+    std::vector<int8_t> face_kind;
+    std::vector<int64_t> face_vtx_off, face_vtx;
+    std::vector<int64_t> left, right;  // -1 when absent
+    std::vector<double> nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z, fcx, fcy, fcz, area;
+
+    // cells, slot-major padded to MF (slot k of cell c at c*MF+k; -1 / 0 padding)
+    std::vector<int8_t> cell_kind;
+    std::vector<int64_t> cell_vtx_off, cell_vtx;
+    std::vector<int32_t> nfaces;
+    std::vector<int64_t> cell_face, cell_nbr;
+    std::vector<int8_t> outsign;
+    std::vector<double> ccx, ccy, ccz, volume;  // N+G entries (ghost volume 0)
+    std::vector<double> r;                      // 6 per valid cell: r11 r12 r22 r13 r23 r33
+
+    // boundaries in sorted tag order
+    std::vector<BoundarySpec> bounds;
+    std::vector<std::vector<int64_t>> bound_faces, bound_ghosts;
+    std::vector<int64_t> ghost_face, ghost_bound, ghost_src;  // per ghost (index g = id - N)
+};
+
+// GridBlock::init_grid_block and friends (grid.h:89-167, 180-232, 340-443),
+// Interfaces geometry (interface.h:180-323), Cells geometry (cell.h:228-300),
+// WLSGradient::compute_weights (gradient.h:119-162).
+void build_mesh(const GridInput& in, const std::vector<BoundarySpec>& bounds, bool need_lsq,
+                Mesh& m);
+
+}  // namespace ibisgb

@@ -301,7 +301,7 @@ def make_config(dim, boundaries, *, flux="hanel", ldfss_delta=2.0, order=2,
         "viscous_flux": {"enabled": viscous, "signal_factor": signal_factor},
         "solver": solver or runge_kutta(),
         "grid": {"boundaries": copy.deepcopy(boundaries), "dimensions": dim,
-                 "motion": {"type": "static"}},
+                 "motion": {"enabled": False}},
         "gas_model": gas,
         "transport_properties": {
             "viscosity": {"type": "sutherland", "mu_0": mu_0, "T_0": T_0, "T_s": T_s},

@@ -1,0 +1,165 @@
+"""Python face of the GB300 residual engine, mirroring ibis's host interface.
+
+``Simulation`` bundles what ibis keeps in ``Sim<T>`` (src/simulation/simulation/
+simulation.h:13-23: GridBlock, FiniteVolume, IdealGas, TransportProperties) plus
+the RungeKutta driver state, and exposes the same operations under the
+reference's names:
+
+* ``compute_dudt``     FiniteVolume<T>::compute_dudt   (finite_volume.cpp:56-96)
+* ``estimate_dt``      FiniteVolume<T>::estimate_dt    (finite_volume.cpp:130-184)
+* ``count_bad_cells``  FiniteVolume<T>::count_bad_cells (finite_volume.cpp:257-270)
+* ``take_steps``       RungeKutta::take_step, n times  (runge_kutta.cpp:131-203)
+* ``L2_norms``         ConservedQuantities::L2_norms of the first stage
+                       (conserved_quantities.cpp:40-69)
+
+Every call goes through the C ABI of libibisgb.so (include/ibisgb.h); arrays
+are numpy (host) or torch CUDA tensors (device, zero copy).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import PRECISION, RkStatus, Sizes, check
+
+DUMPS = {"left": (0, np.int64), "right": (1, np.int64), "cell_faces": (2, np.int64),
+         "outsigns": (3, np.int32), "neighbours": (4, np.int64), "ghost_source": (5, np.int64),
+         "face_geometry": (6, np.float64), "cell_geometry": (7, np.float64),
+         "limiter_branches": (8, np.uint32), "limiters": (9, np.float64),
+         "face_flux": (10, np.float64)}
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Simulation:
+    """One ibis simulation (one grid block) on the current CUDA device.
+
+    ``config`` is a config.json document (dict or JSON text, as written by
+    ibis's prep step); ``grid`` is an ``ibis_gb300.grids.Su2Grid`` or the path
+    of an SU2 file."""
+
+    def __init__(self, config, grid):
+        L = _lib.load()
+        text = config if isinstance(config, str) else json.dumps(config)
+        self.config = json.loads(text)
+        h = C.c_void_p()
+        if isinstance(grid, (str, os.PathLike)):
+            rc = L.ibisgb_create(text.encode(), os.fspath(grid).encode(), C.byref(h))
+        else:
+            names, m_off, e_types, e_off, e_conn = grid.marker_arrays()
+            xyz = np.ascontiguousarray(grid.xyz, np.float64)
+            ct = np.ascontiguousarray(grid.cell_types, np.int32)
+            co = np.ascontiguousarray(grid.cell_offsets, np.int64)
+            cv = np.ascontiguousarray(grid.cell_conn, np.int64)
+            rc = L.ibisgb_create_from_arrays(text.encode(), grid.dim, xyz.shape[0], _ptr(xyz),
+                                             grid.num_cells, _ptr(ct), _ptr(co), _ptr(cv),
+                                             len(grid.markers), names.encode(), _ptr(m_off),
+                                             _ptr(e_types), _ptr(e_off), _ptr(e_conn), C.byref(h))
+        check(rc, None)
+        self._h = h
+        s = Sizes()
+        check(L.ibisgb_get_sizes(h, C.byref(s)), h)
+        self.num_cells, self.num_ghost_cells, self.num_faces = s.num_cells, s.num_ghost_cells, s.num_faces
+        self.dim, self.max_faces, self.n_conserved = s.dim, s.max_faces_per_cell, s.n_conserved
+        self.num_boundaries = s.num_boundaries
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().ibisgb_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, name, *args):
+        check(getattr(_lib.load(), name)(self._h, *args), self._h)
+
+    # ---------------------------------------------------------------- state
+    def set_primitives(self, T, p, vx, vy, vz=None):
+        """Initial condition of the valid cells (NativeBinaryInput::read + primatives_to_conserved)."""
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (T, p, vx, vy)]
+        vz_a = None if vz is None else np.ascontiguousarray(vz, np.float64)
+        for a in arrs + ([vz_a] if vz_a is not None else []):
+            if a.shape != (self.num_cells,):
+                raise ValueError(f"expected {self.num_cells} values per field")
+        self._call("ibisgb_set_primitives", *[_ptr(a) for a in arrs],
+                   None if vz_a is None else _ptr(vz_a))
+
+    def primitives(self) -> dict:
+        N = self.num_cells
+        out = {k: np.empty(N) for k in ("rho", "p", "T", "e", "vx", "vy", "vz")}
+        self._call("ibisgb_get_primitives", *[_ptr(out[k]) for k in ("rho", "p", "T", "e", "vx", "vy", "vz")])
+        return out
+
+    def conserved(self) -> np.ndarray:
+        out = np.empty((self.num_cells, self.n_conserved))
+        self._call("ibisgb_get_conserved", _ptr(out))
+        return out
+
+    # ------------------------------------------------------------- residual
+    def compute_dudt(self, precision: str = "f64") -> np.ndarray:
+        """dU/dt of the valid cells, (N, n_conserved) in the reference's cell order."""
+        out = np.empty((self.num_cells, self.n_conserved))
+        self._call("ibisgb_residual", PRECISION[precision], _ptr(out))
+        return out
+
+    def compute_dudt_into(self, out, precision: str = "f64", stream=None):
+        """As compute_dudt into a CUDA tensor of shape (N, n_conserved), float64."""
+        if not (out.is_cuda and out.dtype.is_floating_point and out.element_size() == 8 and out.is_contiguous()):
+            raise ValueError("out must be a contiguous float64 CUDA tensor")
+        if tuple(out.shape) != (self.num_cells, self.n_conserved):
+            raise ValueError("out has the wrong shape")
+        s = None if stream is None else C.c_void_p(stream.cuda_stream)
+        self._call("ibisgb_residual_device", PRECISION[precision], C.c_void_p(out.data_ptr()), s)
+        return out
+
+    def estimate_dt(self) -> float:
+        dt = C.c_double()
+        self._call("ibisgb_estimate_dt", C.byref(dt))
+        return dt.value
+
+    def count_bad_cells(self) -> int:
+        n = C.c_int64()
+        self._call("ibisgb_count_bad_cells", C.byref(n))
+        return n.value
+
+    # ----------------------------------------------------------- time march
+    def take_steps(self, n: int, precision: str = "f64") -> dict:
+        """n explicit Runge-Kutta steps on the device; returns t, dt, stable_dt, steps."""
+        st = RkStatus()
+        self._call("ibisgb_rk_run", PRECISION[precision], int(n), C.byref(st))
+        return {"t": st.t, "dt": st.dt, "stable_dt": st.stable_dt, "steps": st.steps,
+                "bad_cells": st.bad_cells}
+
+    def L2_norms(self) -> np.ndarray:
+        """global, mass, momentum_x, momentum_y, momentum_z, energy of the first-stage residual."""
+        out = np.empty(6)
+        self._call("ibisgb_l2_norms", _ptr(out))
+        return out
+
+    def synchronize(self):
+        self._call("ibisgb_synchronize")
+
+    # ---------------------------------------------------------------- dumps
+    def dump(self, name: str) -> np.ndarray:
+        which, dt = DUMPS[name]
+        N, F, G, MF, NT, nc = (self.num_cells, self.num_faces, self.num_ghost_cells, self.max_faces,
+                               self.num_cells + self.num_ghost_cells, self.n_conserved)
+        shape = {"left": (F,), "right": (F,), "cell_faces": (N, MF), "outsigns": (N, MF),
+                 "neighbours": (N, MF), "ghost_source": (G,), "face_geometry": (13, F),
+                 "cell_geometry": (4, NT), "limiter_branches": (N, 5), "limiters": (5, N),
+                 "face_flux": (F, nc)}[name]
+        out = np.empty(shape, dt)
+        self._call("ibisgb_get_dump", which, _ptr(out), out.nbytes)
+        return out

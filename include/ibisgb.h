@@ -1,0 +1,159 @@
+/*
+ * ibisgb — GB300-native residual engine for ibis's compressible finite-volume path.
+ *
+ * C ABI of libibisgb.so.  Plain pointers and sizes only; no C++ exceptions cross
+ * this boundary.  Every function returns 0 on success or a negative IBISGB_ERR_*
+ * code, with a message from ibisgb_last_error().
+ *
+ * A context owns one grid, its device memory and one CUDA stream.  It is not
+ * thread-safe: use one context per host thread.  Host pointers passed in are
+ * owned by the caller and copied before the call returns; *_device entry points
+ * take device pointers and run on the context's stream.
+ *
+ * Array conventions follow ibis: cells and faces are in the reference's
+ * numbering (cells in SU2 file order; faces numbered by first appearance while
+ * scanning cells, src/grid/grid/grid.h:113-133; ghost cells N.. in boundary-tag
+ * order, grid.h:406-443).  Conserved quantities are row-major (cell, component)
+ * with components (mass, momentum_x, momentum_y[, momentum_z], energy), like
+ * ConservedQuantities' View<T**>(n, dim+2) (conserved_quantities.cpp:15-23).
+ */
+#ifndef IBISGB_H
+#define IBISGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IBISGB_OK 0
+#define IBISGB_ERR_CONFIG (-1)    /* bad or unsupported config.json content */
+#define IBISGB_ERR_GRID (-2)      /* unreadable or inconsistent grid */
+#define IBISGB_ERR_CUDA (-3)      /* CUDA runtime failure (no device, OOM, launch error) */
+#define IBISGB_ERR_BAD_CELLS (-4) /* T < 0, rho < 0 or non-finite rho after a step */
+#define IBISGB_ERR_ARG (-5)       /* null or inconsistent argument */
+#define IBISGB_ERR_TIMEOUT (-6)   /* a bounded device wait ran out */
+#define IBISGB_ERR_STATE (-7)     /* call out of order (e.g. no initial condition yet) */
+
+/* Arithmetic of the residual.  F64: everything in double (fused multiply-add
+ * allowed).  MIXED: reconstruction, gradients, limiters and fluxes in float,
+ * face fluxes accumulated into cell residuals, state update and
+ * conserved->primitive inversion in double.  F64_EXACT: double with the
+ * reference's operation order and no fused multiply-add, for bitwise parity. */
+#define IBISGB_F64 0
+#define IBISGB_MIXED 1
+#define IBISGB_F64_EXACT 2
+
+typedef struct ibisgb_ctx ibisgb_ctx;
+
+typedef struct {
+    int64_t num_cells;       /* valid cells N */
+    int64_t num_ghost_cells; /* ghost cells G (ids N..N+G-1) */
+    int64_t num_faces;       /* faces F */
+    int32_t dim;             /* 2 or 3 */
+    int32_t max_faces_per_cell;
+    int32_t n_conserved;     /* dim + 2 */
+    int32_t num_boundaries;  /* boundary tags in config.json */
+} ibisgb_sizes;
+
+typedef struct {
+    double t;          /* simulated time after the last step */
+    double dt;         /* last time step */
+    double stable_dt;  /* last CFL-stable estimate (FiniteVolume::estimate_dt) */
+    int64_t steps;     /* steps taken by this context */
+    int64_t bad_cells; /* bad cells after the last step */
+} ibisgb_rk_status;
+
+/* Build a context from a config.json document and an SU2 grid file.
+ * Replaces GridBlock<T>(file, config) (src/grid/grid/grid.h:40-42, 89-167),
+ * FiniteVolume<T>(grid, config) (src/finite_volume/finite_volume/finite_volume.cpp:13-54),
+ * IdealGas(json)/TransportProperties(json) (src/gas/gas/gas_model.h:58-62,
+ * transport_properties.h:91-109) and RungeKutta's tableau/CFL set-up
+ * (src/solvers/solvers/runge_kutta.cpp:21-80). */
+int ibisgb_create(const char* config_json, const char* su2_path, ibisgb_ctx** out);
+
+/* Same, from grid arrays instead of an SU2 file: VTK element codes (3 line,
+ * 5 tri, 9 quad, 10 tet, 12 hex, 13 wedge, 14 pyramid), CSR connectivity;
+ * markers named by newline-separated marker_names, marker m owning elements
+ * marker_offsets[m]..marker_offsets[m+1]-1.  Equivalent to GridIO's SU2 reader
+ * output (src/grid/grid/grid_io.cpp:218-268). */
+int ibisgb_create_from_arrays(const char* config_json, int32_t dim, int64_t num_vertices,
+                              const double* xyz, int64_t num_cells, const int32_t* cell_types,
+                              const int64_t* cell_offsets, const int64_t* cell_vertices,
+                              int32_t num_markers, const char* marker_names,
+                              const int64_t* marker_offsets, const int32_t* element_types,
+                              const int64_t* element_offsets, const int64_t* element_vertices,
+                              ibisgb_ctx** out);
+
+void ibisgb_destroy(ibisgb_ctx* ctx);
+
+/* Message of the last error on ctx (or of the last failed create when ctx is NULL). */
+const char* ibisgb_last_error(const ibisgb_ctx* ctx);
+
+int ibisgb_get_sizes(const ibisgb_ctx* ctx, ibisgb_sizes* out);
+
+/* Initial condition on the valid cells (T, p, vx, vy[, vz]; vz may be NULL in 2-D);
+ * rho and internal energy follow from update_thermo_from_pT.  Replaces
+ * NativeBinaryInput::read (src/io/io/native.cpp:263-339) + primatives_to_conserved
+ * (src/finite_volume/finite_volume/primative_conserved_conversion.cpp:31-51). */
+int ibisgb_set_primitives(ibisgb_ctx* ctx, const double* T, const double* p, const double* vx,
+                          const double* vy, const double* vz);
+
+/* Primitives of the valid cells in the current state (any pointer may be NULL).
+ * Replaces the FlowStates read-back of FVIO::write (src/io/io/io.cpp:106-129). */
+int ibisgb_get_primitives(ibisgb_ctx* ctx, double* rho, double* p, double* T, double* e,
+                          double* vx, double* vy, double* vz);
+
+/* Conserved state of the valid cells, N x n_conserved row-major. */
+int ibisgb_get_conserved(ibisgb_ctx* ctx, double* U);
+
+/* dU/dt of the valid cells (N x n_conserved row-major) at the current state,
+ * including the pre-reconstruction / pre-viscous boundary actions.  Replaces
+ * FiniteVolume<T>::compute_dudt (src/finite_volume/finite_volume/finite_volume.cpp:56-96). */
+int ibisgb_residual(ibisgb_ctx* ctx, int32_t precision, double* dudt);
+
+/* As ibisgb_residual with a device output pointer, on `stream` (a cudaStream_t,
+ * NULL for the context's stream).  For callers that keep data in HBM (torch). */
+int ibisgb_residual_device(ibisgb_ctx* ctx, int32_t precision, double* dudt_device, void* stream);
+
+/* CFL-stable time step of the current state.  Replaces FiniteVolume<T>::estimate_dt
+ * (finite_volume.cpp:130-184); in viscous runs the face states of the last
+ * residual evaluation are used, as in the reference. */
+int ibisgb_estimate_dt(ibisgb_ctx* ctx, double* dt);
+
+/* Bad cells (T<0, rho<0, NaN/Inf rho) in the current state.  Replaces
+ * FiniteVolume<T>::count_bad_cells (finite_volume.cpp:257-270). */
+int ibisgb_count_bad_cells(ibisgb_ctx* ctx, int64_t* n);
+
+/* n_steps explicit Runge-Kutta steps on the device (CUDA graph per step),
+ * dt = min(cfl(t) * stable_dt, 1.5 * dt_prev, max_time - t[, plot clip]).
+ * Replaces RungeKutta::take_step (src/solvers/solvers/runge_kutta.cpp:131-203)
+ * inside Solver::solve's loop (src/solvers/solvers/solver.cpp:25-59); returns
+ * IBISGB_ERR_BAD_CELLS after the first step that leaves bad cells. */
+int ibisgb_rk_run(ibisgb_ctx* ctx, int32_t precision, int64_t n_steps, ibisgb_rk_status* status);
+
+/* L2 norms of the first-stage residual of the last step: global, mass,
+ * momentum_x, momentum_y, momentum_z, energy.  Replaces
+ * ConservedQuantities<T>::L2_norms (conserved_quantities.cpp:40-69) on k_[0]
+ * (runge_kutta.cpp:264). */
+int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]);
+
+/* Internal arrays in reference numbering, for parity checks.
+ * which: 0 face left cell (int64 F), 1 face right cell (int64 F),
+ * 2 cell faces (int64 N x max_faces, -1 padded), 3 outsigns (int32 N x max_faces),
+ * 4 cell neighbours (int64 N x max_faces), 5 ghost source cell (int64 G),
+ * 6 face geometry (double 13 x F: n, t1, t2, centre, area),
+ * 7 cell geometry (double 4 x (N+G): centroid, volume),
+ * 8 limiter branch codes of the last residual (uint32 N x 5),
+ * 9 limiter values of the last residual (double 5 x N),
+ * 10 face fluxes of the last residual (double F x n_conserved). */
+int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
+
+/* Wait for all work on the context's stream. */
+int ibisgb_synchronize(ibisgb_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IBISGB_H */

@@ -1,0 +1,161 @@
+"""Parity of the sm_103a residual / Runge-Kutta kernels with the oracle.
+
+Tolerances (per cell, relative to the gross flux through the cell, see
+tests/cases.py:gross_flux_scale):
+  * f64_exact (reference operation order, no FMA): bitwise for inviscid cases;
+    viscous cases differ only through pow() in Sutherland's law: <= 1e-14.
+  * f64 (FMA contraction allowed): <= 1e-12.
+  * mixed (float reconstruction/flux, double accumulation): <= 2e-5.
+Limiter branch selection must be identical in both double builds.
+"""
+import numpy as np
+import pytest
+
+from ibis_gb300 import Simulation, grids
+from ibis_gb300._lib import IbisgbError
+from oracle.oracle import Oracle
+from tests.cases import case, gross_flux_scale, per_cell_rel_err
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("ramp", {}),
+    ("ramp", {"flux": "ausmdv"}),
+    ("ramp", {"flux": "ldfss2"}),
+    ("ramp", {"flux": "rusanov"}),
+    ("ramp", {"thermo": "rho_p"}),
+    ("ramp", {"thermo": "rho_T"}),
+    ("ramp", {"thermo": "p_T"}),
+    ("ramp", {"limiter": "unlimited"}),
+    ("ramp", {"order": 1}),
+    ("plate", {}),
+    ("box", {}),
+    ("box", {"flux": "ausmdv"}),
+    ("box_inout", {}),
+    ("subsonic", {}),
+]
+
+
+def ids(c):
+    return c[0] + "-" + "-".join(f"{k}={v}" for k, v in c[1].items())
+
+
+def pair(name, kw):
+    g, c, st = case(name, **kw)
+    sim, ref = Simulation(c, g), Oracle(c, g)
+    sim.set_primitives(*st)
+    ref.set_initial_condition(*st)
+    return sim, ref
+
+
+@pytest.mark.parametrize("name,kw", CASES, ids=[ids(c) for c in CASES])
+def test_residual_parity(name, kw):
+    sim, ref = pair(name, kw)
+    r_ref, br_ref = ref.residual(branches=True)
+    scale = gross_flux_scale(ref)
+    viscous = ref_viscous = sim.config["viscous_flux"]["enabled"]
+    limited = sim.config["convective_flux"]["reconstruction_order"] == 2 and \
+        sim.config["convective_flux"]["limiter"]["type"] == "barth_jespersen"
+
+    r = sim.compute_dudt("f64_exact")
+    if viscous:
+        assert per_cell_rel_err(r, r_ref, scale).max() <= 1e-14
+    else:
+        assert np.array_equal(r, r_ref), np.abs(r - r_ref).max()
+    if limited:
+        assert np.array_equal(sim.dump("limiter_branches"), br_ref)
+
+    r = sim.compute_dudt("f64")
+    assert per_cell_rel_err(r, r_ref, scale).max() <= 1e-12
+    if limited:
+        assert np.array_equal(sim.dump("limiter_branches"), br_ref)
+
+    r = sim.compute_dudt("mixed")
+    assert per_cell_rel_err(r, r_ref, scale).max() <= 2e-5
+    del ref_viscous
+
+
+@pytest.mark.parametrize("name", ["ramp", "plate", "box"])
+def test_estimate_dt(name):
+    sim, ref = pair(name, {})
+    ref.residual()
+    sim.compute_dudt("f64")  # viscous dt uses the face states of the last residual
+    assert sim.estimate_dt() == pytest.approx(ref.estimate_dt(), rel=1e-13)
+
+
+@pytest.mark.parametrize("name", ["ramp", "box", "plate"])
+def test_rk_trajectory(name):
+    steps = 6
+    sim, ref = pair(name, {})
+    ref.rk_initialise()
+    o = ref.rk_steps(steps)
+    U_ref = ref.conserved()
+    st = sim.take_steps(steps, "f64_exact")
+    assert st["steps"] == steps
+    assert st["dt"] == pytest.approx(o["dt"], rel=1e-14)
+    U = sim.conserved()
+    scale = np.abs(U_ref).max(axis=0)
+    if sim.config["viscous_flux"]["enabled"]:
+        assert (np.abs(U - U_ref) / scale).max() <= 1e-13
+    else:
+        assert np.array_equal(U, U_ref), (np.abs(U - U_ref) / scale).max()
+    norms = sim.L2_norms()
+    assert np.allclose(norms, o["norms"], rtol=1e-11, atol=1e-300)
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("mixed", 1e-6)])
+def test_rk_trajectory_fast_paths(precision, tol):
+    """L2 density error of the fast paths against the FP64 oracle after 20 steps
+    of the compression ramp from its uniform Mach 2 inflow state."""
+    g, c, inf = grids.ramp_case(48, 24)
+    sim, ref = Simulation(c, g), Oracle(c, g)
+    n = sim.num_cells
+    st = (np.full(n, inf["T"]), np.full(n, inf["p"]), np.full(n, inf["vx"]), np.full(n, inf["vy"]))
+    sim.set_primitives(*st)
+    ref.set_initial_condition(*st)
+    ref.rk_initialise()
+    ref.rk_steps(20)
+    rho_ref = ref.conserved()[:, 0]
+    sim.take_steps(20, precision)
+    rho = sim.conserved()[:, 0]
+    assert np.linalg.norm(rho - rho_ref) / np.linalg.norm(rho_ref) <= tol
+
+
+def test_uniform_stream_stays_uniform():
+    """tests/minimal/uniform_stream: a uniform supersonic stream is steady."""
+    gas = grids.ideal_gas()
+    inflow = grids.flow_state(gas, 300.0, 1e5, 800.0, 100.0, 50.0)
+    g = grids.box_3d(6)
+    b = {t: (grids.supersonic_inflow(inflow) if t in ("west", "south", "bottom") else grids.supersonic_outflow())
+         for t in ["west", "east", "south", "north", "bottom", "top"]}
+    sim = Simulation(grids.make_config(3, b, gas=gas), g)
+    n = sim.num_cells
+    sim.set_primitives(np.full(n, 300.0), np.full(n, 1e5), np.full(n, 800.0), np.full(n, 100.0), np.full(n, 50.0))
+    for prec in ("f64_exact", "f64", "mixed"):
+        assert np.abs(sim.compute_dudt(prec)).max() < 1e-6
+    U0 = sim.conserved()
+    sim.take_steps(10, "mixed")
+    assert np.abs(sim.conserved() - U0).max() <= 1e-9 * np.abs(U0).max()
+
+
+def test_bad_cells_stop_the_run():
+    """count_bad_cells -> Solver::solve returns 1 (solver.cpp:38-43): a NaN placed
+    in the host initial state stops the time march with IBISGB_ERR_BAD_CELLS."""
+    g, c, st = case("ramp")
+    sim = Simulation(c, g)
+    T, p, vx, vy, _ = st
+    p = p.copy()
+    p[7] = np.nan
+    sim.set_primitives(T, p, vx, vy)
+    with pytest.raises(IbisgbError) as e:
+        sim.take_steps(5, "f64")
+    assert e.value.code == -4
+    assert sim.count_bad_cells() > 0
+
+
+def test_residual_into_torch_tensor():
+    torch = pytest.importorskip("torch")
+    sim, ref = pair("box", {})
+    out = torch.empty((sim.num_cells, sim.n_conserved), dtype=torch.float64, device="cuda")
+    sim.compute_dudt_into(out, "f64_exact", stream=torch.cuda.current_stream())
+    assert np.array_equal(out.cpu().numpy(), ref.residual())
