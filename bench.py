@@ -1,0 +1,293 @@
+"""Benchmark: Mcell-updates/s of the explicit RK residual path on GB300.
+
+Workload (the residual-throughput case): 3-D Euler on a periodic unit box of
+n^3 hexahedra (default 256^3 = 16.8M cells), ideal gas gamma=1.4, rho=1 and p=1
+plus seeded Fourier modes, divergence-free velocity at rms Mach 0.3; ibis's
+default numerics (Hanel flux, 2nd-order MUSCL, Barth-Jespersen, rho_u thermo
+pair), ssp-rk3.  One cell-update = one valid cell through one RK stage; one
+bench step = one RK step (3 stages).  `value` is the mixed-precision path
+(float reconstruction/flux, double accumulation/update); the plain FP64 path
+and the mixed path's L2 density error against it are reported alongside.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 256]
+Under torchrun each rank advances its own box (weak scaling, no collective on
+the data path); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic bytes per 3-D cell-update (FP64 state, geometry at the variant's
+# precision): read U^(s), U^n, write U^(s+1) + cell geometry + 3.01 faces/cell
+B_ALG_3D = {"mixed": 268.0, "f64": 393.0}
+KERNELS_PER_STEP = 12  # ssp-rk3: (recon, face, update) x 3 + local dt, dt control, stage-1 combine
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="box cells per side")
+    ap.add_argument("--cpu-n", type=int, default=96, help="box size of the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle samples during the timed region."""
+
+    def __init__(self, device: int):
+        self.device, self.samples, self.proc, self.thread = device, [], None, None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_case(n):
+    from ibis_gb300 import grids
+    grid, config = grids.box_case(n)
+    ic = grids.box_initial_condition(n, config["gas_model"], seed=0)
+    return grid, config, ic
+
+
+def cpu_sample(n, steps):
+    """The oracle (CPU restatement of the reference) on an n^3 box: Mcell-updates/s."""
+    from oracle.oracle import Oracle, num_threads
+    grid, config, ic = make_case(n)
+    o = Oracle(config, grid)
+    o.set_initial_condition(*ic)
+    o.rk_initialise()
+    o.rk_steps(1)  # warm-up
+    t = time.perf_counter()
+    o.rk_steps(steps)
+    dt = time.perf_counter() - t
+    return 3.0 * n ** 3 * steps / dt / 1e6, num_threads(), dt
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the oracle port of the reference's CPU path, all host threads."""
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle, num_threads
+    n = args.cpu_n
+    grid, config, ic = make_case(n)
+    o = Oracle(config, grid)
+    o.set_initial_condition(*ic)
+    o.rk_initialise()
+    o.rk_steps(args.warmup)
+    t = time.perf_counter()
+    o.rk_steps(args.steps)
+    dt = time.perf_counter() - t
+    value = 3.0 * n ** 3 * args.steps / dt / 1e6
+    sample = (f"oracle port (C++ restatement of ibis's FP64 path, OpenMP) on a {n}^3 periodic box, "
+              f"{args.steps} ssp-rk3 steps; the 256^3 grid does not fit a bounded CPU run")
+    line = {"impl": "reference", "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"3-D Euler periodic box {n}^3, ssp-rk3, Hanel, MUSCL + Barth-Jespersen, rho_u"},
+            "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": num_threads(),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from ibis_gb300 import Simulation
+
+    n = args.n
+    grid, config, ic = make_case(n)
+    sim = Simulation(config, grid)
+    N = sim.num_cells
+    del grid
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # --- headline: mixed precision, device-resident state
+    sim.set_primitives(*ic)
+    sim.take_steps(args.warmup, "mixed")
+    barrier()
+    with ClockSampler(local) as clk:
+        st = sim.take_steps(args.steps, "mixed")
+        barrier()
+    ms_mixed = max_over_ranks(st["device_ms"])
+    rho_mixed = sim.conserved()[:, 0].copy()
+    value = world * N * 3.0 * args.steps / (ms_mixed / 1e3) / 1e6
+
+    # --- plain FP64 path over the same steps from the same state, and its accuracy reference
+    sim.set_primitives(*ic)
+    sim.take_steps(args.warmup, "f64")
+    barrier()
+    st64 = sim.take_steps(args.steps, "f64")
+    barrier()
+    ms_f64 = max_over_ranks(st64["device_ms"])
+    rho_f64 = sim.conserved()[:, 0]
+    value_f64 = world * N * 3.0 * args.steps / (ms_f64 / 1e3) / 1e6
+    l2_err = float(np.linalg.norm(rho_mixed - rho_f64) / np.linalg.norm(rho_f64))
+    max_err = float(np.abs(rho_mixed - rho_f64).max() / np.abs(rho_f64).max())
+
+    # --- kernel breakdown of one residual evaluation (CUDA events on the context stream)
+    kt = sim.kernel_times("mixed", reps=5)
+
+    # --- end to end through the C ABI with host (pinned) buffers: per step,
+    # upload of the conserved state, one RK step, read-back of the new state
+    nc = sim.n_conserved
+    host_in = torch.empty((N, nc), dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty((N, nc), dtype=torch.float64, pin_memory=True).numpy()
+    sim.set_primitives(*ic)
+    sim.conserved(out=host_in)
+    e2e_steps = max(3, min(10, args.steps))
+    for _ in range(2):
+        sim.set_conserved(host_in)
+        sim.take_steps(1, "mixed")
+        sim.conserved(out=host_out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_conserved(host_in)
+        sim.take_steps(1, "mixed")
+        sim.conserved(out=host_out)
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * N * 3.0 * e2e_steps / e2e_s / 1e6
+
+    peak, peak_kind = measured_peak_hbm()
+    stage_ms = ms_mixed / args.steps / 3.0
+    achieved = B_ALG_3D["mixed"] * N / (stage_ms / 1e3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "rk_stage_box_mixed_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            t = json.load(f)
+        if t.get("n") == n:
+            traffic = t["dram_bytes_per_stage"]
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, secs = cpu_sample(args.cpu_n, 4)
+        cpu = {"value": v, "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
+               "sample": f"oracle (C++ restatement of ibis's FP64 path, OpenMP) on a {args.cpu_n}^3 "
+                         f"periodic box, 4 ssp-rk3 steps ({secs:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 flux / f64 accumulate+update (mixed)", "data": "synthetic",
+            "config": {"workload": f"3-D Euler periodic box {n}^3 (residual-throughput case), ssp-rk3, "
+                                   f"Hanel, 2nd-order MUSCL + Barth-Jespersen, rho_u, mixed precision",
+                       "cells_per_gpu": N, "faces_per_gpu": sim.num_faces, "stages_per_step": 3,
+                       "l2": "inputs larger than L2 (state + geometry several GB per GPU), no flush",
+                       "parallelism": f"replicas x{world}"},
+            "f64": {"value": value_f64, "ms_per_step": ms_f64 / args.steps,
+                    "mixed_speedup": value / value_f64},
+            "accuracy": {"rho_rel_l2_err_mixed_vs_f64": l2_err, "rho_rel_max_err_mixed_vs_f64": max_err,
+                         "steps": args.warmup + args.steps},
+            "kernel_ms": {k: round(v, 4) for k, v in kt.items()},
+            "roofline": {"bound": "hbm", "kernel": "rk_stage (recon + face + update kernels of one stage)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "bytes_per_cell_update": B_ALG_3D["mixed"],
+                         "traffic": traffic},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 8 * nc * N,
+                    "d2h_bytes_per_step": 8 * nc * N, "steps": e2e_steps},
+            "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

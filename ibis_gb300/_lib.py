@@ -33,7 +33,7 @@ class Sizes(C.Structure):
 
 class RkStatus(C.Structure):
     _fields_ = [("t", C.c_double), ("dt", C.c_double), ("stable_dt", C.c_double),
-                ("steps", C.c_int64), ("bad_cells", C.c_int64)]
+                ("steps", C.c_int64), ("bad_cells", C.c_int64), ("device_ms", C.c_double)]
 
 
 _lib = None
@@ -73,6 +73,9 @@ def load(build_if_missing: bool = True):
     L.ibisgb_l2_norms.argtypes = [_P, _P]
     L.ibisgb_get_dump.argtypes = [_P, C.c_int32, _P, C.c_int64]
     L.ibisgb_synchronize.argtypes = [_P]
+    L.ibisgb_set_conserved.argtypes = [_P, _P]
+    L.ibisgb_get_stream.argtypes = [_P, C.POINTER(_P)]
+    L.ibisgb_kernel_times.argtypes = [_P, C.c_int32, C.c_int32, _P]
     _lib = L
     return L
 

@@ -522,16 +522,83 @@ struct ibisgb_ctx {
             CUDA_OK(cudaGraphInstantiate(&graph[gi], g, 0));
             CUDA_OK(cudaGraphDestroy(g));
         }
+        cudaEvent_t e0, e1;
+        CUDA_OK(cudaEventCreate(&e0));
+        CUDA_OK(cudaEventCreate(&e1));
+        CUDA_OK(cudaEventRecord(e0, stream));
         for (int64_t i = 0; i < n; i++) CUDA_OK(cudaGraphLaunch(graph[gi], stream));
+        CUDA_OK(cudaEventRecord(e1, stream));
         state_changed(prec);
         StepCtl c;
         CUDA_OK(cudaMemcpyAsync(&c, ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, stream));
         CUDA_OK(cudaStreamSynchronize(stream));
+        float ms = 0.f;
+        CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
         if (st) {
             st->t = c.t; st->dt = c.dt; st->stable_dt = c.stable_dt; st->steps = c.steps;
             st->bad_cells = (int64_t)c.bad_cells;
+            st->device_ms = ms;
         }
         if (c.bad_cells > 0) throw std::runtime_error("bad cells");
+    }
+
+    void kernel_times(int prec, int reps, double out[4]) {
+        ensure_prims(prec);
+        DevView v = view(prec);
+        KernelOps o = ops(prec);
+        const bool reco = prm.order == 2;
+        cudaEvent_t ev[5];
+        for (auto& e : ev) CUDA_OK(cudaEventCreate(&e));
+        double acc[4] = {0, 0, 0, 0};
+        for (int r = 0; r < reps + 1; r++) {  // first round is a warm-up
+            CUDA_OK(cudaEventRecord(ev[0], stream));
+            o.recon(v, prm, reco, stream);
+            CUDA_OK(cudaEventRecord(ev[1], stream));
+            o.face_flux(v, prm, reco, stream);
+            CUDA_OK(cudaEventRecord(ev[2], stream));
+            o.update(v, prm, 0, 0, nullptr, stream);
+            CUDA_OK(cudaEventRecord(ev[3], stream));
+            CUDA_OK(cudaGetLastError());
+            CUDA_OK(cudaEventSynchronize(ev[3]));
+            if (r == 0) continue;
+            float a, b, c, d;
+            CUDA_OK(cudaEventElapsedTime(&a, ev[0], ev[1]));
+            CUDA_OK(cudaEventElapsedTime(&b, ev[1], ev[2]));
+            CUDA_OK(cudaEventElapsedTime(&c, ev[2], ev[3]));
+            CUDA_OK(cudaEventElapsedTime(&d, ev[0], ev[3]));
+            acc[0] += a; acc[1] += b; acc[2] += c; acc[3] += d;
+        }
+        for (auto& e : ev) cudaEventDestroy(e);
+        for (int k = 0; k < 4; k++) out[k] = reps > 0 ? acc[k] / reps : 0.0;
+    }
+
+    void set_conserved(const double* rows) {
+        if (!rows) throw ArgError("U is null");
+        ensure_device();
+        const int64_t N = mesh.N;
+        const size_t bytes = sizeof(double) * nc() * N;
+        out.alloc(bytes);
+        CUDA_OK(cudaMemcpyAsync(out.p, rows, bytes, cudaMemcpyHostToDevice, stream));
+        launch_rows_to_soa(out.as<double>(), U.as<double>(), (int)N, nc(), stream);
+        CUDA_OK(cudaGetLastError());
+        if (!have_state) reset_rk();
+        have_state = true;
+        ic_prims.clear();
+        s64.prims_current = false;
+        s32.prims_current = false;
+    }
+
+    void get_conserved(double* rows) {
+        if (!have_state) throw StateError("no initial condition");
+        const int64_t N = mesh.N;
+        const size_t bytes = sizeof(double) * nc() * N;
+        out.alloc(bytes);
+        launch_soa_to_rows(U.as<double>(), out.as<double>(), (int)N, nc(), stream);
+        CUDA_OK(cudaGetLastError());
+        CUDA_OK(cudaMemcpyAsync(rows, out.p, bytes, cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
     }
 
     void get_primitives(double* out7[7]) {
@@ -701,16 +768,27 @@ int ibisgb_get_primitives(ibisgb_ctx* ctx, double* rho, double* p, double* T, do
 
 int ibisgb_get_conserved(ibisgb_ctx* ctx, double* out) {
     if (!ctx || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->get_conserved(out); });
+}
+
+int ibisgb_set_conserved(ibisgb_ctx* ctx, const double* U) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->set_conserved(U); });
+}
+
+int ibisgb_get_stream(ibisgb_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (!ctx->have_state) throw StateError("no initial condition");
         ctx->ensure_device();
-        const int64_t N = ctx->mesh.N;
-        const int nc = ctx->nc();
-        std::vector<double> soa(nc * N);
-        CUDA_OK(cudaMemcpyAsync(soa.data(), ctx->U.p, sizeof(double) * nc * N, cudaMemcpyDeviceToHost, ctx->stream));
-        CUDA_OK(cudaStreamSynchronize(ctx->stream));
-        for (int64_t i = 0; i < N; i++)
-            for (int q = 0; q < nc; q++) out[i * nc + q] = soa[q * N + i];
+        *stream = (void*)ctx->stream;
+    });
+}
+
+int ibisgb_kernel_times(ibisgb_ctx* ctx, int32_t precision, int32_t reps, double out[4]) {
+    if (!ctx || !out || reps < 0) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        ctx->kernel_times(precision, reps, out);
     });
 }
 

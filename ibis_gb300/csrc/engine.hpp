@@ -140,7 +140,8 @@ KernelOps kernels_mixed();
 void launch_dt_finalize(StepCtl* ctl, cudaStream_t s);
 void launch_reset_dt(StepCtl* ctl, cudaStream_t s);
 void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s);
-void launch_count_bad(const void* prim, bool is_float, int N, int NT, unsigned long long* out,
-                      cudaStream_t s);
+// row-major (N x nc) <-> slot-major ([nc][N]) conserved state
+void launch_rows_to_soa(const double* rows, double* soa, int N, int nc, cudaStream_t s);
+void launch_soa_to_rows(const double* soa, double* rows, int N, int nc, cudaStream_t s);
 
 }  // namespace ibisgb

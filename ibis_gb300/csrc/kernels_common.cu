@@ -94,6 +94,28 @@ void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t
     k_l2_final<<<1, 32, 0, s>>>(out6 + 6, nblocks, out6);
 }
 
-void launch_count_bad(const void*, bool, int, int, unsigned long long*, cudaStream_t) {}
+namespace {
+__global__ void k_rows_to_soa(const double* rows, double* soa, int N, int nc) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * nc) return;
+    int i = (int)(t / nc), q = (int)(t % nc);
+    soa[(size_t)q * N + i] = rows[t];
+}
+__global__ void k_soa_to_rows(const double* soa, double* rows, int N, int nc) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * nc) return;
+    int i = (int)(t / nc), q = (int)(t % nc);
+    rows[t] = soa[(size_t)q * N + i];
+}
+}  // namespace
+
+void launch_rows_to_soa(const double* rows, double* soa, int N, int nc, cudaStream_t s) {
+    long long n = (long long)N * nc;
+    k_rows_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rows, soa, N, nc);
+}
+void launch_soa_to_rows(const double* soa, double* rows, int N, int nc, cudaStream_t s) {
+    long long n = (long long)N * nc;
+    k_soa_to_rows<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(soa, rows, N, nc);
+}
 
 }  // namespace ibisgb

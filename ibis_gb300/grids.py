@@ -380,35 +380,35 @@ def box_case(n=64, **kw):
 
 
 def box_initial_condition(n: int, gas: dict, seed=0, kmax=4, amp=0.05, mach_rms=0.3):
-    """rho=1, p=1 plus Fourier modes |k|<=kmax with random phases at ``amp``
-    relative amplitude; solenoidal random velocity scaled to rms Mach
-    ``mach_rms``.  Returns (T, p, vx, vy, vz) on the n^3 cells (cell order
-    i + n (j + n k))."""
+    """rho=1, p=1 plus the sum of Fourier modes 0<|k|<=kmax with seeded random
+    phases at ``amp`` relative amplitude; a divergence-free velocity (curl of a
+    random vector potential A_c = sum_k cos(2 pi k.x + phi_kc)/|k|^2) scaled to
+    rms Mach ``mach_rms``.  Sampled at the cell centres x = (i + 1/2)/n by
+    inverse FFT.  Returns (T, p, vx, vy, vz) in cell order i + n (j + n k)."""
     rng = np.random.default_rng(seed)
-    c = (np.arange(n) + 0.5) / n
-    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
     ks = [(a, b, d) for a in range(-kmax, kmax + 1) for b in range(-kmax, kmax + 1)
           for d in range(-kmax, kmax + 1) if 0 < a * a + b * b + d * d <= kmax * kmax]
-    rho_p = np.zeros_like(X)
-    p_p = np.zeros_like(X)
-    u = np.zeros((3,) + X.shape)
+    spec = np.zeros((5, n, n, n), np.complex128)  # rho, p, ux, uy, uz; axes (k_z, k_y, k_x)
     for (a, b, d) in ks:
-        th = 2 * np.pi * (a * X + b * Y + d * Z)
-        rho_p += np.cos(th + rng.uniform(0, 2 * np.pi))
-        p_p += np.cos(th + rng.uniform(0, 2 * np.pi))
-        # velocity = curl of the vector potential A_c = cos(th + phi_c)/|k|^2, exactly
-        # divergence free: dA_c/dx_j = -2 pi k_j sin(th + phi_c)/|k|^2
+        ph = rng.uniform(0, 2 * np.pi, 5)
+        shift = np.exp(1j * np.pi * (a + b + d) / n)  # samples at (j + 1/2)/n
+        idx = (d % n, b % n, a % n)
+        spec[0][idx] += np.exp(1j * ph[0]) * shift
+        spec[1][idx] += np.exp(1j * ph[1]) * shift
+        # sin(theta + phi) = Re(-i e^{i(theta + phi)}); dA_c/dx_j = -2 pi k_j sin(...)/|k|^2
         k = (a, b, d)
         k2 = float(a * a + b * b + d * d)
-        s = [np.sin(th + rng.uniform(0, 2 * np.pi)) for _ in range(3)]
-        dA = lambda c, j: -2 * np.pi * k[j] * s[c] / k2  # noqa: E731
-        u[0] += dA(2, 1) - dA(1, 2)
-        u[1] += dA(0, 2) - dA(2, 0)
-        u[2] += dA(1, 0) - dA(0, 1)
+        e = [-1j * np.exp(1j * ph[2 + c]) * shift for c in range(3)]
+        dA = lambda c, j: -2 * np.pi * k[j] * e[c] / k2  # noqa: E731
+        spec[2][idx] += dA(2, 1) - dA(1, 2)
+        spec[3][idx] += dA(0, 2) - dA(2, 0)
+        spec[4][idx] += dA(1, 0) - dA(0, 1)
+    fields = np.fft.ifftn(spec, axes=(1, 2, 3)).real * (n ** 3)
+    rho_p, p_p, u = fields[0], fields[1], fields[2:5]
     rho = 1.0 + amp * rho_p / np.abs(rho_p).max()
     p = 1.0 + amp * p_p / np.abs(p_p).max()
     a_mean = math.sqrt(gas["gamma"] * gas["R"] * 1.0)
-    u *= mach_rms * a_mean / math.sqrt((u ** 2).sum(0).mean())
+    u = u * (mach_rms * a_mean / math.sqrt((u ** 2).sum(0).mean()))
     T = p / (rho * gas["R"])
     f = lambda v: np.ascontiguousarray(v.reshape(-1))  # noqa: E731  (k slowest, i fastest)
     return f(T), f(p), f(u[0]), f(u[1]), f(u[2])

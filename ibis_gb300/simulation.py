@@ -102,10 +102,31 @@ class Simulation:
         self._call("ibisgb_get_primitives", *[_ptr(out[k]) for k in ("rho", "p", "T", "e", "vx", "vy", "vz")])
         return out
 
-    def conserved(self) -> np.ndarray:
-        out = np.empty((self.num_cells, self.n_conserved))
+    def conserved(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Conserved state (N, n_conserved); ``out`` may be a (pinned) host buffer."""
+        if out is None:
+            out = np.empty((self.num_cells, self.n_conserved))
         self._call("ibisgb_get_conserved", _ptr(out))
         return out
+
+    def set_conserved(self, U: np.ndarray) -> None:
+        """Replace the conserved state (N, n_conserved), e.g. from a pinned host buffer."""
+        U = np.ascontiguousarray(U, np.float64)
+        if U.shape != (self.num_cells, self.n_conserved):
+            raise ValueError("U has the wrong shape")
+        self._call("ibisgb_set_conserved", _ptr(U))
+
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t as an integer (torch.cuda.ExternalStream(ptr))."""
+        s = C.c_void_p()
+        self._call("ibisgb_get_stream", C.byref(s))
+        return s.value or 0
+
+    def kernel_times(self, precision: str = "mixed", reps: int = 10) -> dict:
+        """Mean device ms of the residual's kernels (CUDA events on the context stream)."""
+        out = np.zeros(4)
+        self._call("ibisgb_kernel_times", PRECISION[precision], int(reps), _ptr(out))
+        return {"recon": out[0], "face": out[1], "update": out[2], "residual": out[3]}
 
     # ------------------------------------------------------------- residual
     def compute_dudt(self, precision: str = "f64") -> np.ndarray:
@@ -140,7 +161,7 @@ class Simulation:
         st = RkStatus()
         self._call("ibisgb_rk_run", PRECISION[precision], int(n), C.byref(st))
         return {"t": st.t, "dt": st.dt, "stable_dt": st.stable_dt, "steps": st.steps,
-                "bad_cells": st.bad_cells}
+                "bad_cells": st.bad_cells, "device_ms": st.device_ms}
 
     def L2_norms(self) -> np.ndarray:
         """global, mass, momentum_x, momentum_y, momentum_z, energy of the first-stage residual."""

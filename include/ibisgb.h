@@ -62,6 +62,7 @@ typedef struct {
     double stable_dt;  /* last CFL-stable estimate (FiniteVolume::estimate_dt) */
     int64_t steps;     /* steps taken by this context */
     int64_t bad_cells; /* bad cells after the last step */
+    double device_ms;  /* device time of the steps of this call (CUDA events on the context stream) */
 } ibisgb_rk_status;
 
 /* Build a context from a config.json document and an SU2 grid file.
@@ -106,6 +107,24 @@ int ibisgb_get_primitives(ibisgb_ctx* ctx, double* rho, double* p, double* T, do
 
 /* Conserved state of the valid cells, N x n_conserved row-major. */
 int ibisgb_get_conserved(ibisgb_ctx* ctx, double* U);
+
+/* Replace the conserved state of the valid cells (N x n_conserved row-major,
+ * host memory; pinned memory copies fastest); primitives and ghost cells follow
+ * from conserved_to_primatives (primative_conserved_conversion.cpp:4-23).  The
+ * state write of Jfnk::apply_update_ (src/solvers/solvers/jfnk.cpp:63-93) and
+ * of a restart. */
+int ibisgb_set_conserved(ibisgb_ctx* ctx, const double* U);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that record events
+ * or order their own work against the context. */
+int ibisgb_get_stream(ibisgb_ctx* ctx, void** stream);
+
+/* Mean device time in milliseconds, over `reps` launches timed with CUDA
+ * events on the context stream, of the kernels of one residual evaluation:
+ * out[0] gradients + limiters, out[1] face fluxes, out[2] surface integral,
+ * out[3] the whole evaluation.  A profiling aid with no counterpart in ibis,
+ * which only labels its Kokkos kernels. */
+int ibisgb_kernel_times(ibisgb_ctx* ctx, int32_t precision, int32_t reps, double out[4]);
 
 /* dU/dt of the valid cells (N x n_conserved row-major) at the current state,
  * including the pre-reconstruction / pre-viscous boundary actions.  Replaces
