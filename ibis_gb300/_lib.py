@@ -76,6 +76,7 @@ def load(build_if_missing: bool = True):
     L.ibisgb_set_conserved.argtypes = [_P, _P]
     L.ibisgb_get_stream.argtypes = [_P, C.POINTER(_P)]
     L.ibisgb_kernel_times.argtypes = [_P, C.c_int32, C.c_int32, _P]
+    L.ibisgb_l2_norms_noalloc.argtypes = [_P, C.c_int64, C.c_int32, _P, _P]
     _lib = L
     return L
 

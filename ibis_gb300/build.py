@@ -34,6 +34,7 @@ UNITS = {
     "kernels_f64.cu": "nvcc",
     "kernels_mixed.cu": "nvcc",
     "kernels_exact.cu": "nvcc-nofma",
+    "noalloc.cu": "nvcc",
 }
 
 

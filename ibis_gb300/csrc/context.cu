@@ -629,6 +629,11 @@ struct ibisgb_ctx {
 
 namespace {
 thread_local std::string g_create_error;
+}  // namespace
+
+void ibisgb::set_thread_error(const std::string& msg) { g_create_error = msg; }
+
+namespace {
 
 template <class F>
 int guarded(ibisgb_ctx* ctx, F&& f) {

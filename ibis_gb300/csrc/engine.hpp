@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -140,6 +141,9 @@ KernelOps kernels_mixed();
 void launch_dt_finalize(StepCtl* ctl, cudaStream_t s);
 void launch_reset_dt(StepCtl* ctl, cudaStream_t s);
 void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s);
+// message returned by ibisgb_last_error(NULL) on this thread
+void set_thread_error(const std::string& msg);
+
 // row-major (N x nc) <-> slot-major ([nc][N]) conserved state
 void launch_rows_to_soa(const double* rows, double* soa, int N, int nc, cudaStream_t s);
 void launch_soa_to_rows(const double* soa, double* rows, int N, int nc, cudaStream_t s);

@@ -171,6 +171,28 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
 /* Wait for all work on the context's stream. */
 int ibisgb_synchronize(ibisgb_ctx* ctx);
 
+/* Largest residual (in cells) that ibisgb_l2_norms_noalloc accepts.  Its
+ * scratch is one fixed array of 4096 x 6 doubles (192 KiB) that every GPU
+ * which loads the library keeps until the process exits. */
+#define IBISGB_NOALLOC_MAX_CELLS 16777216
+
+/* L2 norms (global, mass, momentum_x, momentum_y, momentum_z, energy) of a
+ * residual already in device memory (dudt_device: num_cells x n_conserved
+ * row-major, as ibisgb_residual_device writes it) into norms_device (6 doubles
+ * of device memory), on `stream`, without allocating anything.  This entry
+ * point has no counterpart in the reference; it is ibisgb_l2_norms for callers
+ * that cannot call cudaMalloc: code whose device memory is owned by a caching
+ * allocator that leaves no room for a raw allocation, and time loops that must
+ * not stall on the device synchronization of cudaMalloc/cudaFree.
+ * num_cells above IBISGB_NOALLOC_MAX_CELLS, or n_conserved other than 4 or 5,
+ * are rejected with IBISGB_ERR_ARG; errors are read with ibisgb_last_error(NULL).
+ * The first call on a device looks up the scratch array's device address with
+ * that device current: make that first call before any stream capture.  All
+ * calls share the one scratch array (each call writes every slot it reads), so
+ * calls whose work overlaps on the GPU race: serialize them. */
+int ibisgb_l2_norms_noalloc(const double* dudt_device, int64_t num_cells, int32_t n_conserved,
+                            double* norms_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
