@@ -3,7 +3,8 @@
 Host code is compiled without FMA contraction (-ffp-contract=off) so that grid
 preprocessing reproduces the reference's geometry bit for bit on both x86 and
 aarch64 hosts; kernels_exact.cu is compiled with -fmad=false for the
-bitwise-parity FP64 path.  Object files are rebuilt only when a source or
+bitwise-parity FP64 path and kernels_mixed.cu with --use_fast_math (float
+division and square root to within 2 ulp, denormals flushed) for the mixed path.  Object files are rebuilt only when a source or
 header changes.
 """
 from __future__ import annotations
@@ -32,7 +33,7 @@ UNITS = {
     "context.cu": "nvcc",
     "kernels_common.cu": "nvcc",
     "kernels_f64.cu": "nvcc",
-    "kernels_mixed.cu": "nvcc",
+    "kernels_mixed.cu": "nvcc-fast",
     "kernels_exact.cu": "nvcc-nofma",
     "noalloc.cu": "nvcc",
 }
@@ -62,7 +63,8 @@ def _compile(unit: str, kind: str, verbose: bool) -> str:
     if kind == "cxx":
         cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-c", src, "-o", obj]
     else:
-        cmd = [_nvcc()] + NVCC_FLAGS + (["-fmad=false"] if kind == "nvcc-nofma" else []) + ["-c", src, "-o", obj]
+        extra = {"nvcc-nofma": ["-fmad=false"], "nvcc-fast": ["--use_fast_math"]}.get(kind, [])
+        cmd = [_nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
     stamp = obj + ".sha"
     dig = _digest(unit, cmd[1:])
     if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == dig:

@@ -69,7 +69,7 @@ void upload(DBuf& b, const std::vector<T>& v, cudaStream_t s) {
 
 // State buffers of one storage type (double for F64 / F64_EXACT, float for MIXED).
 struct StateBufs {
-    DBuf cc, r, face;                              // geometry
+    DBuf cc, r, face, lsqw;                        // geometry
     DBuf prim, vghost, grad, phi, vgrad, flux;     // state and intermediates
     bool geometry = false;
     bool prims_current = false;
@@ -121,7 +121,7 @@ struct ibisgb_ctx {
 
     // connectivity and per-cell data shared by all arithmetics
     DBuf cell_face, cell_nbr, outsign, nfaces, left, right, ghost_src, ghost_face, ghost_bound,
-        bounds, feed_off, feed_ghost, vol;
+        bounds, feed_off, feed_ghost, vol, inv_vol;
     DBuf U, k, vsig, ctl, l2, out, branches;
     StateBufs s64, s32;
     std::vector<double> ic_prims;  // host IC primitives (7 x NT), kept until the first update
@@ -189,6 +189,10 @@ struct ibisgb_ctx {
             if (grid.contains("motion") && grid.at("motion").contains("enabled") &&
                 grid.at("motion").at("enabled").as_bool())
                 throw ConfigError("moving grids are not supported");
+            prm.fR = (float)prm.R; prm.fCv = (float)prm.Cv; prm.fCp = (float)prm.Cp;
+            prm.fgamma = (float)prm.gamma; prm.fgR = prm.fgamma * prm.fR; prm.feps = (float)prm.eps;
+            prm.fdelta = (float)prm.delta; prm.fmu0 = (float)prm.mu0; prm.fT0 = (float)prm.T0;
+            prm.fTs = (float)prm.Ts; prm.fPr = (float)prm.Pr; prm.inv_Cv = 1.0 / prm.Cv;
             const Json& solver = config.at("solver");
             if (solver.at("name").as_string() == "runge_kutta") parse_rk(solver);
         } catch (const ConfigError&) {
@@ -316,6 +320,8 @@ struct ibisgb_ctx {
         upload(feed_off, off, stream); upload(feed_ghost, fg, stream);
         std::vector<double> v(mesh.volume.begin(), mesh.volume.begin() + N);
         upload(vol, v, stream);
+        for (auto& x : v) x = 1.0 / x;
+        upload(inv_vol, v, stream);
         U.alloc(sizeof(double) * nc() * N);
         k.alloc(sizeof(double) * nc() * N * stages());
         vsig.alloc(sizeof(double) * F);
@@ -339,6 +345,10 @@ struct ibisgb_ctx {
         for (int q = 0; q < 13; q++)
             for (int64_t f = 0; f < F; f++) fc[q * F + f] = (Gm)(*fa[q])[f];
         upload(s.cc, cc, stream); upload(s.r, r, stream); upload(s.face, fc, stream);
+        if (!mesh.lsqw.empty()) {
+            std::vector<Gm> w(mesh.lsqw.begin(), mesh.lsqw.end());
+            upload(s.lsqw, w, stream);
+        }
         size_t P = sizeof(Gm);
         s.prim.alloc(P * 7 * NT);
         s.vghost.alloc(P * 5 * std::max<int64_t>(mesh.G, 1));
@@ -370,6 +380,7 @@ struct ibisgb_ctx {
         v.ghost_bound = ghost_bound.as<int>(); v.bounds = bounds.as<BoundDev>();
         v.feed_off = feed_off.as<int>(); v.feed_ghost = feed_ghost.as<int>();
         v.cc = s.cc.p; v.r = s.r.p; v.face = s.face.p; v.vol = vol.as<double>();
+        v.inv_vol = inv_vol.as<double>(); v.lsqw = s.lsqw.p;
         v.prim = s.prim.p; v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
         v.U = U.as<double>(); v.k = k.as<double>(); v.ctl = ctl.as<StepCtl>();

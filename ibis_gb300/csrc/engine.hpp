@@ -52,6 +52,10 @@ struct FvParams {
     double signal_factor;  // viscous dt signal factor
     double R, Cv, Cp, gamma;
     double mu0, T0, Ts, Pr;
+    // float copies for the float kernels (rounded on the host, so that the
+    // device does no double->float conversions) and host-side reciprocals
+    float fR, fCv, fCp, fgamma, fgR, feps, fdelta, fmu0, fT0, fTs, fPr;
+    double inv_Cv;
 };
 
 // Device-side control block of the explicit Runge-Kutta step
@@ -95,7 +99,9 @@ struct DevView {
     const void* cc;
     const void* r;
     const void* face;
-    const double* vol;  // N
+    const double* vol;      // N
+    const double* inv_vol;  // N, 1/volume (fast paths)
+    const void* lsqw;       // [3][MF][N] least-squares weights per neighbour slot (type Gm, fast paths)
     // state (type P)
     void* prim;    // [7][NT]: rho, p, T, e, vx, vy, vz
     void* vghost;  // [5][G]: p, T, vx, vy, vz after the pre-viscous-gradient actions

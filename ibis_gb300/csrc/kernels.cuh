@@ -42,9 +42,14 @@ IBISGB_HD void thermo_vars(int kind, int& a, int& b) {
     }
 }
 
-struct State64 {
-    double rho, p, T, e, vx, vy, vz;
+template <class S>
+struct StateT {
+    S rho, p, T, e, vx, vy, vz;
 };
+using State64 = StateT<double>;
+
+IBISGB_HD double real_of(double x) { return x; }
+IBISGB_HD double real_of(float x) { return (double)x; }
 
 // primitive index of viscous variable q (0 T, 1 vx, 2 vy, 3 vz)
 IBISGB_HD int visc_prim(int q) { return q == 0 ? 2 : 3 + q; }
@@ -52,15 +57,15 @@ IBISGB_HD int visc_prim(int q) { return q == 0 ? 2 : 3 + q; }
 // ---------------------------------------------------------------------------
 // Ghost-cell actions on one ghost (boundary.cpp:9-400), in double.
 // ---------------------------------------------------------------------------
-template <class Gm>
-__device__ void apply_actions(const Action* acts, int n, State64& gh, const State64& src,
+template <class S, class Gm>
+__device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const StateT<S>& src,
                               const Gm* face, int F, int f, const FvParams& prm) {
     for (int a = 0; a < n; a++) {
         const Action& A = acts[a];
         switch (A.kind) {
             case aFlowStateCopy:
-                gh.T = A.fs[0]; gh.p = A.fs[1]; gh.rho = A.fs[2]; gh.e = A.fs[3];
-                gh.vx = A.fs[4]; gh.vy = A.fs[5]; gh.vz = A.fs[6];
+                gh.T = S(A.fs[0]); gh.p = S(A.fs[1]); gh.rho = S(A.fs[2]); gh.e = S(A.fs[3]);
+                gh.vx = S(A.fs[4]); gh.vy = S(A.fs[5]); gh.vz = S(A.fs[6]);
                 break;
             case aInternalCopy:
             case aPeriodicCopy:
@@ -68,13 +73,13 @@ __device__ void apply_actions(const Action* acts, int n, State64& gh, const Stat
                 break;
             case aReflectNormal: {
                 gh.T = src.T; gh.p = src.p; gh.rho = src.rho; gh.e = src.e;
-                double x = src.vx, y = src.vy, z = src.vz;
-                double nx = face[f], ny = face[F + f], nz = face[2 * F + f];
-                double t1x = face[3 * F + f], t1y = face[4 * F + f], t1z = face[5 * F + f];
-                double t2x = face[6 * F + f], t2y = face[7 * F + f], t2z = face[8 * F + f];
-                double xs = -(x * nx + y * ny + z * nz);
-                double ys = x * t1x + y * t1y + z * t1z;
-                double zs = x * t2x + y * t2y + z * t2z;
+                S x = src.vx, y = src.vy, z = src.vz;
+                S nx = S(face[f]), ny = S(face[F + f]), nz = S(face[2 * F + f]);
+                S t1x = S(face[3 * F + f]), t1y = S(face[4 * F + f]), t1z = S(face[5 * F + f]);
+                S t2x = S(face[6 * F + f]), t2y = S(face[7 * F + f]), t2z = S(face[8 * F + f]);
+                S xs = -(x * nx + y * ny + z * nz);
+                S ys = x * t1x + y * t1y + z * t1z;
+                S zs = x * t2x + y * t2y + z * t2z;
                 gh.vx = xs * nx + ys * t1x + zs * t2x;
                 gh.vy = xs * ny + ys * t1y + zs * t2y;
                 gh.vz = xs * nz + ys * t1z + zs * t2z;
@@ -84,40 +89,40 @@ __device__ void apply_actions(const Action* acts, int n, State64& gh, const Stat
                 gh.vx = -src.vx; gh.vy = -src.vy; gh.vz = -src.vz;
                 break;
             case aFixTemperature:
-                gh.T = 2 * A.value - src.T;
+                gh.T = S(2.0) * S(A.value) - src.T;
                 break;
             case aSubsonicInflow: {
-                double nx = face[f], ny = face[F + f], nz = face[2 * F + f];
-                double vc = nx * (A.fs[4] - src.vx) + ny * (A.fs[5] - src.vy) + nz * (A.fs[6] - src.vz);
-                double sos = sqrt(prm.gamma * prm.R * src.T);
-                double rho_ref = src.rho;
-                double p_in = A.fs[1];
-                double p_face = 0.5 * (p_in + src.p - rho_ref * sos * vc);
-                double rho_face = A.fs[2] + (p_face - p_in) / sos / sos;
-                double vxf = A.fs[4] - nx * (p_in - p_face) / (rho_ref * sos);
-                double vyf = A.fs[5] - ny * (p_in - p_face) / (rho_ref * sos);
-                double vzf = A.fs[6] - nz * (p_in - p_face) / (rho_ref * sos);
-                gh.p = 2 * p_face - src.p;
-                gh.rho = 2 * rho_face - src.rho;
-                gh.T = gh.p / (gh.rho * prm.R);
-                gh.e = prm.Cv * gh.T;
-                gh.vx = 2 * vxf - src.vx; gh.vy = 2 * vyf - src.vy; gh.vz = 2 * vzf - src.vz;
+                S nx = S(face[f]), ny = S(face[F + f]), nz = S(face[2 * F + f]);
+                S vc = nx * (S(A.fs[4]) - src.vx) + ny * (S(A.fs[5]) - src.vy) + nz * (S(A.fs[6]) - src.vz);
+                S sos = d_sqrt<S>(S(prm.gamma) * S(prm.R) * src.T);
+                S rho_ref = src.rho;
+                S p_in = S(A.fs[1]);
+                S p_face = S(0.5) * (p_in + src.p - rho_ref * sos * vc);
+                S rho_face = S(A.fs[2]) + (p_face - p_in) / sos / sos;
+                S vxf = S(A.fs[4]) - nx * (p_in - p_face) / (rho_ref * sos);
+                S vyf = S(A.fs[5]) - ny * (p_in - p_face) / (rho_ref * sos);
+                S vzf = S(A.fs[6]) - nz * (p_in - p_face) / (rho_ref * sos);
+                gh.p = S(2.0) * p_face - src.p;
+                gh.rho = S(2.0) * rho_face - src.rho;
+                gh.T = gh.p / (gh.rho * S(prm.R));
+                gh.e = S(prm.Cv) * gh.T;
+                gh.vx = S(2.0) * vxf - src.vx; gh.vy = S(2.0) * vyf - src.vy; gh.vz = S(2.0) * vzf - src.vz;
                 break;
             }
             case aSubsonicOutflow: {
-                double nx = face[f], ny = face[F + f], nz = face[2 * F + f];
-                double p_face = A.value;
-                double rho_ref = src.rho, p_ref = src.p;
-                double sos = sqrt(prm.gamma * prm.R * src.T);
-                double rho_face = src.rho + (p_face - p_ref) / sos / sos;
-                double vxf = src.vx + nx * (p_ref - p_face) / (rho_ref * sos);
-                double vyf = src.vy + ny * (p_ref - p_face) / (rho_ref * sos);
-                double vzf = src.vz + nz * (p_ref - p_face) / (rho_ref * sos);
-                gh.p = 2 * p_face - src.p;
-                gh.rho = 2 * rho_face - src.rho;
-                gh.T = gh.p / (gh.rho * prm.R);
-                gh.e = prm.Cv * gh.T;
-                gh.vx = 2 * vxf - src.vx; gh.vy = 2 * vyf - src.vy; gh.vz = 2 * vzf - src.vz;
+                S nx = S(face[f]), ny = S(face[F + f]), nz = S(face[2 * F + f]);
+                S p_face = S(A.value);
+                S rho_ref = src.rho, p_ref = src.p;
+                S sos = d_sqrt<S>(S(prm.gamma) * S(prm.R) * src.T);
+                S rho_face = src.rho + (p_face - p_ref) / sos / sos;
+                S vxf = src.vx + nx * (p_ref - p_face) / (rho_ref * sos);
+                S vyf = src.vy + ny * (p_ref - p_face) / (rho_ref * sos);
+                S vzf = src.vz + nz * (p_ref - p_face) / (rho_ref * sos);
+                gh.p = S(2.0) * p_face - src.p;
+                gh.rho = S(2.0) * rho_face - src.rho;
+                gh.T = gh.p / (gh.rho * S(prm.R));
+                gh.e = S(prm.Cv) * gh.T;
+                gh.vx = S(2.0) * vxf - src.vx; gh.vy = S(2.0) * vyf - src.vy; gh.vz = S(2.0) * vzf - src.vz;
                 break;
             }
         }
@@ -127,38 +132,38 @@ __device__ void apply_actions(const Action* acts, int n, State64& gh, const Stat
 // Fill ghost g from the state of its source cell: pre-reconstruction actions
 // into the primitive arrays, then the pre-viscous-gradient actions on top of
 // them into the viscous ghost arrays (p, T, vx, vy, vz).
-template <class P, class Gm>
-__device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const State64& src) {
+template <class P, class Gm, class S = double>
+__device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const StateT<S>& src) {
     const BoundDev& B = v.bounds[v.ghost_bound[g]];
     const Gm* face = (const Gm*)v.face;
     int f = v.ghost_face[g];
-    State64 gh = src;
-    apply_actions<Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm);
+    StateT<S> gh = src;
+    apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm);
     P* pr = (P*)v.prim;
     const int NT = v.NT, id = v.N + g;
     pr[id] = (P)gh.rho; pr[NT + id] = (P)gh.p; pr[2 * NT + id] = (P)gh.T; pr[3 * NT + id] = (P)gh.e;
     pr[4 * NT + id] = (P)gh.vx; pr[5 * NT + id] = (P)gh.vy; pr[6 * NT + id] = (P)gh.vz;
     if (prm.viscous) {
-        apply_actions<Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm);
+        apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm);
         P* vg = (P*)v.vghost;
         vg[g] = (P)gh.p; vg[v.G + g] = (P)gh.T; vg[2 * v.G + g] = (P)gh.vx;
         vg[3 * v.G + g] = (P)gh.vy; vg[4 * v.G + g] = (P)gh.vz;
     }
 }
 
-template <class P>
-__device__ State64 load_state64(const DevView& v, int c) {
+template <class P, class S>
+__device__ StateT<S> load_state(const DevView& v, int c) {
     const P* pr = (const P*)v.prim;
     const int NT = v.NT;
-    return State64{(double)pr[c], (double)pr[NT + c], (double)pr[2 * NT + c], (double)pr[3 * NT + c],
-                   (double)pr[4 * NT + c], (double)pr[5 * NT + c], (double)pr[6 * NT + c]};
+    return StateT<S>{S(pr[c]), S(pr[NT + c]), S(pr[2 * NT + c]), S(pr[3 * NT + c]),
+                     S(pr[4 * NT + c]), S(pr[5 * NT + c]), S(pr[6 * NT + c])};
 }
 
-template <class P, class Gm>
+template <class P, class Gm, class S = double>
 __global__ void __launch_bounds__(kBlock) k_ghost_fill(DevView v, FvParams prm) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= v.G) return;
-    fill_ghost<P, Gm>(v, prm, g, load_state64<P>(v, v.ghost_src[g]));
+    fill_ghost<P, Gm, S>(v, prm, g, load_state<P, S>(v, v.ghost_src[g]));
 }
 
 // ---------------------------------------------------------------------------
@@ -183,10 +188,12 @@ __global__ void __launch_bounds__(kBlock) k_recon(DevView v, FvParams prm, int r
     const bool lim = reconstruct && prm.limiter;
 
     R xi = (R)cc[i], yi = (R)cc[NT + i], zi = DIM == 3 ? (R)cc[2 * NT + i] : R(0.0);
-    R r11 = (R)rr[i], r12 = (R)rr[N + i], r22 = (R)rr[2 * N + i];
-    R r13 = R(0.0), r23 = R(0.0), r33 = R(0.0);
-    if (DIM == 3) { r13 = (R)rr[3 * N + i]; r23 = (R)rr[4 * N + i]; r33 = (R)rr[5 * N + i]; }
-    R beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+    R r11 = R(1.0), r12 = R(0.0), r22 = R(1.0), r13 = R(0.0), r23 = R(0.0), r33 = R(1.0), beta = R(0.0);
+    if (EXACT) {
+        r11 = (R)rr[i]; r12 = (R)rr[N + i]; r22 = (R)rr[2 * N + i];
+        if (DIM == 3) { r13 = (R)rr[3 * N + i]; r23 = (R)rr[4 * N + i]; r33 = (R)rr[5 * N + i]; }
+        beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+    }
 
     R ui[NV], gx[NV], gy[NV], gz[NV], umin[NV], umax[NV];
 #pragma unroll
@@ -204,17 +211,26 @@ __global__ void __launch_bounds__(kBlock) k_recon(DevView v, FvParams prm, int r
     }
 
     const int nf = v.nfaces[i];
+    const Gm* W = (const Gm*)v.lsqw;
+    const int MF = v.MF;
     for (int s = 0; s < nf; s++) {
         const int nb = v.cell_nbr[s * N + i];
-        R dx = (R)cc[nb] - xi, dy = (R)cc[NT + nb] - yi;
-        R dz = DIM == 3 ? (R)cc[2 * NT + nb] - zi : R(0.0);
-        R a1 = dx / (r11 * r11);
-        R a2 = R(1.0) / (r22 * r22) * (dy - r12 / r11 * dx);
-        R a3 = R(0.0);
-        if (DIM == 3) a3 = R(1.0) / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx);
-        R w1 = a1 - r12 / r11 * a2 + beta * a3;
-        R w2 = a2 - r23 / r22 * a3;
-        R w3 = a3;
+        R w1, w2, w3;
+        if (!EXACT) {  // weights precomputed on the host from the same formulas
+            w1 = (R)W[s * N + i];
+            w2 = (R)W[(MF + s) * N + i];
+            w3 = DIM == 3 ? (R)W[(2 * MF + s) * N + i] : R(0.0);
+        } else {
+            R dx = (R)cc[nb] - xi, dy = (R)cc[NT + nb] - yi;
+            R dz = DIM == 3 ? (R)cc[2 * NT + nb] - zi : R(0.0);
+            R a1 = dx / (r11 * r11);
+            R a2 = R(1.0) / (r22 * r22) * (dy - r12 / r11 * dx);
+            R a3 = R(0.0);
+            if (DIM == 3) a3 = R(1.0) / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx);
+            w1 = a1 - r12 / r11 * a2 + beta * a3;
+            w2 = a2 - r23 / r22 * a3;
+            w3 = a3;
+        }
         if (reconstruct) {
 #pragma unroll
             for (int q = 0; q < NV; q++) {
@@ -245,22 +261,48 @@ __global__ void __launch_bounds__(kBlock) k_recon(DevView v, FvParams prm, int r
 #pragma unroll
         for (int q = 0; q < NV; q++) { phi[q] = R(1.0); code[q] = 0u; }
         if (lim) {
-            const R eps = (R)prm.eps;
-            for (int s = 0; s < nf; s++) {
-                const int f = v.cell_face[s * N + i];
-                R dx = (R)fcen[f] - xi, dy = (R)fcen[F + f] - yi;
-                R dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+            const R eps = par<R>(prm.eps, prm.feps);
+            if (EXACT || v.branches) {
+                // face by face, as limiter.cpp:141-156, recording the branch taken
+                for (int s = 0; s < nf; s++) {
+                    const int f = v.cell_face[s * N + i];
+                    R dx = (R)fcen[f] - xi, dy = (R)fcen[F + f] - yi;
+                    R dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+#pragma unroll
+                    for (int q = 0; q < NV; q++) {
+                        R d2 = DIM == 3 ? gx[q] * dx + gy[q] * dy + gz[q] * dz : gx[q] * dx + gy[q] * dy;
+                        int sg = (d2 > R(0.0)) - (d2 < R(0.0));
+                        d2 = (R)sg * (d_abs(d2) + eps);
+                        if (sg != 0) {
+                            R ratio = sg > 0 ? (umax[q] - ui[q]) / d2 : (umin[q] - ui[q]) / d2;
+                            code[q] |= (unsigned)(sg > 0 ? 1 : 2) << (2 * s);
+                            if (!(phi[q] < ratio)) code[q] = (code[q] & 0xFFFFu) | ((unsigned)(s + 1) << 16);
+                            phi[q] = d_min(phi[q], ratio);
+                        }
+                    }
+                }
+            } else {
+                // Same value with two divisions per variable: (U_max - U_i) / (d + eps)
+                // decreases with d, and IEEE division and addition round monotonically,
+                // so the minimum over faces is taken at the largest projection of each sign.
+                R tpos[NV], tneg[NV];
+#pragma unroll
+                for (int q = 0; q < NV; q++) { tpos[q] = R(0.0); tneg[q] = R(0.0); }
+                for (int s = 0; s < nf; s++) {
+                    const int f = v.cell_face[s * N + i];
+                    R dx = (R)fcen[f] - xi, dy = (R)fcen[F + f] - yi;
+                    R dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+#pragma unroll
+                    for (int q = 0; q < NV; q++) {
+                        R d2 = DIM == 3 ? gx[q] * dx + gy[q] * dy + gz[q] * dz : gx[q] * dx + gy[q] * dy;
+                        tpos[q] = d_max(tpos[q], d2);
+                        tneg[q] = d_min(tneg[q], d2);
+                    }
+                }
 #pragma unroll
                 for (int q = 0; q < NV; q++) {
-                    R d2 = DIM == 3 ? gx[q] * dx + gy[q] * dy + gz[q] * dz : gx[q] * dx + gy[q] * dy;
-                    int sg = (d2 > R(0.0)) - (d2 < R(0.0));
-                    d2 = (R)sg * (d_abs(d2) + eps);
-                    if (sg != 0) {
-                        R ratio = sg > 0 ? (umax[q] - ui[q]) / d2 : (umin[q] - ui[q]) / d2;
-                        code[q] |= (unsigned)(sg > 0 ? 1 : 2) << (2 * s);
-                        if (!(phi[q] < ratio)) code[q] = (code[q] & 0xFFFFu) | ((unsigned)(s + 1) << 16);
-                        phi[q] = d_min(phi[q], ratio);
-                    }
+                    if (tpos[q] > R(0.0)) phi[q] = d_min(phi[q], (umax[q] - ui[q]) / (tpos[q] + eps));
+                    if (tneg[q] < R(0.0)) phi[q] = d_min(phi[q], (umin[q] - ui[q]) / (tneg[q] - eps));
                 }
             }
             P* pout = (P*)v.phi;
@@ -360,7 +402,7 @@ __global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int re
     switch (prm.flux) {
         case kHanel: flux_hanel<R, DIM>(S[0], S[1], gm, Fl); break;
         case kAusmdv: flux_ausmdv<R, DIM>(S[0], S[1], gm, Fl); break;
-        case kLdfss2: flux_ldfss2<R, DIM>(S[0], S[1], gm, (R)prm.delta, Fl); break;
+        case kLdfss2: flux_ldfss2<R, DIM, EXACT>(S[0], S[1], gm, par<R>(prm.delta, prm.fdelta), Fl); break;
         default: flux_rusanov<R, DIM>(S[0], S[1], gm, Fl); break;
     }
     // transform_to_global (convective_flux.cpp:145-177)
@@ -421,8 +463,9 @@ __global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int re
         R vx = R(0.5) * (vstate(l, 2) + vstate(r, 2));
         R vy = R(0.5) * (vstate(l, 3) + vstate(r, 3));
         R vz = DIM == 3 ? R(0.5) * (vstate(l, 4) + vstate(r, 4)) : R(0.0);
-        R mu = sutherland<R, EXACT>(T, (R)prm.mu0, (R)prm.T0, (R)prm.Ts);
-        R k = gm.Cp * mu / (R)prm.Pr;
+        R mu = sutherland<R, EXACT>(T, par<R>(prm.mu0, prm.fmu0), par<R>(prm.T0, prm.fT0),
+                                    par<R>(prm.Ts, prm.fTs));
+        R k = gm.Cp * mu / par<R>(prm.Pr, prm.fPr);
         R lambda = R(-2.0 / 3.0) * mu;
         const R *gT = g[0], *gx = g[1], *gy = g[2], *gz = g[3];
         R bulk = lambda * (gx[0] + gy[1] + gz[2]);
@@ -440,9 +483,9 @@ __global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int re
         if (DIM == 3) mz -= nx * txz + ny * tyz + nz * tzz;
         en -= nx * thx + ny * thy + nz * thz;
         // time-step signal (estimate_dt, finite_volume.cpp:167-175), in double
-        double mud = (double)mu, kd = (double)k;
+        double mud = real_of(mu), kd = real_of(k);
         double Prf = mud * prm.Cp / kd;
-        v.vsig[f] = (prm.gamma / (double)rho) * (mud / Prf);
+        v.vsig[f] = (prm.gamma / real_of(rho)) * (mud / Prf);
     }
     P* fo = (P*)v.flux;
     fo[f] = (P)Fl[0];
@@ -458,16 +501,27 @@ __global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int re
 // update, conserved->primitive inversion (primative_conserved_conversion.cpp:4-23)
 // and the ghost cells fed by this cell.
 // ---------------------------------------------------------------------------
-template <class P, class Gm, int DIM>
+template <class P, class Gm, int DIM, bool EXACT>
 __device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, const double* u) {
-    // conserved_to_primatives in double
-    double rho = u[0];
-    double vx = u[1] / rho;
-    double vy = u[2] / rho;
-    double vz = DIM == 3 ? u[3] / rho : 0.0;
-    double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
-    double e = u[DIM + 1] / rho - ke;
-    double T = e / prm.Cv;
+    // conserved_to_primatives in double (primative_conserved_conversion.cpp:4-23); the fast
+    // paths replace the divisions by one reciprocal (the FP64 pipe is GB300's scarcest unit)
+    double rho = u[0], vx, vy, vz, e, T;
+    if (EXACT) {
+        vx = u[1] / rho;
+        vy = u[2] / rho;
+        vz = DIM == 3 ? u[3] / rho : 0.0;
+        double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
+        e = u[DIM + 1] / rho - ke;
+        T = e / prm.Cv;
+    } else {
+        const double ir = 1.0 / rho;
+        vx = u[1] * ir;
+        vy = u[2] * ir;
+        vz = DIM == 3 ? u[3] * ir : 0.0;
+        double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
+        e = u[DIM + 1] * ir - ke;
+        T = e * prm.inv_Cv;
+    }
     double p = rho * prm.R * T;
     P* pr = (P*)v.prim;
     const int NT = v.NT;
@@ -483,7 +537,17 @@ IBISGB_HD void count_bad(StepCtl* ctl, const State64& s) {
     if (s.T < 0.0 || s.rho < 0.0 || isnan(s.rho) || isinf(s.rho)) atomicAdd(&ctl->bad_cells, 1ull);
 }
 
-template <class P, class Gm, int DIM>
+// Error-free transformations for the float accumulation of the mixed build
+// (Knuth's TwoSum, and the product error through an FMA).
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
+    float s = __fadd_rn(hi, p);
+    float bb = __fsub_rn(s, hi);
+    float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
+template <class P, class Gm, int DIM, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int mode, int stage,
                                                    double* out_rm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -492,22 +556,53 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
     const int N = v.N, F = v.F;
     const Gm* area = (const Gm*)v.face + 12 * F;
     const P* fl = (const P*)v.flux;
-    double acc[NC];
-#pragma unroll
-    for (int q = 0; q < NC; q++) acc[q] = 0.0;
     const int nf = v.nfaces[i];
-    for (int s = 0; s < nf; s++) {
-        const int f = v.cell_face[s * N + i];
-        const double a = -(double)area[f] * (double)v.outsign[s * N + i];
-#pragma unroll
-        for (int q = 0; q < NC; q++) acc[q] += (double)fl[q * F + f] * a;
-    }
-    const double vol = v.vol[i];
     double ks[NC];
+    if (sizeof(P) == sizeof(float)) {
+        // Mixed: each face term (float flux x area) is summed as an unevaluated
+        // float pair (hi + lo, ~48-bit significand: the exact products' rounding
+        // errors and every addition error are kept), then formed in double once.
+        float hi[NC], lo[NC];
+#pragma unroll
+        for (int q = 0; q < NC; q++) { hi[q] = 0.f; lo[q] = 0.f; }
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const float a = -(float)area[f] * (float)v.outsign[s * N + i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                const float x = (float)fl[q * F + f];
+                const float pr = __fmul_rn(x, a);
+                const float pe = __fmaf_rn(x, a, -pr);  // exact error of the product
+                two_sum_acc(hi[q], lo[q], pr);
+                lo[q] = __fadd_rn(lo[q], pe);
+            }
+        }
+        const double iv = v.inv_vol[i];
+#pragma unroll
+        for (int q = 0; q < NC; q++) ks[q] = ((double)hi[q] + (double)lo[q]) * iv;
+    } else {
+        double acc[NC];
+#pragma unroll
+        for (int q = 0; q < NC; q++) acc[q] = 0.0;
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const double a = -(double)area[f] * (double)v.outsign[s * N + i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) acc[q] += (double)fl[q * F + f] * a;
+        }
+        if (EXACT) {
+            const double vol = v.vol[i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) ks[q] = acc[q] / vol;
+        } else {
+            const double iv = v.inv_vol[i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) ks[q] = acc[q] * iv;
+        }
+    }
     double* kk = v.k + (size_t)stage * NC * N;
 #pragma unroll
     for (int q = 0; q < NC; q++) {
-        ks[q] = acc[q] / vol;
         kk[q * N + i] = ks[q];
         if (out_rm) out_rm[(size_t)i * NC + q] = ks[q];
     }
@@ -531,7 +626,7 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
                 u[q] += kj * c;
             }
         }
-        commit_state<P, Gm, DIM>(v, prm, i, u);
+        commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
     } else {
         // solution update (runge_kutta.cpp:185-193)
         for (int j = 0; j < ctl->stages; j++) {
@@ -544,13 +639,13 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
         }
 #pragma unroll
         for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
-        count_bad(v.ctl, commit_state<P, Gm, DIM>(v, prm, i, u));
+        count_bad(v.ctl, commit_state<P, Gm, DIM, EXACT>(v, prm, i, u));
     }
 }
 
 // Solution update from stored stage derivatives (single-stage tableaus, where
 // dt is only known after the one residual evaluation).
-template <class P, class Gm, int DIM>
+template <class P, class Gm, int DIM, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_finalize(DevView v, FvParams prm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N || v.ctl->halt) return;
@@ -566,11 +661,11 @@ __global__ void __launch_bounds__(kBlock) k_finalize(DevView v, FvParams prm) {
     }
 #pragma unroll
     for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
-    count_bad(v.ctl, commit_state<P, Gm, DIM>(v, prm, i, u));
+    count_bad(v.ctl, commit_state<P, Gm, DIM, EXACT>(v, prm, i, u));
 }
 
 // State of stage `stage` from U and k_0..k_{stage-1} (after dt is known), then primitives and ghosts.
-template <class P, class Gm, int DIM>
+template <class P, class Gm, int DIM, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_combine(DevView v, FvParams prm, int stage) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N || v.ctl->halt) return;
@@ -586,10 +681,10 @@ __global__ void __launch_bounds__(kBlock) k_combine(DevView v, FvParams prm, int
 #pragma unroll
         for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
     }
-    commit_state<P, Gm, DIM>(v, prm, i, u);
+    commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
 }
 
-template <class P, class Gm, int DIM>
+template <class P, class Gm, int DIM, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_prims_from_U(DevView v, FvParams prm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
@@ -597,43 +692,49 @@ __global__ void __launch_bounds__(kBlock) k_prims_from_U(DevView v, FvParams prm
     double u[NC];
 #pragma unroll
     for (int q = 0; q < NC; q++) u[q] = v.U[q * v.N + i];
-    commit_state<P, Gm, DIM>(v, prm, i, u);
+    commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
 }
 
 // Local CFL time step of each valid cell, min-reduced into ctl->dt_bits
-// (FiniteVolume::estimate_dt, finite_volume.cpp:130-184).
-template <class P, class Gm, int DIM, bool FROM_U>
+// (FiniteVolume::estimate_dt, finite_volume.cpp:130-184).  The mixed build
+// evaluates the inviscid signal in float from its float state.
+template <class P, class Gm, int DIM>
 __global__ void __launch_bounds__(kBlock) k_local_dt(DevView v, FvParams prm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double local = 1.0e308 * 10.0;
     if (i < v.N) {
         const int N = v.N, F = v.F, NT = v.NT;
         const Gm* fg = (const Gm*)v.face;
-        double vx, vy, vz, T;
-        if (FROM_U) {
-            double rho = v.U[i];
-            vx = v.U[N + i] / rho;
-            vy = v.U[2 * N + i] / rho;
-            vz = DIM == 3 ? v.U[3 * N + i] / rho : 0.0;
-            double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
-            T = (v.U[(DIM + 1) * N + i] / rho - ke) / prm.Cv;
-        } else {
-            const P* pr = (const P*)v.prim;
-            vx = (double)pr[4 * NT + i]; vy = (double)pr[5 * NT + i]; vz = (double)pr[6 * NT + i];
-            T = (double)pr[2 * NT + i];
-        }
-        const double a = sqrt(prm.gamma * prm.R * T);
-        const double vol = v.vol[i];
-        double src = 0.0, srv = 0.0;
+        const P* pr = (const P*)v.prim;
         const int nf = v.nfaces[i];
-        for (int s = 0; s < nf; s++) {
-            const int f = v.cell_face[s * N + i];
-            const double A = (double)fg[12 * F + f];
-            const double dot = vx * (double)fg[f] + vy * (double)fg[F + f] + vz * (double)fg[2 * F + f];
-            src += (fabs(dot) + a) * A;
-            if (prm.viscous) {
-                double tmp = v.vsig[f] * A * A;
-                srv += tmp / vol;
+        double src = 0.0, srv = 0.0;
+        const double vol = v.vol[i];
+        if (sizeof(P) == sizeof(float)) {
+            const float vx = (float)pr[4 * NT + i], vy = (float)pr[5 * NT + i];
+            const float vz = DIM == 3 ? (float)pr[6 * NT + i] : 0.f;
+            const float a = sqrtf(prm.fgR * (float)pr[2 * NT + i]);
+            float sf = 0.f;
+            for (int s = 0; s < nf; s++) {
+                const int f = v.cell_face[s * N + i];
+                const float A = (float)fg[12 * F + f];
+                float dot = vx * (float)fg[f] + vy * (float)fg[F + f];
+                if (DIM == 3) dot += vz * (float)fg[2 * F + f];
+                sf += (fabsf(dot) + a) * A;
+                if (prm.viscous) srv += v.vsig[f] * (double)A * (double)A / vol;
+            }
+            src = (double)sf;
+        } else {
+            const double vx = (double)pr[4 * NT + i], vy = (double)pr[5 * NT + i], vz = (double)pr[6 * NT + i];
+            const double a = sqrt(prm.gamma * prm.R * (double)pr[2 * NT + i]);
+            for (int s = 0; s < nf; s++) {
+                const int f = v.cell_face[s * N + i];
+                const double A = (double)fg[12 * F + f];
+                const double dot = vx * (double)fg[f] + vy * (double)fg[F + f] + vz * (double)fg[2 * F + f];
+                src += (fabs(dot) + a) * A;
+                if (prm.viscous) {
+                    double tmp = v.vsig[f] * A * A;
+                    srv += tmp / vol;
+                }
             }
         }
         local = vol / (src + prm.signal_factor * srv);
@@ -670,25 +771,24 @@ struct Launch {
     }
     static void update(const DevView& v, const FvParams& p, int mode, int stage, double* out,
                        cudaStream_t s) {
-        if (v.dim == 3) k_update<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
-        else k_update<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
+        if (v.dim == 3) k_update<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
+        else k_update<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
     }
     static void combine(const DevView& v, const FvParams& p, int stage, cudaStream_t s) {
-        if (v.dim == 3) k_combine<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
-        else k_combine<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
+        if (v.dim == 3) k_combine<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
+        else k_combine<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
     }
     static void prims_from_U(const DevView& v, const FvParams& p, cudaStream_t s) {
-        if (v.dim == 3) k_prims_from_U<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
-        else k_prims_from_U<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        if (v.dim == 3) k_prims_from_U<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        else k_prims_from_U<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
     }
     static void local_dt(const DevView& v, const FvParams& p, cudaStream_t s) {
-        constexpr bool FROM_U = sizeof(P) < sizeof(double);
-        if (v.dim == 3) k_local_dt<P, Gm, 3, FROM_U><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
-        else k_local_dt<P, Gm, 2, FROM_U><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        if (v.dim == 3) k_local_dt<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        else k_local_dt<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
     }
     static void finalize(const DevView& v, const FvParams& p, cudaStream_t s) {
-        if (v.dim == 3) k_finalize<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
-        else k_finalize<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        if (v.dim == 3) k_finalize<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
+        else k_finalize<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
     }
     static KernelOps ops() {
         return KernelOps{&ghost_fill, &recon, &face_flux, &update, &combine, &prims_from_U, &local_dt,

@@ -485,6 +485,27 @@ void build_mesh(const GridInput& in, const std::vector<BoundarySpec>& bounds_in,
             rr[0] = r11; rr[1] = r12; rr[2] = r22;
             if (m.dim == 3) { rr[3] = r13; rr[4] = r23; rr[5] = r33; }
         }
+        // the weights WLSGradient::compute_gradients applies to each neighbour
+        // difference (gradient.h:89-107), stored per neighbour slot
+        m.lsqw.assign(3 * (size_t)MF * N, 0.0);
+#pragma omp parallel for schedule(static)
+        for (int64_t c = 0; c < N; c++) {
+            const double* rr = &m.r[c * 6];
+            double r11 = rr[0], r12 = rr[1], r22 = rr[2], r13 = 0.0, r23 = 0.0, r33 = 0.0;
+            if (m.dim == 3) { r13 = rr[3]; r23 = rr[4]; r33 = rr[5]; }
+            double beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+            for (int k = 0; k < m.nfaces[c]; k++) {
+                int64_t nb = m.cell_nbr[c * MF + k];
+                double dx = m.ccx[nb] - m.ccx[c], dy = m.ccy[nb] - m.ccy[c], dz = m.ccz[nb] - m.ccz[c];
+                double a1 = dx / (r11 * r11);
+                double a2 = 1.0 / (r22 * r22) * (dy - r12 / r11 * dx);
+                double a3 = 0.0;
+                if (m.dim == 3) a3 = 1.0 / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx);
+                m.lsqw[(0 * (size_t)MF + k) * N + c] = a1 - r12 / r11 * a2 + beta * a3;
+                m.lsqw[(1 * (size_t)MF + k) * N + c] = a2 - r23 / r22 * a3;
+                m.lsqw[(2 * (size_t)MF + k) * N + c] = a3;
+            }
+        }
     }
 }
 

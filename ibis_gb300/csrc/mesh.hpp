@@ -75,6 +75,7 @@ struct Mesh {
     std::vector<int8_t> outsign;
     std::vector<double> ccx, ccy, ccz, volume;  // N+G entries (ghost volume 0)
     std::vector<double> r;                      // 6 per valid cell: r11 r12 r22 r13 r23 r33
+    std::vector<double> lsqw;                   // [3][MF][N] gradient weights of each neighbour slot
 
     // boundaries in sorted tag order
     std::vector<BoundarySpec> bounds;

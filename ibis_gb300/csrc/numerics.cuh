@@ -32,12 +32,18 @@ template <> IBISGB_HD float d_copysign<float>(float m, float s) { return copysig
 template <class R> IBISGB_HD R d_min(R a, R b) { return (b < a) ? b : a; }
 template <class R> IBISGB_HD R d_max(R a, R b) { return (a < b) ? b : a; }
 
+// A parameter in the arithmetic of the kernel: the double value, or its float
+// copy prepared on the host for float kernels.
+template <class R> IBISGB_HD R par(double d, float) { return R(d); }
+template <> IBISGB_HD float par<float>(double, float f) { return f; }
+
 // Gas constants in the arithmetic of the kernel.
 template <class R>
 struct Gas {
     R R_, Cv, Cp, gamma, gR;  // gR = gamma * R, as in speed_of_sound_ (gas_model.h:27-30)
     IBISGB_HD explicit Gas(const FvParams& p)
-        : R_((R)p.R), Cv((R)p.Cv), Cp((R)p.Cp), gamma((R)p.gamma), gR((R)p.gamma * (R)p.R) {}
+        : R_(par<R>(p.R, p.fR)), Cv(par<R>(p.Cv, p.fCv)), Cp(par<R>(p.Cp, p.fCp)),
+          gamma(par<R>(p.gamma, p.fgamma)), gR(par<R>(p.gamma * p.R, p.fgR)) {}
     IBISGB_HD R sound(R T) const { return d_sqrt<R>(gR * T); }
 };
 
@@ -151,8 +157,9 @@ IBISGB_HD void flux_ausmdv(const FaceSide<R>& L, const FaceSide<R>& Rt, const Ga
     }
 }
 
-// LDFSS(2) flux (flux_calculators/ldfss2.cpp:9-90)
-template <class R, int DIM>
+// LDFSS(2) flux (flux_calculators/ldfss2.cpp:9-90); EXACT keeps the
+// reference's pow(x, 2.0), the fast paths square instead.
+template <class R, int DIM, bool EXACT>
 IBISGB_HD void flux_ldfss2(const FaceSide<R>& L, const FaceSide<R>& Rt, const Gas<R>& gm, R delta,
                            R* F) {
     R rL = L.r, pL = L.p, pLrL = pL / rL, uL = L.u, vL = L.v, wL = L.w;
@@ -175,7 +182,8 @@ IBISGB_HD void flux_ldfss2(const FaceSide<R>& L, const FaceSide<R>& Rt, const Ga
     R PR = R(0.25) * (MR - R(1.0)) * (MR - R(1.0)) * (R(2.0) + MR);
     R DL = alphaL * (R(1.0) + betaL) - betaL * PL;
     R DR = alphaR * (R(1.0) + betaR) - betaR * PR;
-    R Mhalf = R(0.25) * betaL * betaR * d_pow(d_sqrt(R(0.5) * (ML * ML + MR * MR)) - R(1.0), R(2.0));
+    R mb = d_sqrt(R(0.5) * (ML * ML + MR * MR)) - R(1.0);
+    R Mhalf = R(0.25) * betaL * betaR * (EXACT ? d_pow(mb, R(2.0)) : mb * mb);
     R MhalfL = Mhalf * (R(1.0) - ((pL - pR) / (pL + pR) + delta * (d_abs(pL - pR) / pL)));
     R MhalfR = Mhalf * (R(1.0) + ((pL - pR) / (pL + pR) - delta * (d_abs(pL - pR) / pR)));
     R CL = alphaL * (R(1.0) + betaL) * ML - betaL * MpL - MhalfL;
