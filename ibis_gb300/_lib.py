@@ -31,6 +31,13 @@ class Sizes(C.Structure):
                 ("num_boundaries", C.c_int32)]
 
 
+class NewtonStatus(C.Structure):
+    _fields_ = [("relative_residual", C.c_double), ("residual_norms", C.c_double * 6),
+                ("gmres_iterations", C.c_int32), ("gmres_converged", C.c_int32),
+                ("gmres_residual", C.c_double), ("dt_star", C.c_double), ("cfl", C.c_double),
+                ("step", C.c_int64)]
+
+
 class RkStatus(C.Structure):
     _fields_ = [("t", C.c_double), ("dt", C.c_double), ("stable_dt", C.c_double),
                 ("steps", C.c_int64), ("bad_cells", C.c_int64), ("device_ms", C.c_double)]
@@ -77,6 +84,10 @@ def load(build_if_missing: bool = True):
     L.ibisgb_get_stream.argtypes = [_P, C.POINTER(_P)]
     L.ibisgb_kernel_times.argtypes = [_P, C.c_int32, C.c_int32, _P]
     L.ibisgb_l2_norms_noalloc.argtypes = [_P, C.c_int64, C.c_int32, _P, _P]
+    L.ibisgb_jvp.argtypes = [_P, _P, _P, C.c_double, C.c_int32]
+    L.ibisgb_jvp_device.argtypes = [_P, _P, _P, C.c_double, C.c_int32, _P]
+    L.ibisgb_steady_initialise.argtypes = [_P, C.c_int32]
+    L.ibisgb_newton_step.argtypes = [_P, C.c_int32, C.POINTER(NewtonStatus)]
     _lib = L
     return L
 

@@ -36,6 +36,7 @@ UNITS = {
     "kernels_mixed.cu": "nvcc-fast",
     "kernels_exact.cu": "nvcc-nofma",
     "noalloc.cu": "nvcc",
+    "kernels_tangent.cu": "nvcc-nofma",
 }
 
 

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <memory>
 #include <stdexcept>
@@ -111,6 +112,26 @@ struct ibisgb_ctx {
     Mesh mesh;
     std::vector<BoundDev> bounds_host;
 
+    // steady-state / JFNK settings (SteadyState ctor steady_state.cpp:176-221, Jfnk jfnk.cpp:7-23)
+    struct Steady {
+        bool configured = false;
+        int max_steps = 1000;
+        double tolerance = 1e-5;
+        bool fgmres = false;
+        int max_iters = 50, max_prec_iters = 5;
+        double tol = 1e-2, prec_tol = 1e-1;
+        int cfl_kind = 0;  // 0 constant, 1 linear_interpolate(step), 2 residual_based
+        double cfl = 0.5;
+        std::vector<double> cfl_t, cfl_v;
+        double rb_threshold = 0.1, rb_power = 0.8, rb_start = 1.0, rb_max = 1e8;
+        double rb_prev_cfl = 1.0, rb_prev_res = 1.0;
+        double norms[6] = {0, 0, 0, 0, 0, 0}, initial[6] = {0, 0, 0, 0, 0, 0};
+        int64_t step = 0;
+        bool initialised = false;
+    } steady;
+    StateBufs sdual;        // dual-number state of the tangent (double geometry from s64)
+    DBuf rhs, dU, kv, kw, kr0, kz, kH, kpart, kscal;  // Krylov storage
+
     // Runge-Kutta settings (RungeKutta ctor, runge_kutta.cpp:21-80)
     bool rk_configured = false;
     StepCtl ctl_host{};
@@ -195,6 +216,7 @@ struct ibisgb_ctx {
             prm.fTs = (float)prm.Ts; prm.fPr = (float)prm.Pr; prm.inv_Cv = 1.0 / prm.Cv;
             const Json& solver = config.at("solver");
             if (solver.at("name").as_string() == "runge_kutta") parse_rk(solver);
+            if (solver.at("name").as_string() == "steady_state") parse_steady(solver);
         } catch (const ConfigError&) {
             throw;
         } catch (const std::exception& e) {
@@ -230,6 +252,49 @@ struct ibisgb_ctx {
         c.plot_frequency = sc.at("plot_frequency").as_double();
         dt_init = sc.at("dt_init").as_double();
         rk_configured = true;
+    }
+
+    void parse_steady(const Json& sc) {
+        Steady& st = steady;
+        st.max_steps = (int)sc.at("max_steps").as_int();
+        st.tolerance = sc.at("tolerance").as_double();
+        const Json& ls = sc.at("linear_solver");  // make_linear_solver, gmres.cpp:305-318
+        std::string lt = ls.at("type").as_string();
+        if (lt == "gmres") {
+            st.max_iters = (int)ls.at("max_iters").as_int();
+            st.tol = ls.at("tol").as_double();
+        } else if (lt == "fgmres") {
+            st.fgmres = true;
+            st.max_iters = (int)ls.at("max_iters").as_int();
+            st.tol = ls.at("tolerance").as_double();
+            st.max_prec_iters = (int)ls.at("max_preconditioner_iters").as_int();
+            st.prec_tol = ls.at("preconditioner_tolerance").as_double();
+        } else {
+            throw ConfigError("Unknown linear solver " + lt);
+        }
+        const Json& cfl = sc.at("cfl");  // make_cfl_schedule, cfl.cpp:157-169
+        if (cfl.is_number()) {
+            st.cfl = cfl.as_double();
+        } else {
+            std::string ct = cfl.at("type").as_string();
+            if (ct == "constant") {
+                st.cfl = cfl.at("value").as_double();
+            } else if (ct == "linear_interpolate") {
+                st.cfl_kind = 1;
+                st.cfl_t = cfl.at("times").as_doubles();
+                st.cfl_v = cfl.at("cfls").as_doubles();
+            } else if (ct == "residual_based") {
+                st.cfl_kind = 2;
+                st.rb_threshold = cfl.at("growth_threshold").as_double();
+                st.rb_power = cfl.at("power").as_double();
+                st.rb_start = cfl.at("start_cfl").as_double();
+                st.rb_max = cfl.at("max_cfl").as_double();
+                st.rb_prev_cfl = st.rb_start;
+            } else {
+                throw ConfigError("Unknown CFL schedule " + ct);
+            }
+        }
+        st.configured = true;
     }
 
     std::vector<BoundarySpec> boundary_specs() {
@@ -413,10 +478,11 @@ struct ibisgb_ctx {
         s.prims_current = true;
     }
 
+    // prec < 0: the conserved state changed outside a kernel build (no prims current)
     void state_changed(int prec) {
         ic_prims.clear();
-        s64.prims_current = !is_mixed(prec);
-        s32.prims_current = is_mixed(prec);
+        s64.prims_current = prec >= 0 && !is_mixed(prec);
+        s32.prims_current = prec >= 0 && is_mixed(prec);
     }
 
     void set_primitives(const double* T, const double* p, const double* vx, const double* vy, const double* vz) {
@@ -553,6 +619,254 @@ struct ibisgb_ctx {
             st->device_ms = ms;
         }
         if (c.bad_cells > 0) throw std::runtime_error("bad cells");
+    }
+
+    // ----- tangent (SteadyStateLinearisation::matrix_vector_product) ---------
+    DevView tangent_view() {
+        ensure_device();
+        upload_geometry<double>(s64);
+        if (!sdual.geometry) {
+            const int64_t N = mesh.N, NT = mesh.NT(), F = mesh.F;
+            const size_t D = 2 * sizeof(double);
+            sdual.prim.alloc(D * 7 * NT);
+            sdual.vghost.alloc(D * 5 * std::max<int64_t>(mesh.G, 1));
+            sdual.grad.alloc(D * 15 * N);
+            sdual.phi.alloc(D * 5 * N);
+            sdual.vgrad.alloc(D * 12 * N);
+            sdual.flux.alloc(D * nc() * F);
+            sdual.geometry = true;
+        }
+        DevView v = view(IBISGB_F64);
+        v.prim = sdual.prim.p; v.vghost = sdual.vghost.p; v.grad = sdual.grad.p; v.phi = sdual.phi.p;
+        v.vgrad = sdual.vgrad.p; v.flux = sdual.flux.p;
+        return v;
+    }
+
+    // out = inv_dt * v - dR/dU v on device rows (N x nc)
+    void jvp(const double* v_dev, double* out_dev, double inv_dt, bool reconstruct) {
+        if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
+        DevView v = tangent_view();
+        launch_tangent(v, prm, v_dev, inv_dt, reconstruct && prm.order == 2, out_dev, stream);
+        CUDA_OK(cudaGetLastError());
+    }
+
+    size_t nvars() const { return (size_t)mesh.N * nc(); }
+
+    void ensure_krylov(int m) {
+        const size_t n = nvars();
+        rhs.alloc(sizeof(double) * n);
+        dU.alloc(sizeof(double) * n);
+        kw.alloc(sizeof(double) * n);
+        kr0.alloc(sizeof(double) * n);
+        kv.alloc(sizeof(double) * n * (m + 1));
+        kz.alloc(sizeof(double) * n * (m + 1));
+        kH.alloc(sizeof(double) * (m + 1) * (m + 1));
+        kpart.alloc(sizeof(double) * dot_scratch_doubles());
+        kscal.alloc(sizeof(double) * (2 * m + 8));
+    }
+
+    struct GmresOut {
+        bool success = false;
+        int iters = 0;
+        double residual = -1.0;
+    };
+
+    // Un-restarted GMRES with modified Gram-Schmidt (Gmres::solve, gmres.cpp:119-182).
+    // A(x, out) applies the operator on device rows; the Krylov basis lives in V
+    // (m+1 columns of n), Hessenberg entries are produced on the device and
+    // copied once per Arnoldi step for the Givens rotations on the host.
+    template <class Op>
+    GmresOut gmres(Op&& A, const double* b, double* x, int m_cfg, double tol, double* V, double* Z,
+                   const std::function<void(const double*, double*)>* precond) {
+        const size_t n = nvars();
+        const int m = (int)std::min<size_t>((size_t)m_cfg, n);
+        double* w = kw.as<double>();
+        double* r0 = kr0.as<double>();
+        double* H = kH.as<double>();  // column-major (m+1) per column
+        double* scal = kscal.as<double>();
+        double* part = kpart.as<double>();
+        GmresOut res;
+        A(x, w);  // compute_r0_
+        launch_sub(r0, b, w, (long long)n, stream);
+        launch_dot(r0, r0, (long long)n, part, scal, true, stream);
+        double beta = 0.0;
+        CUDA_OK(cudaMemcpyAsync(&beta, scal, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+        if (beta < tol) {
+            res.success = true;
+            res.residual = beta;
+            return res;
+        }
+        launch_scale_inv(V, r0, (long long)n, scal, stream);
+        std::vector<double> h((m + 1) * (m + 1), 0.0), cs(m + 1, 0.0), sn(m + 1, 0.0), g(m + 2, 0.0);
+        g[0] = beta;
+        res.residual = 1.0;
+        for (int j = 0; j < m; j++) {
+            double* vj = V + (size_t)j * n;
+            const double* col = vj;
+            if (precond) {  // FGmres::solve: z_j = P^-1 v_j (gmres.cpp:257-264)
+                (*precond)(vj, Z + (size_t)j * n);
+                col = Z + (size_t)j * n;
+            }
+            A(col, w);
+            double* Hj = H + (size_t)j * (m + 1);
+            for (int i = 0; i <= j; i++) {
+                launch_dot(w, V + (size_t)i * n, (long long)n, part, Hj + i, false, stream);
+                launch_axpy_neg(w, V + (size_t)i * n, (long long)n, Hj + i, stream);
+            }
+            launch_dot(w, w, (long long)n, part, Hj + j + 1, true, stream);
+            launch_scale_inv(V + (size_t)(j + 1) * n, w, (long long)n, Hj + j + 1, stream);
+            CUDA_OK(cudaGetLastError());
+            CUDA_OK(cudaMemcpyAsync(&h[(size_t)j * (m + 1)], Hj, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, stream));
+            CUDA_OK(cudaStreamSynchronize(stream));
+            double* hc = &h[(size_t)j * (m + 1)];
+            // rotate the new column into upper-triangular form (apply_rotations_to_hessenberg_, gmres.cpp:22-74)
+            for (int i = 0; i < j; i++) {
+                double t = cs[i] * hc[i] + sn[i] * hc[i + 1];
+                hc[i + 1] = -sn[i] * hc[i] + cs[i] * hc[i + 1];
+                hc[i] = t;
+            }
+            double denom = std::sqrt(hc[j] * hc[j] + hc[j + 1] * hc[j + 1]);
+            sn[j] = hc[j + 1] / denom;
+            cs[j] = hc[j] / denom;
+            hc[j] = cs[j] * hc[j] + sn[j] * hc[j + 1];
+            hc[j + 1] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            double r = std::fabs(g[j + 1]);
+            res.residual = r / beta;
+            res.iters = j + 1;
+            if (r < tol * beta) {
+                res.success = true;
+                break;
+            }
+        }
+        // upper-triangular solve and x += V y (or Z y)   (gmres.cpp:170-179)
+        const int k = res.iters;
+        std::vector<double> y(k, 0.0);
+        for (int i = k - 1; i >= 0; i--) {
+            double sum = g[i];
+            for (int c = i + 1; c < k; c++) sum -= h[(size_t)c * (m + 1) + i] * y[c];
+            y[i] = sum / h[(size_t)i * (m + 1) + i];
+        }
+        CUDA_OK(cudaMemcpyAsync(scal, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, stream));
+        launch_gemv_add(x, precond ? Z : V, (long long)n, k, scal, stream);
+        CUDA_OK(cudaGetLastError());
+        CUDA_OK(cudaStreamSynchronize(stream));
+        return res;
+    }
+
+    // real residual rows into rhs and the norms of it (SteadyStateLinearisation::eval_rhs, steady_state.cpp:130-165)
+    void eval_rhs(int prec) {
+        residual(prec, rhs.as<double>(), false);
+        launch_l2_norms(k.as<double>(), (int)mesh.N, nc(), l2.as<double>(), stream);
+        CUDA_OK(cudaGetLastError());
+        CUDA_OK(cudaMemcpyAsync(steady.norms, l2.p, sizeof(double) * 6, cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+    }
+
+    void steady_initialise(int prec) {  // Jfnk::initialise, jfnk.cpp:25-30
+        if (!steady.configured) throw ConfigError("config.json solver is not steady_state");
+        ensure_prims(prec);
+        ensure_krylov(steady.max_iters);
+        eval_rhs(prec);
+        std::memcpy(steady.initial, steady.norms, sizeof(steady.norms));
+        steady.step = 0;
+        steady.rb_prev_cfl = steady.rb_start;
+        steady.rb_prev_res = 1.0;
+        steady.initialised = true;
+    }
+
+    double steady_cfl(int64_t step) {  // Jfnk::calculate_cfl (jfnk.h:39-47), cfl.cpp:94-155
+        Steady& st = steady;
+        if (st.cfl_kind == 2) {
+            double t = st.norms[0] / st.initial[0];
+            if (t > st.rb_threshold) {
+                st.rb_prev_res = t;
+                return st.rb_prev_cfl;
+            }
+            double ratio = st.rb_prev_res / t;
+            double c = st.rb_prev_cfl * std::pow(ratio, st.rb_power);
+            c = std::min(c, st.rb_max);
+            c = std::max(st.rb_start, c);
+            st.rb_prev_res = t;
+            st.rb_prev_cfl = c;
+            return c;
+        }
+        if (st.cfl_kind == 0) return st.cfl;
+        double t = (double)step;
+        const auto &ts = st.cfl_t, &cs = st.cfl_v;
+        if (t <= ts[0]) return cs[0];
+        size_t nn = ts.size();
+        if (t >= ts[nn - 1]) return cs[nn - 1];
+        for (size_t i = 0; i + 1 < nn; i++)
+            if (t >= ts[i] && t < ts[i + 1]) return cs[i] + (t - ts[i]) / (ts[i + 1] - ts[i]) * (cs[i + 1] - cs[i]);
+        return cs[nn - 1];
+    }
+
+    // one Newton step of the JFNK solver (Jfnk::step, jfnk.cpp:39-61)
+    void newton_step(int prec, ibisgb_newton_status* out) {
+        if (!steady.initialised) steady_initialise(prec);
+        Steady& st = steady;
+        const size_t n = nvars();
+        double stable = estimate_dt(prec);
+        double cfl = steady_cfl(st.step);
+        double dt_star = cfl * stable;
+        double inv = 1 / dt_star;
+        CUDA_OK(cudaMemsetAsync(dU.p, 0, sizeof(double) * n, stream));
+        auto A = [&](const double* x, double* y) { jvp(x, y, inv, true); };
+        GmresOut r;
+        if (st.fgmres) {
+            // FGmres with an inner GMRES on the first-order linearisation (steady_state.cpp:47-50)
+            std::function<void(const double*, double*)> P = [&](const double* vin, double* zout) {
+                CUDA_OK(cudaMemsetAsync(zout, 0, sizeof(double) * n, stream));
+                auto A1 = [&](const double* x, double* y) { jvp(x, y, inv, false); };
+                inner_gmres(A1, vin, zout, st.max_prec_iters, st.prec_tol);
+            };
+            r = gmres(A, rhs.as<double>(), dU.as<double>(), st.max_iters, st.tol, kv.as<double>(),
+                      kz.as<double>(), &P);
+        } else {
+            r = gmres(A, rhs.as<double>(), dU.as<double>(), st.max_iters, st.tol, kv.as<double>(), nullptr, nullptr);
+        }
+        // apply_update_ (jfnk.cpp:63-93) and the new residual
+        launch_add_rows(U.as<double>(), dU.as<double>(), (int)mesh.N, nc(), stream);
+        CUDA_OK(cudaGetLastError());
+        state_changed(-1);
+        ensure_prims(prec);
+        eval_rhs(prec);
+        st.step++;
+        if (out) {
+            out->relative_residual = st.norms[0] / st.initial[0];
+            for (int q = 0; q < 6; q++) out->residual_norms[q] = st.norms[q];
+            out->gmres_iterations = r.iters;
+            out->gmres_converged = r.success ? 1 : 0;
+            out->gmres_residual = r.residual;
+            out->dt_star = dt_star;
+            out->cfl = cfl;
+            out->step = st.step;
+        }
+    }
+
+    // the preconditioner's own GMRES, with separate Krylov storage
+    DBuf pv, pw, pr0, pH, ppart, pscal;
+    template <class Op>
+    void inner_gmres(Op&& A, const double* b, double* x, int m, double tol) {
+        const size_t n = nvars();
+        pv.alloc(sizeof(double) * n * (m + 1));
+        // reuse the outer storage layout through a temporary swap of the work buffers
+        std::swap(kw.p, pw.p); std::swap(kw.bytes, pw.bytes);
+        std::swap(kr0.p, pr0.p); std::swap(kr0.bytes, pr0.bytes);
+        std::swap(kH.p, pH.p); std::swap(kH.bytes, pH.bytes);
+        std::swap(kscal.p, pscal.p); std::swap(kscal.bytes, pscal.bytes);
+        kw.alloc(sizeof(double) * n);
+        kr0.alloc(sizeof(double) * n);
+        kH.alloc(sizeof(double) * (m + 1) * (m + 1));
+        kscal.alloc(sizeof(double) * (2 * m + 8));
+        gmres(A, b, x, m, tol, pv.as<double>(), nullptr, nullptr);
+        std::swap(kw.p, pw.p); std::swap(kw.bytes, pw.bytes);
+        std::swap(kr0.p, pr0.p); std::swap(kr0.bytes, pr0.bytes);
+        std::swap(kH.p, pH.p); std::swap(kH.bytes, pH.bytes);
+        std::swap(kscal.p, pscal.p); std::swap(kscal.bytes, pscal.bytes);
     }
 
     void kernel_times(int prec, int reps, double out[4]) {
@@ -938,6 +1252,57 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
             }
             default: throw ArgError("unknown dump");
         }
+    });
+}
+
+int ibisgb_jvp_device(ibisgb_ctx* ctx, const double* v_device, double* out_device, double inv_dt_star,
+                      int32_t allow_reconstruction, void* stream) {
+    if (!ctx || !v_device || !out_device) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        ctx->ensure_device();
+        if (user && user != ctx->stream) {
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+        }
+        ctx->jvp(v_device, out_device, inv_dt_star, allow_reconstruction != 0);
+        if (ev) {
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        }
+    });
+}
+
+int ibisgb_jvp(ibisgb_ctx* ctx, const double* v, double* out, double inv_dt_star,
+               int32_t allow_reconstruction) {
+    if (!ctx || !v || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_device();
+        const size_t n = ctx->nvars();
+        ctx->ensure_krylov(1);
+        CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, v, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->jvp(ctx->kr0.as<double>(), ctx->kw.as<double>(), inv_dt_star, allow_reconstruction != 0);
+        CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        ctx->steady_initialise(precision);
+    });
+}
+
+int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status* status) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        ctx->newton_step(precision, status);
     });
 }
 

@@ -54,6 +54,8 @@ template <> __device__ __forceinline__ Dual d_copysign<Dual>(Dual m, Dual s) {
     double r = copysign(m.re, s.re);
     return Dual(r, (r - m.re) < 1e-15 ? m.du : -m.du);
 }
+__device__ __forceinline__ double real_of(const Dual& x) { return x.re; }
+
 template <> __device__ __forceinline__ Dual d_min<Dual>(Dual a, Dual b) { return a.re < b.re ? a : b; }
 template <> __device__ __forceinline__ Dual d_max<Dual>(Dual a, Dual b) { return a.re > b.re ? a : b; }
 

@@ -147,6 +147,20 @@ KernelOps kernels_mixed();
 void launch_dt_finalize(StepCtl* ctl, cudaStream_t s);
 void launch_reset_dt(StepCtl* ctl, cudaStream_t s);
 void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s);
+// Krylov vector kernels (kernels_common.cu); results stay in device memory
+void launch_dot(const double* a, const double* b, long long n, double* partial, double* out,
+                bool take_sqrt, cudaStream_t s);
+void launch_axpy_neg(double* y, const double* x, long long n, const double* c, cudaStream_t s);
+void launch_scale_inv(double* out, const double* in, long long n, const double* d, cudaStream_t s);
+void launch_sub(double* out, const double* a, const double* b, long long n, cudaStream_t s);
+void launch_gemv_add(double* x, const double* V, long long n, int m, const double* y, cudaStream_t s);
+void launch_add_rows(double* U, const double* dU, int N, int nc, cudaStream_t s);
+int dot_scratch_doubles();
+
+// tangent of the residual: out = inv_dt * v - dR/dU v (kernels_tangent.cu); v, out: N x nc rows
+void launch_tangent(const DevView& v, const FvParams& p, const double* vt, double inv_dt,
+                    bool reconstruct, double* out, cudaStream_t s);
+
 // message returned by ibisgb_last_error(NULL) on this thread
 void set_thread_error(const std::string& msg);
 

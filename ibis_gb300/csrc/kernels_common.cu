@@ -94,6 +94,102 @@ void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t
     k_l2_final<<<1, 32, 0, s>>>(out6 + 6, nblocks, out6);
 }
 
+// ---------------------------------------------------------------------------
+// Krylov vector kernels (dense_linear_algebra.h:184-309 on the device).  Dots
+// and norms are deterministic two-pass reductions whose result stays in device
+// memory, so a modified Gram-Schmidt sweep never waits for the host.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kDotBlocks = 608;  // 4 per SM
+
+__global__ void k_dot_partial(const double* a, const double* b, long long n, double* partial) {
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * kRB + threadIdx.x; i < n; i += (long long)gridDim.x * kRB)
+        s += a[i] * b[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    __shared__ double w[kRB / 32];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kRB / 32; k++) t += w[k];
+        partial[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_dot_final(const double* partial, int nb, double* out, int take_sqrt) {
+    __shared__ double sh[kRB];
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += kRB) s += partial[b];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kRB / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = take_sqrt ? sqrt(sh[0]) : sh[0];
+}
+
+// y += x * (-c[0])   (add_scaled_vector(w, v_i, -H(i, j)), gmres.cpp:147)
+__global__ void k_axpy_neg(double* y, const double* x, long long n, const double* c) {
+    const double a = -c[0];
+    for (long long i = (long long)blockIdx.x * kRB + threadIdx.x; i < n; i += (long long)gridDim.x * kRB)
+        y[i] += x[i] * a;
+}
+
+// out = in * (1 / d[0])   (scale(w, v, 1.0 / H(j+1, j)), gmres.cpp:150)
+__global__ void k_scale_inv(double* out, const double* in, long long n, const double* d) {
+    const double a = 1.0 / d[0];
+    for (long long i = (long long)blockIdx.x * kRB + threadIdx.x; i < n; i += (long long)gridDim.x * kRB)
+        out[i] = in[i] * a;
+}
+
+__global__ void k_sub(double* out, const double* a, const double* b, long long n) {
+    for (long long i = (long long)blockIdx.x * kRB + threadIdx.x; i < n; i += (long long)gridDim.x * kRB)
+        out[i] = a[i] - b[i];
+}
+
+// x += V y with V column c at V + c * n   (gemv + add_scaled_vector, gmres.cpp:170-179)
+__global__ void k_gemv_add(double* x, const double* V, long long n, int m, const double* y) {
+    for (long long i = (long long)blockIdx.x * kRB + threadIdx.x; i < n; i += (long long)gridDim.x * kRB) {
+        double d = 0.0;
+        for (int c = 0; c < m; c++) d += V[(size_t)c * n + i] * y[c];
+        x[i] += d * 1.0;
+    }
+}
+
+// U[q][i] += dU[i * nc + q]   (Jfnk::apply_update_, jfnk.cpp:63-76)
+__global__ void k_add_rows(double* U, const double* dU, int N, int nc) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * nc) return;
+    int i = (int)(t / nc), q = (int)(t % nc);
+    U[(size_t)q * N + i] += dU[t];
+}
+}  // namespace
+
+void launch_dot(const double* a, const double* b, long long n, double* partial, double* out,
+                bool take_sqrt, cudaStream_t s) {
+    k_dot_partial<<<kDotBlocks, kRB, 0, s>>>(a, b, n, partial);
+    k_dot_final<<<1, kRB, 0, s>>>(partial, kDotBlocks, out, take_sqrt ? 1 : 0);
+}
+void launch_axpy_neg(double* y, const double* x, long long n, const double* c, cudaStream_t s) {
+    k_axpy_neg<<<kDotBlocks, kRB, 0, s>>>(y, x, n, c);
+}
+void launch_scale_inv(double* out, const double* in, long long n, const double* d, cudaStream_t s) {
+    k_scale_inv<<<kDotBlocks, kRB, 0, s>>>(out, in, n, d);
+}
+void launch_sub(double* out, const double* a, const double* b, long long n, cudaStream_t s) {
+    k_sub<<<kDotBlocks, kRB, 0, s>>>(out, a, b, n);
+}
+void launch_gemv_add(double* x, const double* V, long long n, int m, const double* y, cudaStream_t s) {
+    k_gemv_add<<<kDotBlocks, kRB, 0, s>>>(x, V, n, m, y);
+}
+void launch_add_rows(double* U, const double* dU, int N, int nc, cudaStream_t s) {
+    long long n = (long long)N * nc;
+    k_add_rows<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(U, dU, N, nc);
+}
+int dot_scratch_doubles() { return kDotBlocks; }
+
 namespace {
 __global__ void k_rows_to_soa(const double* rows, double* soa, int N, int nc) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -13,6 +13,10 @@ namespace ibisgb {
 
 #define IBISGB_HD __device__ __forceinline__
 
+struct Dual;  // dual.cuh
+template <class R> constexpr bool kIsDual = false;
+template <> constexpr bool kIsDual<Dual> = true;
+
 template <class R> IBISGB_HD R d_sqrt(R x);
 template <> IBISGB_HD double d_sqrt<double>(double x) { return sqrt(x); }
 template <> IBISGB_HD float d_sqrt<float>(float x) { return sqrtf(x); }
@@ -158,7 +162,8 @@ IBISGB_HD void flux_ausmdv(const FaceSide<R>& L, const FaceSide<R>& Rt, const Ga
 }
 
 // LDFSS(2) flux (flux_calculators/ldfss2.cpp:9-90); EXACT keeps the
-// reference's pow(x, 2.0), the fast paths square instead.
+// reference's pow(x, 2.0), the fast paths square instead.  The tangent squares
+// too: the reference's dual pow adds 0*log(x), which is NaN for x < 0.
 template <class R, int DIM, bool EXACT>
 IBISGB_HD void flux_ldfss2(const FaceSide<R>& L, const FaceSide<R>& Rt, const Gas<R>& gm, R delta,
                            R* F) {
@@ -183,7 +188,7 @@ IBISGB_HD void flux_ldfss2(const FaceSide<R>& L, const FaceSide<R>& Rt, const Ga
     R DL = alphaL * (R(1.0) + betaL) - betaL * PL;
     R DR = alphaR * (R(1.0) + betaR) - betaR * PR;
     R mb = d_sqrt(R(0.5) * (ML * ML + MR * MR)) - R(1.0);
-    R Mhalf = R(0.25) * betaL * betaR * (EXACT ? d_pow(mb, R(2.0)) : mb * mb);
+    R Mhalf = R(0.25) * betaL * betaR * ((EXACT && !kIsDual<R>) ? d_pow(mb, R(2.0)) : mb * mb);
     R MhalfL = Mhalf * (R(1.0) - ((pL - pR) / (pL + pR) + delta * (d_abs(pL - pR) / pL)));
     R MhalfR = Mhalf * (R(1.0) + ((pL - pR) / (pL + pR) - delta * (d_abs(pL - pR) / pR)));
     R CL = alphaL * (R(1.0) + betaL) * ML - betaL * MpL - MhalfL;

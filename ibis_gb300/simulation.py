@@ -24,7 +24,7 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import PRECISION, RkStatus, Sizes, check
+from ._lib import PRECISION, NewtonStatus, RkStatus, Sizes, check
 
 DUMPS = {"left": (0, np.int64), "right": (1, np.int64), "cell_faces": (2, np.int64),
          "outsigns": (3, np.int32), "neighbours": (4, np.int64), "ghost_source": (5, np.int64),
@@ -162,6 +162,41 @@ class Simulation:
         self._call("ibisgb_rk_run", PRECISION[precision], int(n), C.byref(st))
         return {"t": st.t, "dt": st.dt, "stable_dt": st.stable_dt, "steps": st.steps,
                 "bad_cells": st.bad_cells, "device_ms": st.device_ms}
+
+    # ------------------------------------------------------- steady / JFNK
+    def matrix_vector_product(self, v, inv_dt_star: float = 0.0, allow_reconstruction: bool = True):
+        """inv_dt_star * v - (dR/dU) v for v of shape (N, n_conserved) (host arrays);
+        SteadyStateLinearisation::matrix_vector_product (steady_state.cpp:52-128)."""
+        v = np.ascontiguousarray(v, np.float64).reshape(-1)
+        if v.size != self.num_cells * self.n_conserved:
+            raise ValueError("v has the wrong size")
+        out = np.empty_like(v)
+        self._call("ibisgb_jvp", _ptr(v), _ptr(out), float(inv_dt_star), int(allow_reconstruction))
+        return out.reshape(self.num_cells, self.n_conserved)
+
+    def matrix_vector_product_into(self, v, out, inv_dt_star: float = 0.0,
+                                   allow_reconstruction: bool = True, stream=None):
+        """Device version for CUDA float64 tensors of shape (N, n_conserved)."""
+        for t in (v, out):
+            if not (t.is_cuda and t.element_size() == 8 and t.is_contiguous()):
+                raise ValueError("expected contiguous float64 CUDA tensors")
+        s = None if stream is None else C.c_void_p(stream.cuda_stream)
+        self._call("ibisgb_jvp_device", C.c_void_p(v.data_ptr()), C.c_void_p(out.data_ptr()),
+                   float(inv_dt_star), int(allow_reconstruction), s)
+        return out
+
+    def steady_initialise(self, precision: str = "f64"):
+        """Jfnk::initialise: residual and initial norms at the current state."""
+        self._call("ibisgb_steady_initialise", PRECISION[precision])
+
+    def newton_step(self, precision: str = "f64") -> dict:
+        """One JFNK step (Jfnk::step): GMRES on (I/dt* - J) dU = R(U), U += dU."""
+        st = NewtonStatus()
+        self._call("ibisgb_newton_step", PRECISION[precision], C.byref(st))
+        return {"relative_residual": st.relative_residual, "residual_norms": list(st.residual_norms),
+                "gmres_iterations": st.gmres_iterations, "gmres_converged": bool(st.gmres_converged),
+                "gmres_residual": st.gmres_residual, "dt_star": st.dt_star, "cfl": st.cfl,
+                "step": st.step}
 
     def L2_norms(self) -> np.ndarray:
         """global, mass, momentum_x, momentum_y, momentum_z, energy of the first-stage residual."""

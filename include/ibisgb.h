@@ -168,6 +168,46 @@ int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]);
  * 10 face fluxes of the last residual (double F x n_conserved). */
 int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
 
+/* Result of one Newton step of the steady solver. */
+typedef struct {
+    double relative_residual; /* global L2 norm of the residual / its initial value */
+    double residual_norms[6]; /* global, mass, momentum_x, momentum_y, momentum_z, energy */
+    int32_t gmres_iterations;
+    int32_t gmres_converged;
+    double gmres_residual;    /* |g_{k}| / beta of the last GMRES iteration */
+    double dt_star;           /* pseudo time step cfl * stable dt */
+    double cfl;
+    int64_t step;             /* Newton steps taken since ibisgb_steady_initialise */
+} ibisgb_newton_status;
+
+/* out = inv_dt_star * v - (dR/dU) v on device vectors of N x n_conserved rows
+ * (index cell * n_conserved + component), at the current state, on `stream`
+ * (NULL: the context stream).  Replaces the dual-number evaluation of
+ * SteadyStateLinearisation::matrix_vector_product
+ * (src/solvers/solvers/steady_state.cpp:52-128) with a hand-written tangent of
+ * the residual kernels that follows ibis's Dual<T> rules (dual.h:11-346).
+ * inv_dt_star = 1/dt* gives the reference's operator; 0 gives -J v.
+ * allow_reconstruction = 0 is the first-order linearisation used as the
+ * FGMRES preconditioner (steady_state.cpp:47-50). */
+int ibisgb_jvp_device(ibisgb_ctx* ctx, const double* v_device, double* out_device, double inv_dt_star,
+                      int32_t allow_reconstruction, void* stream);
+
+/* As ibisgb_jvp_device with host vectors. */
+int ibisgb_jvp(ibisgb_ctx* ctx, const double* v, double* out, double inv_dt_star,
+               int32_t allow_reconstruction);
+
+/* Residual and initial norms of the steady solver at the current state
+ * (Jfnk::initialise, src/solvers/solvers/jfnk.cpp:25-30).  `precision` is the
+ * arithmetic of the real residual; the tangent is always double. */
+int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision);
+
+/* One Jacobian-free Newton-Krylov step: dt* = cfl * estimate_dt, GMRES (or
+ * FGMRES) on (I/dt* - J) dU = R(U) with the tangent operator, U += dU, new
+ * residual norms.  Replaces Jfnk::step / apply_update_ (jfnk.cpp:39-93) with
+ * Gmres::solve / FGmres::solve (src/linear_algebra/linear_algebra/gmres.cpp:119-303)
+ * on device vectors. */
+int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status* status);
+
 /* Wait for all work on the context's stream. */
 int ibisgb_synchronize(ibisgb_ctx* ctx);
 
