@@ -8,6 +8,6 @@ as hand-written sm_103a CUDA kernels behind the C ABI of libibisgb.so
 interface (``Simulation``), the grid/config generators of the benchmark cases
 (``grids``) and the build recipe (``build``).
 """
-from .simulation import Simulation  # noqa: F401
+from .simulation import Batch, Simulation  # noqa: F401
 
-__all__ = ["Simulation"]
+__all__ = ["Batch", "Simulation"]

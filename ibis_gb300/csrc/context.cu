@@ -137,6 +137,15 @@ struct ibisgb_ctx {
     StepCtl ctl_host{};
     double dt_init = -1.0;
 
+    // batched ensembles: one control block (and dt_init) per case, the case of
+    // every valid cell, and the offsets of each case's cells / faces / ghosts
+    int n_cases = 1;
+    std::vector<StepCtl> case_ctl;
+    std::vector<double> case_dt_init;
+    std::vector<int64_t> cell_off, face_off, ghost_off;
+    std::vector<StepCtl> last_ctl;
+    DBuf case_of;
+
     cudaStream_t stream = nullptr;
     int device = 0;
 
@@ -149,6 +158,7 @@ struct ibisgb_ctx {
     bool have_state = false;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
     double last_l2[6] = {0, 0, 0, 0, 0, 0};
+    double last_ms = 0.0;
 
     ~ibisgb_ctx() {
         for (auto& g : graph)
@@ -323,10 +333,7 @@ struct ibisgb_ctx {
         prm.dim = in.dim;
         std::vector<BoundarySpec> specs = boundary_specs();
         build_mesh(in, specs, prm.viscous || prm.order > 1, mesh);
-        const int64_t N = mesh.N, F = mesh.F, G = mesh.G;
-        const int64_t lim = std::numeric_limits<int>::max();
-        if (15 * N >= lim || 5 * F >= lim || 7 * (N + G) >= lim)
-            throw ConfigError("grid too large for 32-bit device indexing");
+        check_index_range();
         for (const auto& b : mesh.bounds) {  // BoundaryCondition ctor, boundary.cpp:494-515
             const Json& bj = config.at("grid").at("boundaries").at(b.tag);
             BoundDev d{};
@@ -340,6 +347,65 @@ struct ibisgb_ctx {
             }
             bounds_host.push_back(d);
         }
+    }
+
+    void check_index_range() const {
+        const int64_t N = mesh.N, F = mesh.F, G = mesh.G;
+        const int64_t lim = std::numeric_limits<int>::max();
+        if (15 * N >= lim || 5 * F >= lim || 7 * (N + G) >= lim || 3 * (int64_t)mesh.MF * N >= lim)
+            throw ConfigError("grid too large for 32-bit device indexing");
+    }
+
+    // Batched ensemble from single-case contexts (see ibisgb_batch_create).
+    void merge(ibisgb_ctx* const* cs, int n) {
+        std::vector<const Mesh*> parts;
+        for (int i = 0; i < n; i++) {
+            if (!cs[i]) throw ArgError("case " + std::to_string(i) + " is null");
+            const ibisgb_ctx& c = *cs[i];
+            if (c.n_cases != 1) throw ArgError("case " + std::to_string(i) + " is itself a batch");
+            if (!same_scheme(cs[0]->prm, c.prm))
+                throw ConfigError("case " + std::to_string(i) +
+                                  ": cases of a batch must share flux, reconstruction, gas and transport settings");
+            if (!c.rk_configured || !cs[0]->rk_configured || !same_tableau(cs[0]->ctl_host, c.ctl_host))
+                throw ConfigError("case " + std::to_string(i) +
+                                  ": cases of a batch must use runge_kutta with the same Butcher tableau");
+            parts.push_back(&c.mesh);
+        }
+        const ibisgb_ctx& a = *cs[0];
+        config = a.config;
+        prm = a.prm;
+        rk_configured = true;
+        ctl_host = a.ctl_host;
+        dt_init = a.dt_init;
+        std::vector<int64_t> bound_off;
+        try {
+            merge_meshes(parts, mesh, cell_off, ghost_off, face_off, bound_off);
+        } catch (const std::runtime_error& e) {
+            throw ConfigError(e.what());
+        }
+        check_index_range();
+        for (int i = 0; i < n; i++) {
+            bounds_host.insert(bounds_host.end(), cs[i]->bounds_host.begin(), cs[i]->bounds_host.end());
+            case_ctl.push_back(cs[i]->ctl_host);
+            case_dt_init.push_back(cs[i]->dt_init);
+        }
+        n_cases = n;
+    }
+
+    static bool same_scheme(const FvParams& a, const FvParams& b) {
+        return a.dim == b.dim && a.flux == b.flux && a.thermo == b.thermo && a.order == b.order &&
+               a.limiter == b.limiter && a.viscous == b.viscous && a.eps == b.eps && a.delta == b.delta &&
+               a.signal_factor == b.signal_factor && a.R == b.R && a.Cv == b.Cv && a.Cp == b.Cp &&
+               a.gamma == b.gamma && a.mu0 == b.mu0 && a.T0 == b.T0 && a.Ts == b.Ts && a.Pr == b.Pr;
+    }
+    static bool same_tableau(const StepCtl& a, const StepCtl& b) {
+        if (a.stages != b.stages) return false;
+        for (int i = 0; i < a.stages; i++) {
+            if (a.b[i] != b.b[i]) return false;
+            for (int j = 0; j < i; j++)
+                if (a.a[i][j] != b.a[i][j]) return false;
+        }
+        return true;
     }
 
     // Device buffers are created on the first call that needs the GPU, so that
@@ -391,7 +457,13 @@ struct ibisgb_ctx {
         k.alloc(sizeof(double) * nc() * N * stages());
         vsig.alloc(sizeof(double) * F);
         CUDA_OK(cudaMemsetAsync(vsig.p, 0, sizeof(double) * F, stream));
-        ctl.alloc(sizeof(StepCtl));
+        ctl.alloc(sizeof(StepCtl) * n_cases);
+        if (n_cases > 1) {
+            std::vector<int> co(N);
+            for (int c = 0; c < n_cases; c++)
+                for (int64_t i = cell_off[c]; i < cell_off[c + 1]; i++) co[i] = c;
+            upload(case_of, co, stream);
+        }
         l2.alloc(sizeof(double) * (6 + 6 * 304));
         CUDA_OK(cudaStreamSynchronize(stream));
     }
@@ -449,6 +521,8 @@ struct ibisgb_ctx {
         v.prim = s.prim.p; v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
         v.U = U.as<double>(); v.k = k.as<double>(); v.ctl = ctl.as<StepCtl>();
+        v.case_of = n_cases > 1 ? case_of.as<int>() : nullptr;
+        v.n_cases = n_cases;
         v.branches = nullptr;
         return v;
     }
@@ -517,17 +591,23 @@ struct ibisgb_ctx {
     }
 
     void reset_rk() {
-        StepCtl c = ctl_host;
-        c.t = 0.0;
-        c.time_since_last_plot = 0.0;
-        c.dt = dt_init > 0 ? dt_init : std::numeric_limits<double>::max();
-        c.dt_bits = 0x7FF0000000000000ull;
-        c.bad_cells = 0;
-        c.steps = 0;
-        if (!rk_configured) c.stages = 1;
-        c.halt = 0;
-        c.max_time = rk_configured ? ctl_host.max_time : std::numeric_limits<double>::max();
-        CUDA_OK(cudaMemcpyAsync(ctl.p, &c, sizeof(StepCtl), cudaMemcpyHostToDevice, stream));
+        std::vector<StepCtl> all(n_cases);
+        for (int cs = 0; cs < n_cases; cs++) {
+            StepCtl c = n_cases > 1 ? case_ctl[cs] : ctl_host;
+            const double dti = n_cases > 1 ? case_dt_init[cs] : dt_init;
+            c.t = 0.0;
+            c.time_since_last_plot = 0.0;
+            c.dt = dti > 0 ? dti : std::numeric_limits<double>::max();
+            c.dt_bits = 0x7FF0000000000000ull;
+            c.bad_cells = 0;
+            c.steps = 0;
+            if (!rk_configured) c.stages = 1;
+            c.halt = 0;
+            if (!rk_configured) c.max_time = std::numeric_limits<double>::max();
+            all[cs] = c;
+        }
+        last_ctl = all;
+        CUDA_OK(cudaMemcpyAsync(ctl.p, all.data(), sizeof(StepCtl) * n_cases, cudaMemcpyHostToDevice, stream));
         CUDA_OK(cudaStreamSynchronize(stream));
     }
 
@@ -551,14 +631,18 @@ struct ibisgb_ctx {
     double estimate_dt(int prec) {
         ensure_prims(prec);
         DevView v = view(prec);
-        launch_reset_dt(v.ctl, stream);
+        launch_reset_dt(v.ctl, n_cases, stream);
         ops(prec).local_dt(v, prm, stream);
         CUDA_OK(cudaGetLastError());
-        unsigned long long bits = 0;
-        CUDA_OK(cudaMemcpyAsync(&bits, &((StepCtl*)ctl.p)->dt_bits, sizeof(bits), cudaMemcpyDeviceToHost, stream));
+        std::vector<StepCtl> c(n_cases);
+        CUDA_OK(cudaMemcpyAsync(c.data(), ctl.p, sizeof(StepCtl) * n_cases, cudaMemcpyDeviceToHost, stream));
         CUDA_OK(cudaStreamSynchronize(stream));
-        double dt;
-        std::memcpy(&dt, &bits, sizeof(dt));
+        double dt = std::numeric_limits<double>::infinity();
+        for (const StepCtl& x : c) {
+            double d;
+            std::memcpy(&d, &x.dt_bits, sizeof(d));
+            dt = std::min(dt, d);
+        }
         return dt;
     }
 
@@ -572,7 +656,7 @@ struct ibisgb_ctx {
         o.face_flux(v, prm, reco, stream);
         o.update(v, prm, 1, 0, nullptr, stream);
         o.local_dt(v, prm, stream);
-        launch_dt_finalize(v.ctl, stream);
+        launch_dt_finalize(v.ctl, n_cases, stream);
         if (S == 1) {
             o.finalize(v, prm, stream);
             return;
@@ -606,13 +690,21 @@ struct ibisgb_ctx {
         for (int64_t i = 0; i < n; i++) CUDA_OK(cudaGraphLaunch(graph[gi], stream));
         CUDA_OK(cudaEventRecord(e1, stream));
         state_changed(prec);
-        StepCtl c;
-        CUDA_OK(cudaMemcpyAsync(&c, ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, stream));
+        last_ctl.resize(n_cases);
+        CUDA_OK(cudaMemcpyAsync(last_ctl.data(), ctl.p, sizeof(StepCtl) * n_cases, cudaMemcpyDeviceToHost, stream));
         CUDA_OK(cudaStreamSynchronize(stream));
         float ms = 0.f;
         CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        last_ms = ms;
+        StepCtl c = last_ctl[0];
+        for (const StepCtl& x : last_ctl) {  // batch: minimum times, maximum steps, total bad cells
+            c.t = std::min(c.t, x.t); c.dt = std::min(c.dt, x.dt); c.stable_dt = std::min(c.stable_dt, x.stable_dt);
+            c.steps = std::max(c.steps, x.steps);
+        }
+        c.bad_cells = 0;
+        for (const StepCtl& x : last_ctl) c.bad_cells += x.bad_cells;
         if (st) {
             st->t = c.t; st->dt = c.dt; st->stable_dt = c.stable_dt; st->steps = c.steps;
             st->bad_cells = (int64_t)c.bad_cells;
@@ -766,6 +858,7 @@ struct ibisgb_ctx {
     }
 
     void steady_initialise(int prec) {  // Jfnk::initialise, jfnk.cpp:25-30
+        if (n_cases > 1) throw StateError("steady-state solves run one case per context, not on a batch");
         if (!steady.configured) throw ConfigError("config.json solver is not steady_state");
         ensure_prims(prec);
         ensure_krylov(steady.max_iters);
@@ -806,6 +899,7 @@ struct ibisgb_ctx {
 
     // one Newton step of the JFNK solver (Jfnk::step, jfnk.cpp:39-61)
     void newton_step(int prec, ibisgb_newton_status* out) {
+        if (n_cases > 1) throw StateError("steady-state solves run one case per context, not on a batch");
         if (!steady.initialised) steady_initialise(prec);
         Steady& st = steady;
         const size_t n = nvars();
@@ -1303,6 +1397,49 @@ int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status*
     return guarded(ctx, [&] {
         if (precision < 0 || precision > 2) throw ArgError("unknown precision");
         ctx->newton_step(precision, status);
+    });
+}
+
+int ibisgb_batch_create(ibisgb_ctx* const* cases, int32_t n_cases, ibisgb_ctx** out) {
+    if (!out || !cases || n_cases < 1) {
+        g_create_error = "ibisgb_batch_create: null argument or no cases";
+        return IBISGB_ERR_ARG;
+    }
+    *out = nullptr;
+    auto ctx = std::make_unique<ibisgb_ctx>();
+    int rc = guarded(ctx.get(), [&] { ctx->merge(cases, n_cases); });
+    if (rc != IBISGB_OK) {
+        g_create_error = ctx->err;
+        return rc;
+    }
+    *out = ctx.release();
+    return IBISGB_OK;
+}
+
+int ibisgb_batch_layout(const ibisgb_ctx* ctx, int32_t* n_cases, int64_t* cell_offsets,
+                        int64_t* face_offsets, int64_t* ghost_offsets) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    const int n = ctx->n_cases;
+    if (n_cases) *n_cases = n;
+    for (int c = 0; c <= n; c++) {
+        const bool one = n == 1;
+        if (cell_offsets) cell_offsets[c] = one ? (c ? ctx->mesh.N : 0) : ctx->cell_off[c];
+        if (face_offsets) face_offsets[c] = one ? (c ? ctx->mesh.F : 0) : ctx->face_off[c];
+        if (ghost_offsets) ghost_offsets[c] = one ? (c ? ctx->mesh.G : 0) : ctx->ghost_off[c];
+    }
+    return IBISGB_OK;
+}
+
+int ibisgb_batch_status(ibisgb_ctx* ctx, ibisgb_rk_status* per_case) {
+    if (!ctx || !per_case) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (ctx->last_ctl.size() != (size_t)ctx->n_cases) throw StateError("no Runge-Kutta state yet");
+        for (int c = 0; c < ctx->n_cases; c++) {
+            const StepCtl& x = ctx->last_ctl[c];
+            per_case[c].t = x.t; per_case[c].dt = x.dt; per_case[c].stable_dt = x.stable_dt;
+            per_case[c].steps = x.steps; per_case[c].bad_cells = (int64_t)x.bad_cells;
+            per_case[c].device_ms = ctx->last_ms;
+        }
     });
 }
 

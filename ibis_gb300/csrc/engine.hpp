@@ -112,7 +112,9 @@ struct DevView {
     double* vsig;  // [F]: viscous time-step signal (gamma/rho)(mu/Pr) per face
     double* U;     // [nc][N]
     double* k;     // [stages][nc][N]
-    StepCtl* ctl;
+    StepCtl* ctl;            // one control block per case
+    const int* case_of;      // case of each valid cell (batched ensembles), or null for one case
+    int n_cases;
     unsigned* branches;  // optional [N][5] limiter branch codes
 };
 
@@ -144,8 +146,8 @@ KernelOps kernels_f64_exact();
 KernelOps kernels_mixed();
 
 // precision-independent kernels (kernels_common.cu)
-void launch_dt_finalize(StepCtl* ctl, cudaStream_t s);
-void launch_reset_dt(StepCtl* ctl, cudaStream_t s);
+void launch_dt_finalize(StepCtl* ctl, int n_cases, cudaStream_t s);
+void launch_reset_dt(StepCtl* ctl, int n_cases, cudaStream_t s);
 void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s);
 // Krylov vector kernels (kernels_common.cu); results stay in device memory
 void launch_dot(const double* a, const double* b, long long n, double* partial, double* out,

@@ -532,6 +532,9 @@ __device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, co
     return s;
 }
 
+// control block of the case cell i belongs to
+IBISGB_HD StepCtl* ctl_of(const DevView& v, int i) { return v.case_of ? v.ctl + v.case_of[i] : v.ctl; }
+
 // count_bad_cells (finite_volume.cpp:257-270)
 IBISGB_HD void count_bad(StepCtl* ctl, const State64& s) {
     if (s.T < 0.0 || s.rho < 0.0 || isnan(s.rho) || isinf(s.rho)) atomicAdd(&ctl->bad_cells, 1ull);
@@ -607,7 +610,7 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
         if (out_rm) out_rm[(size_t)i * NC + q] = ks[q];
     }
     if (mode < 2) return;
-    const StepCtl* ctl = v.ctl;
+    StepCtl* ctl = ctl_of(v, i);
     if (ctl->halt) return;
     double u[NC];
 #pragma unroll
@@ -639,7 +642,7 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
         }
 #pragma unroll
         for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
-        count_bad(v.ctl, commit_state<P, Gm, DIM, EXACT>(v, prm, i, u));
+        count_bad(ctl, commit_state<P, Gm, DIM, EXACT>(v, prm, i, u));
     }
 }
 
@@ -648,30 +651,33 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
 template <class P, class Gm, int DIM, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_finalize(DevView v, FvParams prm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.N || v.ctl->halt) return;
+    if (i >= v.N) return;
+    StepCtl* ctl = ctl_of(v, i);
+    if (ctl->halt) return;
     constexpr int NC = DIM + 2;
     const int N = v.N;
     double u[NC];
 #pragma unroll
     for (int q = 0; q < NC; q++) u[q] = v.U[q * N + i];
-    for (int j = 0; j < v.ctl->stages; j++) {
-        const double c = v.ctl->cb[j];
+    for (int j = 0; j < ctl->stages; j++) {
+        const double c = ctl->cb[j];
 #pragma unroll
         for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
     }
 #pragma unroll
     for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
-    count_bad(v.ctl, commit_state<P, Gm, DIM, EXACT>(v, prm, i, u));
+    count_bad(ctl, commit_state<P, Gm, DIM, EXACT>(v, prm, i, u));
 }
 
 // State of stage `stage` from U and k_0..k_{stage-1} (after dt is known), then primitives and ghosts.
 template <class P, class Gm, int DIM, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_combine(DevView v, FvParams prm, int stage) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.N || v.ctl->halt) return;
+    if (i >= v.N) return;
+    const StepCtl* ctl = ctl_of(v, i);
+    if (ctl->halt) return;
     constexpr int NC = DIM + 2;
     const int N = v.N;
-    const StepCtl* ctl = v.ctl;
     double u[NC];
 #pragma unroll
     for (int q = 0; q < NC; q++) u[q] = v.U[q * N + i] + v.k[q * N + i] * ctl->ca[stage][0];
@@ -739,6 +745,20 @@ __global__ void __launch_bounds__(kBlock) k_local_dt(DevView v, FvParams prm) {
         }
         local = vol / (src + prm.signal_factor * srv);
         if (!(local > 0.0)) local = 1.0e308 * 10.0;
+    }
+    if (v.case_of) {
+        // batched ensemble: one min per case; a warp whose cells share a case
+        // (the usual situation, cases are contiguous) reduces before its atomic
+        const int cs = i < v.N ? v.case_of[i] : -1;
+        const int c0 = __shfl_sync(0xffffffffu, cs, 0);
+        if (__all_sync(0xffffffffu, cs == c0)) {
+            for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_down_sync(0xffffffffu, local, o));
+            if ((threadIdx.x & 31) == 0 && c0 >= 0)
+                atomicMin(&v.ctl[c0].dt_bits, (unsigned long long)__double_as_longlong(local));
+        } else if (cs >= 0) {
+            atomicMin(&v.ctl[cs].dt_bits, (unsigned long long)__double_as_longlong(local));
+        }
+        return;
     }
     // warp-shuffle + block min, one atomic per block
     for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_down_sync(0xffffffffu, local, o));

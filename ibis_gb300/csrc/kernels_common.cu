@@ -24,7 +24,10 @@ __device__ double cfl_eval(const StepCtl& c, double t) {
 __device__ double dmin(double a, double b) { return (b < a) ? b : a; }
 
 // RungeKutta::estimate_dt (runge_kutta.cpp:108-119) and the coefficients of the step
-__global__ void k_dt_finalize(StepCtl* c) {
+__global__ void k_dt_finalize(StepCtl* ctl, int n_cases) {
+    const int cs = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cs >= n_cases) return;
+    StepCtl* c = ctl + cs;
     if (c->halt) return;
     if (c->bad_cells > 0 || c->t >= c->max_time) {
         c->halt = 1;
@@ -46,7 +49,10 @@ __global__ void k_dt_finalize(StepCtl* c) {
     c->steps += 1;
 }
 
-__global__ void k_reset_dt(StepCtl* c) { c->dt_bits = 0x7FF0000000000000ull; }
+__global__ void k_reset_dt(StepCtl* ctl, int n_cases) {
+    const int cs = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cs < n_cases) ctl[cs].dt_bits = 0x7FF0000000000000ull;
+}
 
 // sums of squares of k0 per component and in total; one block per chunk,
 // deterministic two-pass reduction (block partials, then one block)
@@ -84,8 +90,12 @@ __global__ void k_l2_final(const double* partial, int nblocks, double* out6) {
 
 }  // namespace
 
-void launch_dt_finalize(StepCtl* ctl, cudaStream_t s) { k_dt_finalize<<<1, 1, 0, s>>>(ctl); }
-void launch_reset_dt(StepCtl* ctl, cudaStream_t s) { k_reset_dt<<<1, 1, 0, s>>>(ctl); }
+void launch_dt_finalize(StepCtl* ctl, int n_cases, cudaStream_t s) {
+    k_dt_finalize<<<(n_cases + 63) / 64, 64, 0, s>>>(ctl, n_cases);
+}
+void launch_reset_dt(StepCtl* ctl, int n_cases, cudaStream_t s) {
+    k_reset_dt<<<(n_cases + 63) / 64, 64, 0, s>>>(ctl, n_cases);
+}
 
 // out6 must hold 6 + 6*nblocks doubles of scratch after the 6 results
 void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s) {

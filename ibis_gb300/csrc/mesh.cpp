@@ -510,3 +510,92 @@ void build_mesh(const GridInput& in, const std::vector<BoundarySpec>& bounds_in,
 }
 
 }  // namespace ibisgb
+
+namespace ibisgb {
+
+// Concatenates independent cases into one mesh: valid cells of all cases first
+// (case order), then the ghost cells of all cases, faces and boundaries in case
+// order.  Ids inside each case are shifted by the case's offsets; element and
+// vertex lists are not carried over (the device kernels do not use them).
+void merge_meshes(const std::vector<const Mesh*>& parts, Mesh& out, std::vector<int64_t>& cell_off,
+                  std::vector<int64_t>& ghost_off, std::vector<int64_t>& face_off,
+                  std::vector<int64_t>& bound_off) {
+    if (parts.empty()) throw std::runtime_error("no cases to merge");
+    const size_t nc = parts.size();
+    out = Mesh{};
+    out.dim = parts[0]->dim;
+    cell_off.assign(nc + 1, 0); ghost_off.assign(nc + 1, 0); face_off.assign(nc + 1, 0);
+    bound_off.assign(nc + 1, 0);
+    bool lsq = !parts[0]->lsqw.empty();
+    for (size_t c = 0; c < nc; c++) {
+        const Mesh& m = *parts[c];
+        if (m.dim != out.dim) throw std::runtime_error("cases of a batch must have the same dimension");
+        if (m.lsqw.empty() != !lsq) throw std::runtime_error("cases of a batch must share the gradient settings");
+        cell_off[c + 1] = cell_off[c] + m.N;
+        ghost_off[c + 1] = ghost_off[c] + m.G;
+        face_off[c + 1] = face_off[c] + m.F;
+        bound_off[c + 1] = bound_off[c] + (int64_t)m.bounds.size();
+        out.MF = std::max(out.MF, m.MF);
+    }
+    const int64_t N = cell_off[nc], G = ghost_off[nc], F = face_off[nc], MF = out.MF;
+    out.N = N; out.G = G; out.F = F;
+    auto cell_id = [&](size_t c, int64_t x) -> int64_t {
+        if (x < 0) return -1;
+        const Mesh& m = *parts[c];
+        return x < m.N ? cell_off[c] + x : N + ghost_off[c] + (x - m.N);
+    };
+    out.left.resize(F); out.right.resize(F);
+    std::vector<double>* fo[13] = {&out.nx, &out.ny, &out.nz, &out.t1x, &out.t1y, &out.t1z, &out.t2x,
+                                   &out.t2y, &out.t2z, &out.fcx, &out.fcy, &out.fcz, &out.area};
+    for (auto* a : fo) a->reserve(F);
+    out.nfaces.resize(N);
+    out.cell_face.assign(N * MF, -1); out.cell_nbr.assign(N * MF, -1); out.outsign.assign(N * MF, 0);
+    out.ccx.resize(N + G); out.ccy.resize(N + G); out.ccz.resize(N + G); out.volume.resize(N + G);
+    if (!parts[0]->r.empty()) out.r.reserve(6 * N);
+    if (lsq) out.lsqw.assign(3 * (size_t)MF * N, 0.0);
+    out.ghost_face.resize(G); out.ghost_bound.resize(G); out.ghost_src.resize(G);
+    for (size_t c = 0; c < nc; c++) {
+        const Mesh& m = *parts[c];
+        for (int64_t f = 0; f < m.F; f++) {
+            out.left[face_off[c] + f] = cell_id(c, m.left[f]);
+            out.right[face_off[c] + f] = cell_id(c, m.right[f]);
+        }
+        const std::vector<double>* fi[13] = {&m.nx, &m.ny, &m.nz, &m.t1x, &m.t1y, &m.t1z, &m.t2x,
+                                             &m.t2y, &m.t2z, &m.fcx, &m.fcy, &m.fcz, &m.area};
+        for (int q = 0; q < 13; q++) fo[q]->insert(fo[q]->end(), fi[q]->begin(), fi[q]->end());
+        for (int64_t i = 0; i < m.N; i++) {
+            const int64_t o = cell_off[c] + i;
+            out.nfaces[o] = m.nfaces[i];
+            for (int k = 0; k < m.MF; k++) {
+                const int64_t fk = m.cell_face[i * m.MF + k];
+                out.cell_face[o * MF + k] = fk < 0 ? -1 : face_off[c] + fk;
+                out.cell_nbr[o * MF + k] = cell_id(c, m.cell_nbr[i * m.MF + k]);
+                out.outsign[o * MF + k] = m.outsign[i * m.MF + k];
+                if (lsq)
+                    for (int d = 0; d < 3; d++)
+                        out.lsqw[(d * (size_t)MF + k) * N + o] = m.lsqw[(d * (size_t)m.MF + k) * m.N + i];
+            }
+        }
+        if (!m.r.empty()) out.r.insert(out.r.end(), m.r.begin(), m.r.end());
+        for (int64_t x = 0; x < m.N + m.G; x++) {
+            const int64_t o = cell_id(c, x);
+            out.ccx[o] = m.ccx[x]; out.ccy[o] = m.ccy[x]; out.ccz[o] = m.ccz[x]; out.volume[o] = m.volume[x];
+        }
+        for (int64_t g = 0; g < m.G; g++) {
+            const int64_t o = ghost_off[c] + g;
+            out.ghost_face[o] = face_off[c] + m.ghost_face[g];
+            out.ghost_bound[o] = bound_off[c] + m.ghost_bound[g];
+            out.ghost_src[o] = cell_id(c, m.ghost_src[g]);
+        }
+        for (size_t b = 0; b < m.bounds.size(); b++) {
+            out.bounds.push_back(m.bounds[b]);
+            std::vector<int64_t> bf, bg;
+            for (int64_t f : m.bound_faces[b]) bf.push_back(face_off[c] + f);
+            for (int64_t x : m.bound_ghosts[b]) bg.push_back(cell_id(c, x));
+            out.bound_faces.push_back(bf);
+            out.bound_ghosts.push_back(bg);
+        }
+    }
+}
+
+}  // namespace ibisgb

@@ -89,4 +89,11 @@ struct Mesh {
 void build_mesh(const GridInput& in, const std::vector<BoundarySpec>& bounds, bool need_lsq,
                 Mesh& m);
 
+// Concatenation of independent cases (batched ensembles): valid cells of all
+// cases first, in case order, then all ghost cells; faces and boundaries in
+// case order.  The offset vectors get one entry per case plus the total.
+void merge_meshes(const std::vector<const Mesh*>& parts, Mesh& out, std::vector<int64_t>& cell_off,
+                  std::vector<int64_t>& ghost_off, std::vector<int64_t>& face_off,
+                  std::vector<int64_t>& bound_off);
+
 }  // namespace ibisgb

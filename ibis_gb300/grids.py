@@ -355,6 +355,25 @@ def ramp_case(ni=256, nj=128, mach=2.0, T=300.0, p=101325.0, angle_deg=15.0, **k
     return grid, make_config(2, bnds, gas=gas, **kw), inflow
 
 
+def ramp_ensemble(n_cases=64, seed=0, smallest=(64, 32), largest=(512, 256), mach=(1.5, 4.0),
+                  angle_deg=(5.0, 20.0), T=(200.0, 400.0), p=101325.0, **kw):
+    """Independent compression-ramp cases for a batched ensemble: grid sizes
+    log-uniform between ``smallest`` and ``largest`` cells (aspect 2:1 kept),
+    inflow Mach, ramp angle and inflow temperature uniform in the given ranges,
+    all drawn from ``seed``.  Returns a list of (grid, config, inflow, params)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(smallest[0]), math.log(largest[0])
+    out = []
+    for _ in range(n_cases):
+        ni = int(round(math.exp(rng.uniform(lo, hi)) / 2.0)) * 2
+        nj = ni * smallest[1] // smallest[0]
+        prm = {"ni": ni, "nj": nj, "mach": float(rng.uniform(*mach)),
+               "angle_deg": float(rng.uniform(*angle_deg)), "T": float(rng.uniform(*T))}
+        g, c, inf = ramp_case(ni, nj, mach=prm["mach"], T=prm["T"], p=p, angle_deg=prm["angle_deg"], **kw)
+        out.append((g, c, inf, prm))
+    return out
+
+
 def flat_plate_case(ni=512, nj=256, mach=2.0, T=220.0, Re_per_m=1e5, Pr=0.71, **kw):
     """2-D laminar flat plate: Sutherland air, Pr=0.71, Mach 2 at T=220 K with
     density chosen for Re=1e5 per metre; adiabatic no-slip wall from x=0."""

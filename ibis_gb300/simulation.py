@@ -62,6 +62,10 @@ class Simulation:
                                              len(grid.markers), names.encode(), _ptr(m_off),
                                              _ptr(e_types), _ptr(e_off), _ptr(e_conn), C.byref(h))
         check(rc, None)
+        self._attach(h)
+
+    def _attach(self, h):
+        L = _lib.load()
         self._h = h
         s = Sizes()
         check(L.ibisgb_get_sizes(h, C.byref(s)), h)
@@ -219,3 +223,42 @@ class Simulation:
         out = np.empty(shape, dt)
         self._call("ibisgb_get_dump", which, _ptr(out), out.nbytes)
         return out
+
+
+class Batch(Simulation):
+    """Independent cases advanced together in one context (``ibisgb_batch_create``).
+
+    The cases' valid cells are concatenated in case order, so every per-cell
+    array of the batch (initial fields, primitives, conserved state, dU/dt) is
+    the cases' arrays stacked; ``split`` cuts one back into per-case pieces.
+    Each case keeps its own boundary conditions and Runge-Kutta control, so
+    ``take_steps`` advances every case by one step of its own dt.  The source
+    ``Simulation`` objects are left unchanged."""
+
+    def __init__(self, cases):
+        L = _lib.load()
+        cases = list(cases)
+        arr = (C.c_void_p * len(cases))(*[c._h.value for c in cases])
+        h = C.c_void_p()
+        check(L.ibisgb_batch_create(arr, len(cases), C.byref(h)), None)
+        self.config = cases[0].config
+        self._attach(h)
+        n = C.c_int32()
+        check(L.ibisgb_batch_layout(h, C.byref(n), None, None, None), h)
+        self.n_cases = n.value
+        self.cell_offsets = np.zeros(self.n_cases + 1, np.int64)
+        self.face_offsets = np.zeros(self.n_cases + 1, np.int64)
+        self.ghost_offsets = np.zeros(self.n_cases + 1, np.int64)
+        check(L.ibisgb_batch_layout(h, None, _ptr(self.cell_offsets), _ptr(self.face_offsets),
+                                    _ptr(self.ghost_offsets)), h)
+
+    def split(self, a):
+        """Per-case views of an array whose first axis runs over the batch's valid cells."""
+        return [a[self.cell_offsets[c]:self.cell_offsets[c + 1]] for c in range(self.n_cases)]
+
+    def case_status(self) -> list:
+        """Runge-Kutta status of every case after the last ``take_steps``."""
+        st = (RkStatus * self.n_cases)()
+        self._call("ibisgb_batch_status", st)
+        return [{"t": x.t, "dt": x.dt, "stable_dt": x.stable_dt, "steps": x.steps,
+                 "bad_cells": x.bad_cells} for x in st]

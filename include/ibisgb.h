@@ -211,6 +211,38 @@ int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status*
 /* Wait for all work on the context's stream. */
 int ibisgb_synchronize(ibisgb_ctx* ctx);
 
+/* Batched ensembles (no counterpart in the reference, which runs one case per
+ * process through Solver::solve, src/solvers/solvers/solver.cpp:25-59).
+ * Merges already-created single-case contexts into one new context whose valid
+ * cells are the cases' cells concatenated in case order, followed by the ghost
+ * cells of all cases; faces and boundaries are concatenated in case order too.
+ * The cases must share the dimension, flux calculator, reconstruction, limiter,
+ * gas and transport settings and the Runge-Kutta tableau; each keeps its own
+ * grid, boundary conditions (inflow states) and Runge-Kutta control (CFL
+ * schedule, max_time, dt_init, and its own t and dt), so one ibisgb_rk_run
+ * advances every case by one step of its own dt in the same kernel launches,
+ * with the results of running each case alone.  A case that reaches max_time
+ * or gets bad cells stops while the others go on.  The batch starts without
+ * state: pass the cases' fields, concatenated in case order, to
+ * ibisgb_set_primitives.  On a batch, ibisgb_rk_run's status holds the minimum
+ * t, dt and stable_dt, the maximum step count and the total bad cells over the
+ * cases, ibisgb_estimate_dt the minimum over the cases, ibisgb_l2_norms the
+ * norms over all cells of all cases, and the steady-state calls are rejected
+ * (IBISGB_ERR_STATE).  The source contexts are not changed and may be destroyed
+ * afterwards. */
+int ibisgb_batch_create(ibisgb_ctx* const* cases, int32_t n_cases, ibisgb_ctx** out);
+
+/* Number of cases of a context (1 for a single case) and, for each case, the
+ * first index of its valid cells, faces and ghost cells (n_cases + 1 entries
+ * each, the last one the total; ghost offsets count from N).  Array arguments
+ * may be NULL. */
+int ibisgb_batch_layout(const ibisgb_ctx* ctx, int32_t* n_cases, int64_t* cell_offsets,
+                        int64_t* face_offsets, int64_t* ghost_offsets);
+
+/* Runge-Kutta status of every case (n_cases entries) after the last
+ * ibisgb_rk_run; device_ms is that of the whole call. */
+int ibisgb_batch_status(ibisgb_ctx* ctx, ibisgb_rk_status* per_case);
+
 /* Largest residual (in cells) that ibisgb_l2_norms_noalloc accepts.  Its
  * scratch is one fixed array of 4096 x 6 doubles (192 KiB) that every GPU
  * which loads the library keeps until the process exits. */
