@@ -299,13 +299,12 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = measured_peak_hbm()
     stage_ms = ms_mixed / args.steps / 3.0
     achieved = B_ALG_3D["mixed"] * N / (stage_ms / 1e3) / 1e9
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "rk_stage_box_mixed_traffic.json")
+    traffic = None  # DRAM bytes of one stage (recon + face + update) from the committed ncu summary
+    tfile = os.path.join(ROOT, "profiles", "rk_stage_box128_mixed_full.md")
     if os.path.exists(tfile):
-        with open(tfile) as f:
-            t = json.load(f)
-        if t.get("n") == n:
-            traffic = t["dram_bytes_per_stage"]
+        for line in open(tfile):
+            if line.startswith(f"traffic_bytes_per_stage_{n}:"):
+                traffic = float(line.split(":")[1].split()[0])
 
     batch = batch_measure(args, barrier) if args.batch_cases > 0 else None
 
