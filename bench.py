@@ -335,7 +335,9 @@ def run_ours(args, world, rank, local):
             "roofline": {"bound": "hbm", "kernel": "rk_stage (recon + face + update kernels of one stage)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "bytes_per_cell_update": B_ALG_3D["mixed"],
-                         "traffic": traffic},
+                         "traffic": traffic, "traffic_per_cell_update": traffic / N if traffic else None,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage "
+                                           "at 128^3, scaled by 8 (profiles/rk_stage_box128_mixed_full.md)"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 8 * nc * N,
                     "d2h_bytes_per_step": 8 * nc * N, "steps": e2e_steps},
