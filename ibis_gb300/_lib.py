@@ -88,6 +88,9 @@ def load(build_if_missing: bool = True):
     L.ibisgb_jvp_device.argtypes = [_P, _P, _P, C.c_double, C.c_int32, _P]
     L.ibisgb_steady_initialise.argtypes = [_P, C.c_int32]
     L.ibisgb_newton_step.argtypes = [_P, C.c_int32, C.POINTER(NewtonStatus)]
+    L.ibisgb_autotune.argtypes = [_P, C.c_int32, _P, _P]
+    L.ibisgb_set_launch_variants.argtypes = [_P, C.c_int32, _P]
+    L.ibisgb_launch_variants.argtypes = [C.POINTER(C.c_int32), _P, _P]
     L.ibisgb_batch_create.argtypes = [_P, C.c_int32, C.POINTER(_P)]
     L.ibisgb_batch_layout.argtypes = [_P, C.POINTER(C.c_int32), _P, _P, _P]
     L.ibisgb_batch_status.argtypes = [_P, _P]

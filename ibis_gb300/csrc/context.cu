@@ -157,6 +157,11 @@ struct ibisgb_ctx {
     std::vector<double> ic_prims;  // host IC primitives (7 x NT), kept until the first update
     bool have_state = false;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    // launch variants of recon / face / update per precision (autotuned)
+    int var[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    bool tuned[3] = {false, false, false};
+    double tune_ms[3][3][kNumVariants] = {};
+    static int gidx(int prec) { return prec == IBISGB_MIXED ? 1 : (prec == IBISGB_F64_EXACT ? 2 : 0); }
     double last_l2[6] = {0, 0, 0, 0, 0, 0};
     double last_ms = 0.0;
 
@@ -224,6 +229,7 @@ struct ibisgb_ctx {
             prm.fgamma = (float)prm.gamma; prm.fgR = prm.fgamma * prm.fR; prm.feps = (float)prm.eps;
             prm.fdelta = (float)prm.delta; prm.fmu0 = (float)prm.mu0; prm.fT0 = (float)prm.T0;
             prm.fTs = (float)prm.Ts; prm.fPr = (float)prm.Pr; prm.inv_Cv = 1.0 / prm.Cv;
+            prm.finv_Cv = (float)prm.inv_Cv;
             const Json& solver = config.at("solver");
             if (solver.at("name").as_string() == "runge_kutta") parse_rk(solver);
             if (solver.at("name").as_string() == "steady_state") parse_steady(solver);
@@ -622,9 +628,10 @@ struct ibisgb_ctx {
             v.branches = branches.as<unsigned>();
         }
         bool reco = prm.order == 2;
-        o.recon(v, prm, reco, stream);
-        o.face_flux(v, prm, reco, stream);
-        o.update(v, prm, 0, 0, out_device, stream);
+        const int* vr = var[gidx(prec)];
+        o.recon(v, prm, reco, vr[0], stream);
+        o.face_flux(v, prm, reco, vr[1], stream);
+        o.update(v, prm, 0, 0, out_device, 0, vr[2], stream);
         CUDA_OK(cudaGetLastError());
     }
 
@@ -652,9 +659,24 @@ struct ibisgb_ctx {
         KernelOps o = ops(prec);
         const bool reco = prm.order == 2;
         const int S = ctl_host.stages;
-        o.recon(v, prm, reco, stream);
-        o.face_flux(v, prm, reco, stream);
-        o.update(v, prm, 1, 0, nullptr, stream);
+        const int* vr = var[gidx(prec)];
+        if (!prm.viscous) {
+            // Inviscid: the step's dt depends only on the primitives of U^n, so
+            // the previous step's last update (or rk_run's prologue) has already
+            // min-reduced it; the first stage's update then forms the next
+            // stage state directly, and the last one reduces the next step's dt.
+            launch_dt_finalize(v.ctl, n_cases, stream);
+            for (int s = 0; s < S; s++) {
+                o.recon(v, prm, reco, vr[0], stream);
+                o.face_flux(v, prm, reco, vr[1], stream);
+                o.update(v, prm, s == S - 1 ? 3 : 2, s, nullptr, s == S - 1, vr[2], stream);
+            }
+            return;
+        }
+        // Viscous: the dt signal needs the viscous face state of stage 0.
+        o.recon(v, prm, reco, vr[0], stream);
+        o.face_flux(v, prm, reco, vr[1], stream);
+        o.update(v, prm, 1, 0, nullptr, 0, vr[2], stream);
         o.local_dt(v, prm, stream);
         launch_dt_finalize(v.ctl, n_cases, stream);
         if (S == 1) {
@@ -663,16 +685,17 @@ struct ibisgb_ctx {
         }
         o.combine(v, prm, 1, stream);
         for (int s = 1; s < S; s++) {
-            o.recon(v, prm, reco, stream);
-            o.face_flux(v, prm, reco, stream);
-            o.update(v, prm, s == S - 1 ? 3 : 2, s, nullptr, stream);
+            o.recon(v, prm, reco, vr[0], stream);
+            o.face_flux(v, prm, reco, vr[1], stream);
+            o.update(v, prm, s == S - 1 ? 3 : 2, s, nullptr, 0, vr[2], stream);
         }
     }
 
     void rk_run(int prec, int64_t n, ibisgb_rk_status* st) {
         if (!rk_configured) throw ConfigError("config.json solver is not runge_kutta");
         ensure_prims(prec);
-        int gi = prec == IBISGB_MIXED ? 1 : (prec == IBISGB_F64_EXACT ? 2 : 0);
+        int gi = gidx(prec);
+        if (!tuned[gi]) autotune(prec);
         if (!graph[gi]) {
             cudaGraph_t g;
             CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -682,6 +705,12 @@ struct ibisgb_ctx {
             CUDA_OK(le);
             CUDA_OK(cudaGraphInstantiate(&graph[gi], g, 0));
             CUDA_OK(cudaGraphDestroy(g));
+        }
+        if (!prm.viscous && n > 0) {  // local dt of the current state for the first step
+            DevView v = view(prec);
+            launch_reset_dt(v.ctl, n_cases, stream);
+            ops(prec).local_dt(v, prm, stream);
+            CUDA_OK(cudaGetLastError());
         }
         cudaEvent_t e0, e1;
         CUDA_OK(cudaEventCreate(&e0));
@@ -963,6 +992,73 @@ struct ibisgb_ctx {
         std::swap(kscal.p, pscal.p); std::swap(kscal.bytes, pscal.bytes);
     }
 
+    // Launch-variant autotuner: times every variant of the recon, face and update
+    // kernels on this grid and state (CUDA events, one warm-up launch and three
+    // timed ones each; update in its residual-only mode) and keeps the fastest.
+    // A variant must be 2% faster than the lower-numbered best to be chosen.
+    // Every variant computes the same bits, so tuning changes only the speed.
+    // Leaves the residual of the current state in stage 0 of k.
+    void autotune(int prec) {
+        ensure_prims(prec);
+        const int gi = gidx(prec);
+        int* vr = var[gi];
+        vr[0] = vr[1] = vr[2] = 0;
+        if (prec != IBISGB_F64_EXACT) {
+            DevView v = view(prec);
+            KernelOps o = ops(prec);
+            const bool reco = prm.order == 2;
+            cudaEvent_t e0, e1;
+            CUDA_OK(cudaEventCreate(&e0));
+            CUDA_OK(cudaEventCreate(&e1));
+            auto timed = [&](const std::function<void()>& launch) {
+                launch();
+                CUDA_OK(cudaEventRecord(e0, stream));
+                for (int r = 0; r < 3; r++) launch();
+                CUDA_OK(cudaEventRecord(e1, stream));
+                CUDA_OK(cudaGetLastError());
+                CUDA_OK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+                return ms / 3.0;
+            };
+            for (int k = 0; k < 3; k++) {
+                if (k == 0 && !reco && !prm.viscous) continue;  // no recon kernel
+                double best = 0.0;
+                for (int w = 0; w < kNumVariants; w++) {
+                    double t;
+                    if (k == 0) t = timed([&] { o.recon(v, prm, reco, w, stream); });
+                    else if (k == 1) t = timed([&] { o.face_flux(v, prm, reco, w, stream); });
+                    else t = timed([&] { o.update(v, prm, 0, 0, nullptr, 0, w, stream); });
+                    tune_ms[gi][k][w] = t;
+                    if (w == 0 || t < 0.98 * best) { best = t; vr[k] = w; }
+                }
+                // leave the chosen kernel's outputs for the next kernel's timing
+                if (k == 0) o.recon(v, prm, reco, vr[0], stream);
+                if (k == 1) o.face_flux(v, prm, reco, vr[1], stream);
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
+        tuned[gi] = true;
+        if (graph[gi]) {
+            cudaGraphExecDestroy(graph[gi]);
+            graph[gi] = nullptr;
+        }
+    }
+
+    void set_variants(int prec, const int* w) {
+        const int gi = gidx(prec);
+        for (int k = 0; k < 3; k++) {
+            if (w[k] < 0 || w[k] >= kNumVariants) throw ArgError("launch variant out of range");
+            var[gi][k] = prec == IBISGB_F64_EXACT ? 0 : w[k];
+        }
+        tuned[gi] = true;
+        if (graph[gi]) {
+            cudaGraphExecDestroy(graph[gi]);
+            graph[gi] = nullptr;
+        }
+    }
+
     void kernel_times(int prec, int reps, double out[4]) {
         ensure_prims(prec);
         DevView v = view(prec);
@@ -973,11 +1069,12 @@ struct ibisgb_ctx {
         double acc[4] = {0, 0, 0, 0};
         for (int r = 0; r < reps + 1; r++) {  // first round is a warm-up
             CUDA_OK(cudaEventRecord(ev[0], stream));
-            o.recon(v, prm, reco, stream);
+            const int* vr = var[gidx(prec)];
+            o.recon(v, prm, reco, vr[0], stream);
             CUDA_OK(cudaEventRecord(ev[1], stream));
-            o.face_flux(v, prm, reco, stream);
+            o.face_flux(v, prm, reco, vr[1], stream);
             CUDA_OK(cudaEventRecord(ev[2], stream));
-            o.update(v, prm, 0, 0, nullptr, stream);
+            o.update(v, prm, 0, 0, nullptr, 0, vr[2], stream);
             CUDA_OK(cudaEventRecord(ev[3], stream));
             CUDA_OK(cudaGetLastError());
             CUDA_OK(cudaEventSynchronize(ev[3]));
@@ -1398,6 +1495,39 @@ int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status*
         if (precision < 0 || precision > 2) throw ArgError("unknown precision");
         ctx->newton_step(precision, status);
     });
+}
+
+int ibisgb_autotune(ibisgb_ctx* ctx, int32_t precision, int32_t variants[3], double* times_ms) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        ctx->autotune(precision);
+        const int gi = ibisgb_ctx::gidx(precision);
+        for (int k = 0; k < 3; k++) {
+            if (variants) variants[k] = ctx->var[gi][k];
+            if (times_ms)
+                for (int w = 0; w < kNumVariants; w++) times_ms[k * kNumVariants + w] = ctx->tune_ms[gi][k][w];
+        }
+    });
+}
+
+int ibisgb_set_launch_variants(ibisgb_ctx* ctx, int32_t precision, const int32_t variants[3]) {
+    if (!ctx || !variants) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        int w[3] = {variants[0], variants[1], variants[2]};
+        ctx->set_variants(precision, w);
+    });
+}
+
+int ibisgb_launch_variants(int32_t* count, int32_t* threads, int32_t* min_blocks) {
+    if (!count) return IBISGB_ERR_ARG;
+    *count = kNumVariants;
+    for (int w = 0; w < kNumVariants; w++) {
+        if (threads) threads[w] = kVariantThreads[w];
+        if (min_blocks) min_blocks[w] = kVariantMinBlocks[w];
+    }
+    return IBISGB_OK;
 }
 
 int ibisgb_batch_create(ibisgb_ctx* const* cases, int32_t n_cases, ibisgb_ctx** out) {

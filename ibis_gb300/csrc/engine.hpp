@@ -54,7 +54,7 @@ struct FvParams {
     double mu0, T0, Ts, Pr;
     // float copies for the float kernels (rounded on the host, so that the
     // device does no double->float conversions) and host-side reciprocals
-    float fR, fCv, fCp, fgamma, fgR, feps, fdelta, fmu0, fT0, fTs, fPr;
+    float fR, fCv, fCp, fgamma, fgR, feps, fdelta, fmu0, fT0, fTs, fPr, finv_Cv;
     double inv_Cv;
 };
 
@@ -119,18 +119,28 @@ struct DevView {
 };
 
 // Launch entry points of one kernel build (one arithmetic).
+// Launch variants of the stage kernels (recon, face, update) for the
+// autotuner: threads per block and minimum resident blocks per SM (which caps
+// the registers per thread at 65536 / (threads x blocks)).  The FP64_EXACT
+// build always uses variant 0.
+constexpr int kNumVariants = 5;
+constexpr int kVariantThreads[kNumVariants] = {256, 256, 256, 256, 512};
+constexpr int kVariantMinBlocks[kNumVariants] = {1, 3, 4, 5, 2};
+
 struct KernelOps {
     // ghosts from their source cells (pre-reconstruction and pre-viscous actions)
     void (*ghost_fill)(const DevView&, const FvParams&, cudaStream_t);
     // gradients + limiters (+ viscous gradients) of every valid cell
-    void (*recon)(const DevView&, const FvParams&, bool reconstruct, cudaStream_t);
+    void (*recon)(const DevView&, const FvParams&, bool reconstruct, int variant, cudaStream_t);
     // face fluxes (convective + viscous)
-    void (*face_flux)(const DevView&, const FvParams&, bool reconstruct, cudaStream_t);
+    void (*face_flux)(const DevView&, const FvParams&, bool reconstruct, int variant, cudaStream_t);
     // surface integral into stage `stage`; mode: 0 residual only (writes k[stage]),
-    // 1 stage 0 of a step (+ local dt min), 2 intermediate stage (+ next stage state),
-    // 3 last stage (+ solution update). out_rowmajor: optional N x nc output of dU/dt.
+    // 1 stage 0 of a step whose dt is not known yet, 2 a stage followed by another
+    // (+ next stage state), 3 last stage (+ solution update). with_dt: also min-reduce
+    // the local time step of the new state into the control blocks (mode 3 only).
+    // out_rowmajor: optional N x nc output of dU/dt.
     void (*update)(const DevView&, const FvParams&, int mode, int stage, double* out_rowmajor,
-                   cudaStream_t);
+                   int with_dt, int variant, cudaStream_t);
     // stage-1 state U + a(1,0) dt k0 -> primitives and ghosts (after dt is known)
     void (*combine)(const DevView&, const FvParams&, int stage, cudaStream_t);
     // primitives (and ghosts) from U

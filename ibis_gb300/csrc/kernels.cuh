@@ -170,8 +170,14 @@ __global__ void __launch_bounds__(kBlock) k_ghost_fill(DevView v, FvParams prm) 
 // k_recon: gradients (WLSGradient::compute_gradients, gradient.h:65-116) and
 // Barth-Jespersen limiters (limiter.cpp:119-159) of every valid cell.
 // ---------------------------------------------------------------------------
-template <class R, class P, class Gm, int DIM, bool EXACT>
-__global__ void __launch_bounds__(kBlock) k_recon(DevView v, FvParams prm, int reconstruct) {
+// The float build stores limiter-scaled gradients (phi * grad) instead of
+// gradients and limiters: the face reconstruction then reads 15 values per side
+// instead of 20.
+template <class P, bool EXACT>
+constexpr bool prescaled_gradients() { return !EXACT && sizeof(P) == sizeof(float); }
+
+template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
+__global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int reconstruct) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     constexpr int NV = DIM == 3 ? 5 : 4;  // reconstructed variables (vz only in 3-D)
@@ -305,13 +311,19 @@ __global__ void __launch_bounds__(kBlock) k_recon(DevView v, FvParams prm, int r
                     if (tneg[q] < R(0.0)) phi[q] = d_min(phi[q], (umin[q] - ui[q]) / (tneg[q] - eps));
                 }
             }
-            P* pout = (P*)v.phi;
+            if (!prescaled_gradients<P, EXACT>()) {
+                P* pout = (P*)v.phi;
 #pragma unroll
-            for (int q = 0; q < NV; q++) pout[q * N + i] = (P)phi[q];
+                for (int q = 0; q < NV; q++) pout[q * N + i] = (P)phi[q];
+            }
             if (v.branches) {
 #pragma unroll
                 for (int q = 0; q < 5; q++) v.branches[i * 5 + q] = q < NV ? code[q] : 0u;
             }
+        }
+        if constexpr (prescaled_gradients<P, EXACT>()) {
+#pragma unroll
+            for (int q = 0; q < NV; q++) { gx[q] = gx[q] * phi[q]; gy[q] = gy[q] * phi[q]; gz[q] = gz[q] * phi[q]; }
         }
 #pragma unroll
         for (int q = 0; q < NV; q++) {
@@ -342,8 +354,8 @@ IBISGB_HD R lin_interp(R value, R lim, const P* g, int N, int q, int c, R dx, R 
     return value + lim * s;
 }
 
-template <class R, class P, class Gm, int DIM, bool EXACT>
-__global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int reconstruct) {
+template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
+__global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int reconstruct) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.F) return;
     const int N = v.N, NT = v.NT, F = v.F, G = v.G;
@@ -354,9 +366,26 @@ __global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int re
     const P* ph = (const P*)v.phi;
     const Gas<R> gm(prm);
     const R nx = (R)fg[f], ny = (R)fg[F + f], nz = DIM == 3 ? (R)fg[2 * F + f] : R(0.0);
-    const R t1x = (R)fg[3 * F + f], t1y = (R)fg[4 * F + f], t1z = DIM == 3 ? (R)fg[5 * F + f] : R(0.0);
-    const R t2x = DIM == 3 ? (R)fg[6 * F + f] : R(0.0), t2y = DIM == 3 ? (R)fg[7 * F + f] : R(0.0);
-    const R t2z = (R)fg[8 * F + f];
+    R t1x, t1y, t1z, t2x, t2y, t2z;
+    if constexpr (!EXACT && sizeof(R) == sizeof(float) && DIM == 3) {
+        // The float build rotates into a frame built from n (any orthonormal
+        // tangents give the same flux up to rounding): t1 = n x e / |n x e| for
+        // the axis e of n's smallest component, t2 = n x t1.
+        const R ax = d_abs(nx), ay = d_abs(ny), az = d_abs(nz);
+        const bool ex = ax <= ay && ax <= az, ey = !ex && ay <= az;
+        t1x = ex ? R(0.0) : (ey ? -nz : ny);
+        t1y = ex ? nz : (ey ? R(0.0) : -nx);
+        t1z = ex ? -ny : (ey ? nx : R(0.0));
+        const R inv = rsqrtf(t1x * t1x + t1y * t1y + t1z * t1z);
+        t1x *= inv; t1y *= inv; t1z *= inv;
+        t2x = ny * t1z - nz * t1y;
+        t2y = nz * t1x - nx * t1z;
+        t2z = nx * t1y - ny * t1x;
+    } else {
+        t1x = (R)fg[3 * F + f]; t1y = (R)fg[4 * F + f]; t1z = DIM == 3 ? (R)fg[5 * F + f] : R(0.0);
+        t2x = DIM == 3 ? (R)fg[6 * F + f] : R(0.0); t2y = DIM == 3 ? (R)fg[7 * F + f] : R(0.0);
+        t2z = (R)fg[8 * F + f];
+    }
     const R fx = (R)fg[9 * F + f], fy = (R)fg[10 * F + f], fz = DIM == 3 ? (R)fg[11 * F + f] : R(0.0);
     int ia, ib;
     thermo_vars(prm.thermo, ia, ib);
@@ -366,11 +395,15 @@ __global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int re
     for (int side = 0; side < 2; side++) {
         const int c = cells[side];
         R q[7];
+        // with reconstruction both sides pass through the thermo closure, which
+        // overwrites the two thermodynamic values that are not interpolated
 #pragma unroll
-        for (int k = 0; k < 7; k++) q[k] = (DIM == 2 && k == 6) ? R(0.0) : (R)pr[k * NT + c];
+        for (int k = 0; k < 7; k++)
+            q[k] = (DIM == 2 && k == 6) || (reconstruct && k < 4 && k != ia && k != ib) ? R(0.0)
+                                                                                    : (R)pr[k * NT + c];
         if (reconstruct && c < N) {
             R dx = fx - (R)cc[c], dy = fy - (R)cc[NT + c], dz = DIM == 3 ? fz - (R)cc[2 * NT + c] : R(0.0);
-            const bool lim = prm.limiter != 0;
+            const bool lim = prm.limiter != 0 && !prescaled_gradients<P, EXACT>();
             auto L = [&](int k) { return lim ? (R)ph[k * N + c] : R(1.0); };
             q[ia] = lin_interp<R, P, DIM>(q[ia], L(0), gr, N, 0, c, dx, dy, dz);
             q[ib] = lin_interp<R, P, DIM>(q[ib], L(1), gr, N, 1, c, dx, dy, dz);
@@ -501,11 +534,45 @@ __global__ void __launch_bounds__(kBlock) k_face(DevView v, FvParams prm, int re
 // update, conserved->primitive inversion (primative_conserved_conversion.cpp:4-23)
 // and the ghost cells fed by this cell.
 // ---------------------------------------------------------------------------
+// 1/x in double for x > 0 of normal range: the hardware's approximate reciprocal
+// (PTX rcp.approx.ftz.f64) refined by two Newton-Raphson steps r <- r + r (1 - x r),
+// each of which squares the relative error; the result is within an ulp or so
+// of the correctly rounded reciprocal.
+__device__ __forceinline__ double recip_newton(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+
 template <class P, class Gm, int DIM, bool EXACT>
 __device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, const double* u) {
     // conserved_to_primatives in double (primative_conserved_conversion.cpp:4-23); the fast
     // paths replace the divisions by one reciprocal (the FP64 pipe is GB300's scarcest unit)
     double rho = u[0], vx, vy, vz, e, T;
+    if (!EXACT && sizeof(P) == sizeof(float)) {
+        // Mixed build: rho, v and e = E/rho - |v|^2/2 in double (the cancellation of
+        // strong expansions happens there); T = e/Cv and p = rho R T are products of
+        // values already rounded to float, so they are formed in float.
+        const double ir = rho > 0.0 ? recip_newton(rho) : 1.0 / rho;
+        vx = u[1] * ir;
+        vy = u[2] * ir;
+        vz = DIM == 3 ? u[3] * ir : 0.0;
+        double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
+        e = u[DIM + 1] * ir - ke;
+        const float rf = (float)rho, ef = (float)e;
+        const float Tf = ef * prm.finv_Cv;
+        const float pf = rf * prm.fR * Tf;
+        P* pr = (P*)v.prim;
+        const int NT = v.NT;
+        pr[i] = (P)rf; pr[NT + i] = (P)pf; pr[2 * NT + i] = (P)Tf; pr[3 * NT + i] = (P)ef;
+        pr[4 * NT + i] = (P)vx; pr[5 * NT + i] = (P)vy; pr[6 * NT + i] = (P)vz;
+        const State64 s{rho, (double)pf, (double)Tf, e, vx, vy, vz};
+        for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
+        return s;
+    }
     if (EXACT) {
         vx = u[1] / rho;
         vy = u[2] / rho;
@@ -536,8 +603,17 @@ __device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, co
 IBISGB_HD StepCtl* ctl_of(const DevView& v, int i) { return v.case_of ? v.ctl + v.case_of[i] : v.ctl; }
 
 // count_bad_cells (finite_volume.cpp:257-270)
+// T < 0, rho < 0, isnan(rho) or isinf(rho), tested on the bit patterns (the
+// same predicates for IEEE doubles, without the FP64 pipe)
+IBISGB_HD bool is_negative(double x) {  // x < 0.0: sign set, nonzero, not NaN
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+    return (b >> 63) && mag != 0 && mag <= 0x7FF0000000000000ull;
+}
 IBISGB_HD void count_bad(StepCtl* ctl, const State64& s) {
-    if (s.T < 0.0 || s.rho < 0.0 || isnan(s.rho) || isinf(s.rho)) atomicAdd(&ctl->bad_cells, 1ull);
+    const unsigned long long rb = (unsigned long long)__double_as_longlong(s.rho);
+    if (is_negative(s.T) || is_negative(s.rho) || ((rb >> 52) & 0x7FFull) == 0x7FFull)
+        atomicAdd(&ctl->bad_cells, 1ull);
 }
 
 // Error-free transformations for the float accumulation of the mixed build
@@ -550,11 +626,85 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
     lo = __fadd_rn(lo, err);
 }
 
+// Local CFL time step of valid cell i from its primitives (FiniteVolume::estimate_dt,
+// finite_volume.cpp:130-184).  The float build evaluates the inviscid signal in
+// float from its float state.
+template <class P, class Gm, int DIM>
+__device__ double cell_local_dt(const DevView& v, const FvParams& prm, int i, P pvx, P pvy, P pvz, P pT) {
+    const int N = v.N, F = v.F;
+    const Gm* fg = (const Gm*)v.face;
+    const int nf = v.nfaces[i];
+    double src = 0.0, srv = 0.0;
+    const double vol = v.vol[i];
+    if (sizeof(P) == sizeof(float)) {
+        const float vx = (float)pvx, vy = (float)pvy;
+        const float vz = DIM == 3 ? (float)pvz : 0.f;
+        const float a = sqrtf(prm.fgR * (float)pT);
+        float sf = 0.f;
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const float A = (float)fg[12 * F + f];
+            float dot = vx * (float)fg[f] + vy * (float)fg[F + f];
+            if (DIM == 3) dot += vz * (float)fg[2 * F + f];
+            sf += (fabsf(dot) + a) * A;
+            if (prm.viscous) srv += v.vsig[f] * (double)A * (double)A / vol;
+        }
+        src = (double)sf;
+    } else {
+        const double vx = (double)pvx, vy = (double)pvy, vz = (double)pvz;
+        const double a = sqrt(prm.gamma * prm.R * (double)pT);
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const double A = (double)fg[12 * F + f];
+            const double dot = vx * (double)fg[f] + vy * (double)fg[F + f] + vz * (double)fg[2 * F + f];
+            src += (fabs(dot) + a) * A;
+            if (prm.viscous) {
+                double tmp = v.vsig[f] * A * A;
+                srv += tmp / vol;
+            }
+        }
+    }
+    double local = vol / (src + prm.signal_factor * srv);
+    if (!(local > 0.0)) local = 1.0e308 * 10.0;
+    return local;
+}
+
+// Min-reduce the local time steps of a block into the control blocks' dt_bits
+// (bits of a positive double order like the double).  Every thread of the
+// block must call it; threads without a cell pass +inf.
+__device__ void reduce_local_dt(const DevView& v, int i, double local) {
+    if (v.case_of) {
+        // batched ensemble: one min per case; a warp whose cells share a case
+        // (the usual situation, cases are contiguous) reduces before its atomic
+        const int cs = i < v.N ? v.case_of[i] : -1;
+        const int c0 = __shfl_sync(0xffffffffu, cs, 0);
+        if (__all_sync(0xffffffffu, cs == c0)) {
+            for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_down_sync(0xffffffffu, local, o));
+            if ((threadIdx.x & 31) == 0 && c0 >= 0)
+                atomicMin(&v.ctl[c0].dt_bits, (unsigned long long)__double_as_longlong(local));
+        } else if (cs >= 0) {
+            atomicMin(&v.ctl[cs].dt_bits, (unsigned long long)__double_as_longlong(local));
+        }
+        return;
+    }
+    // warp-shuffle + block min, one atomic per block (blocks of up to 1024 threads)
+    for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_down_sync(0xffffffffu, local, o));
+    __shared__ double wmin[32];
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double m = threadIdx.x < (blockDim.x >> 5) ? wmin[threadIdx.x] : 1.0e308 * 10.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) atomicMin(&v.ctl->dt_bits, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// One valid cell of k_update; returns the local time step of the new state when
+// with_dt (mode 3), else +inf.
 template <class P, class Gm, int DIM, bool EXACT>
-__global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int mode, int stage,
-                                                   double* out_rm) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.N) return;
+__device__ __forceinline__ double update_cell(const DevView& v, const FvParams& prm, int i, int mode, int stage,
+                                              double* out_rm, int with_dt) {
+    constexpr double kInf = 1.0e308 * 10.0;
     constexpr int NC = DIM + 2;
     const int N = v.N, F = v.F;
     const Gm* area = (const Gm*)v.face + 12 * F;
@@ -609,9 +759,9 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
         kk[q * N + i] = ks[q];
         if (out_rm) out_rm[(size_t)i * NC + q] = ks[q];
     }
-    if (mode < 2) return;
+    if (mode < 2) return kInf;
     StepCtl* ctl = ctl_of(v, i);
-    if (ctl->halt) return;
+    if (ctl->halt) return kInf;
     double u[NC];
 #pragma unroll
     for (int q = 0; q < NC; q++) u[q] = v.U[q * N + i];
@@ -619,7 +769,7 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
         // state of stage s+1 (runge_kutta.cpp:151-181)
         const int ns = stage + 1;
 #pragma unroll
-        for (int q = 0; q < NC; q++) u[q] = u[q] + v.k[q * N + i] * ctl->ca[ns][0];
+        for (int q = 0; q < NC; q++) u[q] = u[q] + (stage == 0 ? ks[q] : v.k[q * N + i]) * ctl->ca[ns][0];
         for (int j = 1; j < ns; j++) {
             if (ctl->a[ns][j] < 1e-14) continue;
             const double c = ctl->ca[ns][j];
@@ -630,20 +780,32 @@ __global__ void __launch_bounds__(kBlock) k_update(DevView v, FvParams prm, int 
             }
         }
         commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
-    } else {
-        // solution update (runge_kutta.cpp:185-193)
-        for (int j = 0; j < ctl->stages; j++) {
-            const double c = ctl->cb[j];
-#pragma unroll
-            for (int q = 0; q < NC; q++) {
-                double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
-                u[q] += kj * c;
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
-        count_bad(ctl, commit_state<P, Gm, DIM, EXACT>(v, prm, i, u));
+        return kInf;
     }
+    // solution update (runge_kutta.cpp:185-193)
+    for (int j = 0; j < ctl->stages; j++) {
+        const double c = ctl->cb[j];
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
+            double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
+            u[q] += kj * c;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
+    const State64 st = commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
+    count_bad(ctl, st);
+    if (!with_dt) return kInf;
+    return cell_local_dt<P, Gm, DIM>(v, prm, i, (P)st.vx, (P)st.vy, (P)st.vz, (P)st.T);
+}
+
+template <class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
+__global__ void __launch_bounds__(BS, MINB) k_update(DevView v, FvParams prm, int mode, int stage,
+                                                   double* out_rm, int with_dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double local = 1.0e308 * 10.0;
+    if (i < v.N) local = update_cell<P, Gm, DIM, EXACT>(v, prm, i, mode, stage, out_rm, with_dt);
+    if (with_dt) reduce_local_dt(v, i, local);
 }
 
 // Solution update from stored stage derivatives (single-stage tableaus, where
@@ -701,75 +863,17 @@ __global__ void __launch_bounds__(kBlock) k_prims_from_U(DevView v, FvParams prm
     commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
 }
 
-// Local CFL time step of each valid cell, min-reduced into ctl->dt_bits
-// (FiniteVolume::estimate_dt, finite_volume.cpp:130-184).  The mixed build
-// evaluates the inviscid signal in float from its float state.
+// Local CFL time step of each valid cell, min-reduced into ctl->dt_bits.
 template <class P, class Gm, int DIM>
 __global__ void __launch_bounds__(kBlock) k_local_dt(DevView v, FvParams prm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double local = 1.0e308 * 10.0;
     if (i < v.N) {
-        const int N = v.N, F = v.F, NT = v.NT;
-        const Gm* fg = (const Gm*)v.face;
         const P* pr = (const P*)v.prim;
-        const int nf = v.nfaces[i];
-        double src = 0.0, srv = 0.0;
-        const double vol = v.vol[i];
-        if (sizeof(P) == sizeof(float)) {
-            const float vx = (float)pr[4 * NT + i], vy = (float)pr[5 * NT + i];
-            const float vz = DIM == 3 ? (float)pr[6 * NT + i] : 0.f;
-            const float a = sqrtf(prm.fgR * (float)pr[2 * NT + i]);
-            float sf = 0.f;
-            for (int s = 0; s < nf; s++) {
-                const int f = v.cell_face[s * N + i];
-                const float A = (float)fg[12 * F + f];
-                float dot = vx * (float)fg[f] + vy * (float)fg[F + f];
-                if (DIM == 3) dot += vz * (float)fg[2 * F + f];
-                sf += (fabsf(dot) + a) * A;
-                if (prm.viscous) srv += v.vsig[f] * (double)A * (double)A / vol;
-            }
-            src = (double)sf;
-        } else {
-            const double vx = (double)pr[4 * NT + i], vy = (double)pr[5 * NT + i], vz = (double)pr[6 * NT + i];
-            const double a = sqrt(prm.gamma * prm.R * (double)pr[2 * NT + i]);
-            for (int s = 0; s < nf; s++) {
-                const int f = v.cell_face[s * N + i];
-                const double A = (double)fg[12 * F + f];
-                const double dot = vx * (double)fg[f] + vy * (double)fg[F + f] + vz * (double)fg[2 * F + f];
-                src += (fabs(dot) + a) * A;
-                if (prm.viscous) {
-                    double tmp = v.vsig[f] * A * A;
-                    srv += tmp / vol;
-                }
-            }
-        }
-        local = vol / (src + prm.signal_factor * srv);
-        if (!(local > 0.0)) local = 1.0e308 * 10.0;
+        const int NT = v.NT;
+        local = cell_local_dt<P, Gm, DIM>(v, prm, i, pr[4 * NT + i], pr[5 * NT + i], pr[6 * NT + i], pr[2 * NT + i]);
     }
-    if (v.case_of) {
-        // batched ensemble: one min per case; a warp whose cells share a case
-        // (the usual situation, cases are contiguous) reduces before its atomic
-        const int cs = i < v.N ? v.case_of[i] : -1;
-        const int c0 = __shfl_sync(0xffffffffu, cs, 0);
-        if (__all_sync(0xffffffffu, cs == c0)) {
-            for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_down_sync(0xffffffffu, local, o));
-            if ((threadIdx.x & 31) == 0 && c0 >= 0)
-                atomicMin(&v.ctl[c0].dt_bits, (unsigned long long)__double_as_longlong(local));
-        } else if (cs >= 0) {
-            atomicMin(&v.ctl[cs].dt_bits, (unsigned long long)__double_as_longlong(local));
-        }
-        return;
-    }
-    // warp-shuffle + block min, one atomic per block
-    for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_down_sync(0xffffffffu, local, o));
-    __shared__ double wmin[kBlock / 32];
-    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = local;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double m = threadIdx.x < kBlock / 32 ? wmin[threadIdx.x] : 1.0e308 * 10.0;
-        for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
-        if (threadIdx.x == 0) atomicMin(&v.ctl->dt_bits, (unsigned long long)__double_as_longlong(m));
-    }
+    reduce_local_dt(v, i, local);
 }
 
 // ---------------------------------------------------------------------------
@@ -780,19 +884,71 @@ struct Launch {
     static void ghost_fill(const DevView& v, const FvParams& p, cudaStream_t s) {
         if (v.G > 0) k_ghost_fill<P, Gm><<<blocks_for(v.G), kBlock, 0, s>>>(v, p);
     }
-    static void recon(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {
+    // Launch variants of the stage kernels (threads per block, minimum resident
+    // blocks per SM, which caps registers per thread), chosen per context by the
+    // autotuner; every variant computes bit-identical results.
+    template <int V>
+    static void recon_v(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {
+        constexpr int BS = kVariantThreads[V], MB = kVariantMinBlocks[V];
+        const unsigned g = (unsigned)((v.N + BS - 1) / BS);
+        if (v.dim == 3) k_recon<R, P, Gm, 3, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
+        else k_recon<R, P, Gm, 2, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
+    }
+    template <int V>
+    static void face_v(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {
+        constexpr int BS = kVariantThreads[V], MB = kVariantMinBlocks[V];
+        const unsigned g = (unsigned)((v.F + BS - 1) / BS);
+        if (v.dim == 3) k_face<R, P, Gm, 3, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
+        else k_face<R, P, Gm, 2, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
+    }
+    template <int V>
+    static void update_v(const DevView& v, const FvParams& p, int mode, int stage, double* out, int with_dt,
+                         cudaStream_t s) {
+        constexpr int BS = kVariantThreads[V], MB = kVariantMinBlocks[V];
+        const unsigned g = (unsigned)((v.N + BS - 1) / BS);
+        if (v.dim == 3) k_update<P, Gm, 3, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, mode, stage, out, with_dt);
+        else k_update<P, Gm, 2, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, mode, stage, out, with_dt);
+    }
+    static void recon(const DevView& v, const FvParams& p, bool reco, int var, cudaStream_t s) {
         if (!reco && !p.viscous) return;
-        if (v.dim == 3) k_recon<R, P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, reco);
-        else k_recon<R, P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, reco);
+        if constexpr (EXACT) {
+            recon_v<0>(v, p, reco, s);
+        } else {
+            switch (var) {
+                case 1: recon_v<1>(v, p, reco, s); break;
+                case 2: recon_v<2>(v, p, reco, s); break;
+                case 3: recon_v<3>(v, p, reco, s); break;
+                case 4: recon_v<4>(v, p, reco, s); break;
+                default: recon_v<0>(v, p, reco, s); break;
+            }
+        }
     }
-    static void face_flux(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {
-        if (v.dim == 3) k_face<R, P, Gm, 3, EXACT><<<blocks_for(v.F), kBlock, 0, s>>>(v, p, reco);
-        else k_face<R, P, Gm, 2, EXACT><<<blocks_for(v.F), kBlock, 0, s>>>(v, p, reco);
+    static void face_flux(const DevView& v, const FvParams& p, bool reco, int var, cudaStream_t s) {
+        if constexpr (EXACT) {
+            face_v<0>(v, p, reco, s);
+        } else {
+            switch (var) {
+                case 1: face_v<1>(v, p, reco, s); break;
+                case 2: face_v<2>(v, p, reco, s); break;
+                case 3: face_v<3>(v, p, reco, s); break;
+                case 4: face_v<4>(v, p, reco, s); break;
+                default: face_v<0>(v, p, reco, s); break;
+            }
+        }
     }
-    static void update(const DevView& v, const FvParams& p, int mode, int stage, double* out,
-                       cudaStream_t s) {
-        if (v.dim == 3) k_update<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
-        else k_update<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, mode, stage, out);
+    static void update(const DevView& v, const FvParams& p, int mode, int stage, double* out, int with_dt,
+                       int var, cudaStream_t s) {
+        if constexpr (EXACT) {
+            update_v<0>(v, p, mode, stage, out, with_dt, s);
+        } else {
+            switch (var) {
+                case 1: update_v<1>(v, p, mode, stage, out, with_dt, s); break;
+                case 2: update_v<2>(v, p, mode, stage, out, with_dt, s); break;
+                case 3: update_v<3>(v, p, mode, stage, out, with_dt, s); break;
+                case 4: update_v<4>(v, p, mode, stage, out, with_dt, s); break;
+                default: update_v<0>(v, p, mode, stage, out, with_dt, s); break;
+            }
+        }
     }
     static void combine(const DevView& v, const FvParams& p, int stage, cudaStream_t s) {
         if (v.dim == 3) k_combine<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);

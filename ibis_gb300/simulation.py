@@ -132,6 +132,33 @@ class Simulation:
         self._call("ibisgb_kernel_times", PRECISION[precision], int(reps), _ptr(out))
         return {"recon": out[0], "face": out[1], "update": out[2], "residual": out[3]}
 
+    # ------------------------------------------------------------ autotuner
+    @staticmethod
+    def launch_variants() -> list:
+        """The launch-variant table: (threads per block, minimum blocks per SM)."""
+        L = _lib.load()
+        n = C.c_int32()
+        check(L.ibisgb_launch_variants(C.byref(n), None, None))
+        th = np.zeros(n.value, np.int32)
+        mb = np.zeros(n.value, np.int32)
+        check(L.ibisgb_launch_variants(C.byref(n), _ptr(th), _ptr(mb)))
+        return list(zip(th.tolist(), mb.tolist()))
+
+    def autotune(self, precision: str = "mixed") -> dict:
+        """Time every launch variant of the recon, face and update kernels on this
+        grid and keep the fastest; returns the choice and the mean times (ms)."""
+        nv = len(self.launch_variants())
+        w = np.zeros(3, np.int32)
+        t = np.zeros(3 * nv)
+        self._call("ibisgb_autotune", PRECISION[precision], _ptr(w), _ptr(t))
+        t = t.reshape(3, nv)
+        return {"variants": dict(zip(("recon", "face", "update"), w.tolist())),
+                "ms": {k: t[i].round(4).tolist() for i, k in enumerate(("recon", "face", "update"))}}
+
+    def set_launch_variants(self, precision: str, recon: int, face: int, update: int) -> None:
+        w = np.array([recon, face, update], np.int32)
+        self._call("ibisgb_set_launch_variants", PRECISION[precision], _ptr(w))
+
     # ------------------------------------------------------------- residual
     def compute_dudt(self, precision: str = "f64") -> np.ndarray:
         """dU/dt of the valid cells, (N, n_conserved) in the reference's cell order."""

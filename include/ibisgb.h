@@ -211,6 +211,28 @@ int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status*
 /* Wait for all work on the context's stream. */
 int ibisgb_synchronize(ibisgb_ctx* ctx);
 
+/* Launch-configuration autotuner (no counterpart in the reference, whose
+ * kernels take Kokkos's default launch shape).  The recon, face and update
+ * kernels of the F64 and MIXED builds each come in ibisgb_launch_variants()
+ * launch variants (threads per block x minimum resident blocks per SM, which
+ * caps registers per thread).  ibisgb_autotune times every variant on the
+ * context's grid and current state (CUDA events; the update kernel in its
+ * residual-only mode), keeps the fastest and returns the choice in variants
+ * (recon, face, update) and, if times_ms is not NULL, the mean time of every
+ * variant (3 x count doubles, kernel-major).  ibisgb_rk_run tunes a precision
+ * by itself on its first call unless variants were set.  All variants give
+ * bit-identical results.  The residual of the current state is left as the
+ * first-stage derivative (what ibisgb_l2_norms reads).  F64_EXACT always uses
+ * variant 0. */
+int ibisgb_autotune(ibisgb_ctx* ctx, int32_t precision, int32_t variants[3], double* times_ms);
+
+/* Fix the launch variants (recon, face, update) of a precision instead of tuning. */
+int ibisgb_set_launch_variants(ibisgb_ctx* ctx, int32_t precision, const int32_t variants[3]);
+
+/* The variant table: count, and per variant the threads per block and minimum
+ * resident blocks per SM (arrays of at least count entries, may be NULL). */
+int ibisgb_launch_variants(int32_t* count, int32_t* threads, int32_t* min_blocks);
+
 /* Batched ensembles (no counterpart in the reference, which runs one case per
  * process through Solver::solve, src/solvers/solvers/solver.cpp:25-59).
  * Merges already-created single-case contexts into one new context whose valid

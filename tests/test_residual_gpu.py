@@ -160,3 +160,28 @@ def test_residual_into_torch_tensor():
     out = torch.empty((sim.num_cells, sim.n_conserved), dtype=torch.float64, device="cuda")
     sim.compute_dudt_into(out, "f64_exact", stream=torch.cuda.current_stream())
     assert np.array_equal(out.cpu().numpy(), ref.residual())
+
+
+@pytest.mark.parametrize("name", ["ramp", "box"])
+@pytest.mark.parametrize("precision", ["mixed", "f64"])
+def test_launch_variants_are_bit_identical(name, precision):
+    """Every launch variant of the autotuner computes the same bits."""
+    g, c, st = case(name)
+    nv = len(Simulation.launch_variants())
+    ref = None
+    for w in range(nv):
+        sim = Simulation(c, g)
+        sim.set_primitives(*st)
+        sim.set_launch_variants(precision, w, w, w)
+        sim.take_steps(4, precision)
+        U = sim.conserved()
+        if ref is None:
+            ref = U
+        assert np.array_equal(U, ref), w
+    sim = Simulation(c, g)
+    sim.set_primitives(*st)
+    tuned = sim.autotune(precision)
+    assert all(0 <= x < nv for x in tuned["variants"].values())
+    assert all(len(v) == nv and min(v) > 0 for v in tuned["ms"].values())
+    sim.take_steps(4, precision)
+    assert np.array_equal(sim.conserved(), ref)
