@@ -152,6 +152,7 @@ def batch_measure(args, barrier):
     # batched: every case in the same launches
     batch.set_primitives(*ic_all)
     tune = batch.autotune("mixed")
+    fused = batch.fused_info()
     batch.take_steps(args.warmup, "mixed")
     barrier()
     t0 = time.perf_counter()
@@ -181,6 +182,7 @@ def batch_measure(args, barrier):
     return {"workload": f"{len(sims)} independent 2-D compression ramps, {cells} cells in all, ssp-rk3, "
                         "Hanel, 2nd-order MUSCL + Barth-Jespersen, mixed precision",
             "cases": len(sims), "cells": cells, "autotune": tune["variants"],
+            "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")},
             "batched": {"value": upd_b / (ms_b / 1e3) / 1e6, "unit": "Mcell-updates/s",
                         "steps": args.batch_steps, "ms_per_step": ms_b / args.batch_steps,
                         "wall_value": upd_b / wall_b / 1e6},
@@ -252,6 +254,7 @@ def run_ours(args, world, rank, local):
     # --- headline: mixed precision, device-resident state
     sim.set_primitives(*ic)
     tune_mixed = sim.autotune("mixed")
+    fused = sim.fused_info()
     sim.take_steps(args.warmup, "mixed")
     barrier()
     with ClockSampler(local) as clk:
@@ -334,7 +337,8 @@ def run_ours(args, world, rank, local):
             "accuracy": {"rho_rel_l2_err_mixed_vs_f64": l2_err, "rho_rel_max_err_mixed_vs_f64": max_err,
                          "steps": args.warmup + args.steps},
             "kernel_ms": {k: round(v, 4) for k, v in kt.items()},
-            "autotune": {"variants_table": Simulation.launch_variants(), "mixed": tune_mixed, "f64": tune_f64},
+            "autotune": {"variants_table": Simulation.launch_variants(), "mixed": tune_mixed, "f64": tune_f64,
+                         "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")}},
             "batch": batch,
             "roofline": {"bound": "hbm", "kernel": "rk_stage (recon + face + update kernels of one stage)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -345,9 +349,9 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 8 * nc * N,
                     "d2h_bytes_per_step": 8 * nc * N, "steps": e2e_steps},
-            "gpu_launches": KERNELS_PER_STEP * args.steps + 2,
-            "gpu_launches_note": "kernels of the timed headline call: one graph of 10 kernels per step, "
-                                 "plus the reset and local-dt prologue of the call",
+            "gpu_launches": (4 if fused["enabled"] else KERNELS_PER_STEP) * args.steps + 2,
+            "gpu_launches_note": "kernels of the timed headline call: one graph per step (dt control + 3 fused "
+                                 "stages, or dt control + 3 x recon/face/update), plus the call's local-dt prologue",
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

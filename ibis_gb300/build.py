@@ -30,6 +30,7 @@ CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wa
 
 UNITS = {
     "mesh.cpp": "cxx",
+    "structured.cpp": "cxx",
     "context.cu": "nvcc",
     "kernels_common.cu": "nvcc",
     "kernels_f64.cu": "nvcc",

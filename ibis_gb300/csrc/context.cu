@@ -16,6 +16,7 @@
 #include "engine.hpp"
 #include "json_lite.hpp"
 #include "mesh.hpp"
+#include "structured.hpp"
 
 using namespace ibisgb;
 
@@ -162,11 +163,27 @@ struct ibisgb_ctx {
     bool tuned[3] = {false, false, false};
     double tune_ms[3][3][kNumVariants] = {};
     static int gidx(int prec) { return prec == IBISGB_MIXED ? 1 : (prec == IBISGB_F64_EXACT ? 2 : 0); }
+
+    // Fused stage on structured blocks (mixed build, inviscid, second order).
+    // The mixed primitives live in two buffers that the fused stages alternate
+    // between; prim_cur names the one holding the current state.
+    int fused_elig = -1;  // -1 not checked yet, 0 not eligible, 1 eligible
+    std::string fused_why;
+    StructuredLayout slay;
+    DBuf sb_blocks, sb_tiles, sb_face, sb_ghost, prim_alt;
+    bool fused_uploaded = false;
+    int prim_cur = 0;
+    int fused_mode = -1;  // -1 the autotuner decides, 0 off, 1 on
+    bool fused_on = false;
+    cudaGraphExec_t graph_fused[2] = {nullptr, nullptr};
+    double fused_ms = 0.0, generic_ms = 0.0;
     double last_l2[6] = {0, 0, 0, 0, 0, 0};
     double last_ms = 0.0;
 
     ~ibisgb_ctx() {
         for (auto& g : graph)
+            if (g) cudaGraphExecDestroy(g);
+        for (auto& g : graph_fused)
             if (g) cudaGraphExecDestroy(g);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -524,7 +541,8 @@ struct ibisgb_ctx {
         v.feed_off = feed_off.as<int>(); v.feed_ghost = feed_ghost.as<int>();
         v.cc = s.cc.p; v.r = s.r.p; v.face = s.face.p; v.vol = vol.as<double>();
         v.inv_vol = inv_vol.as<double>(); v.lsqw = s.lsqw.p;
-        v.prim = s.prim.p; v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
+        v.prim = (is_mixed(prec) && prim_cur) ? prim_alt.p : s.prim.p;
+        v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
         v.U = U.as<double>(); v.k = k.as<double>(); v.ctl = ctl.as<StepCtl>();
         v.case_of = n_cases > 1 ? case_of.as<int>() : nullptr;
@@ -545,10 +563,10 @@ struct ibisgb_ctx {
             const int64_t NT = mesh.NT();
             if (is_mixed(prec)) {
                 std::vector<float> f(ic_prims.begin(), ic_prims.end());
-                CUDA_OK(cudaMemcpyAsync(s.prim.p, f.data(), sizeof(float) * 7 * NT, cudaMemcpyHostToDevice, stream));
+                CUDA_OK(cudaMemcpyAsync(v.prim, f.data(), sizeof(float) * 7 * NT, cudaMemcpyHostToDevice, stream));
                 CUDA_OK(cudaStreamSynchronize(stream));
             } else {
-                CUDA_OK(cudaMemcpyAsync(s.prim.p, ic_prims.data(), sizeof(double) * 7 * NT, cudaMemcpyHostToDevice, stream));
+                CUDA_OK(cudaMemcpyAsync(v.prim, ic_prims.data(), sizeof(double) * 7 * NT, cudaMemcpyHostToDevice, stream));
             }
             ops(prec).ghost_fill(v, prm, stream);
         } else {
@@ -653,6 +671,73 @@ struct ibisgb_ctx {
         return dt;
     }
 
+    // Host-side eligibility of the fused stage (no GPU needed).
+    bool check_fused() {
+        if (fused_elig >= 0) return fused_elig == 1;
+        fused_elig = 0;
+        if (prm.viscous) fused_why = "viscous fluxes take the generic kernels";
+        else if (prm.order != 2) fused_why = "first-order reconstruction takes the generic kernels";
+        else {
+            std::vector<int64_t> offs = n_cases > 1 ? cell_off : std::vector<int64_t>{0, mesh.N};
+            int tx, ty, tz;
+            fused_tile_shape(mesh.dim, &tx, &ty, &tz);
+            if (detect_structured(mesh, offs, tx, ty, tz, slay, &fused_why)) {
+                fused_elig = 1;
+                fused_why.clear();
+            }
+        }
+        return fused_elig == 1;
+    }
+
+    void upload_fused() {
+        if (fused_uploaded) return;
+        ensure_device();
+        upload_geometry<float>(s32);
+        upload(sb_blocks, slay.blocks, stream);
+        upload(sb_tiles, slay.tiles, stream);
+        std::vector<float> fc(slay.face.begin(), slay.face.end());
+        upload(sb_face, fc, stream);
+        upload(sb_ghost, slay.ghost_map, stream);
+        prim_alt.alloc(sizeof(float) * 7 * mesh.NT());
+        CUDA_OK(prepare_fused_stage());
+        CUDA_OK(cudaStreamSynchronize(stream));
+        fused_uploaded = true;
+    }
+
+    SbView sb_view(void* prim_out) const {
+        SbView sb{};
+        sb.blocks = sb_blocks.as<SBlock>();
+        sb.tiles = sb_tiles.as<STile>();
+        sb.num_tiles = (int)slay.tiles.size();
+        sb.face = sb_face.as<float>();
+        sb.SF = (int)slay.num_faces;
+        sb.ghost_map = sb_ghost.as<int>();
+        sb.prim_out = prim_out;
+        return sb;
+    }
+    void* mixed_prim(int which) { return which ? prim_alt.p : s32.prim.p; }
+
+    // one fused Runge-Kutta step starting from primitive buffer `start`
+    void enqueue_fused_step(int start) {
+        const int S = ctl_host.stages;
+        DevView v = view(IBISGB_MIXED);
+        launch_dt_finalize(v.ctl, n_cases, stream);
+        int cur = start;
+        for (int s = 0; s < S; s++) {
+            v.prim = mixed_prim(cur);
+            launch_fused_stage(v, sb_view(mixed_prim(cur ^ 1)), prm, s == S - 1 ? 3 : 2, s, s == S - 1, stream);
+            cur ^= 1;
+        }
+    }
+
+    void drop_mixed_graphs() {
+        for (auto* g : {&graph[1], &graph_fused[0], &graph_fused[1]})
+            if (*g) {
+                cudaGraphExecDestroy(*g);
+                *g = nullptr;
+            }
+    }
+
     // one Runge-Kutta step (RungeKutta::take_step, runge_kutta.cpp:131-203)
     void enqueue_step(int prec) {
         DevView v = view(prec);
@@ -696,7 +781,20 @@ struct ibisgb_ctx {
         ensure_prims(prec);
         int gi = gidx(prec);
         if (!tuned[gi]) autotune(prec);
-        if (!graph[gi]) {
+        const bool fused = is_mixed(prec) && fused_on;
+        if (fused) {
+            for (int par = 0; par < 2; par++) {
+                if (graph_fused[par]) continue;
+                cudaGraph_t g;
+                CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                enqueue_fused_step(par);
+                cudaError_t le = cudaGetLastError();
+                CUDA_OK(cudaStreamEndCapture(stream, &g));
+                CUDA_OK(le);
+                CUDA_OK(cudaGraphInstantiate(&graph_fused[par], g, 0));
+                CUDA_OK(cudaGraphDestroy(g));
+            }
+        } else if (!graph[gi]) {
             cudaGraph_t g;
             CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             enqueue_step(prec);
@@ -716,7 +814,14 @@ struct ibisgb_ctx {
         CUDA_OK(cudaEventCreate(&e0));
         CUDA_OK(cudaEventCreate(&e1));
         CUDA_OK(cudaEventRecord(e0, stream));
-        for (int64_t i = 0; i < n; i++) CUDA_OK(cudaGraphLaunch(graph[gi], stream));
+        if (fused) {
+            for (int64_t i = 0; i < n; i++) {
+                CUDA_OK(cudaGraphLaunch(graph_fused[prim_cur], stream));
+                prim_cur ^= (ctl_host.stages & 1);
+            }
+        } else {
+            for (int64_t i = 0; i < n; i++) CUDA_OK(cudaGraphLaunch(graph[gi], stream));
+        }
         CUDA_OK(cudaEventRecord(e1, stream));
         state_changed(prec);
         last_ctl.resize(n_cases);
@@ -1036,6 +1141,16 @@ struct ibisgb_ctx {
                 if (k == 0) o.recon(v, prm, reco, vr[0], stream);
                 if (k == 1) o.face_flux(v, prm, reco, vr[1], stream);
             }
+            if (is_mixed(prec)) {
+                generic_ms = tune_ms[gi][0][vr[0]] + tune_ms[gi][1][vr[1]] + tune_ms[gi][2][vr[2]];
+                fused_ms = 0.0;
+                if (fused_mode != 0 && check_fused()) {
+                    upload_fused();
+                    SbView sb = sb_view(mixed_prim(prim_cur ^ 1));
+                    fused_ms = timed([&] { launch_fused_stage(v, sb, prm, 0, 0, 0, stream); });
+                }
+                fused_on = fused_mode == 1 || (fused_mode == -1 && fused_ms > 0.0 && fused_ms < generic_ms);
+            }
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
         }
@@ -1044,6 +1159,18 @@ struct ibisgb_ctx {
             cudaGraphExecDestroy(graph[gi]);
             graph[gi] = nullptr;
         }
+        if (is_mixed(prec)) drop_mixed_graphs();
+    }
+
+    // fused stage: -1 the autotuner decides, 0 never, 1 always (if eligible)
+    void set_fused(int mode) {
+        if (mode < -1 || mode > 1) throw ArgError("fused mode must be -1, 0 or 1");
+        if (mode == 1 && !check_fused()) throw ArgError("the fused stage does not apply: " + fused_why);
+        fused_mode = mode;
+        if (mode == 1) upload_fused();
+        if (mode >= 0) fused_on = mode == 1;
+        else tuned[1] = false;
+        drop_mixed_graphs();
     }
 
     void set_variants(int prec, const int* w) {
@@ -1528,6 +1655,25 @@ int ibisgb_launch_variants(int32_t* count, int32_t* threads, int32_t* min_blocks
         if (min_blocks) min_blocks[w] = kVariantMinBlocks[w];
     }
     return IBISGB_OK;
+}
+
+int ibisgb_set_fused(ibisgb_ctx* ctx, int32_t mode) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->set_fused(mode); });
+}
+
+int ibisgb_fused_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, double* times_ms, char* reason,
+                      int32_t reason_len) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        const bool el = ctx->check_fused();
+        if (eligible) *eligible = el ? 1 : 0;
+        if (enabled) *enabled = ctx->fused_on ? 1 : 0;
+        if (times_ms) { times_ms[0] = ctx->fused_ms; times_ms[1] = ctx->generic_ms; }
+        if (reason && reason_len > 0) {
+            std::snprintf(reason, (size_t)reason_len, "%s", ctx->fused_why.c_str());
+        }
+    });
 }
 
 int ibisgb_batch_create(ibisgb_ctx* const* cases, int32_t n_cases, ibisgb_ctx** out) {

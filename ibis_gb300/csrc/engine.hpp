@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include "sblock.hpp"
+
 namespace ibisgb {
 
 enum FluxKind : int { kHanel = 0, kAusmdv = 1, kLdfss2 = 2, kRusanov = 3 };
@@ -156,6 +158,14 @@ KernelOps kernels_f64_exact();
 KernelOps kernels_mixed();
 
 // precision-independent kernels (kernels_common.cu)
+// Fused Runge-Kutta stage on structured blocks (mixed build, inviscid, second
+// order): reads the primitives of v.prim, writes the new state's into
+// sb.prim_out; mode / stage / with_dt as KernelOps::update.
+void launch_fused_stage(const DevView& v, const SbView& sb, const FvParams& prm, int mode, int stage, int with_dt,
+                        cudaStream_t s);
+cudaError_t prepare_fused_stage();              // shared-memory opt-in, once per device
+void fused_tile_shape(int dim, int* tx, int* ty, int* tz);
+
 void launch_dt_finalize(StepCtl* ctl, int n_cases, cudaStream_t s);
 void launch_reset_dt(StepCtl* ctl, int n_cases, cudaStream_t s);
 void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s);

@@ -699,66 +699,17 @@ __device__ void reduce_local_dt(const DevView& v, int i, double local) {
     }
 }
 
-// One valid cell of k_update; returns the local time step of the new state when
-// with_dt (mode 3), else +inf.
+// The part of k_update after the surface integral: the Runge-Kutta combination
+// of `mode`, the primitives and ghosts of the new state (into v.prim) and, with
+// with_dt, the new state's local time step.  ks holds the stage derivative, or,
+// when fold, the mixed build's float pair (hi + lo) * iv stands for it.
 template <class P, class Gm, int DIM, bool EXACT>
-__device__ __forceinline__ double update_cell(const DevView& v, const FvParams& prm, int i, int mode, int stage,
-                                              double* out_rm, int with_dt) {
+__device__ __forceinline__ double update_tail(const DevView& v, const FvParams& prm, int i, int mode, int stage,
+                                              int with_dt, const double* ks, bool fold, const float* hi,
+                                              const float* lo, double iv) {
     constexpr double kInf = 1.0e308 * 10.0;
     constexpr int NC = DIM + 2;
-    const int N = v.N, F = v.F;
-    const Gm* area = (const Gm*)v.face + 12 * F;
-    const P* fl = (const P*)v.flux;
-    const int nf = v.nfaces[i];
-    double ks[NC];
-    if (sizeof(P) == sizeof(float)) {
-        // Mixed: each face term (float flux x area) is summed as an unevaluated
-        // float pair (hi + lo, ~48-bit significand: the exact products' rounding
-        // errors and every addition error are kept), then formed in double once.
-        float hi[NC], lo[NC];
-#pragma unroll
-        for (int q = 0; q < NC; q++) { hi[q] = 0.f; lo[q] = 0.f; }
-        for (int s = 0; s < nf; s++) {
-            const int f = v.cell_face[s * N + i];
-            const float a = -(float)area[f] * (float)v.outsign[s * N + i];
-#pragma unroll
-            for (int q = 0; q < NC; q++) {
-                const float x = (float)fl[q * F + f];
-                const float pr = __fmul_rn(x, a);
-                const float pe = __fmaf_rn(x, a, -pr);  // exact error of the product
-                two_sum_acc(hi[q], lo[q], pr);
-                lo[q] = __fadd_rn(lo[q], pe);
-            }
-        }
-        const double iv = v.inv_vol[i];
-#pragma unroll
-        for (int q = 0; q < NC; q++) ks[q] = ((double)hi[q] + (double)lo[q]) * iv;
-    } else {
-        double acc[NC];
-#pragma unroll
-        for (int q = 0; q < NC; q++) acc[q] = 0.0;
-        for (int s = 0; s < nf; s++) {
-            const int f = v.cell_face[s * N + i];
-            const double a = -(double)area[f] * (double)v.outsign[s * N + i];
-#pragma unroll
-            for (int q = 0; q < NC; q++) acc[q] += (double)fl[q * F + f] * a;
-        }
-        if (EXACT) {
-            const double vol = v.vol[i];
-#pragma unroll
-            for (int q = 0; q < NC; q++) ks[q] = acc[q] / vol;
-        } else {
-            const double iv = v.inv_vol[i];
-#pragma unroll
-            for (int q = 0; q < NC; q++) ks[q] = acc[q] * iv;
-        }
-    }
-    double* kk = v.k + (size_t)stage * NC * N;
-#pragma unroll
-    for (int q = 0; q < NC; q++) {
-        kk[q * N + i] = ks[q];
-        if (out_rm) out_rm[(size_t)i * NC + q] = ks[q];
-    }
+    const int N = v.N;
     if (mode < 2) return kInf;
     StepCtl* ctl = ctl_of(v, i);
     if (ctl->halt) return kInf;
@@ -783,12 +734,24 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
         return kInf;
     }
     // solution update (runge_kutta.cpp:185-193)
-    for (int j = 0; j < ctl->stages; j++) {
-        const double c = ctl->cb[j];
+    if (fold) {
+        for (int j = 0; j < ctl->stages; j++) {
+            if (j == stage) continue;
+            const double c = ctl->cb[j];
 #pragma unroll
-        for (int q = 0; q < NC; q++) {
-            double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
-            u[q] += kj * c;
+            for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
+        }
+        const double c = ctl->cb[stage] * iv;
+#pragma unroll
+        for (int q = 0; q < NC; q++) u[q] = fma((double)lo[q], c, fma((double)hi[q], c, u[q]));
+    } else {
+        for (int j = 0; j < ctl->stages; j++) {
+            const double c = ctl->cb[j];
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
+                u[q] += kj * c;
+            }
         }
     }
 #pragma unroll
@@ -797,6 +760,76 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
     count_bad(ctl, st);
     if (!with_dt) return kInf;
     return cell_local_dt<P, Gm, DIM>(v, prm, i, (P)st.vx, (P)st.vy, (P)st.vz, (P)st.T);
+}
+
+// One valid cell of k_update; returns the local time step of the new state when
+// with_dt (mode 3), else +inf.
+template <class P, class Gm, int DIM, bool EXACT>
+__device__ __forceinline__ double update_cell(const DevView& v, const FvParams& prm, int i, int mode, int stage,
+                                              double* out_rm, int with_dt) {
+    constexpr int NC = DIM + 2;
+    const int N = v.N, F = v.F;
+    const Gm* area = (const Gm*)v.face + 12 * F;
+    const P* fl = (const P*)v.flux;
+    const int nf = v.nfaces[i];
+    double ks[NC];
+    // Mixed, last stage of a multi-stage step: the stage derivative is never read
+    // again, so it is not stored and its float pair goes straight into the update.
+    const bool fold = sizeof(P) == sizeof(float) && mode == 3 && stage > 0 && !out_rm;
+    float hi[NC], lo[NC];
+    double iv = 0.0;
+    if (sizeof(P) == sizeof(float)) {
+        // Mixed: each face term (float flux x area) is summed as an unevaluated
+        // float pair (hi + lo, ~48-bit significand: the exact products' rounding
+        // errors and every addition error are kept), then formed in double once.
+#pragma unroll
+        for (int q = 0; q < NC; q++) { hi[q] = 0.f; lo[q] = 0.f; }
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const float a = -(float)area[f] * (float)v.outsign[s * N + i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                const float x = (float)fl[q * F + f];
+                const float pr = __fmul_rn(x, a);
+                const float pe = __fmaf_rn(x, a, -pr);  // exact error of the product
+                two_sum_acc(hi[q], lo[q], pr);
+                lo[q] = __fadd_rn(lo[q], pe);
+            }
+        }
+        iv = v.inv_vol[i];
+        if (!fold) {
+#pragma unroll
+            for (int q = 0; q < NC; q++) ks[q] = ((double)hi[q] + (double)lo[q]) * iv;
+        }
+    } else {
+        double acc[NC];
+#pragma unroll
+        for (int q = 0; q < NC; q++) acc[q] = 0.0;
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const double a = -(double)area[f] * (double)v.outsign[s * N + i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) acc[q] += (double)fl[q * F + f] * a;
+        }
+        if (EXACT) {
+            const double vol = v.vol[i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) ks[q] = acc[q] / vol;
+        } else {
+            const double iv = v.inv_vol[i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) ks[q] = acc[q] * iv;
+        }
+    }
+    if (!fold) {
+        double* kk = v.k + (size_t)stage * NC * N;
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
+            kk[q * N + i] = ks[q];
+            if (out_rm) out_rm[(size_t)i * NC + q] = ks[q];
+        }
+    }
+    return update_tail<P, Gm, DIM, EXACT>(v, prm, i, mode, stage, with_dt, ks, fold, hi, lo, iv);
 }
 
 template <class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>

@@ -159,6 +159,18 @@ class Simulation:
         w = np.array([recon, face, update], np.int32)
         self._call("ibisgb_set_launch_variants", PRECISION[precision], _ptr(w))
 
+    def set_fused(self, mode: int) -> None:
+        """Fused stage on structured blocks: -1 autotuner decides, 0 off, 1 on."""
+        self._call("ibisgb_set_fused", int(mode))
+
+    def fused_info(self) -> dict:
+        el, en = C.c_int32(), C.c_int32()
+        t = np.zeros(2)
+        why = C.create_string_buffer(256)
+        self._call("ibisgb_fused_info", C.byref(el), C.byref(en), _ptr(t), why, 256)
+        return {"eligible": bool(el.value), "enabled": bool(en.value), "fused_ms": t[0], "generic_ms": t[1],
+                "reason": why.value.decode()}
+
     # ------------------------------------------------------------- residual
     def compute_dudt(self, precision: str = "f64") -> np.ndarray:
         """dU/dt of the valid cells, (N, n_conserved) in the reference's cell order."""

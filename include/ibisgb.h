@@ -233,6 +233,26 @@ int ibisgb_set_launch_variants(ibisgb_ctx* ctx, int32_t precision, const int32_t
  * resident blocks per SM (arrays of at least count entries, may be NULL). */
 int ibisgb_launch_variants(int32_t* count, int32_t* threads, int32_t* min_blocks);
 
+/* Fused Runge-Kutta stage on structured blocks (no counterpart in the
+ * reference).  When every case of the context is a structured block -- quads
+ * or hexahedra numbered lexicographically on an ni x nj [x nk] lattice, the way
+ * a structured grid is written as SU2 -- and the scheme is inviscid and second
+ * order, the MIXED build can run each stage as one tiled kernel that keeps the
+ * tile's state, gradients and fluxes in shared memory.  mode -1 (the default)
+ * lets ibisgb_autotune / the first ibisgb_rk_run choose it when it is faster
+ * than the three-kernel stage, 0 never uses it, 1 always does (IBISGB_ERR_ARG if
+ * the grid or scheme does not qualify).  Its results agree with the
+ * three-kernel MIXED path to rounding (faces are evaluated along the lattice
+ * directions). */
+int ibisgb_set_fused(ibisgb_ctx* ctx, int32_t mode);
+
+/* Whether the fused stage applies to this context (host-side check, no GPU
+ * needed) and is in use, the last tuning times (fused stage, best three-kernel
+ * stage; ms, 2 doubles, may be NULL) and, when it does not apply, why (written
+ * into reason, at most reason_len bytes with the terminating zero). */
+int ibisgb_fused_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, double* times_ms, char* reason,
+                      int32_t reason_len);
+
 /* Batched ensembles (no counterpart in the reference, which runs one case per
  * process through Solver::solve, src/solvers/solvers/solver.cpp:25-59).
  * Merges already-created single-case contexts into one new context whose valid

@@ -1,0 +1,42 @@
+"""Structured-block recognition for the fused stage, on the host (no GPU):
+every grid the structured generators write qualifies, batches of them too,
+and anything else is refused with a reason."""
+import numpy as np
+
+from ibis_gb300 import Batch, Simulation, grids
+from tests.cases import case
+
+
+def test_structured_grids_qualify():
+    for name in ("ramp", "box", "box_inout"):
+        g, c, _ = case(name)
+        info = Simulation(c, g).fused_info()
+        assert info["eligible"], (name, info["reason"])
+        assert not info["enabled"]
+
+
+def test_batches_of_structured_cases_qualify():
+    ens = grids.ramp_ensemble(3, seed=3, smallest=(8, 4), largest=(24, 12))
+    b = Batch([Simulation(c, g) for g, c, _, _ in ens])
+    assert b.fused_info()["eligible"]
+
+
+def test_other_grids_and_schemes_are_refused():
+    g, c, _ = case("plate")
+    info = Simulation(c, g).fused_info()
+    assert not info["eligible"] and "viscous" in info["reason"]
+    g, c, _ = case("ramp", order=1)
+    assert "first-order" in Simulation(c, g).fused_info()["reason"]
+    # the same ramp with its cells renumbered is no longer a lattice
+    g, c, _ = case("ramp")
+    perm = np.random.default_rng(0).permutation(g.num_cells)
+    n = g.cell_offsets[1:] - g.cell_offsets[:-1]
+    conn = [g.cell_conn[g.cell_offsets[k]:g.cell_offsets[k + 1]] for k in range(g.num_cells)]
+    g.cell_conn = np.concatenate([conn[k] for k in perm])
+    g.cell_types = g.cell_types[perm]
+    g.cell_offsets = np.concatenate([[0], np.cumsum(n[perm])])
+    info = Simulation(c, g).fused_info()
+    assert not info["eligible"] and info["reason"]
+    g = grids.unit_square_3x3()
+    bnds = {t: grids.slip_wall() for t in ["slip_wall_bottom", "slip_wall_top", "inflow", "outflow"]}
+    assert Simulation(grids.make_config(2, bnds), g).fused_info()["eligible"]

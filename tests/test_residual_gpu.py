@@ -180,6 +180,7 @@ def test_launch_variants_are_bit_identical(name, precision):
         assert np.array_equal(U, ref), w
     sim = Simulation(c, g)
     sim.set_primitives(*st)
+    sim.set_fused(0)  # the fused stage agrees to rounding only; it has its own tests
     tuned = sim.autotune(precision)
     assert all(0 <= x < nv for x in tuned["variants"].values())
     assert all(len(v) == nv and min(v) > 0 for v in tuned["ms"].values())
