@@ -1098,8 +1098,8 @@ struct ibisgb_ctx {
     }
 
     // Launch-variant autotuner: times every variant of the recon, face and update
-    // kernels on this grid and state (CUDA events, one warm-up launch and three
-    // timed ones each; update in its residual-only mode) and keeps the fastest.
+    // kernels on this grid and state (CUDA events, one warm-up launch, then the
+    // fastest of three; update in its residual-only mode) and keeps the fastest.
     // A variant must be 2% faster than the lower-numbered best to be chosen.
     // Every variant computes the same bits, so tuning changes only the speed.
     // Leaves the residual of the current state in stage 0 of k.
@@ -1112,19 +1112,25 @@ struct ibisgb_ctx {
             DevView v = view(prec);
             KernelOps o = ops(prec);
             const bool reco = prm.order == 2;
-            cudaEvent_t e0, e1;
-            CUDA_OK(cudaEventCreate(&e0));
-            CUDA_OK(cudaEventCreate(&e1));
+            cudaEvent_t ev[4];
+            for (auto& e : ev) CUDA_OK(cudaEventCreate(&e));
+            // one warm-up launch, then the fastest of three individually timed ones
             auto timed = [&](const std::function<void()>& launch) {
                 launch();
-                CUDA_OK(cudaEventRecord(e0, stream));
-                for (int r = 0; r < 3; r++) launch();
-                CUDA_OK(cudaEventRecord(e1, stream));
+                CUDA_OK(cudaEventRecord(ev[0], stream));
+                for (int r = 0; r < 3; r++) {
+                    launch();
+                    CUDA_OK(cudaEventRecord(ev[r + 1], stream));
+                }
                 CUDA_OK(cudaGetLastError());
-                CUDA_OK(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
-                return ms / 3.0;
+                CUDA_OK(cudaEventSynchronize(ev[3]));
+                double best = 0.0;
+                for (int r = 0; r < 3; r++) {
+                    float ms = 0.f;
+                    CUDA_OK(cudaEventElapsedTime(&ms, ev[r], ev[r + 1]));
+                    if (r == 0 || ms < best) best = ms;
+                }
+                return best;
             };
             for (int k = 0; k < 3; k++) {
                 if (k == 0 && !reco && !prm.viscous) continue;  // no recon kernel
@@ -1151,8 +1157,7 @@ struct ibisgb_ctx {
                 }
                 fused_on = fused_mode == 1 || (fused_mode == -1 && fused_ms > 0.0 && fused_ms < generic_ms);
             }
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
+            for (auto& e : ev) cudaEventDestroy(e);
         }
         tuned[gi] = true;
         if (graph[gi]) {

@@ -218,8 +218,8 @@ int ibisgb_synchronize(ibisgb_ctx* ctx);
  * caps registers per thread).  ibisgb_autotune times every variant on the
  * context's grid and current state (CUDA events; the update kernel in its
  * residual-only mode), keeps the fastest and returns the choice in variants
- * (recon, face, update) and, if times_ms is not NULL, the mean time of every
- * variant (3 x count doubles, kernel-major).  ibisgb_rk_run tunes a precision
+ * (recon, face, update) and, if times_ms is not NULL, the time of every
+ * variant (fastest of three launches; 3 x count doubles, kernel-major).  ibisgb_rk_run tunes a precision
  * by itself on its first call unless variants were set.  All variants give
  * bit-identical results.  The residual of the current state is left as the
  * first-stage derivative (what ibisgb_l2_norms reads).  F64_EXACT always uses
