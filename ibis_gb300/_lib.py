@@ -81,11 +81,14 @@ def load(build_if_missing: bool = True):
     L.ibisgb_get_dump.argtypes = [_P, C.c_int32, _P, C.c_int64]
     L.ibisgb_synchronize.argtypes = [_P]
     L.ibisgb_set_conserved.argtypes = [_P, _P]
+    L.ibisgb_set_conserved_device.argtypes = [_P, _P, _P]
     L.ibisgb_get_stream.argtypes = [_P, C.POINTER(_P)]
     L.ibisgb_kernel_times.argtypes = [_P, C.c_int32, C.c_int32, _P]
     L.ibisgb_l2_norms_noalloc.argtypes = [_P, C.c_int64, C.c_int32, _P, _P]
     L.ibisgb_jvp.argtypes = [_P, _P, _P, C.c_double, C.c_int32]
     L.ibisgb_jvp_device.argtypes = [_P, _P, _P, C.c_double, C.c_int32, _P]
+    L.ibisgb_vjp.argtypes = [_P, _P, _P, _P, C.c_int32]
+    L.ibisgb_vjp_device.argtypes = [_P, _P, _P, _P, C.c_int32, _P]
     L.ibisgb_steady_initialise.argtypes = [_P, C.c_int32]
     L.ibisgb_newton_step.argtypes = [_P, C.c_int32, C.POINTER(NewtonStatus)]
     L.ibisgb_autotune.argtypes = [_P, C.c_int32, _P, _P]

@@ -357,6 +357,12 @@ struct ibisgb_ctx {
         std::vector<BoundarySpec> specs = boundary_specs();
         build_mesh(in, specs, prm.viscous || prm.order > 1, mesh);
         check_index_range();
+        // every face needs two sides: a boundary without ghost cells would need a
+        // post-convective flux action, which is not supported
+        for (int64_t f = 0; f < mesh.F; f++)
+            if (mesh.left[f] < 0 || mesh.right[f] < 0)
+                throw ConfigError("a boundary face has no ghost cell (ghost_cells false needs a flux action, "
+                                  "which is not supported)");
         for (const auto& b : mesh.bounds) {  // BoundaryCondition ctor, boundary.cpp:494-515
             const Json& bj = config.at("grid").at("boundaries").at(b.tag);
             BoundDev d{};
@@ -876,6 +882,43 @@ struct ibisgb_ctx {
         CUDA_OK(cudaGetLastError());
     }
 
+    // ----- adjoint: (dR/dU)^T w ------------------------------------------------
+    DBuf adj_qf, adj_self, adj_nba, adj_ga, adj_back, adj_gout;
+    bool adj_ready = false;
+    void ensure_adjoint() {
+        if (adj_ready) return;
+        ensure_device();
+        const int64_t N = mesh.N, F = mesh.F, MF = mesh.MF;
+        adj_qf.alloc(sizeof(double) * 12 * F);
+        adj_self.alloc(sizeof(double) * 7 * N);
+        adj_nba.alloc(sizeof(double) * 5 * MF * N);
+        adj_ga.alloc(sizeof(double) * 7 * std::max<int64_t>(mesh.G, 1));
+        // slot of each valid neighbour that points back through the same face
+        std::vector<signed char> back(MF * N, -1);
+        for (int64_t c = 0; c < N; c++)
+            for (int64_t k = 0; k < MF; k++) {
+                const int64_t nb = mesh.cell_nbr[c * MF + k];
+                if (nb < 0 || nb >= N) continue;
+                const int64_t f = mesh.cell_face[c * MF + k];
+                for (int64_t t = 0; t < MF; t++)
+                    if (mesh.cell_face[nb * MF + t] == f) back[k * N + c] = (signed char)t;
+            }
+        upload(adj_back, back, stream);
+        CUDA_OK(cudaStreamSynchronize(stream));
+        adj_ready = true;
+    }
+
+    void vjp(const double* w_dev, double* out_dev, double* ghost_out_dev, bool reconstruct) {
+        if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
+        if (prm.viscous) throw ConfigError("the adjoint covers inviscid configurations");
+        DevView v = tangent_view();
+        ensure_adjoint();
+        AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
+                     adj_back.as<signed char>()};
+        launch_adjoint(v, prm, w_dev, reconstruct && prm.order == 2, a, out_dev, ghost_out_dev, stream);
+        CUDA_OK(cudaGetLastError());
+    }
+
     size_t nvars() const { return (size_t)mesh.N * nc(); }
 
     void ensure_krylov(int m) {
@@ -1222,14 +1265,18 @@ struct ibisgb_ctx {
         for (int k = 0; k < 4; k++) out[k] = reps > 0 ? acc[k] / reps : 0.0;
     }
 
-    void set_conserved(const double* rows) {
+    void set_conserved(const double* rows, bool device = false) {
         if (!rows) throw ArgError("U is null");
         ensure_device();
         const int64_t N = mesh.N;
         const size_t bytes = sizeof(double) * nc() * N;
-        out.alloc(bytes);
-        CUDA_OK(cudaMemcpyAsync(out.p, rows, bytes, cudaMemcpyHostToDevice, stream));
-        launch_rows_to_soa(out.as<double>(), U.as<double>(), (int)N, nc(), stream);
+        if (device) {
+            launch_rows_to_soa(rows, U.as<double>(), (int)N, nc(), stream);
+        } else {
+            out.alloc(bytes);
+            CUDA_OK(cudaMemcpyAsync(out.p, rows, bytes, cudaMemcpyHostToDevice, stream));
+            launch_rows_to_soa(out.as<double>(), U.as<double>(), (int)N, nc(), stream);
+        }
         CUDA_OK(cudaGetLastError());
         if (!have_state) reset_rk();
         have_state = true;
@@ -1429,6 +1476,26 @@ int ibisgb_set_conserved(ibisgb_ctx* ctx, const double* U) {
     return guarded(ctx, [&] { ctx->set_conserved(U); });
 }
 
+int ibisgb_set_conserved_device(ibisgb_ctx* ctx, const double* U_device, void* stream) {
+    if (!ctx || !U_device) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_device();
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        if (user && user != ctx->stream) {
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+        }
+        ctx->set_conserved(U_device, true);
+        if (ev) {
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        }
+    });
+}
+
 int ibisgb_get_stream(ibisgb_ctx* ctx, void** stream) {
     if (!ctx || !stream) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
@@ -1609,6 +1676,46 @@ int ibisgb_jvp(ibisgb_ctx* ctx, const double* v, double* out, double inv_dt_star
         CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, v, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
         ctx->jvp(ctx->kr0.as<double>(), ctx->kw.as<double>(), inv_dt_star, allow_reconstruction != 0);
         CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ibisgb_vjp_device(ibisgb_ctx* ctx, const double* w_device, double* out_device, double* ghost_out_device,
+                      int32_t allow_reconstruction, void* stream) {
+    if (!ctx || !w_device || !out_device) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        ctx->ensure_device();
+        if (user && user != ctx->stream) {
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+        }
+        ctx->vjp(w_device, out_device, ghost_out_device, allow_reconstruction != 0);
+        if (ev) {
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        }
+    });
+}
+
+int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out, int32_t allow_reconstruction) {
+    if (!ctx || !w || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_device();
+        const size_t n = ctx->nvars();
+        const size_t ng = 7 * (size_t)ctx->mesh.G;
+        ctx->ensure_krylov(1);
+        ctx->adj_gout.alloc(sizeof(double) * std::max(ng, (size_t)1));
+        CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, w, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->vjp(ctx->kr0.as<double>(), ctx->kw.as<double>(), ghost_out ? ctx->adj_gout.as<double>() : nullptr,
+                 allow_reconstruction != 0);
+        CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        if (ghost_out && ng)
+            CUDA_OK(cudaMemcpyAsync(ghost_out, ctx->adj_gout.p, sizeof(double) * ng, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
 }

@@ -166,6 +166,19 @@ void launch_fused_stage(const DevView& v, const SbView& sb, const FvParams& prm,
 cudaError_t prepare_fused_stage();              // shared-memory opt-in, once per device
 void fused_tile_shape(int dim, int* tx, int* ty, int* tz);
 
+// Scratch of the adjoint passes (device pointers; sizes in launch_adjoint's callers).
+struct AdjScratch {
+    double* qf;               // [2][6][F] adjoints of the faces' reconstructed inputs
+    double* self;             // [7][N]    each cell's own primitive adjoint
+    double* nba;              // [5][MF][N] what each cell sends to the neighbour of slot s
+    double* ga;               // [7][G]    ghost primitive adjoints
+    const signed char* back;  // [MF][N]   slot of cell_nbr(i, s) that points back to i
+};
+// out = (dR/dU)^T w for w, out of N x nc rows (inviscid); ghost_out (optional,
+// G x 7 rows): the adjoint of every ghost cell's primitives (rho, p, T, e, v).
+void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool reconstruct, const AdjScratch& a,
+                    double* out, double* ghost_out, cudaStream_t s);
+
 void launch_dt_finalize(StepCtl* ctl, int n_cases, cudaStream_t s);
 void launch_reset_dt(StepCtl* ctl, int n_cases, cudaStream_t s);
 void launch_l2_norms(const double* k0, int N, int nc, double* out6, cudaStream_t s);

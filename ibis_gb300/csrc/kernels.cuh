@@ -354,6 +354,57 @@ IBISGB_HD R lin_interp(R value, R lim, const P* g, int N, int q, int c, R dx, R 
     return value + lim * s;
 }
 
+// One side of a face from its (reconstructed) primitives q (rho, p, T, e, vx,
+// vy, vz): the thermo closure of the interpolated pair when reconstructing, then
+// the velocity in the face frame (transform_to_local_frame, vector3.cpp:141-153).
+template <class R, int DIM, bool EXACT>
+__device__ __forceinline__ void side_state(int thermo, const Gas<R>& gm, bool reconstruct, R (&q)[7], R nx, R ny,
+                                           R nz, R t1x, R t1y, R t1z, R t2x, R t2y, R t2z, FaceSide<R>& S) {
+    if (reconstruct) thermo_close<R>(thermo, gm, q[0], q[1], q[2], q[3]);
+    S.r = q[0]; S.p = q[1]; S.T = q[2];
+    if (DIM == 3) {
+        S.u = q[4] * nx + q[5] * ny + q[6] * nz;
+        S.v = q[4] * t1x + q[5] * t1y + q[6] * t1z;
+        S.w = q[4] * t2x + q[5] * t2y + q[6] * t2z;
+    } else if (EXACT) {
+        S.u = q[4] * nx + q[5] * ny + q[6] * nz;
+        S.v = q[4] * t1x + q[5] * t1y + q[6] * t1z;
+        S.w = R(0.0);
+    } else {
+        S.u = q[4] * nx + q[5] * ny;
+        S.v = q[4] * t1x + q[5] * t1y;
+        S.w = R(0.0);
+    }
+}
+
+// The selected flux calculator in the face frame, rotated back to the global
+// frame (transform_to_global, convective_flux.cpp:145-177): out = mass,
+// momentum x, y, z, energy.
+template <class R, int DIM, bool EXACT>
+__device__ __forceinline__ void convective_flux(const FvParams& prm, const Gas<R>& gm, const FaceSide<R>& L,
+                                                const FaceSide<R>& Rt, R nx, R ny, R nz, R t1x, R t1y, R t1z,
+                                                R t2x, R t2y, R t2z, R (&out)[5]) {
+    R Fl[5];
+    switch (prm.flux) {
+        case kHanel: flux_hanel<R, DIM>(L, Rt, gm, Fl); break;
+        case kAusmdv: flux_ausmdv<R, DIM>(L, Rt, gm, Fl); break;
+        case kLdfss2: flux_ldfss2<R, DIM, EXACT>(L, Rt, gm, par<R>(prm.delta, prm.fdelta), Fl); break;
+        default: flux_rusanov<R, DIM>(L, Rt, gm, Fl); break;
+    }
+    R px = Fl[1], py = Fl[2], pz = DIM == 3 ? Fl[3] : R(0.0);
+    out[0] = Fl[0];
+    out[3] = R(0.0);
+    if (DIM == 3 || EXACT) {
+        out[1] = px * nx + py * t1x + pz * t2x;
+        out[2] = px * ny + py * t1y + pz * t2y;
+        if (DIM == 3) out[3] = px * nz + py * t1z + pz * t2z;
+    } else {
+        out[1] = px * nx + py * t1x;
+        out[2] = px * ny + py * t1y;
+    }
+    out[4] = Fl[4];
+}
+
 template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
 __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int reconstruct) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -407,49 +458,18 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
             auto L = [&](int k) { return lim ? (R)ph[k * N + c] : R(1.0); };
             q[ia] = lin_interp<R, P, DIM>(q[ia], L(0), gr, N, 0, c, dx, dy, dz);
             q[ib] = lin_interp<R, P, DIM>(q[ib], L(1), gr, N, 1, c, dx, dy, dz);
-            thermo_close<R>(prm.thermo, gm, q[0], q[1], q[2], q[3]);
             q[4] = lin_interp<R, P, DIM>(q[4], L(2), gr, N, 2, c, dx, dy, dz);
             q[5] = lin_interp<R, P, DIM>(q[5], L(3), gr, N, 3, c, dx, dy, dz);
             if (DIM == 3) q[6] = lin_interp<R, P, DIM>(q[6], L(4), gr, N, 4, c, dx, dy, dz);
-        } else if (reconstruct) {
-            // ghost side: first-order copy, then the same thermo closure
-            thermo_close<R>(prm.thermo, gm, q[0], q[1], q[2], q[3]);
         }
-        S[side].r = q[0]; S[side].p = q[1]; S[side].T = q[2];
-        // transform_to_local_frame (vector3.cpp:141-153)
-        if (DIM == 3) {
-            S[side].u = q[4] * nx + q[5] * ny + q[6] * nz;
-            S[side].v = q[4] * t1x + q[5] * t1y + q[6] * t1z;
-            S[side].w = q[4] * t2x + q[5] * t2y + q[6] * t2z;
-        } else if (EXACT) {
-            S[side].u = q[4] * nx + q[5] * ny + q[6] * nz;
-            S[side].v = q[4] * t1x + q[5] * t1y + q[6] * t1z;
-            S[side].w = R(0.0);
-        } else {
-            S[side].u = q[4] * nx + q[5] * ny;
-            S[side].v = q[4] * t1x + q[5] * t1y;
-            S[side].w = R(0.0);
-        }
+        // the ghost side is first order but passes through the same thermo closure
+        side_state<R, DIM, EXACT>(prm.thermo, gm, reconstruct, q, nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z,
+                                  S[side]);
     }
-    R Fl[5];
-    switch (prm.flux) {
-        case kHanel: flux_hanel<R, DIM>(S[0], S[1], gm, Fl); break;
-        case kAusmdv: flux_ausmdv<R, DIM>(S[0], S[1], gm, Fl); break;
-        case kLdfss2: flux_ldfss2<R, DIM, EXACT>(S[0], S[1], gm, par<R>(prm.delta, prm.fdelta), Fl); break;
-        default: flux_rusanov<R, DIM>(S[0], S[1], gm, Fl); break;
-    }
-    // transform_to_global (convective_flux.cpp:145-177)
-    R px = Fl[1], py = Fl[2], pz = DIM == 3 ? Fl[3] : R(0.0);
-    R mx, my, mz = R(0.0);
-    if (DIM == 3 || EXACT) {
-        mx = px * nx + py * t1x + pz * t2x;
-        my = px * ny + py * t1y + pz * t2y;
-        if (DIM == 3) mz = px * nz + py * t1z + pz * t2z;
-    } else {
-        mx = px * nx + py * t1x;
-        my = px * ny + py * t1y;
-    }
-    R en = Fl[4];
+    R Fg[5];
+    convective_flux<R, DIM, EXACT>(prm, gm, S[0], S[1], nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z, Fg);
+    R mx = Fg[1], my = Fg[2], mz = Fg[3];
+    R en = Fg[4];
 
     if (prm.viscous) {
         // viscous_flux.cpp:130-232
@@ -521,7 +541,7 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
         v.vsig[f] = (prm.gamma / real_of(rho)) * (mud / Prf);
     }
     P* fo = (P*)v.flux;
-    fo[f] = (P)Fl[0];
+    fo[f] = (P)Fg[0];
     fo[F + f] = (P)mx;
     fo[2 * F + f] = (P)my;
     if (DIM == 3) fo[3 * F + f] = (P)mz;

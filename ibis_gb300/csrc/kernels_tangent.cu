@@ -73,7 +73,321 @@ __global__ void __launch_bounds__(kBlock) k_tan_update(DevView v, FvParams prm, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint: (dR/dU)^T w, the transpose of the tangent above, in three passes
+// that walk the residual backwards.  The forward state (primitives, ghosts,
+// gradients, limiters) is recomputed by the tangent's own kernels with a zero
+// tangent, and every branch (limiter winner, min/max arguments, flux
+// splittings) is taken again from those real values with the Dual rules, so
+// <w, J v> = <J^T w, v> to rounding.  Local derivatives of the face flux and
+// the ghost actions come from dual evaluations seeded one input at a time, in
+// DualA (the derivative of floor is zero; see dual.cuh), which differs from the
+// tangent only for LDFSS2.
+// ---------------------------------------------------------------------------
+
+// inputs of the face flux on each side: the reconstructed pair and velocities
+// when reconstructing (the closure rebuilds the rest), else rho, p, T, v
+template <int DIM>
+__device__ __forceinline__ int face_inputs(int thermo, bool reconstruct, int (&in)[6]) {
+    if (reconstruct) {
+        int ia, ib;
+        thermo_vars(thermo, ia, ib);
+        in[0] = ia; in[1] = ib; in[2] = 4; in[3] = 5; in[4] = 6; in[5] = -1;
+        return DIM == 3 ? 5 : 4;
+    }
+    in[0] = 0; in[1] = 1; in[2] = 2; in[3] = 4; in[4] = 5; in[5] = 6;
+    return DIM == 3 ? 6 : 5;
+}
+
+// Real reconstructed primitives of side cell c of face f (k_face's arithmetic).
+template <int DIM>
+__device__ void side_values(const DevView& v, const FvParams& prm, bool reconstruct, int c, int f, double (&q)[7]) {
+    const Dual* pr = (const Dual*)v.prim;
+    const Dual* gr = (const Dual*)v.grad;
+    const Dual* ph = (const Dual*)v.phi;
+    const double* fg = (const double*)v.face;
+    const double* cc = (const double*)v.cc;
+    const int NT = v.NT, N = v.N, F = v.F;
+    for (int k = 0; k < 7; k++) q[k] = (DIM == 2 && k == 6) ? 0.0 : pr[k * NT + c].re;
+    if (!reconstruct || c >= N) return;
+    const double dx = fg[9 * F + f] - cc[c], dy = fg[10 * F + f] - cc[NT + c];
+    const double dz = DIM == 3 ? fg[11 * F + f] - cc[2 * NT + c] : 0.0;
+    int in[6];
+    const int K = face_inputs<DIM>(prm.thermo, true, in);
+    for (int k = 0; k < K; k++) {
+        const double lim = prm.limiter ? ph[k * N + c].re : 1.0;
+        const double sgr = DIM == 3 ? gr[(3 * k) * N + c].re * dx + gr[(3 * k + 1) * N + c].re * dy +
+                                          gr[(3 * k + 2) * N + c].re * dz
+                                    : gr[(3 * k) * N + c].re * dx + gr[(3 * k + 1) * N + c].re * dy;
+        q[in[k]] = q[in[k]] + lim * sgr;
+    }
+}
+
+// Pass 1, per face: adjoint of the face flux, wbar_F = sum over its valid cells of
+// -outsign A / V w, pulled back to the reconstructed inputs of both sides.
+// Valid sides go to qf[(side * 6 + k) * F + f]; ghost sides to ga[m * G + g].
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, const double* w, int reconstruct,
+                                                     double* qf, double* ga) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.F) return;
+    constexpr int NC = DIM + 2;
+    const int N = v.N, F = v.F, G = v.G;
+    const double* fg = (const double*)v.face;
+    const int cells[2] = {v.left[f], v.right[f]};
+    const double A = fg[12 * F + f];
+    double fb[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int side = 0; side < 2; side++) {
+        const int c = cells[side];
+        if (c >= N) continue;
+        const double sc = (side == 0 ? -A : A) / v.vol[c];
+        for (int q = 0; q < NC; q++) fb[q == NC - 1 ? 4 : q] += sc * w[(size_t)c * NC + q];
+    }
+    double qv[2][7];
+    side_values<DIM>(v, prm, reconstruct, cells[0], f, qv[0]);
+    side_values<DIM>(v, prm, reconstruct, cells[1], f, qv[1]);
+    const DualA nx(fg[f]), ny(fg[F + f]), nz(DIM == 3 ? fg[2 * F + f] : 0.0);
+    const DualA t1x(fg[3 * F + f]), t1y(fg[4 * F + f]), t1z(DIM == 3 ? fg[5 * F + f] : 0.0);
+    const DualA t2x(DIM == 3 ? fg[6 * F + f] : 0.0), t2y(DIM == 3 ? fg[7 * F + f] : 0.0), t2z(fg[8 * F + f]);
+    const Gas<DualA> gm(prm);
+    int in[6];
+    const int K = face_inputs<DIM>(prm.thermo, reconstruct, in);
+    for (int side = 0; side < 2; side++) {
+        for (int k = 0; k < K; k++) {
+            DualA qd[2][7];
+            for (int s2 = 0; s2 < 2; s2++)
+                for (int m = 0; m < 7; m++) qd[s2][m] = DualA(qv[s2][m], (s2 == side && m == in[k]) ? 1.0 : 0.0);
+            FaceSide<DualA> S[2];
+            side_state<DualA, DIM, true>(prm.thermo, gm, reconstruct, qd[0], nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z,
+                                         S[0]);
+            side_state<DualA, DIM, true>(prm.thermo, gm, reconstruct, qd[1], nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z,
+                                         S[1]);
+            DualA Fd[5];
+            convective_flux<DualA, DIM, true>(prm, gm, S[0], S[1], nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z, Fd);
+            double acc = 0.0;
+            for (int q = 0; q < 5; q++) acc += fb[q] * Fd[q].du;
+            const int c = cells[side];
+            if (c < N) qf[(size_t)(side * 6 + k) * F + f] = acc;
+            else ga[(size_t)in[k] * G + (c - N)] = acc;
+        }
+    }
+}
+
+// Pass 2, per valid cell: gathers its faces' input adjoints, reverses the
+// reconstruction, the Barth-Jespersen limiter (its winning face and the min/max
+// neighbours chosen with the Dual rules) and the least-squares gradient.
+// The cell's own primitive adjoint goes to self[m * N + i]; what its
+// neighbours receive goes to nba[(k * MF + s) * N + i] (valid neighbours, read
+// back by pass 3) or into ga (ghost neighbours, each of which has one cell).
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, int reconstruct, const double* qf,
+                                                     double* self, double* nba, double* ga) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    constexpr int NV = DIM == 3 ? 5 : 4;
+    const int N = v.N, F = v.F, G = v.G, NT = v.NT, MF = v.MF;
+    const Dual* pr = (const Dual*)v.prim;
+    const Dual* gr = (const Dual*)v.grad;
+    const Dual* ph = (const Dual*)v.phi;
+    const double* fg = (const double*)v.face;
+    const double* cc = (const double*)v.cc;
+    const double* rr = (const double*)v.r;
+    int in[6];
+    const int K = face_inputs<DIM>(prm.thermo, reconstruct, in);
+    double pb[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const int nf = v.nfaces[i];
+    if (!reconstruct) {
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
+            for (int k = 0; k < K; k++) pb[in[k]] += qf[(size_t)(side * 6 + k) * F + f];
+        }
+        for (int m = 0; m < 7; m++) self[(size_t)m * N + i] = pb[m];
+        return;
+    }
+    const double xi = cc[i], yi = cc[NT + i], zi = DIM == 3 ? cc[2 * NT + i] : 0.0;
+    double ui[NV], g[NV][3], phi[NV], gb[NV][3], phib[NV];
+    for (int k = 0; k < NV; k++) {
+        ui[k] = pr[in[k] * NT + i].re;
+        phi[k] = prm.limiter ? ph[k * N + i].re : 1.0;
+        phib[k] = 0.0;
+        for (int d = 0; d < 3; d++) {
+            g[k][d] = (DIM == 2 && d == 2) ? 0.0 : gr[(3 * k + d) * N + i].re;
+            gb[k][d] = 0.0;
+        }
+    }
+    // reconstruction q_f = q + phi (g . dx) on every face of the cell
+    for (int s = 0; s < nf; s++) {
+        const int f = v.cell_face[s * N + i];
+        const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
+        const double dx = fg[9 * F + f] - xi, dy = fg[10 * F + f] - yi, dz = DIM == 3 ? fg[11 * F + f] - zi : 0.0;
+        for (int k = 0; k < NV; k++) {
+            const double b = qf[(size_t)(side * 6 + k) * F + f];
+            pb[in[k]] += b;
+            const double sgr = DIM == 3 ? g[k][0] * dx + g[k][1] * dy + g[k][2] * dz : g[k][0] * dx + g[k][1] * dy;
+            phib[k] += b * sgr;
+            gb[k][0] += b * phi[k] * dx; gb[k][1] += b * phi[k] * dy;
+            if (DIM == 3) gb[k][2] += b * phi[k] * dz;
+        }
+    }
+    // least-squares weights (k_recon's exact form) and the min / max arguments
+    double r11 = rr[i], r12 = rr[N + i], r22 = rr[2 * N + i], r13 = 0.0, r23 = 0.0, r33 = 1.0;
+    if (DIM == 3) { r13 = rr[3 * N + i]; r23 = rr[4 * N + i]; r33 = rr[5 * N + i]; }
+    const double beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+    double umin[NV], umax[NV];
+    int amin[NV], amax[NV];
+    for (int k = 0; k < NV; k++) { umin[k] = ui[k]; umax[k] = ui[k]; amin[k] = -1; amax[k] = -1; }
+    for (int s = 0; s < nf; s++) {
+        const int nb = v.cell_nbr[s * N + i];
+        for (int k = 0; k < NV; k++) {
+            const double un = pr[in[k] * NT + nb].re;
+            if (!(umin[k] < un)) { umin[k] = un; amin[k] = s; }  // Dual min: ties take the second
+            if (!(umax[k] > un)) { umax[k] = un; amax[k] = s; }
+        }
+    }
+    double extb[NV];  // adjoint of the chosen extreme neighbour value
+    int ext[NV];
+    for (int k = 0; k < NV; k++) { extb[k] = 0.0; ext[k] = -1; }
+    if (prm.limiter) {
+        const double eps = prm.eps;
+        for (int k = 0; k < NV; k++) {
+            // the limiter loop of k_recon: winner = last face whose ratio was taken by min(phi, ratio)
+            double ph_k = 1.0;
+            int win = -1;
+            for (int s = 0; s < nf; s++) {
+                const int f = v.cell_face[s * N + i];
+                const double dx = fg[9 * F + f] - xi, dy = fg[10 * F + f] - yi;
+                const double dz = DIM == 3 ? fg[11 * F + f] - zi : 0.0;
+                double t = DIM == 3 ? g[k][0] * dx + g[k][1] * dy + g[k][2] * dz : g[k][0] * dx + g[k][1] * dy;
+                const int sg = (t > 0.0) - (t < 0.0);
+                const double d2 = (double)sg * (fabs(t) + eps);
+                if (sg != 0) {
+                    const double ratio = sg > 0 ? (umax[k] - ui[k]) / d2 : (umin[k] - ui[k]) / d2;
+                    if (!(ph_k < ratio)) { ph_k = ratio; win = s; }
+                }
+            }
+            if (win < 0) continue;
+            const int f = v.cell_face[win * N + i];
+            const double dx = fg[9 * F + f] - xi, dy = fg[10 * F + f] - yi, dz = DIM == 3 ? fg[11 * F + f] - zi : 0.0;
+            const double t = DIM == 3 ? g[k][0] * dx + g[k][1] * dy + g[k][2] * dz : g[k][0] * dx + g[k][1] * dy;
+            const int sg = (t > 0.0) - (t < 0.0);
+            const double d2 = (double)sg * (fabs(t) + eps);
+            const double delta = sg > 0 ? umax[k] - ui[k] : umin[k] - ui[k];
+            const double db = phib[k] / d2;
+            const double d2b = -phib[k] * delta / (d2 * d2);
+            const double tb = d2b * (double)sg * (t < 0.0 ? -1.0 : 1.0);
+            gb[k][0] += tb * dx; gb[k][1] += tb * dy;
+            if (DIM == 3) gb[k][2] += tb * dz;
+            // delta = u_ext - u_i: the extreme is the cell itself (no net term) or a neighbour
+            ext[k] = sg > 0 ? amax[k] : amin[k];
+            if (ext[k] >= 0) { extb[k] = db; pb[in[k]] -= db; }
+        }
+    }
+    // gradient g = sum_s w_s (u_nb - u_i)
+    for (int s = 0; s < nf; s++) {
+        const int nb = v.cell_nbr[s * N + i];
+        const double dx = cc[nb] - xi, dy = cc[NT + nb] - yi, dz = DIM == 3 ? cc[2 * NT + nb] - zi : 0.0;
+        const double a1 = dx / (r11 * r11);
+        const double a2 = 1.0 / (r22 * r22) * (dy - r12 / r11 * dx);
+        const double a3 = DIM == 3 ? 1.0 / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx) : 0.0;
+        const double w1 = a1 - r12 / r11 * a2 + beta * a3, w2 = a2 - r23 / r22 * a3, w3 = a3;
+        for (int k = 0; k < NV; k++) {
+            double c = w1 * gb[k][0] + w2 * gb[k][1] + (DIM == 3 ? w3 * gb[k][2] : 0.0);
+            pb[in[k]] -= c;
+            if (ext[k] == s) c += extb[k];
+            if (nb < N) nba[((size_t)k * MF + s) * N + i] = c;
+            else ga[(size_t)in[k] * G + (nb - N)] += c;
+        }
+    }
+    for (int m = 0; m < 7; m++) self[(size_t)m * N + i] = pb[m];
+}
+
+// Pass 3, per valid cell: the primitive adjoint (own part, what its valid
+// neighbours sent back through the same face, and the ghosts it fills, through
+// the transposed ghost actions), then back through conserved_to_primatives to U.
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, int reconstruct,
+                                                      const double* self, const double* nba, const double* ga,
+                                                      const signed char* back, double* out, double* gout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    constexpr int NC = DIM + 2, NV = DIM == 3 ? 5 : 4;
+    const int N = v.N, G = v.G, NT = v.NT, MF = v.MF;
+    const Dual* pr = (const Dual*)v.prim;
+    double pb[7];
+    for (int m = 0; m < 7; m++) pb[m] = self[(size_t)m * N + i];
+    if (reconstruct) {
+        int in[6];
+        face_inputs<DIM>(prm.thermo, true, in);
+        const int nf = v.nfaces[i];
+        for (int s = 0; s < nf; s++) {
+            const int nb = v.cell_nbr[s * N + i];
+            if (nb >= N) continue;
+            const int bs = back[s * N + i];
+            if (bs < 0) continue;  // no face back to this cell (cannot happen on a conforming grid)
+            for (int k = 0; k < NV; k++) pb[in[k]] += nba[((size_t)k * MF + bs) * N + nb];
+        }
+    }
+    // ghosts filled from this cell (fill_ghost's pre-reconstruction actions)
+    const double* fg = (const double*)v.face;
+    for (int e = v.feed_off[i]; e < v.feed_off[i + 1]; e++) {
+        const int g = v.feed_ghost[e];
+        double gb[7];
+        for (int m = 0; m < 7; m++) gb[m] = ga[(size_t)m * G + g];
+        if (gout)
+            for (int m = 0; m < 7; m++) gout[(size_t)g * 7 + m] = gb[m];
+        const BoundDev& B = v.bounds[v.ghost_bound[g]];
+        const int f = v.ghost_face[g];
+        for (int m = 0; m < 7; m++) {
+            double sv[7];
+            for (int q = 0; q < 7; q++) sv[q] = pr[q * NT + i].re;
+            StateT<DualA> src{DualA(sv[0], m == 0), DualA(sv[1], m == 1), DualA(sv[2], m == 2),
+                              DualA(sv[3], m == 3), DualA(sv[4], m == 4), DualA(sv[5], m == 5),
+                              DualA(sv[6], m == 6)};
+            StateT<DualA> gh = src;
+            apply_actions<DualA, double>(B.pre, B.n_pre, gh, src, fg, v.F, f, prm);
+            pb[m] += gb[0] * gh.rho.du + gb[1] * gh.p.du + gb[2] * gh.T.du + gb[3] * gh.e.du +
+                     gb[4] * gh.vx.du + gb[5] * gh.vy.du + gb[6] * gh.vz.du;
+        }
+    }
+    // conserved_to_primatives (primative_conserved_conversion.cpp:4-23), one seed per component
+    for (int j = 0; j < NC; j++) {
+        DualA u[NC];
+        for (int q = 0; q < NC; q++) u[q] = DualA(v.U[q * N + i], q == j ? 1.0 : 0.0);
+        DualA rho = u[0];
+        DualA vx = u[1] / rho;
+        DualA vy = u[2] / rho;
+        DualA vz = DIM == 3 ? u[3] / rho : DualA(0.0);
+        DualA ke = DualA(0.5) * (vx * vx + vy * vy + vz * vz);
+        DualA e = u[DIM + 1] / rho - ke;
+        DualA T = e / DualA(prm.Cv);
+        DualA p = rho * DualA(prm.R) * T;
+        out[(size_t)i * NC + j] = pb[0] * rho.du + pb[1] * p.du + pb[2] * T.du + pb[3] * e.du + pb[4] * vx.du +
+                                  pb[5] * vy.du + pb[6] * vz.du;
+    }
+}
+
 }  // namespace k_tan
+
+void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool reconstruct, const AdjScratch& a,
+                    double* out, double* ghost_out, cudaStream_t s) {
+    using namespace k_tan;
+    const unsigned bn = blocks_for(v.N), bf = blocks_for(v.F);
+    if (v.G > 0) cudaMemsetAsync(a.ga, 0, sizeof(double) * 7 * v.G, s);
+    if (v.dim == 3) {
+        k_tan_prims<3><<<bn, kBlock, 0, s>>>(v, p, nullptr);
+        if (reconstruct) k_recon<Dual, Dual, double, 3, true><<<bn, kBlock, 0, s>>>(v, p, 1);
+        k_adj_face<3><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a.qf, a.ga);
+        k_adj_cell<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.qf, a.self, a.nba, a.ga);
+        k_adj_final<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.self, a.nba, a.ga, a.back, out, ghost_out);
+    } else {
+        k_tan_prims<2><<<bn, kBlock, 0, s>>>(v, p, nullptr);
+        if (reconstruct) k_recon<Dual, Dual, double, 2, true><<<bn, kBlock, 0, s>>>(v, p, 1);
+        k_adj_face<2><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a.qf, a.ga);
+        k_adj_cell<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.qf, a.self, a.nba, a.ga);
+        k_adj_final<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.self, a.nba, a.ga, a.back, out, ghost_out);
+    }
+}
 
 void launch_tangent(const DevView& v, const FvParams& p, const double* vt, double inv_dt,
                     bool reconstruct, double* out, cudaStream_t s) {

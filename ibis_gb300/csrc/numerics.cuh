@@ -13,9 +13,11 @@ namespace ibisgb {
 
 #define IBISGB_HD __device__ __forceinline__
 
-struct Dual;  // dual.cuh
+template <bool RefFloor> struct DualT;  // dual.cuh
+using Dual = DualT<true>;
+using DualA = DualT<false>;
 template <class R> constexpr bool kIsDual = false;
-template <> constexpr bool kIsDual<Dual> = true;
+template <bool B> constexpr bool kIsDual<DualT<B>> = true;
 
 template <class R> IBISGB_HD R d_sqrt(R x);
 template <> IBISGB_HD double d_sqrt<double>(double x) { return sqrt(x); }

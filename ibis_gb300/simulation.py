@@ -37,6 +37,15 @@ def _ptr(a: np.ndarray):
     return C.c_void_p(a.ctypes.data)
 
 
+def _stream_arg(stream):
+    """A torch stream as the C ABI's stream argument.  The C ABI reads NULL as
+    "the context's own stream", so torch's legacy default stream (handle 0) is
+    passed as cudaStreamLegacy (handle 1) to keep the call ordered with it."""
+    if stream is None:
+        return None
+    return C.c_void_p(stream.cuda_stream or 1)
+
+
 class Simulation:
     """One ibis simulation (one grid block) on the current CUDA device.
 
@@ -120,6 +129,15 @@ class Simulation:
             raise ValueError("U has the wrong shape")
         self._call("ibisgb_set_conserved", _ptr(U))
 
+    def set_conserved_into(self, U, stream=None) -> None:
+        """Replace the conserved state from a contiguous float64 CUDA tensor (N, n_conserved)."""
+        if not (U.is_cuda and U.element_size() == 8 and U.is_contiguous()):
+            raise ValueError("U must be a contiguous float64 CUDA tensor")
+        if tuple(U.shape) != (self.num_cells, self.n_conserved):
+            raise ValueError("U has the wrong shape")
+        s = _stream_arg(stream)
+        self._call("ibisgb_set_conserved_device", C.c_void_p(U.data_ptr()), s)
+
     def stream_handle(self) -> int:
         """The context's cudaStream_t as an integer (torch.cuda.ExternalStream(ptr))."""
         s = C.c_void_p()
@@ -184,7 +202,7 @@ class Simulation:
             raise ValueError("out must be a contiguous float64 CUDA tensor")
         if tuple(out.shape) != (self.num_cells, self.n_conserved):
             raise ValueError("out has the wrong shape")
-        s = None if stream is None else C.c_void_p(stream.cuda_stream)
+        s = _stream_arg(stream)
         self._call("ibisgb_residual_device", PRECISION[precision], C.c_void_p(out.data_ptr()), s)
         return out
 
@@ -223,9 +241,34 @@ class Simulation:
         for t in (v, out):
             if not (t.is_cuda and t.element_size() == 8 and t.is_contiguous()):
                 raise ValueError("expected contiguous float64 CUDA tensors")
-        s = None if stream is None else C.c_void_p(stream.cuda_stream)
+        s = _stream_arg(stream)
         self._call("ibisgb_jvp_device", C.c_void_p(v.data_ptr()), C.c_void_p(out.data_ptr()),
                    float(inv_dt_star), int(allow_reconstruction), s)
+        return out
+
+    def vector_jacobian_product(self, w, allow_reconstruction: bool = True, ghosts: bool = False):
+        """(dR/dU)^T w for w of shape (N, n_conserved) (host arrays), the transpose of
+        matrix_vector_product's Jacobian; with ghosts, also the adjoint of every
+        ghost cell's primitives (G, 7: rho, p, T, e, vx, vy, vz)."""
+        w = np.ascontiguousarray(w, np.float64).reshape(-1)
+        if w.size != self.num_cells * self.n_conserved:
+            raise ValueError("w has the wrong size")
+        out = np.empty_like(w)
+        g = np.empty((self.num_ghost_cells, 7)) if ghosts else None
+        self._call("ibisgb_vjp", _ptr(w), _ptr(out), None if g is None else _ptr(g), int(allow_reconstruction))
+        out = out.reshape(self.num_cells, self.n_conserved)
+        return (out, g) if ghosts else out
+
+    def vector_jacobian_product_into(self, w, out, ghost_out=None, allow_reconstruction: bool = True,
+                                     stream=None):
+        """Device version for contiguous float64 CUDA tensors (N, n_conserved); ghost_out (G, 7) optional."""
+        for t in (w, out) + ((ghost_out,) if ghost_out is not None else ()):
+            if not (t.is_cuda and t.element_size() == 8 and t.is_contiguous()):
+                raise ValueError("expected contiguous float64 CUDA tensors")
+        s = _stream_arg(stream)
+        g = None if ghost_out is None else C.c_void_p(ghost_out.data_ptr())
+        self._call("ibisgb_vjp_device", C.c_void_p(w.data_ptr()), C.c_void_p(out.data_ptr()), g,
+                   int(allow_reconstruction), s)
         return out
 
     def steady_initialise(self, precision: str = "f64"):

@@ -8,7 +8,10 @@
  * A context owns one grid, its device memory and one CUDA stream.  It is not
  * thread-safe: use one context per host thread.  Host pointers passed in are
  * owned by the caller and copied before the call returns; *_device entry points
- * take device pointers and run on the context's stream.
+ * take device pointers and run on the context's stream, ordered after the work
+ * already queued on the caller's `stream` and before what the caller queues
+ * on it next.  NULL means no ordering (the context stream alone); pass
+ * cudaStreamLegacy, not NULL, for the legacy default stream.
  *
  * Array conventions follow ibis: cells and faces are in the reference's
  * numbering (cells in SU2 file order; faces numbered by first appearance while
@@ -115,6 +118,10 @@ int ibisgb_get_conserved(ibisgb_ctx* ctx, double* U);
  * of a restart. */
 int ibisgb_set_conserved(ibisgb_ctx* ctx, const double* U);
 
+/* As ibisgb_set_conserved from device memory (N x n_conserved rows), ordered
+ * after the work on `stream` (NULL: the context stream). */
+int ibisgb_set_conserved_device(ibisgb_ctx* ctx, const double* U_device, void* stream);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that record events
  * or order their own work against the context. */
 int ibisgb_get_stream(ibisgb_ctx* ctx, void** stream);
@@ -195,6 +202,24 @@ int ibisgb_jvp_device(ibisgb_ctx* ctx, const double* v_device, double* out_devic
 /* As ibisgb_jvp_device with host vectors. */
 int ibisgb_jvp(ibisgb_ctx* ctx, const double* v, double* out, double inv_dt_star,
                int32_t allow_reconstruction);
+
+/* out = (dR/dU)^T w: the adjoint (vector-Jacobian product) of the residual
+ * dU/dt at the current state, for device vectors of N x n_conserved rows, on
+ * `stream` (NULL: the context stream).  No counterpart in the reference, which
+ * has no adjoint; it is the exact transpose of the tangent of
+ * ibisgb_jvp_device (the same Dual rules, every branch -- limiter face,
+ * min/max neighbour, flux splitting -- recomputed from the current state), so
+ * <w, J v> = <J^T w, v> to rounding.  ghost_out_device (may be NULL) receives
+ * the adjoint of every ghost cell's primitives (G x 7 rows: rho, p, T, e, vx,
+ * vy, vz), from which derivatives with respect to boundary states (an inflow
+ * Mach number) follow.  allow_reconstruction = 0 gives the transpose of the
+ * first-order linearisation.  Inviscid configurations only (IBISGB_ERR_CONFIG
+ * otherwise). */
+int ibisgb_vjp_device(ibisgb_ctx* ctx, const double* w_device, double* out_device, double* ghost_out_device,
+                      int32_t allow_reconstruction, void* stream);
+
+/* As ibisgb_vjp_device with host vectors (ghost_out: G x 7, may be NULL). */
+int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out, int32_t allow_reconstruction);
 
 /* Residual and initial norms of the steady solver at the current state
  * (Jfnk::initialise, src/solvers/solvers/jfnk.cpp:25-30).  `precision` is the

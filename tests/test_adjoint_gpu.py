@@ -1,0 +1,116 @@
+"""The adjoint (vector-Jacobian product) kernels of the residual.
+
+* Dot-product test against the tangent: <w, J v> = <J^T w, v> to 1e-12
+  relative, on every inviscid configuration the tangent covers, with and
+  without reconstruction; central differences for LDFSS2, whose tangent keeps
+  the reference's nonlinear dual floor rule.
+* Boundary-state adjoint: the ghost-cell adjoint, contracted with the
+  derivative of the inflow ghost state, against central differences of the
+  residual in the inflow velocity (step 1e-6 relative): 1e-5.
+* torch.autograd: gradcheck of the residual's backward (FP64, limiter-free
+  ramp) and forward-mode jvp against the tangent.
+"""
+import numpy as np
+import pytest
+
+from ibis_gb300 import Simulation, grids
+from tests.cases import case
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(name, **kw):
+    g, c, st = case(name, **kw)
+    sim = Simulation(c, g)
+    sim.set_primitives(*st)
+    return sim, g, c, st
+
+
+@pytest.mark.parametrize("name,kw", [("ramp", {}), ("ramp", {"flux": "ausmdv"}), ("ramp", {"flux": "rusanov"}),
+                                     ("ramp", {"thermo": "rho_p"}),
+                                     ("ramp", {"thermo": "p_T"}), ("ramp", {"limiter": "unlimited"}),
+                                     ("ramp", {"order": 1}), ("box", {}), ("box_inout", {})],
+                         ids=lambda x: x if isinstance(x, str) else "-".join(f"{k}={v}" for k, v in x.items()))
+@pytest.mark.parametrize("recon", [True, False])
+def test_vjp_is_the_transpose_of_the_jvp(name, kw, recon):
+    sim, *_ = _setup(name, **kw)
+    U = sim.conserved()
+    rng = np.random.default_rng(3)
+    scale = np.abs(U).mean(axis=0)
+    v = rng.standard_normal(U.shape) * scale
+    w = rng.standard_normal(U.shape) / scale
+    jv = -sim.matrix_vector_product(v, inv_dt_star=0.0, allow_reconstruction=recon)
+    jtw = sim.vector_jacobian_product(w, allow_reconstruction=recon)
+    lhs, rhs = float(np.sum(w * jv)), float(np.sum(jtw * v))
+    mag = float(np.sum(np.abs(w * jv)))
+    assert abs(lhs - rhs) <= 1e-12 * mag, (lhs, rhs)
+
+
+@pytest.mark.parametrize("flux", ["ldfss2", "hanel"])
+def test_vjp_matches_central_differences(flux):
+    """LDFSS2's tangent keeps the reference's dual floor rule (floor applied to
+    the tangent), which is not linear in the direction, so its adjoint (true
+    derivative, floor' = 0) is checked against central differences instead."""
+    g, c, st = case("ramp", flux=flux, limiter="unlimited")
+    sim = Simulation(c, g)
+    sim.set_primitives(*st)
+    U = sim.conserved()
+    rng = np.random.default_rng(9)
+    scale = np.abs(U).mean(axis=0)
+    v = rng.standard_normal(U.shape) * scale
+    w = rng.standard_normal(U.shape) / scale
+    pred = float(np.sum(sim.vector_jacobian_product(w) * v))
+    h = 1e-6
+    sim.set_conserved(U + h * v)
+    rp = sim.compute_dudt("f64")
+    sim.set_conserved(U - h * v)
+    rm = sim.compute_dudt("f64")
+    fd = float(np.sum(w * (rp - rm) / (2 * h)))
+    assert abs(fd - pred) <= 1e-5 * abs(pred), (fd, pred)
+
+
+def test_inflow_ghost_adjoint_matches_central_differences():
+    g, c, st = case("ramp", limiter="unlimited")
+    sim = Simulation(c, g)
+    sim.set_primitives(*st)
+    U = sim.conserved()
+    rng = np.random.default_rng(5)
+    w = rng.standard_normal(U.shape) / np.abs(U).mean(axis=0)
+    _, gadj = sim.vector_jacobian_product(w, ghosts=True)
+    # inflow ghosts are the first ones (sorted boundary tags: inflow, outflow, top, wall)
+    n_in = int(g.markers["inflow"][0].shape[0])
+    pred = float(gadj[:n_in, 4].sum())  # d/d(inflow vx) of the ghost state is 1 on vx only
+    vx0 = c["grid"]["boundaries"]["inflow"]["pre_reconstruction"][0]["flow_state"]["vx"]
+    h = 1e-6 * abs(vx0)
+    res = []
+    for sgn in (1, -1):
+        cc = grids.make_config.__globals__["copy"].deepcopy(c)
+        cc["grid"]["boundaries"]["inflow"]["pre_reconstruction"][0]["flow_state"]["vx"] = vx0 + sgn * h
+        s2 = Simulation(cc, g)
+        s2.set_conserved(U)
+        res.append(s2.compute_dudt("f64"))
+    fd = float(np.sum(w * (res[0] - res[1]) / (2 * h)))
+    assert abs(fd - pred) <= 1e-5 * abs(pred), (fd, pred)
+
+
+def test_torch_autograd_gradcheck_and_forward_mode():
+    torch = pytest.importorskip("torch")
+    from torch.autograd.forward_ad import dual_level, make_dual, unpack_dual
+    from ibis_gb300.autograd import residual
+    g, c, st = case("ramp", ni=10, nj=6, limiter="unlimited")
+    sim = Simulation(c, g)
+    sim.set_primitives(*st)
+    U0 = torch.tensor(sim.conserved(), dtype=torch.float64, device="cuda")
+    scale = U0.abs().mean(dim=0)
+    rscale = residual(sim, U0).abs().mean(dim=0)
+    # gradcheck in scaled variables (inputs and outputs of order one), so that one
+    # finite-difference step and one tolerance suit every component
+    x = (U0 / scale).clone().requires_grad_(True)
+    f = lambda x: residual(sim, x * scale) / rscale  # noqa: E731
+    assert torch.autograd.gradcheck(f, (x,), eps=1e-6, atol=1e-5, rtol=1e-4, nondet_tol=0.0)
+    v = torch.randn_like(U0) * scale
+    with dual_level():
+        out = residual(sim, make_dual(U0, v))
+        jv = unpack_dual(out).tangent
+    ref = -torch.tensor(sim.matrix_vector_product(v.cpu().numpy(), inv_dt_star=0.0), device="cuda")
+    assert torch.allclose(jv, ref, rtol=1e-12, atol=1e-12 * ref.abs().max().item())
