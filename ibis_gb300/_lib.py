@@ -38,6 +38,11 @@ class NewtonStatus(C.Structure):
                 ("step", C.c_int64)]
 
 
+class AdjointStatus(C.Structure):
+    _fields_ = [("residual_norm", C.c_double), ("gmres_iterations", C.c_int32), ("gmres_converged", C.c_int32),
+                ("gmres_residual", C.c_double), ("dt_star", C.c_double)]
+
+
 class RkStatus(C.Structure):
     _fields_ = [("t", C.c_double), ("dt", C.c_double), ("stable_dt", C.c_double),
                 ("steps", C.c_int64), ("bad_cells", C.c_int64), ("device_ms", C.c_double)]
@@ -89,6 +94,7 @@ def load(build_if_missing: bool = True):
     L.ibisgb_jvp_device.argtypes = [_P, _P, _P, C.c_double, C.c_int32, _P]
     L.ibisgb_vjp.argtypes = [_P, _P, _P, _P, C.c_int32]
     L.ibisgb_vjp_device.argtypes = [_P, _P, _P, _P, C.c_int32, _P]
+    L.ibisgb_adjoint_step.argtypes = [_P, _P, _P, C.c_double, C.POINTER(AdjointStatus)]
     L.ibisgb_steady_initialise.argtypes = [_P, C.c_int32]
     L.ibisgb_newton_step.argtypes = [_P, C.c_int32, C.POINTER(NewtonStatus)]
     L.ibisgb_autotune.argtypes = [_P, C.c_int32, _P, _P]

@@ -1118,6 +1118,48 @@ struct ibisgb_ctx {
         }
     }
 
+    // One pseudo-time step of the steady adjoint J^T lambda + g = 0 (J = dR/dU at
+    // the current state): r = J^T lambda + g, GMRES on (I/dt* - J^T) d = r with
+    // the steady solver's settings, lambda += d.  The continuation converges
+    // wherever the forward pseudo-time iteration does (J^T has J's spectrum) and
+    // becomes one linear solve as the CFL grows.
+    DBuf adj_r, adj_d, adj_norm;
+    void adjoint_step(const double* g, double* lam, double cfl, ibisgb_adjoint_status* out) {
+        if (n_cases > 1) throw StateError("steady-state solves run one case per context, not on a batch");
+        if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
+        const Steady& st = steady;
+        const size_t n = nvars();
+        ensure_krylov(st.max_iters);
+        adj_r.alloc(sizeof(double) * n);
+        adj_d.alloc(sizeof(double) * n);
+        adj_norm.alloc(sizeof(double) * 2);
+        double* r = adj_r.as<double>();
+        double* d = adj_d.as<double>();
+        vjp(lam, r, nullptr, true);
+        launch_axpby(r, g, (long long)n, 1.0, 1.0, stream);  // r = J^T lambda + g
+        launch_dot(r, r, (long long)n, kpart.as<double>(), adj_norm.as<double>(), true, stream);
+        double rnorm = 0.0;
+        CUDA_OK(cudaMemcpyAsync(&rnorm, adj_norm.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        const double stable = estimate_dt(IBISGB_F64);  // synchronizes the stream
+        const double dt_star = cfl * stable, inv = 1.0 / dt_star;
+        CUDA_OK(cudaMemsetAsync(d, 0, sizeof(double) * n, stream));
+        auto A = [&](const double* x, double* y) {
+            vjp(x, y, nullptr, true);
+            launch_axpby(y, x, (long long)n, inv, -1.0, stream);  // y = x / dt* - J^T x
+        };
+        GmresOut res = gmres(A, r, d, st.max_iters, st.tol, kv.as<double>(), nullptr, nullptr);
+        launch_axpby(lam, d, (long long)n, 1.0, 1.0, stream);
+        CUDA_OK(cudaGetLastError());
+        CUDA_OK(cudaStreamSynchronize(stream));
+        if (out) {
+            out->residual_norm = rnorm;
+            out->gmres_iterations = res.iters;
+            out->gmres_converged = res.success ? 1 : 0;
+            out->gmres_residual = res.residual;
+            out->dt_star = dt_star;
+        }
+    }
+
     // the preconditioner's own GMRES, with separate Krylov storage
     DBuf pv, pw, pr0, pH, ppart, pscal;
     template <class Op>
@@ -1640,6 +1682,8 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
                 put(o.data(), sizeof(double) * o.size());
                 break;
             }
+            case 11: put(m.ghost_face.data(), sizeof(int64_t) * G); break;
+            case 12: put(m.ghost_bound.data(), sizeof(int64_t) * G); break;
             default: throw ArgError("unknown dump");
         }
     });
@@ -1718,6 +1762,12 @@ int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out,
                                     ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
+}
+
+int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_device, double cfl,
+                        ibisgb_adjoint_status* status) {
+    if (!ctx || !g_device || !lambda_device || !(cfl > 0.0)) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->adjoint_step(g_device, lambda_device, cfl, status); });
 }
 
 int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision) {

@@ -190,6 +190,7 @@ void launch_scale_inv(double* out, const double* in, long long n, const double* 
 void launch_sub(double* out, const double* a, const double* b, long long n, cudaStream_t s);
 void launch_gemv_add(double* x, const double* V, long long n, int m, const double* y, cudaStream_t s);
 void launch_add_rows(double* U, const double* dU, int N, int nc, cudaStream_t s);
+void launch_axpby(double* y, const double* x, long long n, double a, double b, cudaStream_t s);  // y = a x + b y
 int dot_scratch_doubles();
 
 // tangent of the residual: out = inv_dt * v - dR/dU v (kernels_tangent.cu); v, out: N x nc rows

@@ -168,6 +168,12 @@ __global__ void k_gemv_add(double* x, const double* V, long long n, int m, const
     }
 }
 
+// y = a x + b y
+__global__ void k_axpby(double* y, const double* x, long long n, double a, double b) {
+    for (long long i = (long long)blockIdx.x * kRB + threadIdx.x; i < n; i += (long long)gridDim.x * kRB)
+        y[i] = a * x[i] + b * y[i];
+}
+
 // U[q][i] += dU[i * nc + q]   (Jfnk::apply_update_, jfnk.cpp:63-76)
 __global__ void k_add_rows(double* U, const double* dU, int N, int nc) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -193,6 +199,9 @@ void launch_sub(double* out, const double* a, const double* b, long long n, cuda
 }
 void launch_gemv_add(double* x, const double* V, long long n, int m, const double* y, cudaStream_t s) {
     k_gemv_add<<<kDotBlocks, kRB, 0, s>>>(x, V, n, m, y);
+}
+void launch_axpby(double* y, const double* x, long long n, double a, double b, cudaStream_t s) {
+    k_axpby<<<kDotBlocks, kRB, 0, s>>>(y, x, n, a, b);
 }
 void launch_add_rows(double* U, const double* dU, int N, int nc, cudaStream_t s) {
     long long n = (long long)N * nc;

@@ -142,6 +142,48 @@ def ramp_2d(ni=256, nj=128, length=1.0, height=0.5, ramp_start=0.2, angle_deg=15
     return g
 
 
+def hicks_henne(s: np.ndarray, peak: float, width: float = 3.0) -> np.ndarray:
+    """Hicks-Henne bump sin(pi s^m)^width on s in [0, 1], m = ln 0.5 / ln peak,
+    which is 1 at s = peak and 0 at both ends."""
+    s = np.clip(s, 0.0, 1.0)
+    m = math.log(0.5) / math.log(peak)
+    return np.sin(math.pi * s ** m) ** width
+
+
+def ramp_bump_peaks(n: int = 16) -> np.ndarray:
+    return (np.arange(n) + 0.5) / n
+
+
+def ramp_2d_bumps(ni=512, nj=256, length=1.0, height=0.5, ramp_start=0.2, angle_deg=15.0,
+                  bumps=None) -> Su2Grid:
+    """Compression ramp with its inclined surface perturbed by Hicks-Henne bumps:
+    the wall point at ramp coordinate s = (x - ramp_start) / (length - ramp_start)
+    moves by d(s) = sum_k bumps[k] hicks_henne(s, peak_k) (metres) along the
+    ramp's normal, and every grid point above it by d(s) (1 - eta), eta = j / nj,
+    so the displacement fades to zero at the top boundary.  Peaks are spread
+    evenly over the ramp (ramp_bump_peaks); bumps=None gives ramp_2d."""
+    g = ramp_2d(ni, nj, length, height, ramp_start, angle_deg)
+    if bumps is None:
+        return g
+    bumps = np.asarray(bumps, np.float64)
+    x = np.linspace(0.0, length, ni + 1)
+    sc = (x - ramp_start) / (length - ramp_start)
+    d = np.zeros(ni + 1)
+    on = sc > 0.0
+    for a, pk in zip(bumps, ramp_bump_peaks(len(bumps))):
+        d[on] += a * hicks_henne(sc[on], pk)
+    th = math.radians(angle_deg)
+    nx, ny = -math.sin(th), math.cos(th)
+    eta = np.arange(nj + 1) / nj
+    D = d[:, None] * (1.0 - eta[None, :])  # (ni+1, nj+1)
+    xyz = g.xyz.copy()
+    vid = np.arange((ni + 1) * (nj + 1)).reshape(nj + 1, ni + 1).T  # vertex id = i + (ni+1) j
+    xyz[vid.reshape(-1), 0] += (D * nx).reshape(-1)
+    xyz[vid.reshape(-1), 1] += (D * ny).reshape(-1)
+    g.xyz = xyz
+    return g
+
+
 def stretched_spacing(n: int, total: float, first: float, ratio: float) -> np.ndarray:
     """Wall-normal node positions: geometric growth ``ratio`` from ``first``,
     capped at the uniform spacing that fills ``total`` with the remaining cells.
@@ -372,6 +414,17 @@ def ramp_ensemble(n_cases=64, seed=0, smallest=(64, 32), largest=(512, 256), mac
         g, c, inf = ramp_case(ni, nj, mach=prm["mach"], T=prm["T"], p=p, angle_deg=prm["angle_deg"], **kw)
         out.append((g, c, inf, prm))
     return out
+
+
+def ramp_bump_case(ni=512, nj=256, mach=2.0, T=300.0, p=101325.0, angle_deg=15.0, bumps=None, **kw):
+    """BASELINE config 4's geometry: the compression ramp of ramp_case with its
+    surface perturbed by Hicks-Henne bumps (ramp_2d_bumps).  Returns (grid, config, inflow)."""
+    gas = ideal_gas(287.0)
+    inflow = mach_state(gas, mach, T, p)
+    grid = ramp_2d_bumps(ni, nj, angle_deg=angle_deg, bumps=bumps)
+    bnds = {"inflow": supersonic_inflow(inflow), "outflow": supersonic_outflow(),
+            "wall": slip_wall(), "top": slip_wall()}
+    return grid, make_config(2, bnds, gas=gas, **kw), inflow
 
 
 def flat_plate_case(ni=512, nj=256, mach=2.0, T=220.0, Re_per_m=1e5, Pr=0.71, **kw):

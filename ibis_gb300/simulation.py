@@ -30,7 +30,7 @@ DUMPS = {"left": (0, np.int64), "right": (1, np.int64), "cell_faces": (2, np.int
          "outsigns": (3, np.int32), "neighbours": (4, np.int64), "ghost_source": (5, np.int64),
          "face_geometry": (6, np.float64), "cell_geometry": (7, np.float64),
          "limiter_branches": (8, np.uint32), "limiters": (9, np.float64),
-         "face_flux": (10, np.float64)}
+         "face_flux": (10, np.float64), "ghost_face": (11, np.int64), "ghost_boundary": (12, np.int64)}
 
 
 def _ptr(a: np.ndarray):
@@ -271,6 +271,20 @@ class Simulation:
                    int(allow_reconstruction), s)
         return out
 
+    def adjoint_step(self, g, lam, cfl: float) -> dict:
+        """One pseudo-time step of the steady adjoint J^T lambda = -g (ibisgb_adjoint_step);
+        g and lam are contiguous float64 CUDA tensors (N, n_conserved), lam updated in place."""
+        from ._lib import AdjointStatus
+        for t in (g, lam):
+            if not (t.is_cuda and t.element_size() == 8 and t.is_contiguous()):
+                raise ValueError("expected contiguous float64 CUDA tensors")
+        st = AdjointStatus()
+        self._call("ibisgb_adjoint_step", C.c_void_p(g.data_ptr()), C.c_void_p(lam.data_ptr()), float(cfl),
+                   C.byref(st))
+        return {"residual_norm": st.residual_norm, "gmres_iterations": st.gmres_iterations,
+                "gmres_converged": bool(st.gmres_converged), "gmres_residual": st.gmres_residual,
+                "dt_star": st.dt_star}
+
     def steady_initialise(self, precision: str = "f64"):
         """Jfnk::initialise: residual and initial norms at the current state."""
         self._call("ibisgb_steady_initialise", PRECISION[precision])
@@ -301,7 +315,7 @@ class Simulation:
         shape = {"left": (F,), "right": (F,), "cell_faces": (N, MF), "outsigns": (N, MF),
                  "neighbours": (N, MF), "ghost_source": (G,), "face_geometry": (13, F),
                  "cell_geometry": (4, NT), "limiter_branches": (N, 5), "limiters": (5, N),
-                 "face_flux": (F, nc)}[name]
+                 "face_flux": (F, nc), "ghost_face": (G,), "ghost_boundary": (G,)}[name]
         out = np.empty(shape, dt)
         self._call("ibisgb_get_dump", which, _ptr(out), out.nbytes)
         return out

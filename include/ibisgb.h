@@ -172,7 +172,9 @@ int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]);
  * 7 cell geometry (double 4 x (N+G): centroid, volume),
  * 8 limiter branch codes of the last residual (uint32 N x 5),
  * 9 limiter values of the last residual (double 5 x N),
- * 10 face fluxes of the last residual (double F x n_conserved). */
+ * 10 face fluxes of the last residual (double F x n_conserved),
+ * 11 boundary face of each ghost cell (int64 G), 12 boundary (index in sorted
+ * tag order) of each ghost cell (int64 G). */
 int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
 
 /* Result of one Newton step of the steady solver. */
@@ -220,6 +222,28 @@ int ibisgb_vjp_device(ibisgb_ctx* ctx, const double* w_device, double* out_devic
 
 /* As ibisgb_vjp_device with host vectors (ghost_out: G x 7, may be NULL). */
 int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out, int32_t allow_reconstruction);
+
+/* Result of one pseudo-time step of the steady adjoint. */
+typedef struct {
+    double residual_norm;   /* |J^T lambda + g| before the step */
+    int32_t gmres_iterations;
+    int32_t gmres_converged;
+    double gmres_residual;  /* |g_k| / beta of the last GMRES iteration */
+    double dt_star;         /* cfl * stable dt of the current state */
+} ibisgb_adjoint_status;
+
+/* One step of the discrete adjoint of the steady problem, J^T lambda = -g with
+ * J = dR/dU at the current (converged) state and g = dObjective/dU (device
+ * vectors, N x n_conserved rows): r = J^T lambda + g, then GMRES on
+ * (I/dt* - J^T) d = r (dt* = cfl * the stable time step; GMRES length and
+ * tolerance from the config's steady solver, or 50 and 1e-2) and lambda += d,
+ * in place.  The transposed counterpart of ibisgb_newton_step; no counterpart
+ * in the reference.  Iterate with a growing cfl until residual_norm is small.
+ * With lambda, dObjective/dp = dObjective/dp|_U + lambda . dR/dp for any
+ * parameter p of the boundary states (through ibisgb_vjp's ghost adjoint) or of
+ * the grid. */
+int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_device, double cfl,
+                        ibisgb_adjoint_status* status);
 
 /* Residual and initial norms of the steady solver at the current state
  * (Jfnk::initialise, src/solvers/solvers/jfnk.cpp:25-30).  `precision` is the
