@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--batch-cases", type=int, default=64, help="ramp cases of the batched ensemble (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=200, help="timed RK steps of the batched ensemble")
     ap.add_argument("--seq-steps", type=int, default=40, help="timed RK steps per case, one case at a time")
+    ap.add_argument("--plate-steps", type=int, default=300, help="RK steps of the flat-plate accuracy case (0: skip)")
+    ap.add_argument("--newton-steps", type=int, default=25, help="Newton steps of the ramp JFNK case (0: skip)")
     return ap.parse_args()
 
 
@@ -195,6 +197,99 @@ def batch_measure(args, barrier):
                                             "steps": args.warmup + args.batch_steps}}
 
 
+def plate_measure(args):
+    """Laminar flat plate (512 x 256, wall-normal stretching 1.05 from 1e-5 m, Mach 2,
+    T 220 K, Re 1e5 per metre, Sutherland air with Pr 0.71, adiabatic no-slip wall
+    from x = 0): args.plate_steps RK steps from the uniform inflow state in the
+    mixed and FP64 builds; relative L2 and max errors of density, pressure and
+    wall skin friction of the mixed build against the FP64 one (which matches
+    the FP64 oracle to 1e-12 per cell), and both builds' throughput."""
+    from ibis_gb300 import Simulation, grids
+    g, c, inf = grids.flat_plate_case(512, 256)
+    out = {"workload": "2-D laminar flat plate 512x256, ssp-rk3, Hanel, MUSCL + Barth-Jespersen, viscous",
+           "steps": args.plate_steps}
+    q_inf = 0.5 * inf["rho"] * inf["vx"] ** 2
+    res = {}
+    for prec in ("mixed", "f64"):
+        sim = Simulation(c, g)
+        n = sim.num_cells
+        sim.set_primitives(np.full(n, inf["T"]), np.full(n, inf["p"]), np.full(n, inf["vx"]), np.full(n, inf["vy"]))
+        sim.take_steps(2, prec)
+        st = sim.take_steps(args.plate_steps, prec)
+        pr = sim.primitives()
+        sim.compute_dudt(prec)
+        flux = sim.dump("face_flux_mixed" if prec == "mixed" else "face_flux")
+        sel = sim.dump("ghost_boundary") == sorted(c["grid"]["boundaries"]).index("wall")
+        faces = sim.dump("ghost_face")[sel]
+        ny = sim.dump("face_geometry")[1, faces]
+        cf = -flux[faces, 1] / (ny * q_inf)  # wall shear / dynamic pressure (flux x-momentum = -tau_xy n_y)
+        res[prec] = (pr["rho"], pr["p"], cf)
+        out[f"{prec}_value"] = n * 3.0 * args.plate_steps / (st["device_ms"] / 1e3) / 1e6
+    for k, name in enumerate(("rho", "p", "cf")):
+        a, b = res["mixed"][k], res["f64"][k]
+        out[f"{name}_rel_l2_err"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        out[f"{name}_rel_max_err"] = float(np.abs(a - b).max() / np.abs(b).max())
+    out["unit"] = "Mcell-updates/s"
+    return out
+
+
+def jfnk_measure(args):
+    """Steady Jacobian-free Newton-Krylov on the Hicks-Henne ramp (512 x 256,
+    15 degrees, 16 bump amplitudes U[-0.002, 0.002] m and inflow Mach U[1.5, 3]
+    drawn from seed 0; GMRES of 30 vectors per Newton step, residual-based CFL):
+    args.newton_steps steps from the uniform inflow state with their residual
+    history, and the rates of the tangent (Jv) and adjoint (J^T w) products and
+    of one adjoint continuation step at the final state."""
+    import torch
+    from ibis_gb300 import Simulation, grids
+    from ibis_gb300.adjoint import wall_force
+    rng = np.random.default_rng(0)
+    mach = float(rng.uniform(1.5, 3.0))
+    bumps = rng.uniform(-0.002, 0.002, 16)
+    cfl = {"type": "residual_based", "growth_threshold": 1.0, "power": 1.0, "start_cfl": 2.0, "max_cfl": 1e12}
+    solver = grids.steady_state(cfl=cfl, max_iters=30, tol=1e-3, max_steps=1000)
+    g, c, inf = grids.ramp_bump_case(512, 256, mach=mach, bumps=bumps, solver=solver)
+    sim = Simulation(c, g)
+    n = sim.num_cells
+    sim.set_primitives(np.full(n, inf["T"]), np.full(n, inf["p"]), np.full(n, inf["vx"]), np.full(n, inf["vy"]))
+    sim.steady_initialise("f64")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = [sim.newton_step("f64") for _ in range(args.newton_steps)]
+    torch.cuda.synchronize()
+    newton_s = time.perf_counter() - t0
+    U = torch.tensor(sim.conserved(), dtype=torch.float64, device="cuda")
+    v = torch.randn_like(U) * U.abs().mean(dim=0)
+    out_t = torch.empty_like(U)
+
+    def rate(fn, reps=20):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return reps / (time.perf_counter() - t)
+
+    stream = torch.cuda.current_stream()
+    jv_rate = rate(lambda: sim.matrix_vector_product_into(v, out_t, 1.0, stream=stream))
+    vjp_rate = rate(lambda: sim.vector_jacobian_product_into(v, out_t, stream=stream))
+    _, dJ = wall_force(sim, x_min=0.2)
+    gt = torch.tensor(dJ, dtype=torch.float64, device="cuda")
+    lam = torch.zeros_like(gt)
+    t = time.perf_counter()
+    ast = sim.adjoint_step(gt, lam, 10.0)
+    adj_s = time.perf_counter() - t
+    rel = [h["relative_residual"] for h in hist]
+    return {"workload": f"2-D Hicks-Henne ramp 512x256 (15 deg, Mach {mach:.3f}, 16 bumps), MUSCL + Barth-Jespersen, "
+                        "JFNK with GMRES(30), FP64",
+            "newton_steps": len(hist), "ms_per_newton_step": newton_s * 1e3 / len(hist),
+            "relative_residual": rel[-1], "residual_history": [float(f"{x:.3e}") for x in rel],
+            "gmres_iterations": [h["gmres_iterations"] for h in hist],
+            "jv_per_s": jv_rate, "vjp_per_s": vjp_rate,
+            "adjoint_step_ms": adj_s * 1e3, "adjoint_step_gmres_iterations": ast["gmres_iterations"]}
+
+
 def run_reference(args, world, rank):
     """--impl reference: the oracle port of the reference's CPU path, all host threads."""
     if rank != 0:
@@ -313,6 +408,8 @@ def run_ours(args, world, rank, local):
                 traffic = float(line.split(":")[1].split()[0])
 
     batch = batch_measure(args, barrier) if args.batch_cases > 0 else None
+    plate = plate_measure(args) if args.plate_steps > 0 and rank == 0 else None
+    jfnk = jfnk_measure(args) if args.newton_steps > 0 and rank == 0 else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -340,6 +437,8 @@ def run_ours(args, world, rank, local):
             "autotune": {"variants_table": Simulation.launch_variants(), "mixed": tune_mixed, "f64": tune_f64,
                          "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")}},
             "batch": batch,
+            "plate": plate,
+            "jfnk": jfnk,
             "roofline": {"bound": "hbm", "kernel": "rk_stage (recon + face + update kernels of one stage)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "bytes_per_cell_update": B_ALG_3D["mixed"],

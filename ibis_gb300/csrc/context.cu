@@ -1682,6 +1682,18 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
                 put(o.data(), sizeof(double) * o.size());
                 break;
             }
+            case 13: {  // face fluxes of the last mixed-precision residual / stage
+                std::vector<float> soa(ctx->nc() * F);
+                dev(ctx->s32.flux.p, 0);
+                CUDA_OK(cudaMemcpyAsync(soa.data(), ctx->s32.flux.p, sizeof(float) * soa.size(),
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+                CUDA_OK(cudaStreamSynchronize(ctx->stream));
+                std::vector<double> o(soa.size());
+                for (int64_t f = 0; f < F; f++)
+                    for (int q = 0; q < ctx->nc(); q++) o[f * ctx->nc() + q] = soa[q * F + f];
+                put(o.data(), sizeof(double) * o.size());
+                break;
+            }
             case 11: put(m.ghost_face.data(), sizeof(int64_t) * G); break;
             case 12: put(m.ghost_bound.data(), sizeof(int64_t) * G); break;
             default: throw ArgError("unknown dump");

@@ -30,7 +30,8 @@ DUMPS = {"left": (0, np.int64), "right": (1, np.int64), "cell_faces": (2, np.int
          "outsigns": (3, np.int32), "neighbours": (4, np.int64), "ghost_source": (5, np.int64),
          "face_geometry": (6, np.float64), "cell_geometry": (7, np.float64),
          "limiter_branches": (8, np.uint32), "limiters": (9, np.float64),
-         "face_flux": (10, np.float64), "ghost_face": (11, np.int64), "ghost_boundary": (12, np.int64)}
+         "face_flux": (10, np.float64), "ghost_face": (11, np.int64), "ghost_boundary": (12, np.int64),
+         "face_flux_mixed": (13, np.float64)}
 
 
 def _ptr(a: np.ndarray):
@@ -315,7 +316,8 @@ class Simulation:
         shape = {"left": (F,), "right": (F,), "cell_faces": (N, MF), "outsigns": (N, MF),
                  "neighbours": (N, MF), "ghost_source": (G,), "face_geometry": (13, F),
                  "cell_geometry": (4, NT), "limiter_branches": (N, 5), "limiters": (5, N),
-                 "face_flux": (F, nc), "ghost_face": (G,), "ghost_boundary": (G,)}[name]
+                 "face_flux": (F, nc), "ghost_face": (G,), "ghost_boundary": (G,),
+                 "face_flux_mixed": (F, nc)}[name]
         out = np.empty(shape, dt)
         self._call("ibisgb_get_dump", which, _ptr(out), out.nbytes)
         return out

@@ -174,7 +174,8 @@ int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]);
  * 9 limiter values of the last residual (double 5 x N),
  * 10 face fluxes of the last residual (double F x n_conserved),
  * 11 boundary face of each ghost cell (int64 G), 12 boundary (index in sorted
- * tag order) of each ghost cell (int64 G). */
+ * tag order) of each ghost cell (int64 G), 13 face fluxes of the last MIXED
+ * residual evaluation (double F x n_conserved, from the float fluxes). */
 int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
 
 /* Result of one Newton step of the steady solver. */
