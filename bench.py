@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--batch-cases", type=int, default=64, help="ramp cases of the batched ensemble (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=200, help="timed RK steps of the batched ensemble")
     ap.add_argument("--seq-steps", type=int, default=40, help="timed RK steps per case, one case at a time")
+    ap.add_argument("--fused", default="auto", choices=["auto", "on", "off"],
+                    help="fused stage for structured blocks: let the autotuner choose, force, or disable")
     ap.add_argument("--plate-steps", type=int, default=300, help="RK steps of the flat-plate accuracy case (0: skip)")
     ap.add_argument("--newton-steps", type=int, default=25, help="Newton steps of the ramp JFNK case (0: skip)")
     return ap.parse_args()
@@ -348,6 +350,7 @@ def run_ours(args, world, rank, local):
 
     # --- headline: mixed precision, device-resident state
     sim.set_primitives(*ic)
+    sim.set_fused({"auto": -1, "on": 1, "off": 0}[args.fused])
     tune_mixed = sim.autotune("mixed")
     fused = sim.fused_info()
     sim.take_steps(args.warmup, "mixed")

@@ -567,8 +567,30 @@ __device__ __forceinline__ double recip_newton(double x) {
     return fma(r, e, r);
 }
 
+// float -> double by assembling the bit pattern on the integer pipe (exact: a
+// double holds every float; zero, infinities and NaN keep their form, subnormal
+// floats take the conversion instruction), which keeps the conversions of the
+// mixed update off GB300's narrow FP64 pipe.
+__device__ __forceinline__ double f2d(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned long long man = (unsigned long long)(u & 0x7FFFFFu) << 29;
+    if (ex == 0) return (u & 0x7FFFFFu) ? (double)x : __longlong_as_double((long long)sign);
+    const unsigned long long e11 = ex == 0xFFu ? 0x7FFull : (unsigned long long)(ex + 896u);
+    return __longlong_as_double((long long)(sign | (e11 << 52) | man));
+}
+
+// What the update needs of a committed state: rho (bad-cell test) and the
+// stored temperature and velocity (local time step), at storage precision P.
+template <class P>
+struct Committed {
+    double rho;
+    P T, vx, vy, vz;
+};
+
 template <class P, class Gm, int DIM, bool EXACT>
-__device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, const double* u) {
+__device__ Committed<P> commit_state(const DevView& v, const FvParams& prm, int i, const double* u) {
     // conserved_to_primatives in double (primative_conserved_conversion.cpp:4-23); the fast
     // paths replace the divisions by one reciprocal (the FP64 pipe is GB300's scarcest unit)
     double rho = u[0], vx, vy, vz, e, T;
@@ -585,13 +607,17 @@ __device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, co
         const float rf = (float)rho, ef = (float)e;
         const float Tf = ef * prm.finv_Cv;
         const float pf = rf * prm.fR * Tf;
+        const float vxf = (float)vx, vyf = (float)vy, vzf = (float)vz;
         P* pr = (P*)v.prim;
         const int NT = v.NT;
         pr[i] = (P)rf; pr[NT + i] = (P)pf; pr[2 * NT + i] = (P)Tf; pr[3 * NT + i] = (P)ef;
-        pr[4 * NT + i] = (P)vx; pr[5 * NT + i] = (P)vy; pr[6 * NT + i] = (P)vz;
-        const State64 s{rho, (double)pf, (double)Tf, e, vx, vy, vz};
-        for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
-        return s;
+        pr[4 * NT + i] = (P)vxf; pr[5 * NT + i] = (P)vyf; pr[6 * NT + i] = (P)vzf;
+        const int k0 = v.feed_off[i], k1 = v.feed_off[i + 1];
+        if (k0 < k1) {  // boundary cells: the ghost actions work on the double state
+            const State64 s{rho, f2d(pf), f2d(Tf), e, vx, vy, vz};
+            for (int k = k0; k < k1; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
+        }
+        return Committed<P>{rho, (P)Tf, (P)vxf, (P)vyf, (P)vzf};
     }
     if (EXACT) {
         vx = u[1] / rho;
@@ -616,7 +642,7 @@ __device__ State64 commit_state(const DevView& v, const FvParams& prm, int i, co
     pr[4 * NT + i] = (P)vx; pr[5 * NT + i] = (P)vy; pr[6 * NT + i] = (P)vz;
     const State64 s{rho, p, T, e, vx, vy, vz};
     for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
-    return s;
+    return Committed<P>{rho, (P)T, (P)vx, (P)vy, (P)vz};
 }
 
 // control block of the case cell i belongs to
@@ -630,7 +656,13 @@ IBISGB_HD bool is_negative(double x) {  // x < 0.0: sign set, nonzero, not NaN
     const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
     return (b >> 63) && mag != 0 && mag <= 0x7FF0000000000000ull;
 }
-IBISGB_HD void count_bad(StepCtl* ctl, const State64& s) {
+IBISGB_HD bool is_negative(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned mag = b & 0x7FFFFFFFu;
+    return (b >> 31) && mag != 0 && mag <= 0x7F800000u;
+}
+template <class P>
+IBISGB_HD void count_bad(StepCtl* ctl, const Committed<P>& s) {
     const unsigned long long rb = (unsigned long long)__double_as_longlong(s.rho);
     if (is_negative(s.T) || is_negative(s.rho) || ((rb >> 52) & 0x7FFull) == 0x7FFull)
         atomicAdd(&ctl->bad_cells, 1ull);
@@ -669,7 +701,12 @@ __device__ double cell_local_dt(const DevView& v, const FvParams& prm, int i, P 
             sf += (fabsf(dot) + a) * A;
             if (prm.viscous) srv += v.vsig[f] * (double)A * (double)A / vol;
         }
-        src = (double)sf;
+        if (!prm.viscous) {
+            // the float build's inviscid signal is a float; so is its quotient
+            const float lf = __fdiv_rn((float)vol, sf);
+            return lf > 0.f ? f2d(lf) : 1.0e308 * 10.0;
+        }
+        src = f2d(sf);
     } else {
         const double vx = (double)pvx, vy = (double)pvy, vz = (double)pvz;
         const double a = sqrt(prm.gamma * prm.R * (double)pT);
@@ -763,7 +800,7 @@ __device__ __forceinline__ double update_tail(const DevView& v, const FvParams& 
         }
         const double c = ctl->cb[stage] * iv;
 #pragma unroll
-        for (int q = 0; q < NC; q++) u[q] = fma((double)lo[q], c, fma((double)hi[q], c, u[q]));
+        for (int q = 0; q < NC; q++) u[q] = fma(f2d(lo[q]), c, fma(f2d(hi[q]), c, u[q]));
     } else {
         for (int j = 0; j < ctl->stages; j++) {
             const double c = ctl->cb[j];
@@ -776,10 +813,10 @@ __device__ __forceinline__ double update_tail(const DevView& v, const FvParams& 
     }
 #pragma unroll
     for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
-    const State64 st = commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
+    const Committed<P> st = commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
     count_bad(ctl, st);
     if (!with_dt) return kInf;
-    return cell_local_dt<P, Gm, DIM>(v, prm, i, (P)st.vx, (P)st.vy, (P)st.vz, (P)st.T);
+    return cell_local_dt<P, Gm, DIM>(v, prm, i, st.vx, st.vy, st.vz, st.T);
 }
 
 // One valid cell of k_update; returns the local time step of the new state when
@@ -819,7 +856,7 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
         iv = v.inv_vol[i];
         if (!fold) {
 #pragma unroll
-            for (int q = 0; q < NC; q++) ks[q] = ((double)hi[q] + (double)lo[q]) * iv;
+            for (int q = 0; q < NC; q++) ks[q] = (f2d(hi[q]) + f2d(lo[q])) * iv;
         }
     } else {
         double acc[NC];

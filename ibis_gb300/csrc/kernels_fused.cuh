@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(FusedTile<DIM>::kThreads, DIM == 3 ? 2 : 3)
             double* kk = v.k + (size_t)stage * NC * N;
 #pragma unroll
             for (int q = 0; q < NC; q++) {
-                ks[q] = ((double)hi[q] + (double)lo[q]) * iv;
+                ks[q] = (f2d(hi[q]) + f2d(lo[q])) * iv;
                 kk[q * N + i] = ks[q];
             }
         }

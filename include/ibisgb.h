@@ -267,7 +267,8 @@ int ibisgb_synchronize(ibisgb_ctx* ctx);
  * launch variants (threads per block x minimum resident blocks per SM, which
  * caps registers per thread).  ibisgb_autotune times every variant on the
  * context's grid and current state (CUDA events; the update kernel in its
- * residual-only mode), keeps the fastest and returns the choice in variants
+ * first-stage Runge-Kutta mode, with the primitives it overwrites restored),
+ * keeps the fastest and returns the choice in variants
  * (recon, face, update) and, if times_ms is not NULL, the time of every
  * variant (fastest of three launches; 3 x count doubles, kernel-major).  ibisgb_rk_run tunes a precision
  * by itself on its first call unless variants were set.  All variants give
