@@ -1856,6 +1856,17 @@ int ibisgb_launch_variants(int32_t* count, int32_t* threads, int32_t* min_blocks
     return IBISGB_OK;
 }
 
+int ibisgb_check_conversions(int64_t samples, uint64_t seed, int64_t* mismatches) {
+    if (!mismatches || samples < 0) return IBISGB_ERR_ARG;
+    unsigned long long m = 0;
+    if (check_float_conversions((long long)samples, (unsigned long long)seed, &m) != 0) {
+        g_create_error = "CUDA failure in the conversion self-check";
+        return IBISGB_ERR_CUDA;
+    }
+    *mismatches = (int64_t)m;
+    return IBISGB_OK;
+}
+
 int ibisgb_set_fused(ibisgb_ctx* ctx, int32_t mode) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] { ctx->set_fused(mode); });

@@ -165,6 +165,9 @@ void launch_fused_stage(const DevView& v, const SbView& sb, const FvParams& prm,
                         cudaStream_t s);
 cudaError_t prepare_fused_stage();              // shared-memory opt-in, once per device
 void fused_tile_shape(int dim, int* tx, int* ty, int* tz);
+// The mixed build's integer-pipe float -> double conversion against the
+// conversion instruction on n pseudo-random bit patterns; mismatches counted.
+int check_float_conversions(long long n, unsigned long long seed, unsigned long long* mismatches);
 
 // Scratch of the adjoint passes (device pointers; sizes in launch_adjoint's callers).
 struct AdjScratch {

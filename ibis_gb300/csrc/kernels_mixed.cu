@@ -16,6 +16,37 @@ void launch_fused_stage(const DevView& v, const SbView& sb, const FvParams& prm,
     k_mixed::launch_fused(v, sb, prm, mode, stage, with_dt, s);
 }
 cudaError_t prepare_fused_stage() { return k_mixed::prepare_fused(); }
+// Self-check of the integer-pipe float -> double conversion against the
+// conversion instruction, compiled with the same flags as the kernels that use
+// it: n pseudo-random float bit patterns (splitmix64 from seed).
+namespace {
+__device__ unsigned long long splitmix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__global__ void k_check_conversions(long long n, unsigned long long seed, unsigned long long* bad) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long r = splitmix64(seed + (unsigned long long)t);
+        const float x = __uint_as_float((unsigned)r);
+        const double c = k_mixed::f2d(x), e = (double)x;
+        const bool same_d = __double_as_longlong(c) == __double_as_longlong(e) || (c != c && e != e);
+        if (!same_d) atomicAdd(bad, 1ull);
+    }
+}
+}  // namespace
+
+int check_float_conversions(long long n, unsigned long long seed, unsigned long long* mismatches) {
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return -1;
+    cudaMemset(d, 0, sizeof(unsigned long long));
+    k_check_conversions<<<1216, 256>>>(n, seed, d);
+    cudaError_t e = cudaMemcpy(mismatches, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? 0 : -1;
+}
+
 void fused_tile_shape(int dim, int* tx, int* ty, int* tz) {
     if (dim == 3) {
         *tx = k_mixed::FusedTile<3>::X; *ty = k_mixed::FusedTile<3>::Y; *tz = k_mixed::FusedTile<3>::Z;

@@ -304,6 +304,12 @@ int ibisgb_set_fused(ibisgb_ctx* ctx, int32_t mode);
 int ibisgb_fused_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, double* times_ms, char* reason,
                       int32_t reason_len);
 
+/* Self-check of the mixed build's float -> double conversion, which runs on the
+ * integer pipe (GB300's FP64 pipe is its scarcest unit): compares it bit for
+ * bit with the conversion instruction on `samples` pseudo-random float bit
+ * patterns (seeded), on the current device.  No counterpart in the reference. */
+int ibisgb_check_conversions(int64_t samples, uint64_t seed, int64_t* mismatches);
+
 /* Batched ensembles (no counterpart in the reference, which runs one case per
  * process through Solver::solve, src/solvers/solvers/solver.cpp:25-59).
  * Merges already-created single-case contexts into one new context whose valid

@@ -186,3 +186,13 @@ def test_launch_variants_are_bit_identical(name, precision):
     assert all(len(v) == nv and min(v) > 0 for v in tuned["ms"].values())
     sim.take_steps(4, precision)
     assert np.array_equal(sim.conserved(), ref)
+
+
+def test_integer_pipe_conversions_match_the_instructions():
+    """The mixed update's float -> double conversion (integer bit operations)
+    equals the conversion instruction bit for bit."""
+    import ctypes as C
+    from ibis_gb300 import _lib
+    n = C.c_int64()
+    assert _lib.load().ibisgb_check_conversions(1 << 24, 12345, C.byref(n)) == 0
+    assert n.value == 0
