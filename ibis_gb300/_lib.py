@@ -35,7 +35,7 @@ class NewtonStatus(C.Structure):
     _fields_ = [("relative_residual", C.c_double), ("residual_norms", C.c_double * 6),
                 ("gmres_iterations", C.c_int32), ("gmres_converged", C.c_int32),
                 ("gmres_residual", C.c_double), ("dt_star", C.c_double), ("cfl", C.c_double),
-                ("step", C.c_int64)]
+                ("step", C.c_int64), ("initial_norms", C.c_double * 6)]
 
 
 class AdjointStatus(C.Structure):
@@ -97,6 +97,7 @@ def load(build_if_missing: bool = True):
     L.ibisgb_adjoint_step.argtypes = [_P, _P, _P, C.c_double, C.POINTER(AdjointStatus)]
     L.ibisgb_steady_initialise.argtypes = [_P, C.c_int32]
     L.ibisgb_newton_step.argtypes = [_P, C.c_int32, C.POINTER(NewtonStatus)]
+    L.ibisgb_steady_norms.argtypes = [_P, _P, _P]
     L.ibisgb_autotune.argtypes = [_P, C.c_int32, _P, _P]
     L.ibisgb_set_launch_variants.argtypes = [_P, C.c_int32, _P]
     L.ibisgb_launch_variants.argtypes = [C.POINTER(C.c_int32), _P, _P]

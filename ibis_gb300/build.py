@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libibisgb.so")
+DRIVER = os.path.join(OUT, "ibisgb-run")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -92,6 +93,14 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"linking libibisgb.so failed:\n{r.stdout}\n{r.stderr}")
+    # the host driver (ibisgb-run), a client of the C ABI only
+    src = os.path.join(SRC, "driver", "ibisgb_run.cpp")
+    if not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < max(os.path.getmtime(LIB), os.path.getmtime(src)):
+        cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-I", INCLUDE, src, "-o", DRIVER,
+               "-L", OUT, "-libisgb", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"building ibisgb-run failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

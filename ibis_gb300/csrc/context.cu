@@ -1117,6 +1117,7 @@ struct ibisgb_ctx {
             out->dt_star = dt_star;
             out->cfl = cfl;
             out->step = st.step;
+            for (int q = 0; q < 6; q++) out->initial_norms[q] = st.initial[q];
         }
     }
 
@@ -1812,6 +1813,17 @@ int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision) {
     return guarded(ctx, [&] {
         if (precision < 0 || precision > 2) throw ArgError("unknown precision");
         ctx->steady_initialise(precision);
+    });
+}
+
+int ibisgb_steady_norms(ibisgb_ctx* ctx, double norms[6], double initial[6]) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (!ctx->steady.initialised) throw StateError("call ibisgb_steady_initialise first");
+        for (int q = 0; q < 6; q++) {
+            if (norms) norms[q] = ctx->steady.norms[q];
+            if (initial) initial[q] = ctx->steady.initial[q];
+        }
     });
 }
 

@@ -19,6 +19,7 @@ from __future__ import annotations
 import copy
 import json
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -353,12 +354,39 @@ def make_config(dim, boundaries, *, flux="hanel", ldfss_delta=2.0, order=2,
 
 
 def runge_kutta(cfl=0.5, max_step=2000, max_time=1e30, plot_frequency=-1.0, dt_init=-1.0,
-                tableau=SSP_RK3) -> dict:
+                tableau=SSP_RK3, print_frequency=100, plot_every_n_steps=-1, residual_frequency=-1.0,
+                residuals_every_n_steps=-1) -> dict:
     """RungeKutta solver block (prep.py:862-903); plot_frequency <= 0 leaves dt unclipped."""
     return {"name": "runge_kutta", "cfl": {"type": "constant", "value": cfl}, "max_time": max_time,
-            "max_step": max_step, "print_frequency": 100, "plot_frequency": plot_frequency,
-            "plot_every_n_steps": -1, "dt_init": dt_init, "butcher_tableau": tableau,
-            "residual_frequency": -1.0, "residuals_every_n_steps": -1}
+            "max_step": max_step, "print_frequency": print_frequency, "plot_frequency": plot_frequency,
+            "plot_every_n_steps": plot_every_n_steps, "dt_init": dt_init, "butcher_tableau": tableau,
+            "residual_frequency": residual_frequency, "residuals_every_n_steps": residuals_every_n_steps}
+
+
+def write_case(directory, grid, config, T, p, vx, vy, vz=None):
+    """An ibis case directory as the prep step leaves it: config/config.json,
+    io/grid/0000/block_0000.su2 and the initial flow io/flow/0000 (T, p, vx, vy[,
+    vz] and meta_data.json) in the config's native flow format."""
+    os.makedirs(os.path.join(directory, "config"), exist_ok=True)
+    os.makedirs(os.path.join(directory, "io", "grid", "0000"), exist_ok=True)
+    flow = os.path.join(directory, "io", "flow", "0000")
+    os.makedirs(flow, exist_ok=True)
+    with open(os.path.join(directory, "config", "config.json"), "w") as f:
+        f.write(to_json(config))
+    grid.write(os.path.join(directory, "io", "grid", "0000", "block_0000.su2"))
+    binary = config["io"]["flow_format"] == "native_binary"
+    fields = {"T": T, "p": p, "vx": vx, "vy": vy}
+    if vz is not None:
+        fields["vz"] = vz
+    for name, arr in fields.items():
+        arr = np.ascontiguousarray(arr, np.float64)
+        if binary:
+            arr.tofile(os.path.join(flow, name))
+        else:
+            with open(os.path.join(flow, name), "w") as f:
+                f.write("".join(f"{x:.16f}\n" for x in arr))
+    with open(os.path.join(flow, "meta_data.json"), "w") as f:
+        json.dump({"time": 0.0}, f, indent=4)
 
 
 def steady_state(cfl=None, max_steps=100, tolerance=1e-10, max_iters=30, tol=1e-2,

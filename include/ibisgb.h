@@ -188,6 +188,7 @@ typedef struct {
     double dt_star;           /* pseudo time step cfl * stable dt */
     double cfl;
     int64_t step;             /* Newton steps taken since ibisgb_steady_initialise */
+    double initial_norms[6];  /* the residual norms at ibisgb_steady_initialise */
 } ibisgb_newton_status;
 
 /* out = inv_dt_star * v - (dR/dU) v on device vectors of N x n_conserved rows
@@ -250,6 +251,12 @@ int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_
  * (Jfnk::initialise, src/solvers/solvers/jfnk.cpp:25-30).  `precision` is the
  * arithmetic of the real residual; the tangent is always double. */
 int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision);
+
+/* The steady solver's residual norms at the current state and at
+ * ibisgb_steady_initialise (global, mass, momentum x, y, z, energy; either may
+ * be NULL): Jfnk::residual_norms and the initial norms behind
+ * Jfnk::relative_residual_norms (jfnk.h). */
+int ibisgb_steady_norms(ibisgb_ctx* ctx, double norms[6], double initial[6]);
 
 /* One Jacobian-free Newton-Krylov step: dt* = cfl * estimate_dt, GMRES (or
  * FGMRES) on (I/dt* - J) dU = R(U) with the tangent operator, U += dU, new
