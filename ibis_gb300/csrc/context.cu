@@ -520,7 +520,7 @@ struct ibisgb_ctx {
         size_t P = sizeof(Gm);
         s.prim.alloc(P * 7 * NT);
         s.vghost.alloc(P * 5 * std::max<int64_t>(mesh.G, 1));
-        s.grad.alloc(P * 15 * N);
+        s.grad.alloc(P * 16 * N);  // 15 x N, or the mixed build's 16 packed floats per cell
         s.phi.alloc(P * 5 * N);
         s.vgrad.alloc(P * 12 * N);
         s.flux.alloc(P * nc() * F);
