@@ -51,6 +51,7 @@ def parse():
                     help="fused stage for structured blocks: let the autotuner choose, force, or disable")
     ap.add_argument("--plate-steps", type=int, default=300, help="RK steps of the flat-plate accuracy case (0: skip)")
     ap.add_argument("--newton-steps", type=int, default=25, help="Newton steps of the ramp JFNK case (0: skip)")
+    ap.add_argument("--sweep", default="64,128", help="smaller box sizes timed beside the headline (empty: none)")
     return ap.parse_args()
 
 
@@ -197,6 +198,26 @@ def batch_measure(args, barrier):
             "speedup_vs_device_only": (upd_b / (ms_b / 1e3)) / (upd_s / (dev_ms / 1e3)),
             "rho_rel_l2_err_mixed_vs_f64": {"max": max(errs), "median": float(np.median(errs)),
                                             "steps": args.warmup + args.batch_steps}}
+
+
+def sweep_measure(args):
+    """The residual-throughput sweep of the box at the smaller sizes (the headline
+    size is the main line): mixed and FP64 Mcell-updates/s, 20 timed steps each."""
+    from ibis_gb300 import Simulation
+    out = {}
+    for n in [int(x) for x in args.sweep.split(",") if x.strip()]:
+        grid, config, ic = make_case(n)
+        sim = Simulation(config, grid)
+        del grid
+        row = {}
+        for prec in ("mixed", "f64"):
+            sim.set_primitives(*ic)
+            sim.take_steps(3, prec)
+            st = sim.take_steps(20, prec)
+            row[prec] = sim.num_cells * 3.0 * 20 / (st["device_ms"] / 1e3) / 1e6
+        row["fused_stage"] = sim.fused_info()["enabled"]
+        out[f"{n}^3"] = row
+    return out
 
 
 def plate_measure(args):
@@ -412,6 +433,7 @@ def run_ours(args, world, rank, local):
 
     batch = batch_measure(args, barrier) if args.batch_cases > 0 else None
     plate = plate_measure(args) if args.plate_steps > 0 and rank == 0 else None
+    sweep = sweep_measure(args) if args.sweep and rank == 0 else None
     jfnk = jfnk_measure(args) if args.newton_steps > 0 and rank == 0 else None
 
     cpu = None
@@ -440,6 +462,7 @@ def run_ours(args, world, rank, local):
             "autotune": {"variants_table": Simulation.launch_variants(), "mixed": tune_mixed, "f64": tune_f64,
                          "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")}},
             "batch": batch,
+            "sweep": sweep,
             "plate": plate,
             "jfnk": jfnk,
             "roofline": {"bound": "hbm", "kernel": "rk_stage (recon + face + update kernels of one stage)",
