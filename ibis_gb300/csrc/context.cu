@@ -72,7 +72,7 @@ void upload(DBuf& b, const std::vector<T>& v, cudaStream_t s) {
 
 // State buffers of one storage type (double for F64 / F64_EXACT, float for MIXED).
 struct StateBufs {
-    DBuf cc, r, face, lsqw;                        // geometry
+    DBuf cc, r, face, lsqw, lsqd;                  // geometry
     DBuf prim, vghost, grad, phi, vgrad, flux;     // state and intermediates
     bool geometry = false;
     bool prims_current = false;
@@ -517,6 +517,19 @@ struct ibisgb_ctx {
             std::vector<Gm> w(mesh.lsqw.begin(), mesh.lsqw.end());
             upload(s.lsqw, w, stream);
         }
+        if (sizeof(Gm) == sizeof(float) && prm.order == 2) {
+            // the limiter's face offsets, per face slot: coalesced instead of gathered
+            const int64_t MF = mesh.MF;
+            std::vector<Gm> d(3 * MF * N, Gm(0));
+            const std::vector<double>* fcs[3] = {&mesh.fcx, &mesh.fcy, &mesh.fcz};
+            const std::vector<double>* ccs[3] = {&mesh.ccx, &mesh.ccy, &mesh.ccz};
+            for (int64_t c = 0; c < N; c++)
+                for (int64_t k = 0; k < mesh.nfaces[c]; k++) {
+                    const int64_t f = mesh.cell_face[c * MF + k];
+                    for (int a = 0; a < 3; a++) d[(a * MF + k) * N + c] = (Gm)((*fcs[a])[f] - (*ccs[a])[c]);
+                }
+            upload(s.lsqd, d, stream);
+        }
         size_t P = sizeof(Gm);
         s.prim.alloc(P * 7 * NT);
         s.vghost.alloc(P * 5 * std::max<int64_t>(mesh.G, 1));
@@ -549,6 +562,7 @@ struct ibisgb_ctx {
         v.feed_off = feed_off.as<int>(); v.feed_ghost = feed_ghost.as<int>();
         v.cc = s.cc.p; v.r = s.r.p; v.face = s.face.p; v.vol = vol.as<double>();
         v.inv_vol = inv_vol.as<double>(); v.lsqw = s.lsqw.p;
+        v.lsqd = s.lsqd.p;
         v.prim = (is_mixed(prec) && prim_cur) ? prim_alt.p : s.prim.p;
         v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();

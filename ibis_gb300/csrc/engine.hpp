@@ -104,6 +104,7 @@ struct DevView {
     const double* vol;      // N
     const double* inv_vol;  // N, 1/volume (fast paths)
     const void* lsqw;       // [3][MF][N] least-squares weights per neighbour slot (type Gm, fast paths)
+    const void* lsqd;       // [3][MF][N] face centre minus cell centroid per face slot (float build), or null
     // state (type P)
     void* prim;    // [7][NT]: rho, p, T, e, vx, vy, vz
     void* vghost;  // [5][G]: p, T, vx, vy, vz after the pre-viscous-gradient actions

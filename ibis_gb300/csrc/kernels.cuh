@@ -297,10 +297,17 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                 R tpos[NV], tneg[NV];
 #pragma unroll
                 for (int q = 0; q < NV; q++) { tpos[q] = R(0.0); tneg[q] = R(0.0); }
+                const Gm* D = (const Gm*)v.lsqd;
                 for (int s = 0; s < nf; s++) {
-                    const int f = v.cell_face[s * N + i];
-                    R dx = (R)fcen[f] - xi, dy = (R)fcen[F + f] - yi;
-                    R dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+                    R dx, dy, dz;
+                    if (D) {  // face offsets stored per slot
+                        dx = (R)D[s * N + i]; dy = (R)D[(MF + s) * N + i];
+                        dz = DIM == 3 ? (R)D[(2 * MF + s) * N + i] : R(0.0);
+                    } else {
+                        const int f = v.cell_face[s * N + i];
+                        dx = (R)fcen[f] - xi; dy = (R)fcen[F + f] - yi;
+                        dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+                    }
 #pragma unroll
                     for (int q = 0; q < NV; q++) {
                         R d2 = DIM == 3 ? gx[q] * dx + gy[q] * dy + gz[q] * dz : gx[q] * dx + gy[q] * dy;
