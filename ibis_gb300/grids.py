@@ -24,7 +24,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-VTK_LINE, VTK_TRI, VTK_QUAD, VTK_TETRA, VTK_HEX = 3, 5, 9, 10, 12
+VTK_LINE, VTK_TRI, VTK_QUAD, VTK_TETRA, VTK_HEX, VTK_WEDGE, VTK_PYRAMID = 3, 5, 9, 10, 12, 13, 14
 
 
 @dataclass
@@ -114,6 +114,96 @@ def structured_2d(X: np.ndarray, Y: np.ndarray, bottom_tags=None) -> Su2Grid:
     n = ni * nj
     return Su2Grid(2, xyz, np.full(n, VTK_QUAD, np.int32), np.arange(0, 4 * n + 1, 4, dtype=np.int64),
                    conn.reshape(-1).astype(np.int64), markers)
+
+
+def _cells(g: Su2Grid):
+    return [g.cell_conn[g.cell_offsets[c]:g.cell_offsets[c + 1]] for c in range(g.num_cells)]
+
+
+def _grid_from_cells(g: Su2Grid, types, cells, markers, xyz=None) -> Su2Grid:
+    lens = np.array([len(c) for c in cells], np.int64)
+    return Su2Grid(g.dim, g.xyz if xyz is None else xyz, np.asarray(types, np.int32),
+                   np.concatenate([[0], np.cumsum(lens)]).astype(np.int64),
+                   np.concatenate(cells).astype(np.int64), markers)
+
+
+def _split_marker_quads(g: Su2Grid, faces: set) -> dict:
+    """Boundary quads split into the two triangles that are faces of the cells
+    (the diagonal through the first vertex, or the other one)."""
+    out = {}
+    for tag, (types, offs, conn) in g.markers.items():
+        tris = []
+        for e in range(len(types)):
+            a, b, c, d = conn[offs[e]:offs[e + 1]]
+            if frozenset((a, b, c)) in faces:
+                tris += [(a, b, c), (a, c, d)]
+            else:
+                tris += [(a, b, d), (b, c, d)]
+        out[tag] = (np.full(len(tris), VTK_TRI, np.int32), np.arange(0, 3 * len(tris) + 1, 3, dtype=np.int64),
+                    np.asarray(tris, np.int64).reshape(-1))
+    return out
+
+
+def triangulate_2d(g: Su2Grid) -> Su2Grid:
+    """Each quad (v0, v1, v2, v3) as two triangles, the diagonal alternating
+    with the cell index; the boundary markers are unchanged."""
+    cells, types = [], []
+    for k, (a, b, c, d) in enumerate(_cells(g)):
+        if k % 2 == 0:
+            cells += [np.array([a, b, c]), np.array([a, c, d])]
+        else:
+            cells += [np.array([a, b, d]), np.array([b, c, d])]
+        types += [VTK_TRI, VTK_TRI]
+    return _grid_from_cells(g, types, cells, g.markers)
+
+
+def tetrahedralize(g: Su2Grid) -> Su2Grid:
+    """Each hexahedron as six tetrahedra around its diagonal v0-v6 (conforming
+    between neighbours of a lexicographic hex grid); boundary quads split to match."""
+    cells, faces = [], set()
+    for h in _cells(g):
+        for t in ((0, 1, 2, 6), (0, 2, 3, 6), (0, 3, 7, 6), (0, 7, 4, 6), (0, 4, 5, 6), (0, 5, 1, 6)):
+            tet = h[list(t)]
+            cells.append(tet)
+            for f in ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)):
+                faces.add(frozenset(tet[list(f)]))
+    return _grid_from_cells(g, [VTK_TETRA] * len(cells), cells, _split_marker_quads(g, faces))
+
+
+def prisms_3d(g: Su2Grid) -> Su2Grid:
+    """Each hexahedron as two wedges (triangular prisms) split by its v0-v2 / v4-v6
+    diagonal plane; the bottom and top boundary quads split to match."""
+    cells, faces = [], set()
+    for h in _cells(g):
+        for w in ((0, 1, 2, 4, 5, 6), (0, 2, 3, 4, 6, 7)):
+            wed = h[list(w)]
+            cells.append(wed)
+            faces.add(frozenset(wed[[0, 1, 2]]))
+            faces.add(frozenset(wed[[3, 4, 5]]))
+    markers = {}
+    split = _split_marker_quads(g, faces)
+    for tag, m in g.markers.items():
+        conn = m[2].reshape(-1, 4)
+        if all(frozenset(q[[0, 1, 2]]) in faces or frozenset(q[[0, 1, 3]]) in faces for q in conn):
+            markers[tag] = split[tag]  # a face of triangles
+        else:
+            markers[tag] = m
+    return _grid_from_cells(g, [VTK_WEDGE] * len(cells), cells, markers)
+
+
+def pyramids_3d(g: Su2Grid) -> Su2Grid:
+    """Each hexahedron as six pyramids on its faces with the apex at a new vertex
+    at the hex centre; the boundary quads are the pyramids' bases, unchanged."""
+    cells, extra = [], []
+    nv = g.xyz.shape[0]
+    hex_faces = ((0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (1, 2, 6, 5), (2, 3, 7, 6), (3, 0, 4, 7))
+    for h in _cells(g):
+        apex = nv + len(extra)
+        extra.append(g.xyz[h].mean(axis=0))
+        for f in hex_faces:
+            cells.append(np.concatenate([h[list(f)], [apex]]))
+    xyz = np.vstack([g.xyz, np.asarray(extra)])
+    return _grid_from_cells(g, [VTK_PYRAMID] * len(cells), cells, g.markers, xyz)
 
 
 def unit_square_3x3() -> Su2Grid:

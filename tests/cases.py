@@ -51,6 +51,26 @@ def case(name, **kw):
              "south": grids.fixed_temperature_no_slip_wall(320.0), "north": grids.slip_wall()}
         c = grids.make_config(2, b, gas=gas, viscous=True, **kw)
         return g, c, random_state(g.num_cells, 300.0, 1e5, 100.0, 2, seed=5, amp=0.03)
+    if name in ("tri", "tet", "wedge", "pyramid", "tiny2d", "tiny3d"):
+        # other element types (every one the reference reads) and the smallest grids,
+        # supersonic inflow on the first tag, slip walls and outflow on the others
+        if name == "tri":
+            X, Y = np.meshgrid(np.linspace(0, 1, 9), np.linspace(0, 0.5, 6), indexing="ij")
+            g = grids.triangulate_2d(grids.structured_2d(X, Y))
+        elif name == "tiny2d":
+            X, Y = np.meshgrid(np.linspace(0, 1, 3), np.linspace(0, 0.5, 2), indexing="ij")
+            g = grids.structured_2d(X, Y)  # 2 x 1 cells
+        elif name == "tiny3d":
+            g = grids.box_3d(1)  # one hexahedron
+        else:
+            make = {"tet": grids.tetrahedralize, "wedge": grids.prisms_3d, "pyramid": grids.pyramids_3d}[name]
+            g = make(grids.box_3d(3))
+        dim = g.dim
+        inflow = grids.flow_state(gas, 300.0, 1e5, 600.0, 80.0, 40.0 if dim == 3 else 0.0)
+        b = {t: (grids.supersonic_inflow(inflow) if i == 0 else
+                 grids.slip_wall() if i % 2 else grids.supersonic_outflow()) for i, t in enumerate(g.markers)}
+        c = grids.make_config(dim, b, gas=gas, **kw)
+        return g, c, random_state(g.num_cells, 300.0, 1e5, 600.0, dim, seed=6, amp=0.05)
     raise KeyError(name)
 
 

@@ -29,7 +29,8 @@ def _setup(name, **kw):
 @pytest.mark.parametrize("name,kw", [("ramp", {}), ("ramp", {"flux": "ausmdv"}), ("ramp", {"flux": "rusanov"}),
                                      ("ramp", {"thermo": "rho_p"}),
                                      ("ramp", {"thermo": "p_T"}), ("ramp", {"limiter": "unlimited"}),
-                                     ("ramp", {"order": 1}), ("box", {}), ("box_inout", {})],
+                                     ("ramp", {"order": 1}), ("box", {}), ("box_inout", {}), ("tri", {}),
+                                     ("tet", {}), ("wedge", {}), ("pyramid", {}), ("tiny2d", {})],
                          ids=lambda x: x if isinstance(x, str) else "-".join(f"{k}={v}" for k, v in x.items()))
 @pytest.mark.parametrize("recon", [True, False])
 def test_vjp_is_the_transpose_of_the_jvp(name, kw, recon):

@@ -21,7 +21,8 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, s), s
 
 
-@pytest.mark.parametrize("name", ["ramp", "plate", "box", "box_inout", "subsonic"])
+@pytest.mark.parametrize("name", ["ramp", "plate", "box", "box_inout", "subsonic", "tri", "tet", "wedge", "pyramid",
+                                  "tiny2d", "tiny3d"])
 def test_numbering_and_geometry_match_oracle(name):
     g, c, _ = case(name)
     sim, o = Simulation(c, g), Oracle(c, g)
