@@ -55,3 +55,112 @@ class Residual(torch.autograd.Function):
 def residual(sim, U):
     """dU/dt of `sim` at conserved state U (float64 CUDA tensor, N x n_conserved)."""
     return Residual.apply(U, sim)
+
+
+def _tableau(sim):
+    """The Butcher tableau of the config's Runge-Kutta block: a (strictly lower), b."""
+    bt = sim.config["solver"]["butcher_tableau"]
+    b = list(bt["b"])
+    s = len(b)
+    a = [[0.0] * s for _ in range(s)]
+    for i, row in enumerate(bt.get("a", [])):
+        for j, x in enumerate(row):
+            a[i + 1][j] = x
+    return a, b
+
+
+def _rk_step(sim, U, dt, a, b):
+    """One explicit RK step of the FP64 residual with a given dt: the stage
+    combination of RungeKutta::take_step (runge_kutta.cpp:131-203), including its
+    a(i, j) < 1e-14 skip, on device tensors; returns U_new and the stage states."""
+    S = len(b)
+    ks, states = [], []
+    for i in range(S):
+        Ui = U.clone()
+        for j in range(i):
+            if j > 0 and a[i][j] < 1e-14:
+                continue
+            Ui.add_(ks[j], alpha=dt * a[i][j])
+        states.append(Ui)
+        ks.append(residual_raw(sim, Ui))
+    Un = U.clone()
+    for j in range(S):
+        Un.add_(ks[j], alpha=dt * b[j])
+    return Un, states
+
+
+def residual_raw(sim, U):
+    stream = torch.cuda.current_stream()
+    sim.set_conserved_into(U.contiguous(), stream=stream)
+    out = torch.empty_like(U)
+    sim.compute_dudt_into(out, "f64_exact", stream=stream)
+    return out
+
+
+def _vjp_raw(sim, U, w):
+    stream = torch.cuda.current_stream()
+    sim.set_conserved_into(U.contiguous(), stream=stream)
+    out = torch.empty_like(U)
+    sim.vector_jacobian_product_into(w.contiguous(), out, stream=stream)
+    return out
+
+
+class RungeKuttaSteps(torch.autograd.Function):
+    """U_N after N explicit Runge-Kutta steps of the given time steps dts, as a
+    differentiable function of U_0.  The backward pass is the discrete adjoint of
+    the RK scheme: for each step in reverse, stage by stage,
+        kbar_m = dt b_m lam + sum_{l > m} dt a(l, m) Ubar_l,   Ubar_m = (dR/dU)(U^(m))^T kbar_m,
+        lam <- lam + sum_m Ubar_m,
+    with the adjoint kernel at every stage state.  Only every `checkpoint`-th
+    state is kept from the forward pass; the states inside a segment are
+    recomputed from its checkpoint when the reverse sweep reaches it, and the
+    limiter and flux branches are taken again from those states.  The time steps
+    are frozen (inputs), as an adjoint of a fixed time discretisation."""
+
+    @staticmethod
+    def forward(ctx, U0, sim, dts, checkpoint):
+        a, b = _tableau(sim)
+        U = U0.detach().clone()
+        saved = {0: U.clone()}
+        for n, dt in enumerate(dts):
+            U, _ = _rk_step(sim, U, float(dt), a, b)
+            if (n + 1) % checkpoint == 0 and n + 1 < len(dts):
+                saved[n + 1] = U.clone()
+        ctx.sim, ctx.dts, ctx.checkpoint, ctx.saved, ctx.tab = sim, list(dts), checkpoint, saved, (a, b)
+        return U
+
+    @staticmethod
+    def backward(ctx, gN):
+        sim, dts, C = ctx.sim, ctx.dts, ctx.checkpoint
+        a, b = ctx.tab
+        S = len(b)
+        lam = gN.contiguous().clone()
+        N = len(dts)
+        seg_starts = sorted(ctx.saved)
+        for s0 in reversed(seg_starts):
+            s1 = min(s0 + C, N)
+            # recompute the states of this segment from its checkpoint
+            states_n = [ctx.saved[s0]]
+            for n in range(s0, s1 - 1):
+                states_n.append(_rk_step(sim, states_n[-1], float(dts[n]), a, b)[0])
+            for n in reversed(range(s0, s1)):
+                dt = float(dts[n])
+                _, stages = _rk_step(sim, states_n[n - s0], dt, a, b)
+                Ubar = [None] * S
+                for m in reversed(range(S)):
+                    kbar = lam * (dt * b[m])
+                    for l in range(m + 1, S):
+                        if m > 0 and a[l][m] < 1e-14:
+                            continue
+                        if a[l][m] != 0.0:
+                            kbar = kbar + Ubar[l] * (dt * a[l][m])
+                    Ubar[m] = _vjp_raw(sim, stages[m], kbar)
+                for m in range(S):
+                    lam = lam + Ubar[m]
+        return lam, None, None, None
+
+
+def rk_steps(sim, U0, dts, checkpoint: int = 8):
+    """U after len(dts) RK steps of sim's tableau from U0 (float64 CUDA tensor,
+    N x n_conserved), differentiable in U0 with checkpointed reverse sweeps."""
+    return RungeKuttaSteps.apply(U0, sim, list(dts), int(checkpoint))
