@@ -899,7 +899,7 @@ struct ibisgb_ctx {
     }
 
     // ----- adjoint: (dR/dU)^T w ------------------------------------------------
-    DBuf adj_qf, adj_self, adj_nba, adj_ga, adj_back, adj_gout;
+    DBuf adj_qf, adj_self, adj_nba, adj_ga, adj_back, adj_gout, adj_qv, adj_qg, adj_gav;
     bool adj_ready = false;
     void ensure_adjoint() {
         if (adj_ready) return;
@@ -907,8 +907,13 @@ struct ibisgb_ctx {
         const int64_t N = mesh.N, F = mesh.F, MF = mesh.MF;
         adj_qf.alloc(sizeof(double) * 12 * F);
         adj_self.alloc(sizeof(double) * 7 * N);
-        adj_nba.alloc(sizeof(double) * 5 * MF * N);
+        adj_nba.alloc(sizeof(double) * 7 * MF * N);
         adj_ga.alloc(sizeof(double) * 7 * std::max<int64_t>(mesh.G, 1));
+        if (prm.viscous) {
+            adj_qv.alloc(sizeof(double) * 10 * F);
+            adj_qg.alloc(sizeof(double) * 24 * F);
+            adj_gav.alloc(sizeof(double) * 5 * std::max<int64_t>(mesh.G, 1));
+        }
         // slot of each valid neighbour that points back through the same face
         std::vector<signed char> back(MF * N, -1);
         for (int64_t c = 0; c < N; c++)
@@ -926,11 +931,10 @@ struct ibisgb_ctx {
 
     void vjp(const double* w_dev, double* out_dev, double* ghost_out_dev, bool reconstruct) {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
-        if (prm.viscous) throw ConfigError("the adjoint covers inviscid configurations");
         DevView v = tangent_view();
         ensure_adjoint();
         AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
-                     adj_back.as<signed char>()};
+                     adj_back.as<signed char>(), adj_qv.as<double>(), adj_qg.as<double>(), adj_gav.as<double>()};
         launch_adjoint(v, prm, w_dev, reconstruct && prm.order == 2, a, out_dev, ghost_out_dev, stream);
         CUDA_OK(cudaGetLastError());
     }

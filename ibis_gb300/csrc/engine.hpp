@@ -174,12 +174,15 @@ int check_float_conversions(long long n, unsigned long long seed, unsigned long 
 struct AdjScratch {
     double* qf;               // [2][6][F] adjoints of the faces' reconstructed inputs
     double* self;             // [7][N]    each cell's own primitive adjoint
-    double* nba;              // [5][MF][N] what each cell sends to the neighbour of slot s
+    double* nba;              // [7][MF][N] primitive adjoints each cell sends to the neighbour of slot s
     double* ga;               // [7][G]    ghost primitive adjoints
     const signed char* back;  // [MF][N]   slot of cell_nbr(i, s) that points back to i
+    double* qv;               // [2][5][F] viscous: adjoints of the sides' p, T, v (valid sides)
+    double* qg;               // [2][12][F] viscous: adjoints of the sides' viscous gradients
+    double* gav;              // [5][G]    viscous: adjoints of the ghosts' pre-viscous p, T, v
 };
-// out = (dR/dU)^T w for w, out of N x nc rows (inviscid); ghost_out (optional,
-// G x 7 rows): the adjoint of every ghost cell's primitives (rho, p, T, e, v).
+// out = (dR/dU)^T w for w, out of N x nc rows; ghost_out (optional, G x 7 rows):
+// the adjoint of every ghost cell's primitives (rho, p, T, e, v).
 void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool reconstruct, const AdjScratch& a,
                     double* out, double* ghost_out, cudaStream_t s);
 

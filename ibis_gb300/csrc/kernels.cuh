@@ -427,6 +427,68 @@ __device__ __forceinline__ void convective_flux(const FvParams& prm, const Gas<R
     out[4] = Fl[4];
 }
 
+// Viscous stress and heat flux through a face (viscous_flux.cpp:130-232) from
+// the states of both sides (p, T, vx, vy, vz: the cells' primitives, or a ghost's
+// pre-viscous values) and the viscous gradients (T, vx, vy, vz: 3 components
+// each) of the two cells; a boundary face passes its interior cell's gradients
+// for both and interior = false.  ex, ey, ez: centroid of the right cell minus
+// the left (interior faces).  out: the x, y, z momentum and energy terms that
+// the face flux loses; also the face density, viscosity and conductivity.
+template <class R, int DIM, bool EXACT>
+__device__ __forceinline__ void viscous_face(const FvParams& prm, const Gas<R>& gm, bool interior, const R (&sl)[5],
+                                             const R (&sr)[5], const R (&gl)[12], const R (&gr)[12], R ex, R ey,
+                                             R ez, R nx, R ny, R nz, R (&out)[4], R& rho, R& mu, R& k) {
+    constexpr int NW = DIM == 3 ? 4 : 3;
+    R g[4][3];
+    if (!interior) {
+#pragma unroll
+        for (int q = 0; q < NW; q++)
+            for (int d = 0; d < 3; d++) g[q][d] = gl[3 * q + d];
+    } else {
+        R len_e = d_sqrt(ex * ex + ey * ey + ez * ez);
+        R ehx = ex / len_e, ehy = ey / len_e, ehz = ez / len_e;
+        R edn = ehx * nx + ehy * ny + ehz * nz;
+        // hasselbacher_average_ (viscous_flux.cpp:84-98), variable order T, vx, vy, vz
+#pragma unroll
+        for (int q = 0; q < NW; q++) {
+            R ax = R(0.5) * (gl[3 * q] + gr[3 * q]);
+            R ay = R(0.5) * (gl[3 * q + 1] + gr[3 * q + 1]);
+            R az = R(0.5) * (gl[3 * q + 2] + gr[3 * q + 2]);
+            R ade = ax * ehx + ay * ehy + az * ehz;
+            R corr = ade - (sr[1 + q] - sl[1 + q]) / len_e;
+            g[q][0] = ax - corr * nx / edn;
+            g[q][1] = ay - corr * ny / edn;
+            g[q][2] = az - corr * nz / edn;
+        }
+    }
+    if (DIM == 2) { g[3][0] = R(0.0); g[3][1] = R(0.0); g[3][2] = R(0.0); }
+    // face state: average of p, T, v (average_pT, gas_state.h:219-225) + update_thermo_from_pT
+    R p = R(0.5) * (sl[0] + sr[0]);
+    R T = R(0.5) * (sl[1] + sr[1]);
+    rho = p / (gm.R_ * T);
+    R vx = R(0.5) * (sl[2] + sr[2]);
+    R vy = R(0.5) * (sl[3] + sr[3]);
+    R vz = DIM == 3 ? R(0.5) * (sl[4] + sr[4]) : R(0.0);
+    mu = sutherland<R, EXACT>(T, par<R>(prm.mu0, prm.fmu0), par<R>(prm.T0, prm.fT0), par<R>(prm.Ts, prm.fTs));
+    k = gm.Cp * mu / par<R>(prm.Pr, prm.fPr);
+    R lambda = R(-2.0 / 3.0) * mu;
+    const R *gT = g[0], *gx = g[1], *gy = g[2], *gz = g[3];
+    R bulk = lambda * (gx[0] + gy[1] + gz[2]);
+    R txx = R(2.0) * mu * gx[0] + bulk;
+    R tyy = R(2.0) * mu * gy[1] + bulk;
+    R tzz = R(2.0) * mu * gz[2] + bulk;
+    R txy = mu * (gx[1] + gy[0]);
+    R txz = mu * (gx[2] + gz[0]);
+    R tyz = mu * (gy[2] + gz[1]);
+    R thx = vx * txx + vy * txy + vz * txz + k * gT[0];
+    R thy = vx * txy + vy * tyy + vz * tyz + k * gT[1];
+    R thz = vx * txz + vy * tyz + vz * tzz + k * gT[2];
+    out[0] = nx * txx + ny * txy + nz * txz;
+    out[1] = nx * txy + ny * tyy + nz * tyz;
+    out[2] = nx * txz + ny * tyz + nz * tzz;
+    out[3] = nx * thx + ny * thy + nz * thz;
+}
+
 template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
 __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int reconstruct) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -515,69 +577,34 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
     R en = Fg[4];
 
     if (prm.viscous) {
-        // viscous_flux.cpp:130-232
+        // viscous_flux.cpp:130-232; the states and gradients of both sides, then viscous_face
         const int l = cells[0], r = cells[1];
         const bool lv = l < N, rv = r < N;
         const P* vgd = (const P*)v.vgrad;
         const P* vgh = (const P*)v.vghost;
-        constexpr int NW = DIM == 3 ? 4 : 3;
-        R g[4][3];
-        // visc states of both sides (ghost: pre-viscous values)
-        auto vstate = [&](int c, int k) -> R {  // k: 0 p, 1 T, 2 vx, 3 vy, 4 vz
+        // visc states of both sides (ghost: pre-viscous values): p, T, vx, vy, vz
+        auto vstate = [&](int c, int k) -> R {
             if (c >= N) return (R)vgh[k * G + (c - N)];
             return (R)pr[(k == 0 ? 1 : visc_prim(k - 1)) * NT + c];
         };
-        if (!lv || !rv) {
-            const int in = lv ? l : r;
+        R sl[5], sr[5], gl[12], grr[12];
 #pragma unroll
-            for (int q = 0; q < NW; q++)
-                for (int d = 0; d < 3; d++) g[q][d] = (R)vgd[(3 * q + d) * N + in];
-        } else {
-            R ex = (R)cc[r] - (R)cc[l], ey = (R)cc[NT + r] - (R)cc[NT + l];
-            R ez = DIM == 3 ? (R)cc[2 * NT + r] - (R)cc[2 * NT + l] : R(0.0);
-            R len_e = d_sqrt(ex * ex + ey * ey + ez * ez);
-            R ehx = ex / len_e, ehy = ey / len_e, ehz = ez / len_e;
-            R edn = ehx * nx + ehy * ny + ehz * nz;
-            // hasselbacher_average_ (viscous_flux.cpp:84-98), variable order vx, vy, vz, T
+        for (int k = 0; k < 5; k++) { sl[k] = vstate(l, k); sr[k] = vstate(r, k); }
+        const bool interior = lv && rv;
+        const int gl_c = interior ? l : (lv ? l : r), gr_c = interior ? r : gl_c;
 #pragma unroll
-            for (int q = 0; q < NW; q++) {
-                R ax = R(0.5) * ((R)vgd[(3 * q) * N + l] + (R)vgd[(3 * q) * N + r]);
-                R ay = R(0.5) * ((R)vgd[(3 * q + 1) * N + l] + (R)vgd[(3 * q + 1) * N + r]);
-                R az = R(0.5) * ((R)vgd[(3 * q + 2) * N + l] + (R)vgd[(3 * q + 2) * N + r]);
-                R ade = ax * ehx + ay * ehy + az * ehz;
-                R corr = ade - ((R)pr[visc_prim(q) * NT + r] - (R)pr[visc_prim(q) * NT + l]) / len_e;
-                g[q][0] = ax - corr * nx / edn;
-                g[q][1] = ay - corr * ny / edn;
-                g[q][2] = az - corr * nz / edn;
-            }
+        for (int k = 0; k < 12; k++) { gl[k] = (R)vgd[k * N + gl_c]; grr[k] = (R)vgd[k * N + gr_c]; }
+        R ex = R(0.0), ey = R(0.0), ez = R(0.0);
+        if (interior) {
+            ex = (R)cc[r] - (R)cc[l]; ey = (R)cc[NT + r] - (R)cc[NT + l];
+            ez = DIM == 3 ? (R)cc[2 * NT + r] - (R)cc[2 * NT + l] : R(0.0);
         }
-        if (DIM == 2) { g[3][0] = R(0.0); g[3][1] = R(0.0); g[3][2] = R(0.0); }
-        // face state: average of p, T, v (average_pT, gas_state.h:219-225) + update_thermo_from_pT
-        R p = R(0.5) * (vstate(l, 0) + vstate(r, 0));
-        R T = R(0.5) * (vstate(l, 1) + vstate(r, 1));
-        R rho = p / (gm.R_ * T);
-        R vx = R(0.5) * (vstate(l, 2) + vstate(r, 2));
-        R vy = R(0.5) * (vstate(l, 3) + vstate(r, 3));
-        R vz = DIM == 3 ? R(0.5) * (vstate(l, 4) + vstate(r, 4)) : R(0.0);
-        R mu = sutherland<R, EXACT>(T, par<R>(prm.mu0, prm.fmu0), par<R>(prm.T0, prm.fT0),
-                                    par<R>(prm.Ts, prm.fTs));
-        R k = gm.Cp * mu / par<R>(prm.Pr, prm.fPr);
-        R lambda = R(-2.0 / 3.0) * mu;
-        const R *gT = g[0], *gx = g[1], *gy = g[2], *gz = g[3];
-        R bulk = lambda * (gx[0] + gy[1] + gz[2]);
-        R txx = R(2.0) * mu * gx[0] + bulk;
-        R tyy = R(2.0) * mu * gy[1] + bulk;
-        R tzz = R(2.0) * mu * gz[2] + bulk;
-        R txy = mu * (gx[1] + gy[0]);
-        R txz = mu * (gx[2] + gz[0]);
-        R tyz = mu * (gy[2] + gz[1]);
-        R thx = vx * txx + vy * txy + vz * txz + k * gT[0];
-        R thy = vx * txy + vy * tyy + vz * tyz + k * gT[1];
-        R thz = vx * txz + vy * tyz + vz * tzz + k * gT[2];
-        mx -= nx * txx + ny * txy + nz * txz;
-        my -= nx * txy + ny * tyy + nz * tyz;
-        if (DIM == 3) mz -= nx * txz + ny * tyz + nz * tzz;
-        en -= nx * thx + ny * thy + nz * thz;
+        R vt[4], rho, mu, k;
+        viscous_face<R, DIM, EXACT>(prm, gm, interior, sl, sr, gl, grr, ex, ey, ez, nx, ny, nz, vt, rho, mu, k);
+        mx -= vt[0];
+        my -= vt[1];
+        if (DIM == 3) mz -= vt[2];
+        en -= vt[3];
         // time-step signal (estimate_dt, finite_volume.cpp:167-175), in double
         double mud = real_of(mu), kd = real_of(k);
         double Prf = mud * prm.Cp / kd;

@@ -126,9 +126,13 @@ __device__ void side_values(const DevView& v, const FvParams& prm, bool reconstr
 // Pass 1, per face: adjoint of the face flux, wbar_F = sum over its valid cells of
 // -outsign A / V w, pulled back to the reconstructed inputs of both sides.
 // Valid sides go to qf[(side * 6 + k) * F + f]; ghost sides to ga[m * G + g].
+// Viscous: also to the sides' p, T, v (qv, or the ghost's gav) and viscous
+// gradients (qg), through viscous_face.
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, const double* w, int reconstruct,
-                                                     double* qf, double* ga) {
+                                                     AdjScratch a) {
+    double* qf = a.qf;
+    double* ga = a.ga;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.F) return;
     constexpr int NC = DIM + 2;
@@ -171,31 +175,140 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
             else ga[(size_t)in[k] * G + (c - N)] = acc;
         }
     }
+    if (!prm.viscous) return;
+    // viscous terms (subtracted from the flux): states p, T, v of both sides and
+    // the viscous gradients of the valid cells, one dual seed each
+    const Dual* pr = (const Dual*)v.prim;
+    const Dual* vgd = (const Dual*)v.vgrad;
+    const Dual* vgh = (const Dual*)v.vghost;
+    const double* cc = (const double*)v.cc;
+    const int NT = v.NT;
+    const int l = cells[0], r = cells[1];
+    const bool interior = l < N && r < N;
+    const int gsrc[2] = {interior ? l : (l < N ? l : r), interior ? r : (l < N ? l : r)};
+    double sv[2][5], gv[2][12];
+    for (int side = 0; side < 2; side++) {
+        const int c = cells[side];
+        for (int k = 0; k < 5; k++)
+            sv[side][k] = c >= N ? vgh[k * G + (c - N)].re : pr[(k == 0 ? 1 : visc_prim(k - 1)) * NT + c].re;
+        for (int k = 0; k < 12; k++) gv[side][k] = vgd[k * N + gsrc[side]].re;
+    }
+    DualA ex(0.0), ey(0.0), ez(0.0);
+    if (interior) {
+        ex = DualA(cc[r] - cc[l]);
+        ey = DualA(cc[NT + r] - cc[NT + l]);
+        ez = DualA(DIM == 3 ? cc[2 * NT + r] - cc[2 * NT + l] : 0.0);
+    }
+    // the terms are subtracted from the momentum and energy fluxes
+    const double tb[4] = {-fb[1], -fb[2], -fb[3], -fb[4]};
+    auto eval = [&](int which, int side, int k) {
+        DualA sl[5], sr[5], gl[12], gr[12];
+        for (int q = 0; q < 5; q++) {
+            sl[q] = DualA(sv[0][q], which == 0 && side == 0 && q == k ? 1.0 : 0.0);
+            sr[q] = DualA(sv[1][q], which == 0 && side == 1 && q == k ? 1.0 : 0.0);
+        }
+        for (int q = 0; q < 12; q++) {
+            // a boundary face uses its interior cell's gradients on both sides: one seed for both
+            const bool seed_l = which == 1 && q == k && (side == 0 || !interior);
+            const bool seed_r = which == 1 && q == k && (side == 1 || !interior);
+            gl[q] = DualA(gv[0][q], seed_l ? 1.0 : 0.0);
+            gr[q] = DualA(gv[1][q], seed_r ? 1.0 : 0.0);
+        }
+        DualA out[4], rho, mu, kk;
+        viscous_face<DualA, DIM, true>(prm, gm, interior, sl, sr, gl, gr, ex, ey, ez, nx, ny, nz, out, rho, mu, kk);
+        return tb[0] * out[0].du + tb[1] * out[1].du + tb[2] * out[2].du + tb[3] * out[3].du;
+    };
+    for (int side = 0; side < 2; side++) {
+        const int c = cells[side];
+        for (int k = 0; k < 5; k++) {
+            const double b = eval(0, side, k);
+            if (c < N) a.qv[(size_t)(side * 5 + k) * F + f] = b;
+            else a.gav[(size_t)k * G + (c - N)] = b;
+        }
+    }
+    // gradients: per valid side; a boundary face's one set of gradients is seeded once
+    for (int side = 0; side < 2; side++) {
+        const int c = cells[side];
+        for (int k = 0; k < 12; k++) {
+            double b = 0.0;
+            if (c < N && (interior || side == (l < N ? 0 : 1))) b = eval(1, side, k);
+            a.qg[(size_t)(side * 12 + k) * F + f] = b;
+        }
+    }
 }
 
 // Pass 2, per valid cell: gathers its faces' input adjoints, reverses the
 // reconstruction, the Barth-Jespersen limiter (its winning face and the min/max
 // neighbours chosen with the Dual rules) and the least-squares gradient.
-// The cell's own primitive adjoint goes to self[m * N + i]; what its
-// neighbours receive goes to nba[(k * MF + s) * N + i] (valid neighbours, read
-// back by pass 3) or into ga (ghost neighbours, each of which has one cell).
+// Viscous: also the faces' adjoints of the cell's p, T, v and viscous gradients,
+// and the viscous least squares reversed.  The cell's own primitive adjoint
+// goes to self[m * N + i]; what its neighbours receive, by primitive m, goes to
+// nba[(m * MF + s) * N + i] (valid neighbours, read back by pass 3) or into ga
+// / gav (ghost neighbours, each of which has one cell).
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, int reconstruct, const double* qf,
-                                                     double* self, double* nba, double* ga) {
+__global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, int reconstruct, AdjScratch a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
+    const double* qf = a.qf;
+    double* self = a.self;
+    double* nba = a.nba;
+    double* ga = a.ga;
     constexpr int NV = DIM == 3 ? 5 : 4;
     const int N = v.N, F = v.F, G = v.G, NT = v.NT, MF = v.MF;
     const Dual* pr = (const Dual*)v.prim;
     const Dual* gr = (const Dual*)v.grad;
     const Dual* ph = (const Dual*)v.phi;
-    const double* fg = (const double*)v.face;
-    const double* cc = (const double*)v.cc;
-    const double* rr = (const double*)v.r;
     int in[6];
     const int K = face_inputs<DIM>(prm.thermo, reconstruct, in);
     double pb[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     const int nf = v.nfaces[i];
+    for (int s = 0; s < MF; s++)
+        for (int m = 0; m < 7; m++) nba[((size_t)m * MF + s) * N + i] = 0.0;
+    const double* fg = (const double*)v.face;
+    const double* cc = (const double*)v.cc;
+    const double* rr = (const double*)v.r;
+    const double xi = cc[i], yi = cc[NT + i], zi = DIM == 3 ? cc[2 * NT + i] : 0.0;
+    // least-squares weights of slot s (k_recon's exact form)
+    double r11 = rr[i], r12 = rr[N + i], r22 = rr[2 * N + i], r13 = 0.0, r23 = 0.0, r33 = 1.0;
+    if (DIM == 3) { r13 = rr[3 * N + i]; r23 = rr[4 * N + i]; r33 = rr[5 * N + i]; }
+    const double beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+    auto weights = [&](int nb, double& w1, double& w2, double& w3) {
+        const double dx = cc[nb] - xi, dy = cc[NT + nb] - yi, dz = DIM == 3 ? cc[2 * NT + nb] - zi : 0.0;
+        const double a1 = dx / (r11 * r11);
+        const double a2 = 1.0 / (r22 * r22) * (dy - r12 / r11 * dx);
+        const double a3 = DIM == 3 ? 1.0 / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx) : 0.0;
+        w1 = a1 - r12 / r11 * a2 + beta * a3;
+        w2 = a2 - r23 / r22 * a3;
+        w3 = a3;
+    };
+    if (prm.viscous) {
+        // viscous: the faces' adjoints of this cell's p, T, v and of its viscous
+        // gradients, then the gradients' least squares reversed onto the neighbours
+        // (valid cells' T, v; ghosts' pre-viscous values)
+        constexpr int NW = DIM == 3 ? 4 : 3;
+        double hb[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
+            const double q5[5] = {a.qv[(size_t)(side * 5 + 0) * F + f], a.qv[(size_t)(side * 5 + 1) * F + f],
+                                  a.qv[(size_t)(side * 5 + 2) * F + f], a.qv[(size_t)(side * 5 + 3) * F + f],
+                                  a.qv[(size_t)(side * 5 + 4) * F + f]};
+            pb[1] += q5[0]; pb[2] += q5[1]; pb[4] += q5[2]; pb[5] += q5[3]; pb[6] += q5[4];
+            for (int q = 0; q < 4; q++)
+                for (int d = 0; d < 3; d++) hb[q][d] += a.qg[(size_t)(side * 12 + 3 * q + d) * F + f];
+        }
+        for (int s = 0; s < nf; s++) {
+            const int nb = v.cell_nbr[s * N + i];
+            double w1, w2, w3;
+            weights(nb, w1, w2, w3);
+            for (int q = 0; q < NW; q++) {
+                const double c = w1 * hb[q][0] + w2 * hb[q][1] + (DIM == 3 ? w3 * hb[q][2] : 0.0);
+                pb[visc_prim(q)] -= c;
+                if (nb < N) nba[((size_t)visc_prim(q) * MF + s) * N + i] += c;
+                else a.gav[(size_t)(1 + q) * G + (nb - N)] += c;
+            }
+        }
+    }
     if (!reconstruct) {
         for (int s = 0; s < nf; s++) {
             const int f = v.cell_face[s * N + i];
@@ -205,7 +318,6 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
         for (int m = 0; m < 7; m++) self[(size_t)m * N + i] = pb[m];
         return;
     }
-    const double xi = cc[i], yi = cc[NT + i], zi = DIM == 3 ? cc[2 * NT + i] : 0.0;
     double ui[NV], g[NV][3], phi[NV], gb[NV][3], phib[NV];
     for (int k = 0; k < NV; k++) {
         ui[k] = pr[in[k] * NT + i].re;
@@ -230,10 +342,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
             if (DIM == 3) gb[k][2] += b * phi[k] * dz;
         }
     }
-    // least-squares weights (k_recon's exact form) and the min / max arguments
-    double r11 = rr[i], r12 = rr[N + i], r22 = rr[2 * N + i], r13 = 0.0, r23 = 0.0, r33 = 1.0;
-    if (DIM == 3) { r13 = rr[3 * N + i]; r23 = rr[4 * N + i]; r33 = rr[5 * N + i]; }
-    const double beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+    // the min / max arguments
     double umin[NV], umax[NV];
     int amin[NV], amax[NV];
     for (int k = 0; k < NV; k++) { umin[k] = ui[k]; umax[k] = ui[k]; amin[k] = -1; amax[k] = -1; }
@@ -286,16 +395,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
     // gradient g = sum_s w_s (u_nb - u_i)
     for (int s = 0; s < nf; s++) {
         const int nb = v.cell_nbr[s * N + i];
-        const double dx = cc[nb] - xi, dy = cc[NT + nb] - yi, dz = DIM == 3 ? cc[2 * NT + nb] - zi : 0.0;
-        const double a1 = dx / (r11 * r11);
-        const double a2 = 1.0 / (r22 * r22) * (dy - r12 / r11 * dx);
-        const double a3 = DIM == 3 ? 1.0 / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx) : 0.0;
-        const double w1 = a1 - r12 / r11 * a2 + beta * a3, w2 = a2 - r23 / r22 * a3, w3 = a3;
+        double w1, w2, w3;
+        weights(nb, w1, w2, w3);
         for (int k = 0; k < NV; k++) {
             double c = w1 * gb[k][0] + w2 * gb[k][1] + (DIM == 3 ? w3 * gb[k][2] : 0.0);
             pb[in[k]] -= c;
             if (ext[k] == s) c += extb[k];
-            if (nb < N) nba[((size_t)k * MF + s) * N + i] = c;
+            if (nb < N) nba[((size_t)in[k] * MF + s) * N + i] += c;
             else ga[(size_t)in[k] * G + (nb - N)] += c;
         }
     }
@@ -306,26 +412,27 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
 // neighbours sent back through the same face, and the ghosts it fills, through
 // the transposed ghost actions), then back through conserved_to_primatives to U.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, int reconstruct,
-                                                      const double* self, const double* nba, const double* ga,
-                                                      const signed char* back, double* out, double* gout) {
+__global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, int reconstruct, AdjScratch a,
+                                                      double* out, double* gout) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
+    const double* self = a.self;
+    const double* nba = a.nba;
+    const double* ga = a.ga;
+    const signed char* back = a.back;
     constexpr int NC = DIM + 2, NV = DIM == 3 ? 5 : 4;
     const int N = v.N, G = v.G, NT = v.NT, MF = v.MF;
     const Dual* pr = (const Dual*)v.prim;
     double pb[7];
     for (int m = 0; m < 7; m++) pb[m] = self[(size_t)m * N + i];
-    if (reconstruct) {
-        int in[6];
-        face_inputs<DIM>(prm.thermo, true, in);
+    if (reconstruct || prm.viscous) {
         const int nf = v.nfaces[i];
         for (int s = 0; s < nf; s++) {
             const int nb = v.cell_nbr[s * N + i];
             if (nb >= N) continue;
             const int bs = back[s * N + i];
             if (bs < 0) continue;  // no face back to this cell (cannot happen on a conforming grid)
-            for (int k = 0; k < NV; k++) pb[in[k]] += nba[((size_t)k * MF + bs) * N + nb];
+            for (int m = 0; m < 7; m++) pb[m] += nba[((size_t)m * MF + bs) * N + nb];
         }
     }
     // ghosts filled from this cell (fill_ghost's pre-reconstruction actions)
@@ -338,6 +445,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
             for (int m = 0; m < 7; m++) gout[(size_t)g * 7 + m] = gb[m];
         const BoundDev& B = v.bounds[v.ghost_bound[g]];
         const int f = v.ghost_face[g];
+        double gvb[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (prm.viscous)
+            for (int q = 0; q < 5; q++) gvb[q] = a.gav[(size_t)q * G + g];
         for (int m = 0; m < 7; m++) {
             double sv[7];
             for (int q = 0; q < 7; q++) sv[q] = pr[q * NT + i].re;
@@ -348,6 +458,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
             apply_actions<DualA, double>(B.pre, B.n_pre, gh, src, fg, v.F, f, prm);
             pb[m] += gb[0] * gh.rho.du + gb[1] * gh.p.du + gb[2] * gh.T.du + gb[3] * gh.e.du +
                      gb[4] * gh.vx.du + gb[5] * gh.vy.du + gb[6] * gh.vz.du;
+            if (prm.viscous) {  // the pre-viscous actions continue from the pre-reconstruction ghost
+                apply_actions<DualA, double>(B.visc, B.n_visc, gh, src, fg, v.F, f, prm);
+                pb[m] += gvb[0] * gh.p.du + gvb[1] * gh.T.du + gvb[2] * gh.vx.du + gvb[3] * gh.vy.du +
+                         gvb[4] * gh.vz.du;
+            }
         }
     }
     // conserved_to_primatives (primative_conserved_conversion.cpp:4-23), one seed per component
@@ -374,18 +489,19 @@ void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool r
     using namespace k_tan;
     const unsigned bn = blocks_for(v.N), bf = blocks_for(v.F);
     if (v.G > 0) cudaMemsetAsync(a.ga, 0, sizeof(double) * 7 * v.G, s);
+    if (v.G > 0 && p.viscous) cudaMemsetAsync(a.gav, 0, sizeof(double) * 5 * v.G, s);
     if (v.dim == 3) {
         k_tan_prims<3><<<bn, kBlock, 0, s>>>(v, p, nullptr);
-        if (reconstruct) k_recon<Dual, Dual, double, 3, true><<<bn, kBlock, 0, s>>>(v, p, 1);
-        k_adj_face<3><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a.qf, a.ga);
-        k_adj_cell<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.qf, a.self, a.nba, a.ga);
-        k_adj_final<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.self, a.nba, a.ga, a.back, out, ghost_out);
+        if (reconstruct || p.viscous) k_recon<Dual, Dual, double, 3, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        k_adj_face<3><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a);
+        k_adj_cell<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a);
+        k_adj_final<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a, out, ghost_out);
     } else {
         k_tan_prims<2><<<bn, kBlock, 0, s>>>(v, p, nullptr);
-        if (reconstruct) k_recon<Dual, Dual, double, 2, true><<<bn, kBlock, 0, s>>>(v, p, 1);
-        k_adj_face<2><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a.qf, a.ga);
-        k_adj_cell<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.qf, a.self, a.nba, a.ga);
-        k_adj_final<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a.self, a.nba, a.ga, a.back, out, ghost_out);
+        if (reconstruct || p.viscous) k_recon<Dual, Dual, double, 2, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        k_adj_face<2><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a);
+        k_adj_cell<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a);
+        k_adj_final<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a, out, ghost_out);
     }
 }
 

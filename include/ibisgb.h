@@ -217,8 +217,7 @@ int ibisgb_jvp(ibisgb_ctx* ctx, const double* v, double* out, double inv_dt_star
  * the adjoint of every ghost cell's primitives (G x 7 rows: rho, p, T, e, vx,
  * vy, vz), from which derivatives with respect to boundary states (an inflow
  * Mach number) follow.  allow_reconstruction = 0 gives the transpose of the
- * first-order linearisation.  Inviscid configurations only (IBISGB_ERR_CONFIG
- * otherwise). */
+ * first-order linearisation.  Viscous fluxes are included. */
 int ibisgb_vjp_device(ibisgb_ctx* ctx, const double* w_device, double* out_device, double* ghost_out_device,
                       int32_t allow_reconstruction, void* stream);
 

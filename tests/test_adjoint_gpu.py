@@ -1,8 +1,8 @@
 """The adjoint (vector-Jacobian product) kernels of the residual.
 
 * Dot-product test against the tangent: <w, J v> = <J^T w, v> to 1e-12
-  relative, on every inviscid configuration the tangent covers, with and
-  without reconstruction; central differences for LDFSS2, whose tangent keeps
+  relative, on every configuration the tangent covers (viscous included),
+  with and without reconstruction; central differences for LDFSS2, whose tangent keeps
   the reference's nonlinear dual floor rule.
 * Boundary-state adjoint: the ghost-cell adjoint, contracted with the
   derivative of the inflow ghost state, against central differences of the
@@ -30,7 +30,8 @@ def _setup(name, **kw):
                                      ("ramp", {"thermo": "rho_p"}),
                                      ("ramp", {"thermo": "p_T"}), ("ramp", {"limiter": "unlimited"}),
                                      ("ramp", {"order": 1}), ("box", {}), ("box_inout", {}), ("tri", {}),
-                                     ("tet", {}), ("wedge", {}), ("pyramid", {}), ("tiny2d", {})],
+                                     ("tet", {}), ("wedge", {}), ("pyramid", {}), ("tiny2d", {}),
+                                     ("plate", {}), ("plate", {"order": 1}), ("subsonic", {})],
                          ids=lambda x: x if isinstance(x, str) else "-".join(f"{k}={v}" for k, v in x.items()))
 @pytest.mark.parametrize("recon", [True, False])
 def test_vjp_is_the_transpose_of_the_jvp(name, kw, recon):
