@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--batch-cases", type=int, default=64, help="ramp cases of the batched ensemble (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=200, help="timed RK steps of the batched ensemble")
     ap.add_argument("--seq-steps", type=int, default=40, help="timed RK steps per case, one case at a time")
+    ap.add_argument("--variants", default="",
+                    help="launch variants recon,face,update of the mixed build instead of autotuning (profiling)")
     ap.add_argument("--fused", default="auto", choices=["auto", "on", "off"],
                     help="fused stage for structured blocks: let the autotuner choose, force, or disable")
     ap.add_argument("--plate-steps", type=int, default=300, help="RK steps of the flat-plate accuracy case (0: skip)")
@@ -372,7 +374,12 @@ def run_ours(args, world, rank, local):
     # --- headline: mixed precision, device-resident state
     sim.set_primitives(*ic)
     sim.set_fused({"auto": -1, "on": 1, "off": 0}[args.fused])
-    tune_mixed = sim.autotune("mixed")
+    if args.variants:
+        r, f, u = (int(x) for x in args.variants.split(","))
+        sim.set_launch_variants("mixed", r, f, u)
+        tune_mixed = {"variants": {"recon": r, "face": f, "update": u}, "ms": None}
+    else:
+        tune_mixed = sim.autotune("mixed")
     fused = sim.fused_info()
     sim.take_steps(args.warmup, "mixed")
     barrier()
