@@ -17,6 +17,7 @@
 #include "engine.hpp"
 #include "json_lite.hpp"
 #include "mesh.hpp"
+#include "profile.hpp"
 #include "structured.hpp"
 
 using namespace ibisgb;
@@ -87,10 +88,13 @@ ActionKind parse_action_kind(const std::string& t) {
     if (t == "subsonic_inflow") return aSubsonicInflow;
     if (t == "subsonic_outflow") return aSubsonicOutflow;
     if (t == "periodic_copy") return aPeriodicCopy;
+    if (t == "boundary_layer_profile") return aBoundaryLayer;
     throw ConfigError("Unknown boundary action " + t);
 }
 
-Action parse_action(const Json& a) {  // build_boundary_action, boundary.cpp:448-479
+// build_boundary_action, boundary.cpp:448-479; a boundary_layer_profile's
+// splines go to `profiles` and the action keeps their index.
+Action parse_action(const Json& a, std::vector<BoundaryLayerProfile>& profiles) {
     Action out{};
     out.kind = parse_action_kind(a.at("type").as_string());
     auto fs = [&](const Json& j) {
@@ -102,6 +106,20 @@ Action parse_action(const Json& a) {  // build_boundary_action, boundary.cpp:448
     if (out.kind == aFlowStateCopy || out.kind == aSubsonicInflow) fs(a.at("flow_state"));
     if (out.kind == aFixTemperature) out.value = a.at("temperature").as_double();
     if (out.kind == aSubsonicOutflow) out.value = a.at("pressure").as_double();
+    if (out.kind == aBoundaryLayer) {  // BoundaryLayerProfile ctor, boundary.cpp:48-57
+        const Json& pj = a.at("profile");
+        const std::vector<double> h = pj.at("height").as_doubles();
+        BoundaryLayerProfile bl;
+        try {
+            bl.vx = NaturalSpline(h, pj.at("v").as_doubles());
+            bl.T = NaturalSpline(h, pj.at("T").as_doubles());
+        } catch (const std::runtime_error& e) {
+            throw ConfigError(std::string("boundary_layer_profile: ") + e.what());
+        }
+        bl.p = pj.at("p").as_double();
+        out.table = (int)profiles.size();
+        profiles.push_back(bl);
+    }
     return out;
 }
 
@@ -113,6 +131,7 @@ struct ibisgb_ctx {
     FvParams prm{};
     Mesh mesh;
     std::vector<BoundDev> bounds_host;
+    std::vector<BoundaryLayerProfile> profiles;  // tables of the boundary_layer_profile actions
 
     // steady-state / JFNK settings (SteadyState ctor steady_state.cpp:176-221, Jfnk jfnk.cpp:7-23)
     struct Steady {
@@ -153,7 +172,7 @@ struct ibisgb_ctx {
 
     // connectivity and per-cell data shared by all arithmetics
     DBuf cell_face, cell_nbr, outsign, nfaces, left, right, ghost_src, ghost_face, ghost_bound,
-        bounds, feed_off, feed_ghost, vol, inv_vol;
+        bounds, gfix, feed_off, feed_ghost, vol, inv_vol;
     DBuf U, k, vsig, ctl, l2, out, branches;
     StateBufs s64, s32;
     std::vector<double> ic_prims;  // host IC primitives (7 x NT), kept until the first update
@@ -346,8 +365,6 @@ struct ibisgb_ctx {
                     for (int d = 0; d < 3; d++) s.offset[d] = off.at(d);
                 }
             }
-            if (!b.at("post_convective_flux").elements().empty())
-                throw ConfigError("post_convective_flux actions (constant_flux) are not supported");
             out.push_back(s);
         }
         return out;
@@ -359,22 +376,31 @@ struct ibisgb_ctx {
         std::vector<BoundarySpec> specs = boundary_specs();
         build_mesh(in, specs, prm.viscous || prm.order > 1, mesh);
         check_index_range();
-        // every face needs two sides: a boundary without ghost cells would need a
-        // post-convective flux action, which is not supported
+        // every face needs two sides (boundaries without ghost cells are not supported)
         for (int64_t f = 0; f < mesh.F; f++)
             if (mesh.left[f] < 0 || mesh.right[f] < 0)
-                throw ConfigError("a boundary face has no ghost cell (ghost_cells false needs a flux action, "
-                                  "which is not supported)");
+                throw ConfigError("a boundary face has no ghost cell (ghost_cells false is not supported)");
         for (const auto& b : mesh.bounds) {  // BoundaryCondition ctor, boundary.cpp:494-515
             const Json& bj = config.at("grid").at("boundaries").at(b.tag);
             BoundDev d{};
             for (const Json& a : bj.at("pre_reconstruction").elements()) {
                 if (d.n_pre == kMaxActions) throw ConfigError("too many boundary actions");
-                d.pre[d.n_pre++] = parse_action(a);
+                d.pre[d.n_pre++] = parse_action(a, profiles);
             }
             for (const Json& a : bj.at("pre_viscous_grad").elements()) {
                 if (d.n_visc == kMaxActions) throw ConfigError("too many boundary actions");
-                d.visc[d.n_visc++] = parse_action(a);
+                d.visc[d.n_visc++] = parse_action(a, profiles);
+            }
+            // post_convective_flux (build_flux_action, boundary.cpp:481-492): each
+            // action overwrites the face flux, so the last one is the one that counts
+            for (const Json& a : bj.at("post_convective_flux").elements()) {
+                const std::string t = a.at("type").as_string();
+                if (t != "constant_flux") throw ConfigError("Unknown flux action " + t);
+                const Json& fs = a.at("flow_state");
+                const char* keys[7] = {"T", "p", "rho", "energy", "vx", "vy", "vz"};
+                for (int q = 0; q < 7; q++) d.cfs[q] = fs.at(keys[q]).as_double();
+                d.cflux = 1;
+                prm.cflux = 1;
             }
             bounds_host.push_back(d);
         }
@@ -415,8 +441,17 @@ struct ibisgb_ctx {
             throw ConfigError(e.what());
         }
         check_index_range();
+        prm.cflux = 0;
         for (int i = 0; i < n; i++) {
-            bounds_host.insert(bounds_host.end(), cs[i]->bounds_host.begin(), cs[i]->bounds_host.end());
+            // profile tables of case i follow those of the cases before it
+            const int t0 = (int)profiles.size();
+            profiles.insert(profiles.end(), cs[i]->profiles.begin(), cs[i]->profiles.end());
+            for (BoundDev d : cs[i]->bounds_host) {
+                for (int k = 0; k < d.n_pre; k++) d.pre[k].table += t0;
+                for (int k = 0; k < d.n_visc; k++) d.visc[k].table += t0;
+                bounds_host.push_back(d);
+            }
+            prm.cflux |= cs[i]->prm.cflux;
             case_ctl.push_back(cs[i]->ctl_host);
             case_dt_init.push_back(cs[i]->dt_init);
         }
@@ -473,6 +508,30 @@ struct ibisgb_ctx {
         }
         upload(ghost_src, gs, stream); upload(ghost_face, gf, stream); upload(ghost_bound, gb, stream);
         upload(bounds, bounds_host, stream);
+        if (!profiles.empty()) {
+            // boundary-layer ghost states (boundary.cpp:59-94): T(y), p, rho = p / (R T),
+            // e = Cv T, vx(y) at the ghost centroid's height y
+            const size_t nt = profiles.size();
+            std::vector<double> t(nt * 5 * (size_t)std::max<int64_t>(G, 1), 0.0);
+            for (int64_t g = 0; g < G; g++) {
+                const BoundDev& d = bounds_host[gb[g]];
+                auto fill = [&](const Action& a) {
+                    if (a.kind != aBoundaryLayer) return;
+                    const BoundaryLayerProfile& bl = profiles[a.table];
+                    const double y = mesh.ccy[N + g];
+                    double* o = t.data() + (size_t)a.table * 5 * G;
+                    const double T = bl.T(y);
+                    o[g] = T;
+                    o[G + g] = bl.p;
+                    o[2 * G + g] = bl.p / (prm.R * T);
+                    o[3 * G + g] = prm.Cv * T;
+                    o[4 * G + g] = bl.vx(y);
+                };
+                for (int k = 0; k < d.n_pre; k++) fill(d.pre[k]);
+                for (int k = 0; k < d.n_visc; k++) fill(d.visc[k]);
+            }
+            upload(gfix, t, stream);
+        }
         // ghosts fed by each valid cell (CSR)
         std::vector<int> off(N + 1, 0), fg(G);
         for (int64_t g = 0; g < G; g++) off[gs[g] + 1]++;
@@ -558,7 +617,7 @@ struct ibisgb_ctx {
         v.outsign = outsign.as<signed char>(); v.nfaces = nfaces.as<int>();
         v.left = left.as<int>(); v.right = right.as<int>();
         v.ghost_src = ghost_src.as<int>(); v.ghost_face = ghost_face.as<int>();
-        v.ghost_bound = ghost_bound.as<int>(); v.bounds = bounds.as<BoundDev>();
+        v.ghost_bound = ghost_bound.as<int>(); v.bounds = bounds.as<BoundDev>(); v.gfix = gfix.as<double>();
         v.feed_off = feed_off.as<int>(); v.feed_ghost = feed_ghost.as<int>();
         v.cc = s.cc.p; v.r = s.r.p; v.face = s.face.p; v.vol = vol.as<double>();
         v.inv_vol = inv_vol.as<double>(); v.lsqw = s.lsqw.p;
@@ -698,6 +757,7 @@ struct ibisgb_ctx {
         if (fused_elig >= 0) return fused_elig == 1;
         fused_elig = 0;
         if (prm.viscous) fused_why = "viscous fluxes take the generic kernels";
+        else if (prm.cflux) fused_why = "constant-flux boundaries take the generic kernels";
         else if (prm.order != 2) fused_why = "first-order reconstruction takes the generic kernels";
         else {
             std::vector<int64_t> offs = n_cases > 1 ? cell_off : std::vector<int64_t>{0, mesh.N};

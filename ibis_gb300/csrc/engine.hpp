@@ -23,6 +23,7 @@ enum ActionKind : int {
     aSubsonicInflow = 5,
     aSubsonicOutflow = 6,
     aPeriodicCopy = 7,   // extension: copy of the periodic donor cell
+    aBoundaryLayer = 8,  // boundary_layer_profile: a fixed state per ghost (its centroid height)
 };
 
 constexpr int kMaxActions = 4;
@@ -30,15 +31,18 @@ constexpr int kMaxStages = 8;
 
 struct Action {
     int kind;
+    int table;     // boundary_layer_profile: its table of per-ghost states (DevView::gfix)
     double fs[7];  // T, p, rho, energy, vx, vy, vz
     double value;  // fix_temperature temperature / subsonic_outflow pressure
 };
 
-// The ghost-cell actions of one boundary tag.
+// The ghost-cell and flux actions of one boundary tag.
 struct BoundDev {
     int n_pre, n_visc;
     Action pre[kMaxActions];   // pre_reconstruction
     Action visc[kMaxActions];  // pre_viscous_grad
+    int cflux;                 // post_convective_flux: a constant_flux action (the last one wins)
+    double cfs[7];             // its flow state: T, p, rho, energy, vx, vy, vz
 };
 
 // Gas, transport and finite-volume settings (FiniteVolume ctor, finite_volume.cpp:13-54).
@@ -49,6 +53,7 @@ struct FvParams {
     int order;    // reconstruction order 1 or 2
     int limiter;  // 1: Barth-Jespersen, 0: unlimited
     int viscous;
+    int cflux;             // some boundary has a constant_flux action
     double eps;            // Barth-Jespersen epsilon
     double delta;          // LDFSS2 delta
     double signal_factor;  // viscous dt signal factor
@@ -94,6 +99,7 @@ struct DevView {
     const int* ghost_face;
     const int* ghost_bound;
     const BoundDev* bounds;
+    const double* gfix;  // [tables][5][G]: T, p, rho, e, vx of each boundary-layer profile's ghosts
     // ghosts fed by each valid cell (CSR over valid cells)
     const int* feed_off;
     const int* feed_ghost;

@@ -59,7 +59,8 @@ IBISGB_HD int visc_prim(int q) { return q == 0 ? 2 : 3 + q; }
 // ---------------------------------------------------------------------------
 template <class S, class Gm>
 __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const StateT<S>& src,
-                              const Gm* face, int F, int f, const FvParams& prm) {
+                              const Gm* face, int F, int f, const FvParams& prm, const double* gfix, int G,
+                              int g) {
     for (int a = 0; a < n; a++) {
         const Action& A = acts[a];
         switch (A.kind) {
@@ -91,6 +92,12 @@ __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const St
             case aFixTemperature:
                 gh.T = S(2.0) * S(A.value) - src.T;
                 break;
+            case aBoundaryLayer: {  // boundary.cpp:59-94, evaluated on the host at the ghost's height
+                const double* t = gfix + (size_t)A.table * 5 * G;
+                gh.T = S(t[g]); gh.p = S(t[G + g]); gh.rho = S(t[2 * G + g]); gh.e = S(t[3 * G + g]);
+                gh.vx = S(t[4 * G + g]); gh.vy = S(0.0); gh.vz = S(0.0);
+                break;
+            }
             case aSubsonicInflow: {
                 S nx = S(face[f]), ny = S(face[F + f]), nz = S(face[2 * F + f]);
                 S vc = nx * (S(A.fs[4]) - src.vx) + ny * (S(A.fs[5]) - src.vy) + nz * (S(A.fs[6]) - src.vz);
@@ -138,13 +145,13 @@ __device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const S
     const Gm* face = (const Gm*)v.face;
     int f = v.ghost_face[g];
     StateT<S> gh = src;
-    apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm);
+    apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm, v.gfix, v.G, g);
     P* pr = (P*)v.prim;
     const int NT = v.NT, id = v.N + g;
     pr[id] = (P)gh.rho; pr[NT + id] = (P)gh.p; pr[2 * NT + id] = (P)gh.T; pr[3 * NT + id] = (P)gh.e;
     pr[4 * NT + id] = (P)gh.vx; pr[5 * NT + id] = (P)gh.vy; pr[6 * NT + id] = (P)gh.vz;
     if (prm.viscous) {
-        apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm);
+        apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm, v.gfix, v.G, g);
         P* vg = (P*)v.vghost;
         vg[g] = (P)gh.p; vg[v.G + g] = (P)gh.T; vg[2 * v.G + g] = (P)gh.vx;
         vg[3 * v.G + g] = (P)gh.vy; vg[4 * v.G + g] = (P)gh.vz;
@@ -427,6 +434,30 @@ __device__ __forceinline__ void convective_flux(const FvParams& prm, const Gas<R
     out[4] = Fl[4];
 }
 
+// ConstantFlux::apply (boundary.cpp:404-444) on a fixed grid: the flux of the
+// state fs (T, p, rho, energy, vx, vy, vz) through a face of normal n, in the
+// global frame.  The energy term keeps the reference's vy * n.x.
+template <class R, int DIM>
+__device__ __forceinline__ void constant_flux(const double (&fs)[7], double Cv, R nx, R ny, R nz, R (&out)[5]) {
+    const R vx = R(fs[4]), vy = R(fs[5]), vz = R(fs[6]), p = R(fs[1]);
+    const R u = R(Cv) * R(fs[0]);  // internal_energy: Cv T
+    const R mass = R(fs[2]) * (vx * nx + vy * ny + vz * nz);
+    out[0] = mass;
+    out[1] = p * nx + vx * mass;
+    out[2] = p * ny + vy * mass;
+    out[3] = DIM == 3 ? p * nz + vz * mass : R(0.0);
+    out[4] = mass * (u + R(0.5) * (vx * vx + vy * vy + vz * vz)) + p * (vx * nx + vy * nx + vz * nz);
+}
+
+// The boundary of a face's ghost side when that boundary has a constant_flux
+// action, else null.
+IBISGB_HD const BoundDev* constant_flux_bound(const DevView& v, int l, int r) {
+    const int gc = r >= v.N ? r : (l >= v.N ? l : -1);
+    if (gc < 0) return nullptr;
+    const BoundDev* B = &v.bounds[v.ghost_bound[gc - v.N]];
+    return B->cflux ? B : nullptr;
+}
+
 // Viscous stress and heat flux through a face (viscous_flux.cpp:130-232) from
 // the states of both sides (p, T, vx, vy, vz: the cells' primitives, or a ghost's
 // pre-viscous values) and the viscous gradients (T, vx, vy, vz: 3 components
@@ -573,6 +604,10 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
     }
     R Fg[5];
     convective_flux<R, DIM, EXACT>(prm, gm, S[0], S[1], nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z, Fg);
+    if (prm.cflux) {  // apply_post_convective_flux_bc (finite_volume.cpp:71, 197-209)
+        if (const BoundDev* B = constant_flux_bound(v, cells[0], cells[1]))
+            constant_flux<R, DIM>(B->cfs, prm.Cv, nx, ny, nz, Fg);
+    }
     R mx = Fg[1], my = Fg[2], mz = Fg[3];
     R en = Fg[4];
 

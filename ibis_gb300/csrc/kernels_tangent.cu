@@ -155,7 +155,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
     const DualA t2x(DIM == 3 ? fg[6 * F + f] : 0.0), t2y(DIM == 3 ? fg[7 * F + f] : 0.0), t2z(fg[8 * F + f]);
     const Gas<DualA> gm(prm);
     int in[6];
-    const int K = face_inputs<DIM>(prm.thermo, reconstruct, in);
+    // a constant-flux face's convective flux does not depend on the state
+    const int K = prm.cflux && constant_flux_bound(v, cells[0], cells[1]) ? 0
+                                                                           : face_inputs<DIM>(prm.thermo, reconstruct, in);
     for (int side = 0; side < 2; side++) {
         for (int k = 0; k < K; k++) {
             DualA qd[2][7];
@@ -455,11 +457,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
                               DualA(sv[3], m == 3), DualA(sv[4], m == 4), DualA(sv[5], m == 5),
                               DualA(sv[6], m == 6)};
             StateT<DualA> gh = src;
-            apply_actions<DualA, double>(B.pre, B.n_pre, gh, src, fg, v.F, f, prm);
+            apply_actions<DualA, double>(B.pre, B.n_pre, gh, src, fg, v.F, f, prm, v.gfix, G, g);
             pb[m] += gb[0] * gh.rho.du + gb[1] * gh.p.du + gb[2] * gh.T.du + gb[3] * gh.e.du +
                      gb[4] * gh.vx.du + gb[5] * gh.vy.du + gb[6] * gh.vz.du;
             if (prm.viscous) {  // the pre-viscous actions continue from the pre-reconstruction ghost
-                apply_actions<DualA, double>(B.visc, B.n_visc, gh, src, fg, v.F, f, prm);
+                apply_actions<DualA, double>(B.visc, B.n_visc, gh, src, fg, v.F, f, prm, v.gfix, G, g);
                 pb[m] += gvb[0] * gh.p.du + gvb[1] * gh.T.du + gvb[2] * gh.vx.du + gvb[3] * gh.vy.du +
                          gvb[4] * gh.vz.du;
             }

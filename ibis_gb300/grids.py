@@ -406,6 +406,14 @@ def constant_flux(fs: dict) -> dict:
               post_convective_flux=[{"type": "constant_flux", "flow_state": fs}])
 
 
+def boundary_layer_inflow(height, velocity_profile, temperature_profile, pressure: float) -> dict:
+    """prep.py:549-556: ghosts take vx(y) and T(y) from natural cubic splines over
+    the wall-normal coordinate (at least 4 points), p fixed, vy = vz = 0."""
+    return bc([{"type": "boundary_layer_profile",
+                "profile": {"height": list(map(float, height)), "v": list(map(float, velocity_profile)),
+                            "T": list(map(float, temperature_profile)), "p": float(pressure)}}])
+
+
 def periodic(partner: str, offset) -> dict:
     """Periodic ghost copy from the matching cell across the domain.  An
     extension: the reference has no periodic boundary action."""

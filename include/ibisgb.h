@@ -134,7 +134,8 @@ int ibisgb_get_stream(ibisgb_ctx* ctx, void** stream);
 int ibisgb_kernel_times(ibisgb_ctx* ctx, int32_t precision, int32_t reps, double out[4]);
 
 /* dU/dt of the valid cells (N x n_conserved row-major) at the current state,
- * including the pre-reconstruction / pre-viscous boundary actions.  Replaces
+ * including the pre-reconstruction / pre-viscous boundary actions and the
+ * post-convective constant_flux action.  Replaces
  * FiniteVolume<T>::compute_dudt (src/finite_volume/finite_volume/finite_volume.cpp:56-96). */
 int ibisgb_residual(ibisgb_ctx* ctx, int32_t precision, double* dudt);
 

@@ -69,6 +69,7 @@ def lib():
         L.orc_steady_conserved.argtypes = [C.c_void_p, _dp]
         L.orc_dense_gmres.argtypes = [C.c_int, _dp, _dp, _dp, C.c_int, C.c_double, C.c_void_p,
                                       C.c_int, C.c_double, _dp]
+        L.orc_cubic_spline.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp]
         L.orc_num_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -246,6 +247,16 @@ def dense_gmres(A, b, max_iters, tol, P=None, max_prec_iters=0, prec_tol=0.0):
     if rc != 0:
         raise RuntimeError("oracle gmres failed")
     return x, dict(success=bool(info[0]), n_iters=int(info[1]), residual=info[2])
+
+
+def cubic_spline(x, y, q):
+    """The boundary-layer profile's natural cubic spline through (x, y), evaluated at q."""
+    x = np.ascontiguousarray(x, np.float64)
+    q = np.ascontiguousarray(q, np.float64)
+    out = np.zeros(len(q))
+    if lib().orc_cubic_spline(len(x), x, np.ascontiguousarray(y, np.float64), len(q), q, out) != 0:
+        raise ValueError("cubic spline needs at least 4 points and as many y as x")
+    return out
 
 
 def num_threads() -> int:

@@ -434,6 +434,18 @@ int orc_dense_gmres(int n, const double* A, const double* rhs, double* x, int ma
     }
 }
 
+// ---- natural cubic spline of the boundary-layer profile (cubic_spline.cpp:91-159 tests) ----
+int orc_cubic_spline(int n, const double* x, const double* y, int nq, const double* q, double* out) {
+    try {
+        CubicSpline sp;
+        sp.fit(std::vector<double>(x, x + n), std::vector<double>(y, y + n));
+        for (int i = 0; i < nq; i++) out[i] = sp.eval(q[i]);
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
 int orc_num_threads() {
 #ifdef _OPENMP
     return omp_get_max_threads();

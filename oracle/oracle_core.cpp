@@ -523,6 +523,19 @@ void FiniteVolume<T>::apply_ghost_actions(const std::vector<Action>& acts, FlowS
                 case ActionKind::FixTemperature:  // boundary.cpp:243-277
                     fs.temp[ghost] = 2 * T(a.value) - fs.temp[valid];
                     break;
+                case ActionKind::BoundaryLayerProfile: {  // boundary.cpp:59-94
+                    // the profile at the ghost centroid's height; p, T -> rho, e
+                    double pos = real_part(g.ccy[ghost]);
+                    T tp = a.spline_T.eval(pos);
+                    fs.p[ghost] = a.value;
+                    fs.temp[ghost] = tp;
+                    fs.rho[ghost] = fs.p[ghost] / (gas.R * fs.temp[ghost]);
+                    fs.e[ghost] = gas.Cv * fs.temp[ghost];
+                    fs.vx[ghost] = a.spline_v.eval(pos);
+                    fs.vy[ghost] = 0.0;
+                    fs.vz[ghost] = 0.0;
+                    break;
+                }
                 case ActionKind::SubsonicInflow: {  // boundary.cpp:284-343
                     T nxf = g.nx[f], nyf = g.ny[f], nzf = g.nz[f];
                     T vc = nxf * (a.fs[4] - fs.vx[valid]) + nyf * (a.fs[5] - fs.vy[valid]) +
@@ -1152,6 +1165,59 @@ FvConfig parse_fv_config(const Json& config) {
     return c;
 }
 
+void CubicSpline::fit(const std::vector<double>& xs, const std::vector<double>& ys) {
+    const size_t n = xs.size();
+    if (n < 4) throw std::runtime_error("Insufficient points for cubic spline");
+    if (ys.size() != n) throw std::runtime_error("Cubic spline has different number of x and y points");
+    x = xs;
+    y = ys;
+    const size_t ne = n - 2;  // one equation per interior knot
+    std::vector<double> diag(ne, 0.0), upper(ne, 0.0), rhs(ne, 0.0);
+    for (size_t i = 0; i <= ne; i++) {
+        double dx = x[i + 1] - x[i];
+        double dy = y[i + 1] - y[i];
+        if (i != ne) {
+            diag[i] += dx;
+            rhs[i] -= dy / dx;
+        }
+        if (i == 0) continue;
+        rhs[i - 1] += dy / dx;
+        diag[i - 1] += dx;
+        if (i - 1 < ne - 1) upper[i - 1] += dx;
+    }
+    for (size_t i = 0; i < ne; i++) {
+        rhs[i] *= 6;
+        diag[i] *= 2;
+    }
+    for (size_t i = 1; i < ne; i++) {
+        double w = upper[i - 1] / diag[i - 1];
+        diag[i] = diag[i] - w * upper[i - 1];
+        rhs[i] = rhs[i] - w * rhs[i - 1];
+    }
+    m.assign(n, 0.0);
+    m[n - 2] = rhs[ne - 1] / diag[ne - 1];
+    for (long i = (long)ne - 2; i >= 0; i--) m[i + 1] = (rhs[i] - upper[i] * m[i + 2]) / diag[i];
+}
+
+double CubicSpline::eval(double t) const {
+    if (t <= x.front()) return y.front();
+    if (t >= x.back()) return y.back();
+    size_t idx = 0;
+    for (size_t i = 0; i < x.size(); i++) {
+        if (x[i] >= t) {
+            idx = i - 1;
+            break;
+        }
+    }
+    double dp = x[idx + 1] - t;
+    double dm = t - x[idx];
+    double dxi = x[idx + 1] - x[idx];
+    double a = (m[idx] * dp * dp * dp + m[idx + 1] * dm * dm * dm) / (6 * dxi);
+    double b = (y[idx] / dxi - m[idx] * dxi / 6) * dp;
+    double c = (y[idx + 1] / dxi - m[idx + 1] * dxi / 6) * dm;
+    return a + b + c;
+}
+
 static Action parse_action(const Json& a) {  // boundary.cpp:448-492
     Action out;
     std::string t = a.at("type").as_string();
@@ -1170,6 +1236,14 @@ static Action parse_action(const Json& a) {  // boundary.cpp:448-492
     else if (t == "subsonic_outflow") { out.kind = ActionKind::SubsonicOutflow; out.value = a.at("pressure").as_double(); }
     else if (t == "constant_flux") { out.kind = ActionKind::ConstantFlux; read_fs(a.at("flow_state")); }
     else if (t == "periodic_copy") out.kind = ActionKind::PeriodicCopy;
+    else if (t == "boundary_layer_profile") {  // BoundaryLayerProfile ctor, boundary.cpp:48-57
+        out.kind = ActionKind::BoundaryLayerProfile;
+        const Json& pr = a.at("profile");
+        std::vector<double> h = pr.at("height").as_doubles();
+        out.spline_v.fit(h, pr.at("v").as_doubles());
+        out.spline_T.fit(h, pr.at("T").as_doubles());
+        out.value = pr.at("p").as_double();
+    }
     else throw std::runtime_error("Unknown boundary action " + t);
     return out;
 }

@@ -242,13 +242,30 @@ struct Transport {
 // ---------------------------------------------------------------------------
 enum class ActionKind {
     FlowStateCopy, InternalCopy, InternalCopyReflectNormal, InternalVelCopyReflect,
-    FixTemperature, SubsonicInflow, SubsonicOutflow, ConstantFlux, PeriodicCopy
+    FixTemperature, SubsonicInflow, SubsonicOutflow, ConstantFlux, PeriodicCopy,
+    BoundaryLayerProfile
 };
+
+// Natural cubic spline (src/util/util/cubic_spline.{h,cpp}): second
+// derivatives from the tridiagonal system of the interior knots, assembled and
+// solved (Thomas algorithm) in the reference's operation order; eval clamps to
+// the end values outside [x0, x_{n-1}].  m holds the second derivative at every
+// knot with m[0] = m[n-1] = 0.  The reference stores only n-2 of them and reads
+// the last two knots' values past the end of its array (cubic_spline.cpp:47-48,
+// 80-84; cubic_spline.h:27-37); this restatement uses the natural-spline values
+// that code intends (the solved m[n-2], and m[n-1] = 0).
+struct CubicSpline {
+    std::vector<double> x, y, m;
+    void fit(const std::vector<double>& xs, const std::vector<double>& ys);  // cubic_spline.cpp:9-89
+    double eval(double t) const;                                            // cubic_spline.h:13-38
+};
+
 struct Action {
     ActionKind kind;
     // flow_state_copy / subsonic_inflow / constant_flux: T, p, rho, energy, vx, vy, vz
     double fs[7] = {0, 0, 0, 0, 0, 0, 0};
-    double value = 0.0;  // fix_temperature temperature / subsonic_outflow pressure
+    double value = 0.0;  // fix_temperature temperature / subsonic_outflow pressure / profile pressure
+    CubicSpline spline_v, spline_T;  // boundary_layer_profile: vx(y) and T(y)
 };
 struct BoundaryCondition {
     std::vector<Action> pre_reconstruction, post_convective_flux, pre_viscous_grad;

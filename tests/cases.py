@@ -51,6 +51,34 @@ def case(name, **kw):
              "south": grids.fixed_temperature_no_slip_wall(320.0), "north": grids.slip_wall()}
         c = grids.make_config(2, b, gas=gas, viscous=True, **kw)
         return g, c, random_state(g.num_cells, 300.0, 1e5, 100.0, 2, seed=5, amp=0.03)
+    if name == "bl_plate":  # viscous: boundary-layer inflow profile, constant-flux top, no-slip wall
+        y = 0.05 * (np.linspace(0, 1, 13) ** 1.3)
+        X, Y = np.meshgrid(np.linspace(0, 0.2, 17), y, indexing="ij")
+        g = grids.structured_2d(X, Y)
+        # profile heights start above the first ghost centroid and end below the
+        # top ones, so both clamps of the spline are used
+        h = [0.0015, 0.004, 0.008, 0.013, 0.02, 0.03, 0.04]
+        u = [60.0, 180.0, 320.0, 420.0, 480.0, 500.0, 505.0]
+        T = [340.0, 328.0, 315.0, 306.0, 301.0, 300.0, 300.0]
+        top = grids.flow_state(gas, 300.0, 1e5, 505.0, -15.0)
+        b = {"west": grids.boundary_layer_inflow(h, u, T, 1e5), "east": grids.supersonic_outflow(),
+             "south": grids.adiabatic_no_slip_wall(), "north": grids.constant_flux(top)}
+        c = grids.make_config(2, b, gas=gas, viscous=True, **kw)
+        return g, c, random_state(g.num_cells, 300.0, 1e5, 450.0, 2, seed=7, amp=0.04)
+    if name == "cflux_ramp":  # the ramp with a constant-flux inflow (vy != 0: the vy n.x term counts)
+        g, c, inf = grids.ramp_case(kw.pop("ni", 24), kw.pop("nj", 12), **kw)
+        fs = grids.flow_state(gas, inf["T"], inf["p"], inf["vx"], 0.1 * inf["vx"])
+        c["grid"]["boundaries"]["inflow"] = grids.constant_flux(fs)
+        return g, c, random_state(g.num_cells, inf["T"], inf["p"], inf["vx"], 2, seed=8)
+    if name == "cflux_box":  # 3-D channel with a constant-flux inflow
+        n = kw.pop("n", 5)
+        g = grids.box_3d(n)
+        inflow = grids.flow_state(gas, 300.0, 1e5, 700.0, 30.0, 20.0)
+        b = {"west": grids.constant_flux(inflow), "east": grids.supersonic_outflow(),
+             "south": grids.slip_wall(), "north": grids.slip_wall(), "bottom": grids.slip_wall(),
+             "top": grids.constant_flux(grids.flow_state(gas, 310.0, 1.02e5, 690.0, 25.0, -10.0))}
+        c = grids.make_config(3, b, gas=gas, **kw)
+        return g, c, random_state(g.num_cells, 300.0, 1e5, 700.0, 3, seed=9)
     if name in ("tri", "tet", "wedge", "pyramid", "tiny2d", "tiny3d"):
         # other element types (every one the reference reads) and the smallest grids,
         # supersonic inflow on the first tag, slip walls and outflow on the others

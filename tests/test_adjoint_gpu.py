@@ -31,7 +31,8 @@ def _setup(name, **kw):
                                      ("ramp", {"thermo": "p_T"}), ("ramp", {"limiter": "unlimited"}),
                                      ("ramp", {"order": 1}), ("box", {}), ("box_inout", {}), ("tri", {}),
                                      ("tet", {}), ("wedge", {}), ("pyramid", {}), ("tiny2d", {}),
-                                     ("plate", {}), ("plate", {"order": 1}), ("subsonic", {})],
+                                     ("plate", {}), ("plate", {"order": 1}), ("subsonic", {}), ("bl_plate", {}),
+                                     ("cflux_ramp", {}), ("cflux_box", {})],
                          ids=lambda x: x if isinstance(x, str) else "-".join(f"{k}={v}" for k, v in x.items()))
 @pytest.mark.parametrize("recon", [True, False])
 def test_vjp_is_the_transpose_of_the_jvp(name, kw, recon):

@@ -58,3 +58,28 @@ def test_batch_estimate_dt_and_jvp():
     out = b.matrix_vector_product(v, 1e3)
     for s, vb, ob in zip(sims, b.split(v), b.split(out)):
         assert np.array_equal(ob, s.matrix_vector_product(vb, 1e3))
+
+
+def test_batch_with_profile_and_constant_flux_boundaries():
+    """Each case keeps its own boundary-layer profile table and constant-flux
+    state when merged into a batch."""
+    from tests.cases import case
+    sims, states = [], []
+    for k, scale in enumerate([1.0, 0.8, 1.1]):
+        g, c, st = case("bl_plate")
+        prof = c["grid"]["boundaries"]["west"]["pre_reconstruction"][0]["profile"]
+        prof["v"] = [scale * x for x in prof["v"]]
+        c["grid"]["boundaries"]["north"]["post_convective_flux"][0]["flow_state"]["vx"] *= scale
+        sims.append(Simulation(c, g))
+        sims[-1].set_primitives(*st[:4])
+        states.append(st)
+    b = Batch(sims)
+    b.set_primitives(*[np.concatenate([st[q] for st in states]) for q in range(4)])
+    for prec in ("f64_exact", "mixed"):
+        r = b.compute_dudt(prec)
+        for s, rb in zip(sims, b.split(r)):
+            assert np.array_equal(rb, s.compute_dudt(prec)), prec
+    b.take_steps(3, "f64_exact")
+    for s, Ub in zip(sims, b.split(b.conserved())):
+        s.take_steps(3, "f64_exact")
+        assert np.array_equal(Ub, s.conserved())

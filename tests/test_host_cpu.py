@@ -22,7 +22,7 @@ def test_library_exports_every_declared_symbol():
 
 
 @pytest.mark.parametrize("name", ["ramp", "plate", "box", "box_inout", "subsonic", "tri", "tet", "wedge", "pyramid",
-                                  "tiny2d", "tiny3d"])
+                                  "tiny2d", "tiny3d", "bl_plate", "cflux_box"])
 def test_numbering_and_geometry_match_oracle(name):
     g, c, _ = case(name)
     sim, o = Simulation(c, g), Oracle(c, g)
@@ -92,6 +92,26 @@ def test_errors_come_back_as_codes(tmp_path):
     missing_bc["grid"] = dict(c["grid"], boundaries={k: v for k, v in c["grid"]["boundaries"].items() if k != "wall"})
     with pytest.raises(IbisgbError):
         Simulation(missing_bc, g)
+
+
+def test_flux_and_profile_action_errors():
+    """Unknown flux actions and short spline profiles are configuration errors,
+    as build_flux_action and the CubicSpline constructor throw (boundary.cpp:481-492,
+    cubic_spline.cpp:12-19)."""
+    import copy
+    g, c, _ = case("bl_plate")
+    bad = copy.deepcopy(c)
+    bad["grid"]["boundaries"]["north"]["post_convective_flux"][0]["type"] = "shock_fit"
+    with pytest.raises(IbisgbError) as e:
+        Simulation(bad, g)
+    assert e.value.code == -1 and "shock_fit" in str(e.value)
+    short = copy.deepcopy(c)
+    prof = short["grid"]["boundaries"]["west"]["pre_reconstruction"][0]["profile"]
+    for k in ("height", "v", "T"):
+        prof[k] = prof[k][:3]
+    with pytest.raises(IbisgbError) as e:
+        Simulation(short, g)
+    assert e.value.code == -1 and "Insufficient points" in str(e.value)
 
 
 def test_state_calls_before_initial_condition_are_rejected():

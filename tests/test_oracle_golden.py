@@ -101,3 +101,38 @@ def test_uniform_stream_is_steady(flux, dim):
                             np.full(n, 100.0), np.full(n, 50.0) if dim == 3 else None)
     r = o.residual()
     assert np.abs(r).max() < 1e-9 * 1e5 * 800.0
+
+
+@pytest.mark.parametrize("block", ["cubic_spline", "cubic_spline_2"])
+def test_cubic_spline(golden, block):
+    """The boundary-layer profile's spline against the reference's spline tests."""
+    from oracle.oracle import cubic_spline
+    g = golden[block]
+    q, expected = np.array(g["evals"]).T
+    got = cubic_spline(g["x"], g["y"], q)
+    assert np.allclose(got, expected, rtol=1.19e-5, atol=1.19e-5 * 1e-3)
+
+
+def test_cubic_spline_is_a_natural_spline():
+    """Interpolates, has continuous first derivatives at the knots and zero
+    curvature at both ends; rejects fewer than 4 points."""
+    from oracle.oracle import cubic_spline
+    rng = np.random.default_rng(3)
+    x = np.cumsum(rng.uniform(0.1, 1.0, 9))
+    y = rng.normal(size=9)
+    assert np.allclose(cubic_spline(x, y, x[1:-1]), y[1:-1], rtol=0, atol=1e-12)
+    h = 1e-6
+    for k in range(1, 8):
+        left = (cubic_spline(x, y, [x[k]])[0] - cubic_spline(x, y, [x[k] - h])[0]) / h
+        right = (cubic_spline(x, y, [x[k] + h])[0] - cubic_spline(x, y, [x[k]])[0]) / h
+        assert abs(left - right) < 1e-4 * (1 + abs(left))
+    def curvature(c, d):
+        f = cubic_spline(x, y, [c - d, c, c + d])
+        return (f[0] - 2 * f[1] + f[2]) / d ** 2
+    for end, s in ((x[0], 1), (x[-1], -1)):
+        # the curvature is linear on the end interval: extrapolate it to the end knot
+        d1, d2 = curvature(end + s * 2e-4, 1e-4), curvature(end + s * 4e-4, 1e-4)
+        scale = abs(curvature(end + s * 0.05, 1e-3)) + 1.0
+        assert abs(2 * d1 - d2) < 1e-3 * scale, (d1, d2)
+    with pytest.raises(ValueError):
+        cubic_spline([0, 1, 2], [0, 1, 2], [0.5])

@@ -43,6 +43,10 @@ CASES = [
     ("pyramid", {"flux": "ausmdv", "thermo": "rho_p"}),
     ("tiny2d", {}),
     ("tiny3d", {}),
+    ("bl_plate", {}),
+    ("cflux_ramp", {}),
+    ("cflux_ramp", {"flux": "ldfss2"}),
+    ("cflux_box", {}),
 ]
 
 
@@ -98,7 +102,8 @@ def test_estimate_dt(name):
     assert sim.estimate_dt() == pytest.approx(ref.estimate_dt(), rel=1e-13)
 
 
-@pytest.mark.parametrize("name", ["ramp", "box", "plate", "tri", "tet", "wedge", "pyramid", "tiny2d"])
+@pytest.mark.parametrize("name", ["ramp", "box", "plate", "tri", "tet", "wedge", "pyramid", "tiny2d", "bl_plate",
+                                  "cflux_ramp", "cflux_box"])
 def test_rk_trajectory(name):
     steps = 6
     sim, ref = pair(name, {})

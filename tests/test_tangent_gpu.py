@@ -32,7 +32,8 @@ def steady_pair(name, **kw):
 @pytest.mark.parametrize("name,kw", [("ramp", {}), ("ramp", {"flux": "ausmdv"}), ("ramp", {"flux": "rusanov"}),
                                      ("ramp", {"thermo": "rho_p"}), ("ramp", {"order": 1}),
                                      ("plate", {}), ("box", {}), ("subsonic", {}), ("tri", {}), ("tet", {}),
-                                     ("wedge", {}), ("pyramid", {})],
+                                     ("wedge", {}), ("pyramid", {}), ("bl_plate", {}), ("cflux_ramp", {}),
+                                     ("cflux_box", {})],
                          ids=lambda x: x if isinstance(x, str) else "-".join(f"{k}={v}" for k, v in x.items()))
 def test_jvp_matches_reference_dual_numbers(name, kw):
     sim, ref = steady_pair(name, **kw)
