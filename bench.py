@@ -51,6 +51,9 @@ def parse():
                     help="launch variants recon,face,update of the mixed build instead of autotuning (profiling)")
     ap.add_argument("--fused", default="auto", choices=["auto", "on", "off"],
                     help="fused stage for structured blocks: let the autotuner choose, force, or disable")
+    ap.add_argument("--cell-flux", default="auto", choices=["auto", "on", "off"],
+                    help="per-cell flux path (face fluxes recomputed inside the update kernel): let the "
+                         "autotuner choose, force, or disable")
     ap.add_argument("--plate-steps", type=int, default=300, help="RK steps of the flat-plate accuracy case (0: skip)")
     ap.add_argument("--newton-steps", type=int, default=25, help="Newton steps of the ramp JFNK case (0: skip)")
     ap.add_argument("--sweep", default="64,128", help="smaller box sizes timed beside the headline (empty: none)")
@@ -160,6 +163,7 @@ def batch_measure(args, barrier):
     batch.set_primitives(*ic_all)
     tune = batch.autotune("mixed")
     fused = batch.fused_info()
+    cellf = batch.cell_flux_info()
     batch.take_steps(args.warmup, "mixed")
     barrier()
     t0 = time.perf_counter()
@@ -190,6 +194,7 @@ def batch_measure(args, barrier):
                         "Hanel, 2nd-order MUSCL + Barth-Jespersen, mixed precision",
             "cases": len(sims), "cells": cells, "autotune": tune["variants"],
             "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")},
+            "cell_flux": {k: cellf[k] for k in ("enabled", "variant", "cell_ms", "generic_ms")},
             "batched": {"value": upd_b / (ms_b / 1e3) / 1e6, "unit": "Mcell-updates/s",
                         "steps": args.batch_steps, "ms_per_step": ms_b / args.batch_steps,
                         "wall_value": upd_b / wall_b / 1e6},
@@ -218,6 +223,7 @@ def sweep_measure(args):
             st = sim.take_steps(20, prec)
             row[prec] = sim.num_cells * 3.0 * 20 / (st["device_ms"] / 1e3) / 1e6
         row["fused_stage"] = sim.fused_info()["enabled"]
+        row["cell_flux"] = sim.cell_flux_info()["enabled"]
         out[f"{n}^3"] = row
     return out
 
@@ -374,6 +380,7 @@ def run_ours(args, world, rank, local):
     # --- headline: mixed precision, device-resident state
     sim.set_primitives(*ic)
     sim.set_fused({"auto": -1, "on": 1, "off": 0}[args.fused])
+    sim.set_cell_flux({"auto": -1, "on": 1, "off": 0}[args.cell_flux])
     if args.variants:
         r, f, u = (int(x) for x in args.variants.split(","))
         sim.set_launch_variants("mixed", r, f, u)
@@ -381,6 +388,7 @@ def run_ours(args, world, rank, local):
     else:
         tune_mixed = sim.autotune("mixed")
     fused = sim.fused_info()
+    cellf = sim.cell_flux_info()
     sim.take_steps(args.warmup, "mixed")
     barrier()
     with ClockSampler(local) as clk:
@@ -467,7 +475,8 @@ def run_ours(args, world, rank, local):
                          "steps": args.warmup + args.steps},
             "kernel_ms": {k: round(v, 4) for k, v in kt.items()},
             "autotune": {"variants_table": Simulation.launch_variants(), "mixed": tune_mixed, "f64": tune_f64,
-                         "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")}},
+                         "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")},
+                         "cell_flux": {k: cellf[k] for k in ("enabled", "variant", "cell_ms", "generic_ms")}},
             "batch": batch,
             "sweep": sweep,
             "plate": plate,
@@ -481,9 +490,10 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 8 * nc * N,
                     "d2h_bytes_per_step": 8 * nc * N, "steps": e2e_steps},
-            "gpu_launches": (4 if fused["enabled"] else KERNELS_PER_STEP) * args.steps + 2,
+            "gpu_launches": (4 if fused["enabled"] else 7 if cellf["enabled"] else KERNELS_PER_STEP) * args.steps + 2,
             "gpu_launches_note": "kernels of the timed headline call: one graph per step (dt control + 3 fused "
-                                 "stages, or dt control + 3 x recon/face/update), plus the call's local-dt prologue",
+                                 "stages, dt control + 3 x recon/cell-flux update, or dt control + 3 x "
+                                 "recon/face/update), plus the call's local-dt prologue",
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -197,6 +197,12 @@ struct ibisgb_ctx {
     bool fused_on = false;
     cudaGraphExec_t graph_fused[2] = {nullptr, nullptr};
     double fused_ms = 0.0, generic_ms = 0.0;
+    // Per-cell flux path (mixed, inviscid): recon + k_cell_update per stage, on
+    // the same alternating primitive buffers and per-parity graphs as the fused stage.
+    int cell_mode = -1;  // -1 the autotuner decides, 0 off, 1 on
+    bool cell_on = false;
+    int cell_var = 0;
+    double cell_ms = 0.0;
     DBuf tune_save;
     double last_l2[6] = {0, 0, 0, 0, 0, 0};
     double last_ms = 0.0;
@@ -799,6 +805,32 @@ struct ibisgb_ctx {
     }
     void* mixed_prim(int which) { return which ? prim_alt.p : s32.prim.p; }
 
+    bool cell_eligible() const {
+        return rk_configured && !prm.viscous && !prm.cflux && kernels_mixed().cell_update != nullptr;
+    }
+    std::string cell_why() const {
+        if (!rk_configured) return "the solver is not runge_kutta";
+        if (prm.viscous) return "viscous fluxes take the generic kernels";
+        if (prm.cflux) return "constant-flux boundaries take the generic kernels";
+        return "";
+    }
+
+    // one Runge-Kutta step of the per-cell flux path starting from primitive buffer `start`
+    void enqueue_cell_step(int start) {
+        const int S = ctl_host.stages;
+        DevView v = view(IBISGB_MIXED);
+        KernelOps o = ops(IBISGB_MIXED);
+        const bool reco = prm.order == 2;
+        launch_dt_finalize(v.ctl, n_cases, stream);
+        int cur = start;
+        for (int s = 0; s < S; s++) {
+            v.prim = mixed_prim(cur);
+            o.recon(v, prm, reco, var[1][0], stream);
+            o.cell_update(v, prm, reco, s == S - 1 ? 3 : 2, s, s == S - 1, cell_var, mixed_prim(cur ^ 1), stream);
+            cur ^= 1;
+        }
+    }
+
     // one fused Runge-Kutta step starting from primitive buffer `start`
     void enqueue_fused_step(int start) {
         const int S = ctl_host.stages;
@@ -863,13 +895,15 @@ struct ibisgb_ctx {
         ensure_prims(prec);
         int gi = gidx(prec);
         if (!tuned[gi]) autotune(prec);
-        const bool fused = is_mixed(prec) && fused_on;
+        // the fused stage and the per-cell flux path alternate primitive buffers
+        const bool fused = is_mixed(prec) && (fused_on || cell_on);
         if (fused) {
             for (int par = 0; par < 2; par++) {
                 if (graph_fused[par]) continue;
                 cudaGraph_t g;
                 CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-                enqueue_fused_step(par);
+                if (fused_on) enqueue_fused_step(par);
+                else enqueue_cell_step(par);
                 cudaError_t le = cudaGetLastError();
                 CUDA_OK(cudaStreamEndCapture(stream, &g));
                 CUDA_OK(le);
@@ -1343,7 +1377,32 @@ struct ibisgb_ctx {
                     const double again = timed([&] { launch_fused_stage(v, sb, prm, fm, 0, 0, stream); });
                     fused_ms = std::min(fused_ms, again);
                 }
-                fused_on = fused_mode == 1 || (fused_mode == -1 && fused_ms > 0.0 && fused_ms < generic_ms);
+                // the per-cell flux path: recon (as chosen) + k_cell_update in the same mode,
+                // writing the other primitive buffer (the current one stays as it is)
+                cell_ms = 0.0;
+                if (cell_mode != 0 && cell_eligible()) {
+                    prim_alt.alloc(sizeof(float) * 7 * mesh.NT());
+                    void* other = mixed_prim(prim_cur ^ 1);
+                    const int cm = ctl_host.stages > 1 ? 2 : 0;
+                    double best = 0.0;
+                    for (int w = 0; w < kNumVariants; w++) {
+                        double t = timed([&] { o.cell_update(v, prm, reco, cm, 0, 0, w, other, stream); });
+                        if (w == 0 || t < 0.98 * best) { best = t; cell_var = w; }
+                    }
+                    cell_ms = tune_ms[gi][0][vr[0]] + best;
+                }
+                const double generic = generic_ms;
+                bool f_ok = fused_ms > 0.0, c_ok = cell_ms > 0.0;
+                if (fused_mode == 1) {
+                    fused_on = true;
+                    cell_on = false;
+                } else if (cell_mode == 1 && c_ok) {
+                    fused_on = false;
+                    cell_on = true;
+                } else {
+                    fused_on = fused_mode == -1 && f_ok && fused_ms < generic && (!c_ok || fused_ms < cell_ms);
+                    cell_on = !fused_on && cell_mode == -1 && c_ok && cell_ms < generic;
+                }
             }
             CUDA_OK(cudaStreamSynchronize(stream));
             for (auto& e : ev) cudaEventDestroy(e);
@@ -1363,7 +1422,25 @@ struct ibisgb_ctx {
         fused_mode = mode;
         if (mode == 1) upload_fused();
         if (mode >= 0) fused_on = mode == 1;
-        else tuned[1] = false;
+        if (fused_on) cell_on = false;
+        if (mode < 0) tuned[1] = false;
+        drop_mixed_graphs();
+    }
+
+    // per-cell flux path: -1 the autotuner decides, 0 never, 1 always (if eligible)
+    void set_cell_flux(int mode) {
+        if (mode < -1 || mode > 1) throw ArgError("cell flux mode must be -1, 0 or 1");
+        if (mode == 1 && !cell_eligible()) throw ArgError("the per-cell flux path does not apply: " + cell_why());
+        cell_mode = mode;
+        if (mode == 1) {
+            ensure_device();
+            prim_alt.alloc(sizeof(float) * 7 * mesh.NT());
+            cell_on = true;
+            fused_on = false;
+            if (fused_mode == 1) fused_mode = -1;
+        }
+        if (mode == 0) cell_on = false;
+        if (mode < 0) tuned[1] = false;
         drop_mixed_graphs();
     }
 
@@ -1377,6 +1454,10 @@ struct ibisgb_ctx {
         if (graph[gi]) {
             cudaGraphExecDestroy(graph[gi]);
             graph[gi] = nullptr;
+        }
+        if (is_mixed(prec)) {
+            cell_var = w[2];  // the per-cell flux kernel takes the update's variant
+            drop_mixed_graphs();
         }
     }
 
@@ -1973,6 +2054,22 @@ int ibisgb_fused_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, doub
         if (reason && reason_len > 0) {
             std::snprintf(reason, (size_t)reason_len, "%s", ctx->fused_why.c_str());
         }
+    });
+}
+
+int ibisgb_set_cell_flux(ibisgb_ctx* ctx, int32_t mode) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->set_cell_flux(mode); });
+}
+
+int ibisgb_cell_flux_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, int32_t* variant,
+                          double* times_ms) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (eligible) *eligible = ctx->cell_eligible() ? 1 : 0;
+        if (enabled) *enabled = ctx->cell_on ? 1 : 0;
+        if (variant) *variant = ctx->cell_var;
+        if (times_ms) { times_ms[0] = ctx->cell_ms; times_ms[1] = ctx->generic_ms; }
     });
 }
 

@@ -158,6 +158,11 @@ struct KernelOps {
     void (*local_dt)(const DevView&, const FvParams&, cudaStream_t);
     // U += sum_j b(j) dt k_j, primitives and ghosts (single-stage tableaus)
     void (*finalize)(const DevView&, const FvParams&, cudaStream_t);
+    // mixed build only (else null): face_flux + update of an inviscid Runge-Kutta
+    // stage (mode 2 or 3) in one kernel that recomputes each cell's face fluxes;
+    // the new primitives go to prim_out (not the buffer the view reads)
+    void (*cell_update)(const DevView&, const FvParams&, bool reconstruct, int mode, int stage, int with_dt,
+                        int variant, void* prim_out, cudaStream_t);
 };
 
 KernelOps kernels_f64();

@@ -520,11 +520,14 @@ __device__ __forceinline__ void viscous_face(const FvParams& prm, const Gas<R>& 
     out[3] = nx * thx + ny * thy + nz * thz;
 }
 
-template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
-__global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int reconstruct) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= v.F) return;
-    const int N = v.N, NT = v.NT, F = v.F, G = v.G;
+// The convective flux of face f in the global frame (after the post-convective
+// flux actions): reconstruction of both sides, thermo closure, flux calculator.
+// Also returns the face normal.  Shared by k_face and the per-cell flux path,
+// so that both produce the same bits.
+template <class R, class P, class Gm, int DIM, bool EXACT>
+__device__ __forceinline__ void face_convective(const DevView& v, const FvParams& prm, int f, int reconstruct,
+                                                R (&Fg)[5], R& nx_out, R& ny_out, R& nz_out) {
+    const int N = v.N, NT = v.NT, F = v.F;
     const Gm* fg = (const Gm*)v.face;
     const Gm* cc = (const Gm*)v.cc;
     const P* pr = (const P*)v.prim;
@@ -602,18 +605,32 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
         side_state<R, DIM, EXACT>(prm.thermo, gm, reconstruct, q, nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z,
                                   S[side]);
     }
-    R Fg[5];
     convective_flux<R, DIM, EXACT>(prm, gm, S[0], S[1], nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z, Fg);
     if (prm.cflux) {  // apply_post_convective_flux_bc (finite_volume.cpp:71, 197-209)
         if (const BoundDev* B = constant_flux_bound(v, cells[0], cells[1]))
             constant_flux<R, DIM>(B->cfs, prm.Cv, nx, ny, nz, Fg);
     }
+    nx_out = nx;
+    ny_out = ny;
+    nz_out = nz;
+}
+
+template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
+__global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int reconstruct) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.F) return;
+    const int N = v.N, NT = v.NT, F = v.F, G = v.G;
+    R Fg[5], nx, ny, nz;
+    face_convective<R, P, Gm, DIM, EXACT>(v, prm, f, reconstruct, Fg, nx, ny, nz);
     R mx = Fg[1], my = Fg[2], mz = Fg[3];
     R en = Fg[4];
 
     if (prm.viscous) {
         // viscous_flux.cpp:130-232; the states and gradients of both sides, then viscous_face
-        const int l = cells[0], r = cells[1];
+        const Gm* cc = (const Gm*)v.cc;
+        const P* pr = (const P*)v.prim;
+        const Gas<R> gm(prm);
+        const int l = v.left[f], r = v.right[f];
         const bool lv = l < N, rv = r < N;
         const P* vgd = (const P*)v.vgrad;
         const P* vgh = (const P*)v.vghost;
@@ -783,6 +800,15 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
     lo = __fadd_rn(lo, err);
 }
 
+// hi + lo += x * a, keeping the product's rounding error (an FMA gives it exactly)
+// and the addition's (TwoSum).
+__device__ __forceinline__ void pair_acc(float& hi, float& lo, float x, float a) {
+    const float pr = __fmul_rn(x, a);
+    const float pe = __fmaf_rn(x, a, -pr);
+    two_sum_acc(hi, lo, pr);
+    lo = __fadd_rn(lo, pe);
+}
+
 // Local CFL time step of valid cell i from its primitives (FiniteVolume::estimate_dt,
 // finite_volume.cpp:130-184).  The float build evaluates the inviscid signal in
 // float from its float state.
@@ -950,13 +976,7 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
             const int f = v.cell_face[s * N + i];
             const float a = -(float)area[f] * (float)v.outsign[s * N + i];
 #pragma unroll
-            for (int q = 0; q < NC; q++) {
-                const float x = (float)fl[q * F + f];
-                const float pr = __fmul_rn(x, a);
-                const float pe = __fmaf_rn(x, a, -pr);  // exact error of the product
-                two_sum_acc(hi[q], lo[q], pr);
-                lo[q] = __fadd_rn(lo[q], pe);
-            }
+            for (int q = 0; q < NC; q++) pair_acc(hi[q], lo[q], (float)fl[q * F + f], a);
         }
         iv = v.inv_vol[i];
         if (!fold) {
@@ -1000,6 +1020,64 @@ __global__ void __launch_bounds__(BS, MINB) k_update(DevView v, FvParams prm, in
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double local = 1.0e308 * 10.0;
     if (i < v.N) local = update_cell<P, Gm, DIM, EXACT>(v, prm, i, mode, stage, out_rm, with_dt);
+    if (with_dt) reduce_local_dt(v, i, local);
+}
+
+// Mixed build, inviscid Runge-Kutta stages: the face fluxes are recomputed by
+// each cell that needs them (an interior face twice) and summed straight into
+// the update, instead of being written by k_face and gathered by k_update.  The
+// flux of every face is formed by the same function as k_face's, so the result
+// is the same bits as k_face + k_update.  Trades the flux array's write and
+// gather and one launch for twice the flux arithmetic, which runs on the FP32
+// pipe beside the update's FP64 work.  Cells read their neighbours' primitives
+// while others commit new ones, so the new primitives (and ghosts) go to the
+// other buffer, prim_out.
+template <int DIM, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_cell_update(DevView v, FvParams prm, int reconstruct, int mode,
+                                                        int stage, int with_dt, float* prim_out) {
+    constexpr int NC = DIM + 2;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double local = 1.0e308 * 10.0;
+    if (i < v.N) {
+        const int N = v.N, F = v.F;
+        const float* area = (const float*)v.face + 12 * F;
+        const int nf = v.nfaces[i];
+        float hi[NC], lo[NC];
+#pragma unroll
+        for (int q = 0; q < NC; q++) { hi[q] = 0.f; lo[q] = 0.f; }
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            float Fg[5], nx, ny, nz;
+            face_convective<float, float, float, DIM, false>(v, prm, f, reconstruct, Fg, nx, ny, nz);
+            const float a = -area[f] * (float)v.outsign[s * N + i];
+#pragma unroll
+            for (int q = 0; q < NC; q++) pair_acc(hi[q], lo[q], Fg[q < DIM + 1 ? q : 4], a);
+        }
+        const double iv = v.inv_vol[i];
+        double ks[NC];
+        const bool fold = mode == 3 && stage > 0;
+        if (!fold) {
+            double* kk = v.k + (size_t)stage * NC * N;
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                ks[q] = (f2d(hi[q]) + f2d(lo[q])) * iv;
+                kk[q * N + i] = ks[q];
+            }
+        }
+        DevView vo = v;
+        vo.prim = prim_out;
+        local = update_tail<float, float, DIM, false>(vo, prm, i, mode, stage, with_dt, ks, fold, hi, lo, iv);
+        if (ctl_of(v, i)->halt) {
+            // a halted case keeps its state: carry its primitives into the other buffer
+            const float* pr = (const float*)v.prim;
+            const int NT = v.NT;
+            for (int q = 0; q < 7; q++) prim_out[q * NT + i] = pr[q * NT + i];
+            for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++) {
+                const int id = N + v.feed_ghost[k];
+                for (int q = 0; q < 7; q++) prim_out[q * NT + id] = pr[q * NT + id];
+            }
+        }
+    }
     if (with_dt) reduce_local_dt(v, i, local);
 }
 
@@ -1145,6 +1223,28 @@ struct Launch {
             }
         }
     }
+    template <int V>
+    static void cell_update_v(const DevView& v, const FvParams& p, bool reco, int mode, int stage, int with_dt,
+                              void* po, cudaStream_t s) {
+        constexpr int BS = kVariantThreads[V], MB = kVariantMinBlocks[V];
+        const unsigned g = (unsigned)((v.N + BS - 1) / BS);
+        float* out = (float*)po;
+        if (v.dim == 3) k_cell_update<3, BS, MB><<<g, BS, 0, s>>>(v, p, reco, mode, stage, with_dt, out);
+        else k_cell_update<2, BS, MB><<<g, BS, 0, s>>>(v, p, reco, mode, stage, with_dt, out);
+    }
+    // the mixed build's per-cell flux + update (inviscid Runge-Kutta stages, mode 2 or 3)
+    static void cell_update(const DevView& v, const FvParams& p, bool reco, int mode, int stage, int with_dt,
+                            int var, void* prim_out, cudaStream_t s) {
+        if constexpr (sizeof(P) == sizeof(float) && !EXACT) {
+            switch (var) {
+                case 1: cell_update_v<1>(v, p, reco, mode, stage, with_dt, prim_out, s); break;
+                case 2: cell_update_v<2>(v, p, reco, mode, stage, with_dt, prim_out, s); break;
+                case 3: cell_update_v<3>(v, p, reco, mode, stage, with_dt, prim_out, s); break;
+                case 4: cell_update_v<4>(v, p, reco, mode, stage, with_dt, prim_out, s); break;
+                default: cell_update_v<0>(v, p, reco, mode, stage, with_dt, prim_out, s); break;
+            }
+        }
+    }
     static void combine(const DevView& v, const FvParams& p, int stage, cudaStream_t s) {
         if (v.dim == 3) k_combine<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
         else k_combine<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, stage);
@@ -1163,7 +1263,7 @@ struct Launch {
     }
     static KernelOps ops() {
         return KernelOps{&ghost_fill, &recon, &face_flux, &update, &combine, &prims_from_U, &local_dt,
-                         &finalize};
+                         &finalize, sizeof(P) == sizeof(float) && !EXACT ? &cell_update : nullptr};
     }
 };
 

@@ -190,6 +190,17 @@ class Simulation:
         return {"eligible": bool(el.value), "enabled": bool(en.value), "fused_ms": t[0], "generic_ms": t[1],
                 "reason": why.value.decode()}
 
+    def set_cell_flux(self, mode: int) -> None:
+        """Per-cell flux path of the mixed build: -1 autotuner decides, 0 off, 1 on."""
+        self._call("ibisgb_set_cell_flux", int(mode))
+
+    def cell_flux_info(self) -> dict:
+        el, en, w = C.c_int32(), C.c_int32(), C.c_int32()
+        t = np.zeros(2)
+        self._call("ibisgb_cell_flux_info", C.byref(el), C.byref(en), C.byref(w), _ptr(t))
+        return {"eligible": bool(el.value), "enabled": bool(en.value), "variant": w.value, "cell_ms": t[0],
+                "generic_ms": t[1]}
+
     # ------------------------------------------------------------- residual
     def compute_dudt(self, precision: str = "f64") -> np.ndarray:
         """dU/dt of the valid cells, (N, n_conserved) in the reference's cell order."""

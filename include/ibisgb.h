@@ -284,7 +284,8 @@ int ibisgb_synchronize(ibisgb_ctx* ctx);
  * variant 0. */
 int ibisgb_autotune(ibisgb_ctx* ctx, int32_t precision, int32_t variants[3], double* times_ms);
 
-/* Fix the launch variants (recon, face, update) of a precision instead of tuning. */
+/* Fix the launch variants (recon, face, update) of a precision instead of tuning.
+ * For MIXED the update's variant also applies to the per-cell flux kernel. */
 int ibisgb_set_launch_variants(ibisgb_ctx* ctx, int32_t precision, const int32_t variants[3]);
 
 /* The variant table: count, and per variant the threads per block and minimum
@@ -310,6 +311,24 @@ int ibisgb_set_fused(ibisgb_ctx* ctx, int32_t mode);
  * into reason, at most reason_len bytes with the terminating zero). */
 int ibisgb_fused_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, double* times_ms, char* reason,
                       int32_t reason_len);
+
+/* Per-cell flux path of the MIXED build (inviscid Runge-Kutta stages without
+ * constant-flux boundaries; any grid).  Each stage runs the gradient kernel and
+ * then one kernel in which every cell recomputes the convective fluxes of its
+ * faces and applies the surface integral and the stage update, instead of a
+ * face-flux kernel that stores the fluxes and an update kernel that gathers
+ * them.  Results are bit-identical to the three-kernel stage.  mode -1 (the
+ * default) lets ibisgb_autotune / the first ibisgb_rk_run choose among the
+ * three-kernel stage, this path and the fused stage by their timings; 0 never
+ * uses it; 1 always does (IBISGB_ERR_ARG if the scheme does not qualify).  A
+ * scheduling choice with no counterpart in ibis. */
+int ibisgb_set_cell_flux(ibisgb_ctx* ctx, int32_t mode);
+
+/* Whether the per-cell flux path applies and is in use, its launch variant (an
+ * index into ibisgb_launch_variants) and the last tuning times of one stage
+ * (ms: per-cell flux path, best three-kernel stage; 2 doubles, may be NULL). */
+int ibisgb_cell_flux_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, int32_t* variant,
+                          double* times_ms);
 
 /* Self-check of the mixed build's float -> double conversion, which runs on the
  * integer pipe (GB300's FP64 pipe is its scarcest unit): compares it bit for

@@ -63,7 +63,8 @@ def case(name, **kw):
         top = grids.flow_state(gas, 300.0, 1e5, 505.0, -15.0)
         b = {"west": grids.boundary_layer_inflow(h, u, T, 1e5), "east": grids.supersonic_outflow(),
              "south": grids.adiabatic_no_slip_wall(), "north": grids.constant_flux(top)}
-        c = grids.make_config(2, b, gas=gas, viscous=True, **kw)
+        kw.setdefault("viscous", True)
+        c = grids.make_config(2, b, gas=gas, **kw)
         return g, c, random_state(g.num_cells, 300.0, 1e5, 450.0, 2, seed=7, amp=0.04)
     if name == "cflux_ramp":  # the ramp with a constant-flux inflow (vy != 0: the vy n.x term counts)
         g, c, inf = grids.ramp_case(kw.pop("ni", 24), kw.pop("nj", 12), **kw)
