@@ -294,6 +294,9 @@ struct ibisgb_ctx {
         for (int i = 1; i < c.stages; i++) {
             auto row = rows.at(i - 1).as_doubles();
             for (int j = 0; j < i && j < (int)row.size(); j++) c.a[i][j] = row[j];
+            // the stage combinations skip a(i, j) < 1e-14 (runge_kutta.cpp:161-168)
+            for (int j = 0; j < i; j++)
+                if (!(c.a[i][j] < 1e-14)) c.a_used[i] |= 1u << j;
         }
         for (int i = 0; i < c.stages; i++) c.b[i] = b[i];
         const Json& cfl = sc.at("cfl");  // make_cfl_schedule, cfl.cpp:157-169

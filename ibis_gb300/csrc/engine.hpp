@@ -74,6 +74,7 @@ struct StepCtl {
     double cfl_t[16], cfl_v[16];
     int stages;
     double a[kMaxStages][kMaxStages];  // tableau a(i, j), row i = stage i (>= 1)
+    unsigned a_used[kMaxStages];       // bit j of row i: a(i, j) >= 1e-14 (the terms the stages add)
     double b[kMaxStages];
     double ca[kMaxStages][kMaxStages];  // a(i, j) * dt of the current step
     double cb[kMaxStages];              // b(i) * dt

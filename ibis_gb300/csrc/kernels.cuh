@@ -689,18 +689,34 @@ __device__ __forceinline__ double recip_newton(double x) {
     return fma(r, e, r);
 }
 
-// float -> double by assembling the bit pattern on the integer pipe (exact: a
-// double holds every float; zero, infinities and NaN keep their form, subnormal
-// floats take the conversion instruction), which keeps the conversions of the
-// mixed update off GB300's narrow FP64 pipe.
+// float -> double and double -> float (round to nearest even) by assembling the
+// bit patterns on the integer pipe.  The conversion instructions run on GB300's
+// narrow FP64 pipe, the mixed update's bottleneck.  Only the rare inputs --
+// subnormal floats; doubles outside the normal float range, infinities, NaN --
+// take the instruction, in a function that is called, not inlined, so that no
+// predicated conversion is issued for the common case.  Results are bit for bit
+// the instructions' under this build's flags (checked by ibisgb_check_conversions).
+__device__ __noinline__ double f2d_by_instruction(float x) { return (double)x; }
+__device__ __noinline__ float d2f_by_instruction(double x) { return __double2float_rn(x); }
+
 __device__ __forceinline__ double f2d(float x) {
     const unsigned u = __float_as_uint(x);
     const unsigned ex = (u >> 23) & 0xFFu;
-    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-    const unsigned long long man = (unsigned long long)(u & 0x7FFFFFu) << 29;
-    if (ex == 0) return (u & 0x7FFFFFu) ? (double)x : __longlong_as_double((long long)sign);
-    const unsigned long long e11 = ex == 0xFFu ? 0x7FFull : (unsigned long long)(ex + 896u);
-    return __longlong_as_double((long long)(sign | (e11 << 52) | man));
+    const unsigned man = u & 0x7FFFFFu;
+    if (ex == 0u && man != 0u) return f2d_by_instruction(x);
+    const unsigned e11 = ex == 0xFFu ? 0x7FFu : (ex == 0u ? 0u : ex + 896u);
+    return __hiloint2double((int)((u & 0x80000000u) | (e11 << 20) | (man >> 3)), (int)(man << 29));
+}
+
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ex = (hi >> 20) & 0x7FFu;
+    if (ex - 897u > 253u) return d2f_by_instruction(x);  // float exponent outside 1..254
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // the 23 kept significand bits
+    const unsigned rem = lo & 0x1FFFFFFFu;                   // the 29 dropped ones
+    const unsigned up = (rem > 0x10000000u) | ((rem == 0x10000000u) & m);
+    // a carry out of the significand moves to the next binade (to infinity above the largest float)
+    return __uint_as_float(((hi & 0x80000000u) | ((ex - 896u) << 23)) + m + up);
 }
 
 // What the update needs of a committed state: rho (bad-cell test) and the
@@ -720,16 +736,16 @@ __device__ Committed<P> commit_state(const DevView& v, const FvParams& prm, int 
         // Mixed build: rho, v and e = E/rho - |v|^2/2 in double (the cancellation of
         // strong expansions happens there); T = e/Cv and p = rho R T are products of
         // values already rounded to float, so they are formed in float.
-        const double ir = rho > 0.0 ? recip_newton(rho) : 1.0 / rho;
+        const double ir = recip_newton(rho);  // a state with rho <= 0 is a bad cell either way
         vx = u[1] * ir;
         vy = u[2] * ir;
         vz = DIM == 3 ? u[3] * ir : 0.0;
         double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
         e = u[DIM + 1] * ir - ke;
-        const float rf = (float)rho, ef = (float)e;
+        const float rf = d2f(rho), ef = d2f(e);
         const float Tf = ef * prm.finv_Cv;
         const float pf = rf * prm.fR * Tf;
-        const float vxf = (float)vx, vyf = (float)vy, vzf = (float)vz;
+        const float vxf = d2f(vx), vyf = d2f(vy), vzf = DIM == 3 ? d2f(vz) : 0.f;
         P* pr = (P*)v.prim;
         const int NT = v.NT;
         pr[i] = (P)rf; pr[NT + i] = (P)pf; pr[2 * NT + i] = (P)Tf; pr[3 * NT + i] = (P)ef;
@@ -834,7 +850,7 @@ __device__ double cell_local_dt(const DevView& v, const FvParams& prm, int i, P 
         }
         if (!prm.viscous) {
             // the float build's inviscid signal is a float; so is its quotient
-            const float lf = __fdiv_rn((float)vol, sf);
+            const float lf = __fdiv_rn(d2f(vol), sf);
             return lf > 0.f ? f2d(lf) : 1.0e308 * 10.0;
         }
         src = f2d(sf);
@@ -910,7 +926,7 @@ __device__ __forceinline__ double update_tail(const DevView& v, const FvParams& 
 #pragma unroll
         for (int q = 0; q < NC; q++) u[q] = u[q] + (stage == 0 ? ks[q] : v.k[q * N + i]) * ctl->ca[ns][0];
         for (int j = 1; j < ns; j++) {
-            if (ctl->a[ns][j] < 1e-14) continue;
+            if (!((ctl->a_used[ns] >> j) & 1u)) continue;
             const double c = ctl->ca[ns][j];
 #pragma unroll
             for (int q = 0; q < NC; q++) {
@@ -1117,7 +1133,7 @@ __global__ void __launch_bounds__(kBlock) k_combine(DevView v, FvParams prm, int
 #pragma unroll
     for (int q = 0; q < NC; q++) u[q] = v.U[q * N + i] + v.k[q * N + i] * ctl->ca[stage][0];
     for (int j = 1; j < stage; j++) {
-        if (ctl->a[stage][j] < 1e-14) continue;
+        if (!((ctl->a_used[stage] >> j) & 1u)) continue;
         const double c = ctl->ca[stage][j];
 #pragma unroll
         for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;

@@ -33,6 +33,16 @@ __global__ void k_check_conversions(long long n, unsigned long long seed, unsign
         const double c = k_mixed::f2d(x), e = (double)x;
         const bool same_d = __double_as_longlong(c) == __double_as_longlong(e) || (c != c && e != e);
         if (!same_d) atomicAdd(bad, 1ull);
+        // double -> float on doubles of three kinds: any bit pattern; exponents around
+        // the float range (subnormal results, overflow); exact ties between two floats
+        const unsigned long long r2 = splitmix64(r ^ 0x5DEECE66Dull);
+        unsigned long long bits = r2;
+        if (t % 3 == 1) bits = (r2 & 0x800FFFFFFFFFFFFFull) | ((unsigned long long)(860 + (r % 330)) << 52);
+        if (t % 3 == 2)
+            bits = (r2 & 0x800FFFFFE0000000ull) | 0x10000000ull | ((unsigned long long)(897 + (r % 254)) << 52);
+        const double d = __longlong_as_double((long long)bits);
+        const float g = k_mixed::d2f(d), h = __double2float_rn(d);
+        if (!(__float_as_uint(g) == __float_as_uint(h) || (g != g && h != h))) atomicAdd(bad, 1ull);
     }
 }
 }  // namespace

@@ -330,10 +330,12 @@ int ibisgb_set_cell_flux(ibisgb_ctx* ctx, int32_t mode);
 int ibisgb_cell_flux_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, int32_t* variant,
                           double* times_ms);
 
-/* Self-check of the mixed build's float -> double conversion, which runs on the
- * integer pipe (GB300's FP64 pipe is its scarcest unit): compares it bit for
- * bit with the conversion instruction on `samples` pseudo-random float bit
- * patterns (seeded), on the current device.  No counterpart in the reference. */
+/* Self-check of the mixed build's float -> double and double -> float
+ * conversions, which run on the integer pipe (GB300's FP64 pipe is its scarcest
+ * unit): compares them bit for bit with the conversion instructions on `samples`
+ * pseudo-random float bit patterns and as many doubles (any bit pattern,
+ * exponents around the float range, exact rounding ties), seeded, on the current
+ * device.  No counterpart in the reference. */
 int ibisgb_check_conversions(int64_t samples, uint64_t seed, int64_t* mismatches);
 
 /* Batched ensembles (no counterpart in the reference, which runs one case per
