@@ -385,6 +385,9 @@ struct ibisgb_ctx {
         std::vector<BoundarySpec> specs = boundary_specs();
         build_mesh(in, specs, prm.viscous || prm.order > 1, mesh);
         check_index_range();
+        // the fast kernels visit at most 6 face slots per cell in 3-D, 4 in 2-D (the
+        // most faces of any element type the reference reads)
+        if (mesh.MF > (in.dim == 3 ? 6 : 4)) throw ConfigError("a cell has more faces than any supported element");
         // every face needs two sides (boundaries without ghost cells are not supported)
         for (int64_t f = 0; f < mesh.F; f++)
             if (mesh.left[f] < 0 || mesh.right[f] < 0)

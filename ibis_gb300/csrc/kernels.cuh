@@ -54,6 +54,44 @@ IBISGB_HD double real_of(float x) { return (double)x; }
 // primitive index of viscous variable q (0 T, 1 vx, 2 vy, 3 vz)
 IBISGB_HD int visc_prim(int q) { return q == 0 ? 2 : 3 + q; }
 
+// float -> double and double -> float (round to nearest even) by assembling the
+// bit patterns on the integer pipe.  The conversion instructions run on GB300's
+// narrow FP64 pipe, the mixed update's bottleneck.  Only the rare inputs --
+// subnormal floats; doubles outside the normal float range, infinities, NaN --
+// take the instruction, in a function that is called, not inlined, so that no
+// predicated conversion is issued for the common case.  Results are bit for bit
+// the instructions' under this build's flags (checked by ibisgb_check_conversions).
+__device__ __noinline__ double f2d_by_instruction(float x) { return (double)x; }
+__device__ __noinline__ float d2f_by_instruction(double x) { return __double2float_rn(x); }
+
+__device__ __forceinline__ double f2d(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    const unsigned man = u & 0x7FFFFFu;
+    if (ex == 0u && man != 0u) return f2d_by_instruction(x);
+    const unsigned e11 = ex == 0xFFu ? 0x7FFu : (ex == 0u ? 0u : ex + 896u);
+    return __hiloint2double((int)((u & 0x80000000u) | (e11 << 20) | (man >> 3)), (int)(man << 29));
+}
+
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ex = (hi >> 20) & 0x7FFu;
+    if (ex - 897u > 253u) return d2f_by_instruction(x);  // float exponent outside 1..254
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // the 23 kept significand bits
+    const unsigned rem = lo & 0x1FFFFFFFu;                   // the 29 dropped ones
+    const unsigned up = (rem > 0x10000000u) | ((rem == 0x10000000u) & m);
+    // a carry out of the significand moves to the next binade (to infinity above the largest float)
+    return __uint_as_float(((hi & 0x80000000u) | ((ex - 896u) << 23)) + m + up);
+}
+
+// A value in the storage type P of the state arrays: for the float build the
+// integer-pipe conversion (bit for bit the instruction's), else a cast.
+template <class P, class S>
+__device__ __forceinline__ P to_storage(S x) {
+    if constexpr (sizeof(P) == sizeof(float) && sizeof(S) == sizeof(double) && !kIsDual<S>) return d2f(x);
+    else return (P)x;
+}
+
 // ---------------------------------------------------------------------------
 // Ghost-cell actions on one ghost (boundary.cpp:9-400), in double.
 // ---------------------------------------------------------------------------
@@ -148,13 +186,14 @@ __device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const S
     apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm, v.gfix, v.G, g);
     P* pr = (P*)v.prim;
     const int NT = v.NT, id = v.N + g;
-    pr[id] = (P)gh.rho; pr[NT + id] = (P)gh.p; pr[2 * NT + id] = (P)gh.T; pr[3 * NT + id] = (P)gh.e;
-    pr[4 * NT + id] = (P)gh.vx; pr[5 * NT + id] = (P)gh.vy; pr[6 * NT + id] = (P)gh.vz;
+    pr[id] = to_storage<P>(gh.rho); pr[NT + id] = to_storage<P>(gh.p); pr[2 * NT + id] = to_storage<P>(gh.T);
+    pr[3 * NT + id] = to_storage<P>(gh.e); pr[4 * NT + id] = to_storage<P>(gh.vx);
+    pr[5 * NT + id] = to_storage<P>(gh.vy); pr[6 * NT + id] = to_storage<P>(gh.vz);
     if (prm.viscous) {
         apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm, v.gfix, v.G, g);
         P* vg = (P*)v.vghost;
-        vg[g] = (P)gh.p; vg[v.G + g] = (P)gh.T; vg[2 * v.G + g] = (P)gh.vx;
-        vg[3 * v.G + g] = (P)gh.vy; vg[4 * v.G + g] = (P)gh.vz;
+        vg[g] = to_storage<P>(gh.p); vg[v.G + g] = to_storage<P>(gh.T); vg[2 * v.G + g] = to_storage<P>(gh.vx);
+        vg[3 * v.G + g] = to_storage<P>(gh.vy); vg[4 * v.G + g] = to_storage<P>(gh.vz);
     }
 }
 
@@ -229,8 +268,7 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
     const int nf = v.nfaces[i];
     const Gm* W = (const Gm*)v.lsqw;
     const int MF = v.MF;
-    for (int s = 0; s < nf; s++) {
-        const int nb = v.cell_nbr[s * N + i];
+    auto slot = [&](int s, int nb) {
         R w1, w2, w3;
         if (!EXACT) {  // weights precomputed on the host from the same formulas
             w1 = (R)W[s * N + i];
@@ -268,7 +306,8 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                 if (DIM == 3) hz[q] += w3 * du;
             }
         }
-    }
+    };
+    for (int s = 0; s < nf; s++) slot(s, v.cell_nbr[s * N + i]);
 
     if (reconstruct) {
         P* gout = (P*)v.grad;
@@ -689,34 +728,23 @@ __device__ __forceinline__ double recip_newton(double x) {
     return fma(r, e, r);
 }
 
-// float -> double and double -> float (round to nearest even) by assembling the
-// bit patterns on the integer pipe.  The conversion instructions run on GB300's
-// narrow FP64 pipe, the mixed update's bottleneck.  Only the rare inputs --
-// subnormal floats; doubles outside the normal float range, infinities, NaN --
-// take the instruction, in a function that is called, not inlined, so that no
-// predicated conversion is issued for the common case.  Results are bit for bit
-// the instructions' under this build's flags (checked by ibisgb_check_conversions).
-__device__ __noinline__ double f2d_by_instruction(float x) { return (double)x; }
-__device__ __noinline__ float d2f_by_instruction(double x) { return __double2float_rn(x); }
+// 1/x in double from a float reciprocal seed (the float pipe's MUFU, not the
+// FP64 pipe's) and two Newton steps: the seed's 2^-23 relative error becomes
+// 2^-46, then below double rounding.  Inputs whose value or reciprocal is not
+// a normal float take the double seed, in a call (not inlined, so that its
+// instructions are not issued predicated for the common case).
+__device__ __noinline__ double recip_by_double_seed(double x) { return recip_newton(x); }
 
-__device__ __forceinline__ double f2d(float x) {
-    const unsigned u = __float_as_uint(x);
-    const unsigned ex = (u >> 23) & 0xFFu;
-    const unsigned man = u & 0x7FFFFFu;
-    if (ex == 0u && man != 0u) return f2d_by_instruction(x);
-    const unsigned e11 = ex == 0xFFu ? 0x7FFu : (ex == 0u ? 0u : ex + 896u);
-    return __hiloint2double((int)((u & 0x80000000u) | (e11 << 20) | (man >> 3)), (int)(man << 29));
-}
-
-__device__ __forceinline__ float d2f(double x) {
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const unsigned ex = (hi >> 20) & 0x7FFu;
-    if (ex - 897u > 253u) return d2f_by_instruction(x);  // float exponent outside 1..254
-    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // the 23 kept significand bits
-    const unsigned rem = lo & 0x1FFFFFFFu;                   // the 29 dropped ones
-    const unsigned up = (rem > 0x10000000u) | ((rem == 0x10000000u) & m);
-    // a carry out of the significand moves to the next binade (to infinity above the largest float)
-    return __uint_as_float(((hi & 0x80000000u) | ((ex - 896u) << 23)) + m + up);
+__device__ __forceinline__ double recip_newton_fseed(double x) {
+    const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7FFu;
+    if (ex - 897u > 251u) return recip_by_double_seed(x);  // |x| outside [2^-126, 2^126)
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(d2f(x)));
+    double r = f2d(rf);
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
 }
 
 // What the update needs of a committed state: rho (bad-cell test) and the
@@ -736,7 +764,7 @@ __device__ Committed<P> commit_state(const DevView& v, const FvParams& prm, int 
         // Mixed build: rho, v and e = E/rho - |v|^2/2 in double (the cancellation of
         // strong expansions happens there); T = e/Cv and p = rho R T are products of
         // values already rounded to float, so they are formed in float.
-        const double ir = recip_newton(rho);  // a state with rho <= 0 is a bad cell either way
+        const double ir = recip_newton_fseed(rho);  // a state with rho <= 0 is a bad cell either way
         vx = u[1] * ir;
         vy = u[2] * ir;
         vz = DIM == 3 ? u[3] * ir : 0.0;
@@ -907,13 +935,17 @@ __device__ void reduce_local_dt(const DevView& v, int i, double local) {
 // of `mode`, the primitives and ghosts of the new state (into v.prim) and, with
 // with_dt, the new state's local time step.  ks holds the stage derivative, or,
 // when fold, the mixed build's float pair (hi + lo) * iv stands for it.
-template <class P, class Gm, int DIM, bool EXACT>
-__device__ __forceinline__ double update_tail(const DevView& v, const FvParams& prm, int i, int mode, int stage,
+// MODE >= 0 fixes the mode at compile time (the mixed build's Runge-Kutta
+// launches), so that the other modes' double arithmetic is not issued,
+// predicated off, to the FP64 pipe; MODE = -1 takes the `mode` argument.
+template <class P, class Gm, int DIM, bool EXACT, int MODE = -1>
+__device__ __forceinline__ double update_tail(const DevView& v, const FvParams& prm, int i, int mode_arg, int stage,
                                               int with_dt, const double* ks, bool fold, const float* hi,
                                               const float* lo, double iv) {
     constexpr double kInf = 1.0e308 * 10.0;
     constexpr int NC = DIM + 2;
     const int N = v.N;
+    const int mode = MODE >= 0 ? MODE : mode_arg;
     if (mode < 2) return kInf;
     StepCtl* ctl = ctl_of(v, i);
     if (ctl->halt) return kInf;
@@ -968,10 +1000,11 @@ __device__ __forceinline__ double update_tail(const DevView& v, const FvParams& 
 
 // One valid cell of k_update; returns the local time step of the new state when
 // with_dt (mode 3), else +inf.
-template <class P, class Gm, int DIM, bool EXACT>
-__device__ __forceinline__ double update_cell(const DevView& v, const FvParams& prm, int i, int mode, int stage,
+template <class P, class Gm, int DIM, bool EXACT, int MODE = -1>
+__device__ __forceinline__ double update_cell(const DevView& v, const FvParams& prm, int i, int mode_arg, int stage,
                                               double* out_rm, int with_dt) {
     constexpr int NC = DIM + 2;
+    const int mode = MODE >= 0 ? MODE : mode_arg;
     const int N = v.N, F = v.F;
     const Gm* area = (const Gm*)v.face + 12 * F;
     const P* fl = (const P*)v.flux;
@@ -1027,15 +1060,15 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
             if (out_rm) out_rm[(size_t)i * NC + q] = ks[q];
         }
     }
-    return update_tail<P, Gm, DIM, EXACT>(v, prm, i, mode, stage, with_dt, ks, fold, hi, lo, iv);
+    return update_tail<P, Gm, DIM, EXACT, MODE>(v, prm, i, mode, stage, with_dt, ks, fold, hi, lo, iv);
 }
 
-template <class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
+template <class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1, int MODE = -1>
 __global__ void __launch_bounds__(BS, MINB) k_update(DevView v, FvParams prm, int mode, int stage,
                                                    double* out_rm, int with_dt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double local = 1.0e308 * 10.0;
-    if (i < v.N) local = update_cell<P, Gm, DIM, EXACT>(v, prm, i, mode, stage, out_rm, with_dt);
+    if (i < v.N) local = update_cell<P, Gm, DIM, EXACT, MODE>(v, prm, i, mode, stage, out_rm, with_dt);
     if (with_dt) reduce_local_dt(v, i, local);
 }
 
@@ -1190,13 +1223,22 @@ struct Launch {
         if (v.dim == 3) k_face<R, P, Gm, 3, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
         else k_face<R, P, Gm, 2, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
     }
+    template <int V, int MODE>
+    static void update_vm(const DevView& v, const FvParams& p, int mode, int stage, double* out, int with_dt,
+                          cudaStream_t s) {
+        constexpr int BS = kVariantThreads[V], MB = kVariantMinBlocks[V];
+        const unsigned g = (unsigned)((v.N + BS - 1) / BS);
+        if (v.dim == 3) k_update<P, Gm, 3, EXACT, BS, MB, MODE><<<g, BS, 0, s>>>(v, p, mode, stage, out, with_dt);
+        else k_update<P, Gm, 2, EXACT, BS, MB, MODE><<<g, BS, 0, s>>>(v, p, mode, stage, out, with_dt);
+    }
     template <int V>
     static void update_v(const DevView& v, const FvParams& p, int mode, int stage, double* out, int with_dt,
                          cudaStream_t s) {
-        constexpr int BS = kVariantThreads[V], MB = kVariantMinBlocks[V];
-        const unsigned g = (unsigned)((v.N + BS - 1) / BS);
-        if (v.dim == 3) k_update<P, Gm, 3, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, mode, stage, out, with_dt);
-        else k_update<P, Gm, 2, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, mode, stage, out, with_dt);
+        // the mixed build's Runge-Kutta modes get their own instances (see update_tail)
+        constexpr bool kModes = sizeof(P) == sizeof(float) && !EXACT;
+        if (kModes && mode == 2) update_vm<V, kModes ? 2 : -1>(v, p, mode, stage, out, with_dt, s);
+        else if (kModes && mode == 3) update_vm<V, kModes ? 3 : -1>(v, p, mode, stage, out, with_dt, s);
+        else update_vm<V, -1>(v, p, mode, stage, out, with_dt, s);
     }
     static void recon(const DevView& v, const FvParams& p, bool reco, int var, cudaStream_t s) {
         if (!reco && !p.viscous) return;
