@@ -51,6 +51,10 @@ def parse():
                     help="launch variants recon,face,update of the mixed build instead of autotuning (profiling)")
     ap.add_argument("--fused", default="auto", choices=["auto", "on", "off"],
                     help="fused stage for structured blocks: let the autotuner choose, force, or disable")
+    ap.add_argument("--march", default="auto", choices=["auto", "on", "off"],
+                    help="plane-marching kernel of the fused stage (one 3-D block, TMA-staged planes): let the "
+                         "autotuner choose, force, or take the tile kernel")
+    ap.add_argument("--march-planes", type=int, default=0, help="planes per CTA of the plane-marching kernel (0: tuned)")
     ap.add_argument("--cell-flux", default="auto", choices=["auto", "on", "off"],
                     help="per-cell flux path (face fluxes recomputed inside the update kernel): let the "
                          "autotuner choose, force, or disable")
@@ -380,6 +384,8 @@ def run_ours(args, world, rank, local):
     # --- headline: mixed precision, device-resident state
     sim.set_primitives(*ic)
     sim.set_fused({"auto": -1, "on": 1, "off": 0}[args.fused])
+    if sim.fused_info()["eligible"] and (args.march != "auto" or args.march_planes):
+        sim.set_fused_kind({"auto": -1, "on": 1, "off": 0}[args.march], args.march_planes)
     sim.set_cell_flux({"auto": -1, "on": 1, "off": 0}[args.cell_flux])
     if args.variants:
         r, f, u = (int(x) for x in args.variants.split(","))
@@ -388,6 +394,7 @@ def run_ours(args, world, rank, local):
     else:
         tune_mixed = sim.autotune("mixed")
     fused = sim.fused_info()
+    fkind = sim.fused_kind()
     cellf = sim.cell_flux_info()
     sim.take_steps(args.warmup, "mixed")
     barrier()
@@ -475,7 +482,9 @@ def run_ours(args, world, rank, local):
                          "steps": args.warmup + args.steps},
             "kernel_ms": {k: round(v, 4) for k, v in kt.items()},
             "autotune": {"variants_table": Simulation.launch_variants(), "mixed": tune_mixed, "f64": tune_f64,
-                         "fused_stage": {k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")},
+                         "fused_stage": dict({k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")},
+                                             **{k: fkind[k] for k in ("march", "planes_per_cta", "tile_ms",
+                                                                      "march_ms")}),
                          "cell_flux": {k: cellf[k] for k in ("enabled", "variant", "cell_ms", "generic_ms")}},
             "batch": batch,
             "sweep": sweep,

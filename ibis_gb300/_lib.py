@@ -104,6 +104,9 @@ def load(build_if_missing: bool = True):
     L.ibisgb_set_fused.argtypes = [_P, C.c_int32]
     L.ibisgb_check_conversions.argtypes = [C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]
     L.ibisgb_fused_info.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, C.c_char_p, C.c_int32]
+    L.ibisgb_set_fused_kind.argtypes = [_P, C.c_int32, C.c_int32]
+    L.ibisgb_fused_kind.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P,
+                                    C.c_char_p, C.c_int32]
     L.ibisgb_set_cell_flux.argtypes = [_P, C.c_int32]
     L.ibisgb_cell_flux_info.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P]
     L.ibisgb_batch_create.argtypes = [_P, C.c_int32, C.POINTER(_P)]

@@ -197,6 +197,18 @@ struct ibisgb_ctx {
     bool fused_on = false;
     cudaGraphExec_t graph_fused[2] = {nullptr, nullptr};
     double fused_ms = 0.0, generic_ms = 0.0;
+    // Plane-marching variant of the fused stage (one 3-D block, TMA-staged
+    // planes): the autotuner times it beside the tile kernel and keeps the faster.
+    int march_elig = -1;  // -1 not checked yet, 0 not eligible, 1 eligible
+    std::string march_why;
+    int march_mode = -1;  // -1 the autotuner decides, 0 tile kernel, 1 plane-marching kernel
+    int march_kc_req = 0;  // planes per CTA requested (0: tuned)
+    bool march_on = false;
+    int march_kc = 32;
+    double tile_ms = 0.0, march_ms = 0.0;
+    TmaMap march_map_prim[2], march_map_cc;
+    const void* march_map_base[3] = {nullptr, nullptr, nullptr};
+    DBuf march_fault;
     // Per-cell flux path (mixed, inviscid): recon + k_cell_update per stage, on
     // the same alternating primitive buffers and per-parity graphs as the fused stage.
     int cell_mode = -1;  // -1 the autotuner decides, 0 off, 1 on
@@ -798,6 +810,65 @@ struct ibisgb_ctx {
         fused_uploaded = true;
     }
 
+    // Host-side eligibility of the plane-marching kernel (no GPU needed).
+    bool check_march() {
+        if (march_elig >= 0) return march_elig == 1;
+        march_elig = 0;
+        if (!check_fused()) march_why = fused_why;
+        else if (mesh.dim != 3) march_why = "the plane-marching stage is three-dimensional";
+        else if (slay.blocks.size() != 1 || n_cases != 1) march_why = "the plane-marching stage takes one structured block";
+        else if (slay.blocks[0].c0 % 4 || slay.blocks[0].ni % 4 || mesh.NT() % 4)
+            march_why = "TMA copies need the block's first cell, i-extent and N+G to be multiples of 4";
+        else march_elig = 1;
+        return march_elig == 1;
+    }
+
+    // Tensor maps of the two mixed primitive buffers and of the float centroids
+    // (re-encoded if a buffer moved).
+    void upload_march() {
+        upload_fused();
+        if (!march_fault.p) {
+            march_fault.alloc(sizeof(unsigned));
+            CUDA_OK(cudaMemsetAsync(march_fault.p, 0, sizeof(unsigned), stream));
+            CUDA_OK(prepare_march_stage());
+        }
+        const SBlock& B = slay.blocks[0];
+        const void* bases[3] = {s32.prim.p, prim_alt.p, s32.cc.p};
+        for (int b = 0; b < 3; b++) {
+            if (bases[b] == march_map_base[b]) continue;
+            std::string why;
+            const float* base = (const float*)bases[b] + B.c0;
+            TmaMap* out = b < 2 ? &march_map_prim[b] : &march_map_cc;
+            if (march_encode_map(out, base, B.ni, B.nj, B.nk, b < 2 ? 7 : 3, mesh.NT(), &why) != 0)
+                throw CudaError("plane-marching stage: " + why);
+            march_map_base[b] = bases[b];
+        }
+    }
+
+    // The fused stage the context uses (tile or plane-marching kernel), reading
+    // primitive buffer `cur` and writing the other one.
+    void launch_fused_any(const DevView& v, int cur, int mode, int stage, int with_dt, bool march, int kc) {
+        SbView sb = sb_view(mixed_prim(cur ^ 1));
+        if (march)
+            launch_march_stage(v, sb, slay.blocks[0], prm, march_map_prim[cur], march_map_cc, mode, stage, with_dt, kc,
+                               stream);
+        else
+            launch_fused_stage(v, sb, prm, mode, stage, with_dt, stream);
+    }
+
+    // A TMA copy of the plane-marching stage that did not complete within its wait
+    // limit is reported once, as a CUDA failure of the call that ran it.
+    void check_march_fault() {
+        if (!march_fault.p) return;
+        unsigned f = 0;
+        CUDA_OK(cudaMemcpyAsync(&f, march_fault.p, sizeof(f), cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+        if (f) {
+            CUDA_OK(cudaMemsetAsync(march_fault.p, 0, sizeof(unsigned), stream));
+            throw CudaError("plane-marching stage: a TMA copy did not complete within its wait limit");
+        }
+    }
+
     SbView sb_view(void* prim_out) const {
         SbView sb{};
         sb.blocks = sb_blocks.as<SBlock>();
@@ -807,6 +878,7 @@ struct ibisgb_ctx {
         sb.SF = (int)slay.num_faces;
         sb.ghost_map = sb_ghost.as<int>();
         sb.prim_out = prim_out;
+        sb.fault = march_fault.as<unsigned>();
         return sb;
     }
     void* mixed_prim(int which) { return which ? prim_alt.p : s32.prim.p; }
@@ -845,7 +917,7 @@ struct ibisgb_ctx {
         int cur = start;
         for (int s = 0; s < S; s++) {
             v.prim = mixed_prim(cur);
-            launch_fused_stage(v, sb_view(mixed_prim(cur ^ 1)), prm, s == S - 1 ? 3 : 2, s, s == S - 1, stream);
+            launch_fused_any(v, cur, s == S - 1 ? 3 : 2, s, s == S - 1, march_on, march_kc);
             cur ^= 1;
         }
     }
@@ -903,6 +975,7 @@ struct ibisgb_ctx {
         if (!tuned[gi]) autotune(prec);
         // the fused stage and the per-cell flux path alternate primitive buffers
         const bool fused = is_mixed(prec) && (fused_on || cell_on);
+        if (fused && fused_on && march_on) upload_march();
         if (fused) {
             for (int par = 0; par < 2; par++) {
                 if (graph_fused[par]) continue;
@@ -949,6 +1022,7 @@ struct ibisgb_ctx {
         last_ctl.resize(n_cases);
         CUDA_OK(cudaMemcpyAsync(last_ctl.data(), ctl.p, sizeof(StepCtl) * n_cases, cudaMemcpyDeviceToHost, stream));
         CUDA_OK(cudaStreamSynchronize(stream));
+        if (fused && fused_on && march_on) check_march_fault();
         float ms = 0.f;
         CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
         cudaEventDestroy(e0);
@@ -1374,14 +1448,35 @@ struct ibisgb_ctx {
             if (is_mixed(prec)) {
                 generic_ms = tune_ms[gi][0][vr[0]] + tune_ms[gi][1][vr[1]] + tune_ms[gi][2][vr[2]];
                 fused_ms = 0.0;
+                tile_ms = march_ms = 0.0;
                 if (fused_mode != 0 && check_fused()) {
                     upload_fused();
-                    // the fused stage in the same first-stage mode, writing the other buffer
-                    SbView sb = sb_view(mixed_prim(prim_cur ^ 1));
+                    // the fused stage in the same first-stage mode, writing the other buffer:
+                    // the tile kernel and, on one 3-D block, the plane-marching kernel at
+                    // several chunk lengths; the faster kernel is the fused stage
                     const int fm = ctl_host.stages > 1 ? 2 : 0;
-                    fused_ms = timed([&] { launch_fused_stage(v, sb, prm, fm, 0, 0, stream); });
-                    const double again = timed([&] { launch_fused_stage(v, sb, prm, fm, 0, 0, stream); });
-                    fused_ms = std::min(fused_ms, again);
+                    auto time_fused = [&](bool march, int kc) {
+                        const double a = timed([&] { launch_fused_any(v, prim_cur, fm, 0, 0, march, kc); });
+                        const double b = timed([&] { launch_fused_any(v, prim_cur, fm, 0, 0, march, kc); });
+                        return std::min(a, b);
+                    };
+                    if (march_mode != 1) tile_ms = time_fused(false, 0);
+                    if (march_mode != 0 && check_march()) {
+                        upload_march();
+                        const int nk = slay.blocks[0].nk;
+                        std::vector<int> kcs;
+                        if (march_kc_req > 0) kcs.push_back(march_kc_req);
+                        else
+                            for (int kc : {16, 32, 64})
+                                if (kc < 2 * nk) kcs.push_back(kc);
+                        for (int kc : kcs) {
+                            const double t = time_fused(true, kc);
+                            if (march_ms == 0.0 || t < march_ms) { march_ms = t; march_kc = kc; }
+                        }
+                        check_march_fault();
+                    }
+                    march_on = march_ms > 0.0 && (tile_ms == 0.0 || march_ms < tile_ms);
+                    fused_ms = march_on ? march_ms : tile_ms;
                 }
                 // the per-cell flux path: recon (as chosen) + k_cell_update in the same mode,
                 // writing the other primitive buffer (the current one stays as it is)
@@ -1426,10 +1521,36 @@ struct ibisgb_ctx {
         if (mode < -1 || mode > 1) throw ArgError("fused mode must be -1, 0 or 1");
         if (mode == 1 && !check_fused()) throw ArgError("the fused stage does not apply: " + fused_why);
         fused_mode = mode;
-        if (mode == 1) upload_fused();
+        if (mode == 1) {
+            upload_fused();
+            if (march_mode == 1 || (march_mode == -1 && march_on)) {
+                upload_march();
+                march_on = true;
+                if (march_kc_req > 0) march_kc = march_kc_req;
+            } else {
+                march_on = false;
+            }
+        }
         if (mode >= 0) fused_on = mode == 1;
         if (fused_on) cell_on = false;
         if (mode < 0) tuned[1] = false;
+        drop_mixed_graphs();
+    }
+
+    // kernel of the fused stage: -1 the autotuner decides, 0 the tile kernel, 1 the
+    // plane-marching kernel (kc planes per CTA, 0: tuned)
+    void set_fused_kind(int kind, int kc) {
+        if (kind < -1 || kind > 1) throw ArgError("fused kind must be -1, 0 or 1");
+        if (kc < 0) throw ArgError("planes per CTA must be >= 0");
+        if (kind == 1 && !check_march()) throw ArgError("the plane-marching stage does not apply: " + march_why);
+        march_mode = kind;
+        march_kc_req = kc;
+        if (kind == 1) {
+            upload_march();
+            if (kc > 0) march_kc = kc;
+        }
+        if (kind >= 0) march_on = kind == 1;
+        if (kind < 0 || (kind == 1 && kc == 0)) tuned[1] = false;
         drop_mixed_graphs();
     }
 
@@ -2060,6 +2181,24 @@ int ibisgb_fused_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, doub
         if (reason && reason_len > 0) {
             std::snprintf(reason, (size_t)reason_len, "%s", ctx->fused_why.c_str());
         }
+    });
+}
+
+int ibisgb_set_fused_kind(ibisgb_ctx* ctx, int32_t kind, int32_t planes_per_cta) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->set_fused_kind(kind, planes_per_cta); });
+}
+
+int ibisgb_fused_kind(ibisgb_ctx* ctx, int32_t* march_eligible, int32_t* march_in_use, int32_t* planes_per_cta,
+                      double* times_ms, char* reason, int32_t reason_len) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        const bool el = ctx->check_march();
+        if (march_eligible) *march_eligible = el ? 1 : 0;
+        if (march_in_use) *march_in_use = ctx->march_on ? 1 : 0;
+        if (planes_per_cta) *planes_per_cta = ctx->march_kc;
+        if (times_ms) { times_ms[0] = ctx->tile_ms; times_ms[1] = ctx->march_ms; }
+        if (reason && reason_len > 0) std::snprintf(reason, (size_t)reason_len, "%s", ctx->march_why.c_str());
     });
 }
 

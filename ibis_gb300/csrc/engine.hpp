@@ -178,6 +178,22 @@ void launch_fused_stage(const DevView& v, const SbView& sb, const FvParams& prm,
                         cudaStream_t s);
 cudaError_t prepare_fused_stage();              // shared-memory opt-in, once per device
 void fused_tile_shape(int dim, int* tx, int* ty, int* tz);
+// Plane-marching fused stage for one 3-D structured block (kernels_march.cuh):
+// the same stage as launch_fused_stage, with the block's planes staged into
+// shared memory by TMA; hb is the host copy of sb.blocks[0], kc the planes per CTA.
+struct alignas(128) TmaMap {
+    unsigned char bytes[128];  // a CUtensorMap
+};
+void launch_march_stage(const DevView& v, const SbView& sb, const SBlock& hb, const FvParams& prm,
+                        const TmaMap& prim, const TmaMap& cc, int mode, int stage, int with_dt, int kc,
+                        cudaStream_t s);
+cudaError_t prepare_march_stage();  // shared-memory opt-in, once per device
+// The tensor map of nvar float arrays of one block (base: its first cell;
+// var_stride: elements between variables) in the layout the stage copies.
+// Returns 0, or -1 with *why set.
+int march_encode_map(TmaMap* out, const float* base, int ni, int nj, int nk, int nvar, long long var_stride,
+                     std::string* why);
+constexpr int kMarchTileX = 32, kMarchTileY = 8;
 // The mixed build's integer-pipe float -> double conversion against the
 // conversion instruction on n pseudo-random bit patterns; mismatches counted.
 int check_float_conversions(long long n, unsigned long long seed, unsigned long long* mismatches);

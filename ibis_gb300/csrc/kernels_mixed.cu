@@ -16,6 +16,51 @@ void launch_fused_stage(const DevView& v, const SbView& sb, const FvParams& prm,
     k_mixed::launch_fused(v, sb, prm, mode, stage, with_dt, s);
 }
 cudaError_t prepare_fused_stage() { return k_mixed::prepare_fused(); }
+}  // namespace ibisgb
+
+#include <cudaTypedefs.h>
+
+#include "kernels_march.cuh"
+
+namespace ibisgb {
+static_assert(sizeof(TmaMap) == sizeof(CUtensorMap) && alignof(TmaMap) >= alignof(CUtensorMap),
+              "TmaMap must hold a CUtensorMap");
+static_assert(k_mixed::March::TX == kMarchTileX && k_mixed::March::TY == kMarchTileY, "march tile shape");
+
+void launch_march_stage(const DevView& v, const SbView& sb, const SBlock& hb, const FvParams& prm,
+                        const TmaMap& prim, const TmaMap& cc, int mode, int stage, int with_dt, int kc,
+                        cudaStream_t s) {
+    k_mixed::launch_march(v, sb, hb, prm, &prim, &cc, mode, stage, with_dt, kc, s);
+}
+cudaError_t prepare_march_stage() { return k_mixed::prepare_march(); }
+
+int march_encode_map(TmaMap* out, const float* base, int ni, int nj, int nk, int nvar, long long var_stride,
+                     std::string* why) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            if (why) *why = "the driver has no cuTensorMapEncodeTiled";
+            return -1;
+        }
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    const cuuint64_t dims[4] = {(cuuint64_t)ni, (cuuint64_t)nj, (cuuint64_t)nk, (cuuint64_t)nvar};
+    const cuuint64_t strides[3] = {(cuuint64_t)ni * 4, (cuuint64_t)ni * nj * 4, (cuuint64_t)var_stride * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)k_mixed::March::BW, (cuuint32_t)k_mixed::March::BH, 1, 1};
+    const cuuint32_t elem[4] = {1, 1, 1, 1};
+    const CUresult r = encode((CUtensorMap*)out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)base, dims, strides, box,
+                              elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        if (why) *why = "cuTensorMapEncodeTiled failed (error " + std::to_string((int)r) + ")";
+        return -1;
+    }
+    return 0;
+}
 // Self-check of the integer-pipe float -> double conversion against the
 // conversion instruction, compiled with the same flags as the kernels that use
 // it: n pseudo-random float bit patterns (splitmix64 from seed).

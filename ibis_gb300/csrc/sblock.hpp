@@ -26,6 +26,7 @@ struct SbView {
     int SF;
     const int* ghost_map;
     void* prim_out;         // primitives of the new state (the other buffer)
+    unsigned* fault;        // plane-marching stage: set when a TMA copy did not complete in time
 };
 
 }  // namespace ibisgb

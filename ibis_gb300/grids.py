@@ -568,13 +568,14 @@ def flat_plate_case(ni=512, nj=256, mach=2.0, T=220.0, Re_per_m=1e5, Pr=0.71, **
     return grid, make_config(2, bnds, gas=gas, viscous=True, Pr=Pr, **kw), inflow
 
 
-def box_case(n=64, **kw):
-    """3-D periodic unit box, ideal gas gamma=1.4 with R=1 (so T = p/rho)."""
+def box_case(n=64, ny=None, nz=None, **kw):
+    """3-D periodic unit box of n x ny x nz cells (ny, nz default to n), ideal gas
+    gamma=1.4 with R=1 (so T = p/rho)."""
     gas = ideal_gas(1.0)
     bnds = {"west": periodic("east", (1, 0, 0)), "east": periodic("west", (-1, 0, 0)),
             "south": periodic("north", (0, 1, 0)), "north": periodic("south", (0, -1, 0)),
             "bottom": periodic("top", (0, 0, 1)), "top": periodic("bottom", (0, 0, -1))}
-    return box_3d(n), make_config(3, bnds, gas=gas, **kw)
+    return box_3d(n, ny, nz), make_config(3, bnds, gas=gas, **kw)
 
 
 def box_initial_condition(n: int, gas: dict, seed=0, kmax=4, amp=0.05, mach_rms=0.3):

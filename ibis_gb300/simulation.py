@@ -190,6 +190,20 @@ class Simulation:
         return {"eligible": bool(el.value), "enabled": bool(en.value), "fused_ms": t[0], "generic_ms": t[1],
                 "reason": why.value.decode()}
 
+    def set_fused_kind(self, kind: int, planes_per_cta: int = 0) -> None:
+        """Kernel of the fused stage: -1 autotuner decides, 0 the tile kernel, 1 the
+        plane-marching kernel (one 3-D block), with planes_per_cta planes per CTA
+        (0: tuned)."""
+        self._call("ibisgb_set_fused_kind", int(kind), int(planes_per_cta))
+
+    def fused_kind(self) -> dict:
+        el, on, kc = C.c_int32(), C.c_int32(), C.c_int32()
+        t = np.zeros(2)
+        why = C.create_string_buffer(256)
+        self._call("ibisgb_fused_kind", C.byref(el), C.byref(on), C.byref(kc), _ptr(t), why, 256)
+        return {"march_eligible": bool(el.value), "march": bool(on.value), "planes_per_cta": kc.value,
+                "tile_ms": t[0], "march_ms": t[1], "reason": why.value.decode()}
+
     def set_cell_flux(self, mode: int) -> None:
         """Per-cell flux path of the mixed build: -1 autotuner decides, 0 off, 1 on."""
         self._call("ibisgb_set_cell_flux", int(mode))

@@ -312,6 +312,27 @@ int ibisgb_set_fused(ibisgb_ctx* ctx, int32_t mode);
 int ibisgb_fused_info(ibisgb_ctx* ctx, int32_t* eligible, int32_t* enabled, double* times_ms, char* reason,
                       int32_t reason_len);
 
+/* Kernel of the fused stage.  On one 3-D structured block whose first cell
+ * index, i-extent and N+G are multiples of 4, the fused stage also has a
+ * plane-marching kernel: each CTA owns a 32 x 8 column of cells and marches
+ * along k, with every plane of primitives and centroids staged into shared
+ * memory once by TMA tensor copies, gradients, limiters and fluxes kept on the
+ * SM, and the double update as in the tile kernel.  kind -1 (the default) lets
+ * ibisgb_autotune / the first ibisgb_rk_run time both kernels (and the
+ * marching kernel at 16, 32 and 64 planes per CTA, or at planes_per_cta when
+ * it is > 0) and keep the faster; 0 always takes the tile kernel; 1 always the
+ * plane-marching kernel (IBISGB_ERR_ARG if it does not apply).  Applies when the
+ * fused stage is in use (ibisgb_set_fused).  A scheduling choice with no
+ * counterpart in ibis; the same formulas as the tile kernel. */
+int ibisgb_set_fused_kind(ibisgb_ctx* ctx, int32_t kind, int32_t planes_per_cta);
+
+/* Whether the plane-marching kernel applies (host-side check) and is the fused
+ * stage's kernel, its planes per CTA, the last tuning times of one stage (ms:
+ * tile kernel, plane-marching kernel; 2 doubles, may be NULL; 0 when not timed)
+ * and, when it does not apply, why. */
+int ibisgb_fused_kind(ibisgb_ctx* ctx, int32_t* march_eligible, int32_t* march_in_use, int32_t* planes_per_cta,
+                      double* times_ms, char* reason, int32_t reason_len);
+
 /* Per-cell flux path of the MIXED build (inviscid Runge-Kutta stages without
  * constant-flux boundaries; any grid).  Each stage runs the gradient kernel and
  * then one kernel in which every cell recomputes the convective fluxes of its

@@ -34,9 +34,13 @@ def case(name, **kw):
         g, c = grids.box_case(n, **kw)
         T, p, vx, vy, vz = grids.box_initial_condition(n, c["gas_model"], seed=3)
         return g, c, (T, p, vx, vy, vz)
+    if name == "box_ragged":  # periodic box whose extents are not multiples of the kernels' tiles
+        ni, nj, nk = kw.pop("shape", (36, 12, 10))
+        g, c = grids.box_case(ni, ny=nj, nz=nk, **kw)
+        return g, c, random_state(g.num_cells, 1.0, 1.0, 0.3, 3, seed=10, amp=0.05)
     if name == "box_inout":  # 3-D channel: supersonic in/out, slip walls
         n = kw.pop("n", 5)
-        g = grids.box_3d(n)
+        g = grids.box_3d(*n) if isinstance(n, tuple) else grids.box_3d(n)
         inflow = grids.flow_state(gas, 300.0, 1e5, 700.0, 30.0, 20.0)
         b = {"west": grids.supersonic_inflow(inflow), "east": grids.supersonic_outflow(),
              "south": grids.slip_wall(), "north": grids.slip_wall(), "bottom": grids.slip_wall(),

@@ -40,3 +40,21 @@ def test_other_grids_and_schemes_are_refused():
     g = grids.unit_square_3x3()
     bnds = {t: grids.slip_wall() for t in ["slip_wall_bottom", "slip_wall_top", "inflow", "outflow"]}
     assert Simulation(grids.make_config(2, bnds), g).fused_info()["eligible"]
+
+
+def test_plane_marching_kernel_eligibility():
+    """The plane-marching kernel takes one 3-D block whose i-extent and N+G are
+    multiples of 4 (TMA copies start on 16-byte boundaries); the host says why not."""
+    for name, kw in (("box", {"n": 8}), ("box_ragged", {}), ("box_inout", {"n": (36, 12, 10)})):
+        g, c, _ = case(name, **kw)
+        k = Simulation(c, g).fused_kind()
+        assert k["march_eligible"], (name, k["reason"])
+        assert not k["march"]
+    g, c, _ = case("box", n=6)
+    k = Simulation(c, g).fused_kind()
+    assert not k["march_eligible"] and "multiples of 4" in k["reason"]
+    g, c, _ = case("ramp")
+    k = Simulation(c, g).fused_kind()
+    assert not k["march_eligible"] and "three-dimensional" in k["reason"]
+    g, c, _ = case("plate")
+    assert "viscous" in Simulation(c, g).fused_kind()["reason"]
