@@ -172,7 +172,7 @@ struct ibisgb_ctx {
 
     // connectivity and per-cell data shared by all arithmetics
     DBuf cell_face, cell_nbr, outsign, nfaces, left, right, ghost_src, ghost_face, ghost_bound,
-        bounds, gfix, feed_off, feed_ghost, vol, inv_vol;
+        bounds, gfix, feed_off, feed_ghost, vol, inv_vol, inv_vol2;
     DBuf U, k, vsig, ctl, l2, out, branches;
     StateBufs s64, s32;
     std::vector<double> ic_prims;  // host IC primitives (7 x NT), kept until the first update
@@ -567,6 +567,14 @@ struct ibisgb_ctx {
         upload(vol, v, stream);
         for (auto& x : v) x = 1.0 / x;
         upload(inv_vol, v, stream);
+        {  // 1/volume as two floats whose sum is it to ~2^-48 (the mixed build's residual scaling)
+            std::vector<float> p(2 * (size_t)N);
+            for (int64_t c = 0; c < N; c++) {
+                p[2 * c] = (float)v[c];
+                p[2 * c + 1] = (float)(v[c] - (double)p[2 * c]);
+            }
+            upload(inv_vol2, p, stream);
+        }
         U.alloc(sizeof(double) * nc() * N);
         k.alloc(sizeof(double) * nc() * N * stages());
         vsig.alloc(sizeof(double) * F);
@@ -644,7 +652,7 @@ struct ibisgb_ctx {
         v.ghost_bound = ghost_bound.as<int>(); v.bounds = bounds.as<BoundDev>(); v.gfix = gfix.as<double>();
         v.feed_off = feed_off.as<int>(); v.feed_ghost = feed_ghost.as<int>();
         v.cc = s.cc.p; v.r = s.r.p; v.face = s.face.p; v.vol = vol.as<double>();
-        v.inv_vol = inv_vol.as<double>(); v.lsqw = s.lsqw.p;
+        v.inv_vol = inv_vol.as<double>(); v.inv_vol2 = inv_vol2.as<float2>(); v.lsqw = s.lsqw.p;
         v.lsqd = s.lsqd.p;
         v.prim = (is_mixed(prec) && prim_cur) ? prim_alt.p : s.prim.p;
         v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;

@@ -110,6 +110,7 @@ struct DevView {
     const void* face;
     const double* vol;      // N
     const double* inv_vol;  // N, 1/volume (fast paths)
+    const float2* inv_vol2; // N, 1/volume as a float pair (hi, lo) (mixed build)
     const void* lsqw;       // [3][MF][N] least-squares weights per neighbour slot (type Gm, fast paths)
     const void* lsqd;       // [3][MF][N] face centre minus cell centroid per face slot (float build), or null
     // state (type P)

@@ -728,23 +728,24 @@ __device__ __forceinline__ double recip_newton(double x) {
     return fma(r, e, r);
 }
 
-// 1/x in double from a float reciprocal seed (the float pipe's MUFU, not the
-// FP64 pipe's) and two Newton steps: the seed's 2^-23 relative error becomes
-// 2^-46, then below double rounding.  Inputs whose value or reciprocal is not
-// a normal float take the double seed, in a call (not inlined, so that its
-// instructions are not issued predicated for the common case).
+// Inputs whose value or reciprocal is not a normal float take the double seed,
+// in a call (not inlined, so that its instructions are not issued predicated
+// for the common case).
 __device__ __noinline__ double recip_by_double_seed(double x) { return recip_newton(x); }
 
-__device__ __forceinline__ double recip_newton_fseed(double x) {
+// 1/x in double from a float reciprocal seed refined by one Newton step in
+// double: the seed's relative error (below 2^-22) is squared, so the result is
+// within 2^-44 of 1/x -- far below the float rounding of the primitives the
+// mixed build stores, and it leaves the cancellation E/rho - |v|^2/2 in double.
+// Two FP64 operations (one FMA for the residual, one for the step); inputs
+// outside the normal float range take the double seed and two steps.
+__device__ __forceinline__ double recip_newton1_fseed(double x) {
     const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7FFu;
     if (ex - 897u > 251u) return recip_by_double_seed(x);  // |x| outside [2^-126, 2^126)
     float rf;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(d2f(x)));
-    double r = f2d(rf);
-    double e = fma(-x, r, 1.0);
-    r = fma(r, e, r);
-    e = fma(-x, r, 1.0);
-    return fma(r, e, r);
+    const double r = f2d(rf);
+    return fma(r, fma(-x, r, 1.0), r);
 }
 
 // What the update needs of a committed state: rho (bad-cell test) and the
@@ -764,7 +765,7 @@ __device__ Committed<P> commit_state(const DevView& v, const FvParams& prm, int 
         // Mixed build: rho, v and e = E/rho - |v|^2/2 in double (the cancellation of
         // strong expansions happens there); T = e/Cv and p = rho R T are products of
         // values already rounded to float, so they are formed in float.
-        const double ir = recip_newton_fseed(rho);  // a state with rho <= 0 is a bad cell either way
+        const double ir = recip_newton1_fseed(rho);  // a state with rho <= 0 is a bad cell either way
         vx = u[1] * ir;
         vy = u[2] * ir;
         vz = DIM == 3 ? u[3] * ir : 0.0;
@@ -842,6 +843,19 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
     float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
     hi = s;
     lo = __fadd_rn(lo, err);
+}
+
+// (hi + lo) * s as a double, for s given as the float pair s.x + s.y: the leading
+// product hi * s.x, its exact rounding error (FMA) plus the cross terms hi * s.y
+// and lo * s.x in float, formed in double by one addition (relative error about
+// 2^-46, the precision of the float-pair sum itself).  One FP64 operation
+// instead of the two of (f2d(hi) + f2d(lo)) * s.
+__device__ __forceinline__ double pair_scale(float hi, float lo, float2 s) {
+    const float p = __fmul_rn(hi, s.x);
+    float e = __fmaf_rn(hi, s.x, -p);
+    e = __fmaf_rn(hi, s.y, e);
+    e = __fmaf_rn(lo, s.x, e);
+    return f2d(p) + f2d(e);
 }
 
 // hi + lo += x * a, keeping the product's rounding error (an FMA gives it exactly)
@@ -1027,10 +1041,12 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
 #pragma unroll
             for (int q = 0; q < NC; q++) pair_acc(hi[q], lo[q], (float)fl[q * F + f], a);
         }
-        iv = v.inv_vol[i];
-        if (!fold) {
+        if (fold) {
+            iv = v.inv_vol[i];
+        } else {
+            const float2 ivp = v.inv_vol2[i];
 #pragma unroll
-            for (int q = 0; q < NC; q++) ks[q] = (f2d(hi[q]) + f2d(lo[q])) * iv;
+            for (int q = 0; q < NC; q++) ks[q] = pair_scale(hi[q], lo[q], ivp);
         }
     } else {
         double acc[NC];
@@ -1102,14 +1118,15 @@ __global__ void __launch_bounds__(BS, MINB) k_cell_update(DevView v, FvParams pr
 #pragma unroll
             for (int q = 0; q < NC; q++) pair_acc(hi[q], lo[q], Fg[q < DIM + 1 ? q : 4], a);
         }
-        const double iv = v.inv_vol[i];
         double ks[NC];
         const bool fold = mode == 3 && stage > 0;
+        const double iv = fold ? v.inv_vol[i] : 0.0;
         if (!fold) {
+            const float2 ivp = v.inv_vol2[i];
             double* kk = v.k + (size_t)stage * NC * N;
 #pragma unroll
             for (int q = 0; q < NC; q++) {
-                ks[q] = (f2d(hi[q]) + f2d(lo[q])) * iv;
+                ks[q] = pair_scale(hi[q], lo[q], ivp);
                 kk[q * N + i] = ks[q];
             }
         }

@@ -500,14 +500,15 @@ __device__ __forceinline__ double march_update(const MarchCtx& m, const DevView&
             lo[q] = __fadd_rn(lo[q], pe);
         }
     }
-    const double iv = v.inv_vol[i];
     const bool fold = mode == 3 && stage > 0;
+    const double iv = fold ? v.inv_vol[i] : 0.0;
     double ks[NC];
     if (!fold) {
+        const float2 ivp = v.inv_vol2[i];
         double* kk = v.k + (size_t)stage * NC * N;
 #pragma unroll
         for (int q = 0; q < NC; q++) {
-            ks[q] = (f2d(hi[q]) + f2d(lo[q])) * iv;
+            ks[q] = pair_scale(hi[q], lo[q], ivp);
             kk[q * N + i] = ks[q];
         }
     }
