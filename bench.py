@@ -349,6 +349,15 @@ def jfnk_measure(args):
             "time_to_1e-10_first_order": first}
 
 
+def headline_config(n, world):
+    """The config of the headline line (both arms): the n^3 periodic box."""
+    return {"workload": f"3-D Euler periodic box {n}^3 (residual-throughput case), ssp-rk3, "
+                        f"Hanel, 2nd-order MUSCL + Barth-Jespersen, rho_u",
+            "cells_per_gpu": n ** 3, "faces_per_gpu": 3 * n ** 3 + 3 * n ** 2, "stages_per_step": 3,
+            "l2": "inputs larger than L2 (state + geometry several GB per GPU), no flush",
+            "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args, world, rank):
     """--impl reference: the oracle port of the reference's CPU path, all host threads."""
     if rank != 0:
@@ -365,12 +374,13 @@ def run_reference(args, world, rank):
     dt = time.perf_counter() - t
     value = 3.0 * n ** 3 * args.steps / dt / 1e6
     sample = (f"oracle port (C++ restatement of ibis's FP64 path, OpenMP) on a {n}^3 periodic box, "
-              f"{args.steps} ssp-rk3 steps; the 256^3 grid does not fit a bounded CPU run")
+              f"{args.steps} ssp-rk3 steps per timed call (each bench step is one ssp-rk3 step of that box); "
+              f"the {args.n}^3 grid does not fit a bounded CPU run")
     line = {"impl": "reference", "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"3-D Euler periodic box {n}^3, ssp-rk3, Hanel, MUSCL + Barth-Jespersen, rho_u"},
+            "config": headline_config(args.n, world),
             "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": num_threads(),
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
@@ -495,11 +505,7 @@ def run_ours(args, world, rank, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 flux / f64 accumulate+update (mixed)", "data": "synthetic",
-            "config": {"workload": f"3-D Euler periodic box {n}^3 (residual-throughput case), ssp-rk3, "
-                                   f"Hanel, 2nd-order MUSCL + Barth-Jespersen, rho_u, mixed precision",
-                       "cells_per_gpu": N, "faces_per_gpu": sim.num_faces, "stages_per_step": 3,
-                       "l2": "inputs larger than L2 (state + geometry several GB per GPU), no flush",
-                       "parallelism": f"replicas x{world}"},
+            "config": headline_config(n, world),
             "f64": {"value": value_f64, "ms_per_step": ms_f64 / args.steps,
                     "mixed_speedup": value / value_f64},
             "accuracy": {"rho_rel_l2_err_mixed_vs_f64": l2_err, "rho_rel_max_err_mixed_vs_f64": max_err,
