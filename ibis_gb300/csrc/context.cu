@@ -1627,6 +1627,17 @@ struct ibisgb_ctx {
         for (int k = 0; k < 4; k++) out[k] = reps > 0 ? acc[k] / reps : 0.0;
     }
 
+    // Device address of pinned host memory mapped into this device's address space
+    // (on Grace the GPU reads and writes it over the coherent C2C link), or null.
+    static void* mapped_host(const void* p) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();  // not a CUDA allocation: pageable memory
+            return nullptr;
+        }
+        return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    }
+
     void set_conserved(const double* rows, bool device = false) {
         if (!rows) throw ArgError("U is null");
         ensure_device();
@@ -1634,6 +1645,11 @@ struct ibisgb_ctx {
         const size_t bytes = sizeof(double) * nc() * N;
         if (device) {
             launch_rows_to_soa(rows, U.as<double>(), (int)N, nc(), stream);
+        } else if (const void* d = mapped_host(rows)) {
+            // pinned host rows: the layout kernel reads them in place (one pass, all SMs)
+            launch_rows_to_soa((const double*)d, U.as<double>(), (int)N, nc(), stream);
+            CUDA_OK(cudaGetLastError());
+            CUDA_OK(cudaStreamSynchronize(stream));  // the caller may reuse its buffer on return
         } else {
             out.alloc(bytes);
             CUDA_OK(cudaMemcpyAsync(out.p, rows, bytes, cudaMemcpyHostToDevice, stream));
@@ -1651,6 +1667,13 @@ struct ibisgb_ctx {
         if (!have_state) throw StateError("no initial condition");
         const int64_t N = mesh.N;
         const size_t bytes = sizeof(double) * nc() * N;
+        if (void* d = mapped_host(rows)) {
+            // pinned host rows: the layout kernel writes them in place
+            launch_soa_to_rows(U.as<double>(), (double*)d, (int)N, nc(), stream);
+            CUDA_OK(cudaGetLastError());
+            CUDA_OK(cudaStreamSynchronize(stream));
+            return;
+        }
         out.alloc(bytes);
         launch_soa_to_rows(U.as<double>(), out.as<double>(), (int)N, nc(), stream);
         CUDA_OK(cudaGetLastError());

@@ -108,11 +108,16 @@ int ibisgb_set_primitives(ibisgb_ctx* ctx, const double* T, const double* p, con
 int ibisgb_get_primitives(ibisgb_ctx* ctx, double* rho, double* p, double* T, double* e,
                           double* vx, double* vy, double* vz);
 
-/* Conserved state of the valid cells, N x n_conserved row-major. */
+/* Conserved state of the valid cells, N x n_conserved row-major.  Pinned host
+ * memory (mapped into the device's address space, as cudaHostAlloc memory is
+ * under unified addressing) is written in place by the layout kernel; other
+ * memory receives a copy of a device staging buffer. */
 int ibisgb_get_conserved(ibisgb_ctx* ctx, double* U);
 
 /* Replace the conserved state of the valid cells (N x n_conserved row-major,
- * host memory; pinned memory copies fastest); primitives and ghost cells follow
+ * host memory; pinned memory is read in place by the layout kernel, other memory
+ * is copied through a device staging buffer; U may be reused once the call
+ * returns from pinned memory); primitives and ghost cells follow
  * from conserved_to_primatives (primative_conserved_conversion.cpp:4-23).  The
  * state write of Jfnk::apply_update_ (src/solvers/solvers/jfnk.cpp:63-93) and
  * of a restart. */
