@@ -73,6 +73,22 @@ def dist_setup(args):
     return world, rank, local
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The job's time: the maximum of x over the ranks of the process group
+    (x itself with one process).  The replicas exchange nothing else."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(cells_per_rank, world, stages, steps, seconds):
+    """Mcell-updates/s of the whole job: every rank advances its own replica."""
+    return world * cells_per_rank * stages * steps / seconds / 1e6
+
+
 def measured_peak_hbm():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -408,12 +424,8 @@ def run_ours(args, world, rank, local):
         if dist:
             dist.barrier()
 
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def max_over_ranks_(x):
+        return max_over_ranks(x, dist, "cuda")
 
     # --- headline: mixed precision, device-resident state
     sim.set_primitives(*ic)
@@ -435,9 +447,9 @@ def run_ours(args, world, rank, local):
     with ClockSampler(local) as clk:
         st = sim.take_steps(args.steps, "mixed")
         barrier()
-    ms_mixed = max_over_ranks(st["device_ms"])
+    ms_mixed = max_over_ranks_(st["device_ms"])
     rho_mixed = sim.conserved()[:, 0].copy()
-    value = world * N * 3.0 * args.steps / (ms_mixed / 1e3) / 1e6
+    value = whole_job_rate(N, world, 3, args.steps, ms_mixed / 1e3)
 
     # --- plain FP64 path over the same steps from the same state, and its accuracy reference
     sim.set_primitives(*ic)
@@ -446,9 +458,9 @@ def run_ours(args, world, rank, local):
     barrier()
     st64 = sim.take_steps(args.steps, "f64")
     barrier()
-    ms_f64 = max_over_ranks(st64["device_ms"])
+    ms_f64 = max_over_ranks_(st64["device_ms"])
     rho_f64 = sim.conserved()[:, 0]
-    value_f64 = world * N * 3.0 * args.steps / (ms_f64 / 1e3) / 1e6
+    value_f64 = whole_job_rate(N, world, 3, args.steps, ms_f64 / 1e3)
     l2_err = float(np.linalg.norm(rho_mixed - rho_f64) / np.linalg.norm(rho_f64))
     max_err = float(np.abs(rho_mixed - rho_f64).max() / np.abs(rho_f64).max())
 
@@ -474,8 +486,8 @@ def run_ours(args, world, rank, local):
         sim.take_steps(1, "mixed")
         sim.conserved(out=host_out)
     barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_value = world * N * 3.0 * e2e_steps / e2e_s / 1e6
+    e2e_s = max_over_ranks_(time.perf_counter() - t0)
+    e2e_value = whole_job_rate(N, world, 3, e2e_steps, e2e_s)
 
     peak, peak_kind = measured_peak_hbm()
     stage_ms = ms_mixed / args.steps / 3.0
