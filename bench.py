@@ -98,6 +98,34 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def f64_flops_per_cell_update(n):
+    """FP64 operations per cell-update of the reference algorithm on the n^3
+    periodic box: its exact count (tests/golden/flop_counts.json, from the
+    restatement instantiated on a counting scalar) is A + B/n."""
+    with open(os.path.join(ROOT, "tests", "golden", "flop_counts.json")) as f:
+        fit = json.load(f)["flops_per_cell_update"]
+    return fit["A"] + fit["B"] / n
+
+
+def fp64_roofline(value_mcells, n, sm_mhz):
+    """The plain FP64 path against the FP64 pipe: algorithmic flops (the
+    reference algorithm's count) per second against 2 FP64 FMA lanes per SM per
+    clock (ncu's peak_sustained dfma rate on GB300) x 2 flops x SMs x the
+    sampled SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    flops = f64_flops_per_cell_update(n)
+    achieved = value_mcells * 1e6 * flops / 1e12
+    peak = 2 * 2 * sms * sm_mhz * 1e6 / 1e12
+    return {"bound": "fp64", "flops_per_cell_update": flops, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak,
+            "flops_source": "the reference algorithm (oracle restatement on a counting scalar, "
+                            "tests/golden/flop_counts.json); an FMA counts 2, a division or square root 1; "
+                            "the FP64 build does fewer (precomputed least-squares weights, one reciprocal per "
+                            "cell, two divisions per limited variable), so this is the reference-equivalent rate",
+            "peak_kind": f"2 FP64 FMA lanes/SM/clock x 2 flops x {sms} SMs x {sm_mhz:.0f} MHz (sampled)"}
+
+
 class ClockSampler:
     """nvidia-smi SM clock / throttle samples during the timed region."""
 
@@ -519,7 +547,8 @@ def run_ours(args, world, rank, local):
             "dtype": "f32 flux / f64 accumulate+update (mixed)", "data": "synthetic",
             "config": headline_config(n, world),
             "f64": {"value": value_f64, "ms_per_step": ms_f64 / args.steps,
-                    "mixed_speedup": value / value_f64},
+                    "mixed_speedup": value / value_f64,
+                    "fp64_roofline": fp64_roofline(value_f64, n, clk.summary()["sm_mhz"] or 2070.0)},
             "accuracy": {"rho_rel_l2_err_mixed_vs_f64": l2_err, "rho_rel_max_err_mixed_vs_f64": max_err,
                          "steps": args.warmup + args.steps},
             "kernel_ms": {k: round(v, 4) for k, v in kt.items()},

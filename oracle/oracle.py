@@ -61,6 +61,7 @@ def lib():
         L.orc_count_bad_cells.argtypes = [C.c_void_p]
         L.orc_rk_initialise.argtypes = [C.c_void_p]
         L.orc_rk_steps.argtypes = [C.c_void_p, C.c_int, _dp]
+        L.orc_count_step_flops.argtypes = [C.c_void_p, _lp]
         L.orc_get_conserved.argtypes = [C.c_void_p, _dp]
         L.orc_steady_initialise.argtypes = [C.c_void_p]
         L.orc_jvp.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int]
@@ -202,6 +203,15 @@ class Oracle:
         out = np.zeros(9)
         self._check(lib().orc_rk_steps(self.h, int(n), out))
         return dict(t=out[0], dt=out[1], stable_dt=out[2], norms=out[3:9])
+
+    def count_step_flops(self):
+        """Exact floating-point operation counts of one Runge-Kutta step (with its
+        estimate_dt) from the current initial state: the restatement instantiated
+        on a counting scalar.  Returns add, mul, div, sqrt, pow (arithmetic) and
+        other (abs/min/max/floor/copysign) totals over the grid."""
+        out = np.zeros(6, np.int64)
+        self._check(lib().orc_count_step_flops(self.h, out))
+        return dict(zip(("add", "mul", "div", "sqrt", "pow", "other"), (int(x) for x in out)))
 
     def conserved(self):
         out = np.zeros(self.N * self.nc)

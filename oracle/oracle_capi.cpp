@@ -446,6 +446,40 @@ int orc_cubic_spline(int n, const double* x, const double* y, int nq, const doub
     }
 }
 
+// Exact floating-point operation counts of one RungeKutta::take_step from the
+// real simulation's current primitive state, on a copy of it instantiated on
+// the counting scalar (one thread).  The step includes its estimate_dt.
+// out: additions (and subtractions), multiplications, divisions, square roots,
+// powers, and abs/min/max/floor/copysign, in that order.
+int orc_count_step_flops(void* hp, long long* out) {
+    Handle* h = (Handle*)hp;
+    GUARD_BEGIN
+    if (!h->sim) throw std::runtime_error("orc_count_step_flops: not a real-valued (kind 0) oracle");
+    const Sim<double>& src = *h->sim;
+    std::unique_ptr<Sim<Cnt>> s = build_sim<Cnt>(h->config, h->io);
+    s->init_rk(h->config.at("solver"));
+    for (size_t i = 0; i < src.grid.N; i++) {
+        s->fs.temp[i] = src.fs.temp[i]; s->fs.p[i] = src.fs.p[i]; s->fs.rho[i] = src.fs.rho[i];
+        s->fs.e[i] = src.fs.e[i]; s->fs.vx[i] = src.fs.vx[i]; s->fs.vy[i] = src.fs.vy[i];
+        s->fs.vz[i] = src.fs.vz[i];
+    }
+#ifdef _OPENMP
+    const int nt = omp_get_max_threads();
+    omp_set_num_threads(1);
+#endif
+    s->rk_initialise();
+    g_flops = FlopCounts{};
+    s->rk_take_step();
+    const FlopCounts c = g_flops;
+#ifdef _OPENMP
+    omp_set_num_threads(nt);
+#endif
+    const unsigned long long v[6] = {c.add, c.mul, c.div, c.sqrt, c.pow, c.other};
+    for (int q = 0; q < 6; q++) out[q] = (long long)v[q];
+    return 0;
+    GUARD_END(h, -1)
+}
+
 int orc_num_threads() {
 #ifdef _OPENMP
     return omp_get_max_threads();

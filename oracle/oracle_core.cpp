@@ -1657,7 +1657,16 @@ void lsq_gradient_real(const Grid<double>& g, const std::vector<double>& values,
     lsq_gradient(g, values, grad);
 }
 
+FlopCounts g_flops;
+
 template struct Grid<double>;
+template struct Grid<Cnt>;
+template struct FiniteVolume<Cnt>;
+template struct Sim<Cnt>;
+template std::unique_ptr<Sim<Cnt>> build_sim<Cnt>(const Json&, const GridIO&);
+template void conserved_to_primatives<Cnt>(const Conserved<Cnt>&, FlowStates<Cnt>&, const IdealGas&);
+template void primatives_to_conserved<Cnt>(Conserved<Cnt>&, const FlowStates<Cnt>&);
+template Norms l2_norms<Cnt>(const Conserved<Cnt>&);
 template struct Grid<Dual>;
 template struct FiniteVolume<double>;
 template struct FiniteVolume<Dual>;

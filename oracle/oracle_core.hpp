@@ -127,6 +127,52 @@ inline bool o_isnan(const Dual& d) { return std::isnan(d.re) || std::isnan(d.du)
 inline bool o_isinf(const Dual& d) { return std::isinf(d.re) || std::isinf(d.du); }
 
 // ---------------------------------------------------------------------------
+// Counting scalar: a double that counts the floating-point operations applied to
+// it, so that instantiating the templated restatement on it gives the exact
+// operation count of a residual evaluation or Runge-Kutta step (the plain FP64
+// path's FP64-issue roofline).  The counts are global: count with one thread.
+// abs, min, max, floor and copysign are counted apart from the arithmetic.
+// ---------------------------------------------------------------------------
+struct FlopCounts {
+    unsigned long long add = 0, mul = 0, div = 0, sqrt = 0, pow = 0, other = 0;
+};
+extern FlopCounts g_flops;
+struct Cnt {
+    double v = 0.0;
+    Cnt() = default;
+    Cnt(double x) : v(x) {}
+    Cnt& operator=(double x) { v = x; return *this; }
+    Cnt operator-() const { return Cnt(-v); }
+    Cnt& operator+=(const Cnt& o) { g_flops.add++; v += o.v; return *this; }
+    Cnt& operator-=(const Cnt& o) { g_flops.add++; v -= o.v; return *this; }
+    Cnt& operator*=(const Cnt& o) { g_flops.mul++; v *= o.v; return *this; }
+    Cnt& operator/=(const Cnt& o) { g_flops.div++; v /= o.v; return *this; }
+};
+inline Cnt operator+(const Cnt& a, const Cnt& b) { g_flops.add++; return Cnt(a.v + b.v); }
+inline Cnt operator-(const Cnt& a, const Cnt& b) { g_flops.add++; return Cnt(a.v - b.v); }
+inline Cnt operator*(const Cnt& a, const Cnt& b) { g_flops.mul++; return Cnt(a.v * b.v); }
+inline Cnt operator/(const Cnt& a, const Cnt& b) { g_flops.div++; return Cnt(a.v / b.v); }
+inline bool operator<(const Cnt& a, const Cnt& b) { return a.v < b.v; }
+inline bool operator>(const Cnt& a, const Cnt& b) { return a.v > b.v; }
+inline bool operator<=(const Cnt& a, const Cnt& b) { return a.v <= b.v; }
+inline bool operator>=(const Cnt& a, const Cnt& b) { return a.v >= b.v; }
+inline bool operator==(const Cnt& a, const Cnt& b) { return a.v == b.v; }
+inline bool operator!=(const Cnt& a, const Cnt& b) { return a.v != b.v; }
+inline double real_part(const Cnt& x) { return x.v; }
+inline double dual_part(const Cnt&) { return 0.0; }
+inline void set_real(Cnt& x, double v) { x.v = v; }
+inline void set_dual(Cnt&, double) {}
+inline Cnt o_sqrt(const Cnt& x) { g_flops.sqrt++; return Cnt(std::sqrt(x.v)); }
+inline Cnt o_pow(const Cnt& b, const Cnt& p) { g_flops.pow++; return Cnt(std::pow(b.v, p.v)); }
+inline Cnt o_abs(const Cnt& x) { g_flops.other++; return Cnt(std::fabs(x.v)); }
+inline Cnt o_min(const Cnt& a, const Cnt& b) { g_flops.other++; return (b.v < a.v) ? b : a; }
+inline Cnt o_max(const Cnt& a, const Cnt& b) { g_flops.other++; return (a.v < b.v) ? b : a; }
+inline Cnt o_floor(const Cnt& x) { g_flops.other++; return Cnt(std::floor(x.v)); }
+inline Cnt o_copysign(const Cnt& m, const Cnt& s) { g_flops.other++; return Cnt(std::copysign(m.v, s.v)); }
+inline bool o_isnan(const Cnt& x) { return std::isnan(x.v); }
+inline bool o_isinf(const Cnt& x) { return std::isinf(x.v); }
+
+// ---------------------------------------------------------------------------
 // Grid input (src/grid/grid/grid_io.{h,cpp})
 // ---------------------------------------------------------------------------
 enum class ElemType { Line, Tri, Tetra, Quad, Hex, Wedge, Pyramid };

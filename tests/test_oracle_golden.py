@@ -136,3 +136,26 @@ def test_cubic_spline_is_a_natural_spline():
         assert abs(2 * d1 - d2) < 1e-3 * scale, (d1, d2)
     with pytest.raises(ValueError):
         cubic_spline([0, 1, 2], [0, 1, 2], [0.5])
+
+
+def test_flop_counts_fixture_matches_the_counting_oracle():
+    """tests/golden/flop_counts.json (the reference algorithm's exact operation
+    counts per ssp-rk3 step on the periodic box, used by bench.py for the FP64
+    path's roofline) is what the oracle on its counting scalar gives, and the
+    per cell-update count follows A + B/n."""
+    import json
+    import os
+
+    from ibis_gb300 import grids
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "tests", "golden", "flop_counts.json")) as f:
+        fx = json.load(f)
+    A, B = fx["flops_per_cell_update"]["A"], fx["flops_per_cell_update"]["B"]
+    for n in (8, 12):
+        g, c = grids.box_case(n)
+        o = Oracle(c, g)
+        o.set_initial_condition(*grids.box_initial_condition(n, c["gas_model"], seed=0))
+        got = o.count_step_flops()
+        assert got == fx["counts_per_step"][str(n)]
+        arith = sum(got[k] for k in ("add", "mul", "div", "sqrt", "pow"))
+        assert arith / (3 * n ** 3) == pytest.approx(A + B / n, rel=1e-12)
