@@ -543,7 +543,7 @@ def ramp_ensemble(n_cases=64, seed=0, smallest=(64, 32), largest=(512, 256), mac
 
 
 def ramp_bump_case(ni=512, nj=256, mach=2.0, T=300.0, p=101325.0, angle_deg=15.0, bumps=None, **kw):
-    """BASELINE config 4's geometry: the compression ramp of ramp_case with its
+    """The steady-state (JFNK and adjoint) case's geometry: the compression ramp of ramp_case with its
     surface perturbed by Hicks-Henne bumps (ramp_2d_bumps).  Returns (grid, config, inflow)."""
     gas = ideal_gas(287.0)
     inflow = mach_state(gas, mach, T, p)

@@ -1,5 +1,5 @@
 """Discrete-adjoint gradient of the integrated ramp pressure force (the Hicks-
-Henne ramp of BASELINE config 4, reduced grid) with respect to the inflow Mach
+Henne ramp of the 512 x 256 steady-state case, on a reduced grid) with respect to the inflow Mach
 number and two bump amplitudes, against central differences of the force
 between steady states re-converged at perturbed parameters (relative 1e-5).
 A 10-degree ramp with second-order (unlimited) reconstruction on a grid small
