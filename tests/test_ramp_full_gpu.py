@@ -5,9 +5,9 @@ the uniform inflow state (the reference's RungeKutta defaults, dt unclipped).
 
 * F64_EXACT (the reference's operation order, no FMA): the final state and time
   are the oracle's bit for bit after all 2000 steps.
-* F64 (FMA contraction) and MIXED: relative L2 error of each conserved component
-  against the oracle, <= 1e-9 and <= 5e-5 respectively.  (The mixed build
-  measures 2.2e-5 in density here, against 1.5e-8 on the 256^3 box after 33
+* F64 (FMA contraction): relative L2 error of each conserved component against
+  the oracle <= 1e-12 (measured 7e-14 to 9e-14).  MIXED: density <= 5e-5, every
+  component <= 1e-3 (measured 2.2e-5 to 2.7e-5; density 2.2e-5 here, against 1.5e-8 on the 256^3 box after 33
   steps: with the oblique shock formed, float reconstruction moves Barth-
   Jespersen's min/max decisions in the shock cells.)"""
 import numpy as np
@@ -48,11 +48,12 @@ def test_exact_build_matches_the_oracle_bit_for_bit(ramp):
     assert np.array_equal(U, U_ref), float(np.abs(U - U_ref).max())
 
 
-@pytest.mark.parametrize("precision,tol", [("f64", 1e-9), ("mixed", 5e-5)])
-def test_fast_builds_stay_close_to_the_oracle(ramp, precision, tol):
+@pytest.mark.parametrize("precision,tol_rho,tol", [("f64", 1e-12, 1e-12), ("mixed", 5e-5, 1e-3)])
+def test_fast_builds_stay_close_to_the_oracle(ramp, precision, tol_rho, tol):
     g, c, ic, o, U_ref = ramp
     st, U = _run(g, c, ic, precision)
     assert st["t"] == pytest.approx(o["t"], rel=tol)
-    for q in range(U.shape[1]):
-        err = np.linalg.norm(U[:, q] - U_ref[:, q]) / np.linalg.norm(U_ref[:, q])
-        assert err <= tol, (q, err)
+    errs = [float(np.linalg.norm(U[:, q] - U_ref[:, q]) / np.linalg.norm(U_ref[:, q])) for q in range(U.shape[1])]
+    print(precision, "relative L2 error per conserved component:", errs)
+    assert errs[0] <= tol_rho, errs
+    assert max(errs) <= tol, errs
