@@ -6,10 +6,11 @@ the uniform inflow state (the reference's RungeKutta defaults, dt unclipped).
 * F64_EXACT (the reference's operation order, no FMA): the final state and time
   are the oracle's bit for bit after all 2000 steps.
 * F64 (FMA contraction): relative L2 error of each conserved component against
-  the oracle <= 1e-12 (measured 7e-14 to 9e-14).  MIXED: density <= 5e-5, every
-  component <= 1e-3 (measured 2.2e-5 to 2.7e-5; density 2.2e-5 here, against 1.5e-8 on the 256^3 box after 33
-  steps: with the oblique shock formed, float reconstruction moves Barth-
-  Jespersen's min/max decisions in the shock cells.)"""
+  the oracle <= 1e-12 (measured 7e-14 to 9e-14).
+* MIXED: density <= 5e-5 and every component <= 1e-3 (measured 2.2e-5 to
+  2.7e-5).  On the 256^3 box the mixed build keeps 1.5e-8 after 33 steps; here,
+  with the oblique shock formed, float reconstruction moves Barth-Jespersen's
+  min/max decisions in the shock cells."""
 import numpy as np
 import pytest
 
