@@ -1,0 +1,105 @@
+"""The oracle against an exact solution: Mach 3 flow over a 15-degree expansion
+corner, the reference's exact-solution case
+(tests/exact_solutions/prandtl_meyer_expansion/job.py: AUSMDV, second-order
+unlimited reconstruction, ssp-rk3 at CFL 2 for three flow-through times, ideal
+air, rho = 1.225 kg/m^3 and T = 300 K upstream).  Downstream of the centred
+expansion fan the flow is uniform, turned by 15 degrees, at the Mach number
+whose Prandtl-Meyer angle exceeds the upstream one by 15 degrees, with
+temperature, pressure and density from the isentropic relations.
+
+The corner is a true 15-degree turn on a structured quad grid written here (the
+reference meshes the same domain with gmsh, which is absent; its wall drops by
+(length - x0) sin 15 deg instead of tan 15 deg).  The analytic state uses the
+standard isentropic relations p2/p1 = (T2/T1)^(g/(g-1)), rho2/rho1 =
+(T2/T1)^(1/(g-1)).  The second-order error falls about 4x when the cells are
+halved.  The GPU builds equal the oracle (tests/test_residual_gpu.py), so they
+inherit this check."""
+import math
+
+import numpy as np
+import pytest
+
+from ibis_gb300 import grids
+from oracle.oracle import Oracle
+
+
+def prandtl_meyer(M, g):
+    a = math.sqrt((g + 1) / (g - 1))
+    return a * math.atan(math.sqrt((g - 1) / (g + 1) * (M * M - 1))) - math.atan(math.sqrt(M * M - 1))
+
+
+def mach_after_turn(M1, theta, g):
+    """The Mach number whose Prandtl-Meyer angle is nu(M1) + theta (bisection)."""
+    target = prandtl_meyer(M1, g) + theta
+    lo, hi = M1, 50.0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (mid, hi) if prandtl_meyer(mid, g) < target else (lo, mid)
+    return 0.5 * (lo + hi)
+
+
+def expansion_corner(h):
+    """Run the corner to t = 3 L / u on cells of size h; returns the mean relative
+    errors of M, T, p, rho and the mean flow angle over the uniform region
+    downstream of the fan (0.5 <= x <= 0.85, between 0.02 m above the wall and
+    y = -0.05, clear of the fan's last characteristic)."""
+    th = math.radians(15.0)
+    L, x0, H = 0.9, 0.05, 0.6
+    ni, nj = int(round(L / h)), int(round(H / h))
+    x = np.linspace(0.0, L, ni + 1)
+    yw = np.where(x <= x0, 0.0, -(x - x0) * math.tan(th))
+    X = np.repeat(x[:, None], nj + 1, 1)
+    Y = yw[:, None] + (H - yw[:, None]) * np.linspace(0.0, 1.0, nj + 1)[None, :]
+    g = grids.structured_2d(X, Y, bottom_tags=lambda i: "wall")
+    gas = grids.ideal_gas(287.0)
+    gm = gas["gamma"]
+    M1, T1, rho1 = 3.0, 300.0, 1.225
+    p1 = rho1 * gas["R"] * T1
+    inflow = grids.mach_state(gas, M1, T1, p1)
+    b = {"west": grids.supersonic_inflow(inflow), "east": grids.supersonic_outflow(),
+         "north": grids.supersonic_outflow(), "wall": grids.slip_wall()}
+    tmax = 3 * 1.0 / inflow["vx"]
+    c = grids.make_config(2, b, gas=gas, flux="ausmdv", order=2, limiter="unlimited",
+                          solver=grids.runge_kutta(cfl=2.0, max_step=100000, max_time=tmax))
+    o = Oracle(c, g)
+    n = g.num_cells
+    o.set_initial_condition(np.full(n, T1), np.full(n, p1), np.full(n, inflow["vx"]), np.zeros(n))
+    o.rk_initialise()
+    t = 0.0
+    for _ in range(400):
+        t = o.rk_steps(50)["t"]
+        if t >= tmax * (1 - 1e-12):
+            break
+    assert t >= tmax * (1 - 1e-12) and o.count_bad_cells() == 0
+    M2 = mach_after_turn(M1, th, gm)
+    k = (1 + 0.5 * (gm - 1) * M1 ** 2) / (1 + 0.5 * (gm - 1) * M2 ** 2)
+    exact = {"M": M2, "T": T1 * k, "p": p1 * k ** (gm / (gm - 1)), "rho": rho1 * k ** (1 / (gm - 1))}
+    pr = o.primitives()[:, :o.N]  # rho, p, T, e, vx, vy, vz
+    cen = o.geometry()["centroid"]
+    cx, cy = cen[0][:o.N], cen[1][:o.N]
+    sel = (cx >= 0.5) & (cx <= 0.85) & (cy <= -0.05) & (cy >= -(cx - x0) * math.tan(th) + 0.02)
+    rho, p, T, vx, vy = pr[0][sel], pr[1][sel], pr[2][sel], pr[4][sel], pr[5][sel]
+    got = {"M": np.hypot(vx, vy) / np.sqrt(gm * gas["R"] * T), "T": T, "p": p, "rho": rho}
+    err = {q: float(np.mean(np.abs(got[q] / exact[q] - 1))) for q in exact}
+    return err, float(np.degrees(np.mean(np.arctan2(vy, vx)))), int(sel.sum())
+
+
+@pytest.fixture(scope="module")
+def coarse():
+    return expansion_corner(0.01)
+
+
+def test_expanded_state_matches_prandtl_meyer(coarse):
+    err, angle, cells = coarse
+    assert cells > 200
+    for q, e in err.items():
+        assert e <= 5e-3, (q, err)
+    assert angle == pytest.approx(-15.0, abs=0.05)
+
+
+def test_error_falls_at_second_order(coarse):
+    err, _, _ = coarse
+    fine, angle, _ = expansion_corner(0.005)
+    assert fine["p"] <= err["p"] / 3.0, (err, fine)
+    assert max(fine.values()) <= 1e-3, fine
+    assert angle == pytest.approx(-15.0, abs=0.01)
