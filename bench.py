@@ -98,6 +98,35 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+# The mixed RK stage in use, its name in the roofline block and the committed ncu
+# summary whose stage traffic (traffic_bytes_per_stage_<n>) belongs to it.
+STAGE_PATHS = {
+    "three_kernel": ("rk_stage (recon + face + update kernels of one stage)", "rk_stage_box128_mixed_full.md"),
+    "march": ("k_march_stage (plane-marching fused stage, TMA-staged planes)", "march_stage_box128.md"),
+    "tile": ("k_fused_stage (tile-fused stage)", None),
+    "cell_flux": ("rk_stage (recon + per-cell flux update kernels of one stage)", None),
+}
+
+
+def stage_path(fused_enabled, march, cell_flux_enabled):
+    if fused_enabled:
+        return "march" if march else "tile"
+    return "cell_flux" if cell_flux_enabled else "three_kernel"
+
+
+def stage_traffic(summary, n):
+    """DRAM bytes of one stage at n^3 from a committed ncu summary, or None."""
+    if not summary:
+        return None
+    path = os.path.join(ROOT, "profiles", summary)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith(f"traffic_bytes_per_stage_{n}:"):
+            return float(line.split(":")[1].split()[0])
+    return None
+
+
 def f64_flops_per_cell_update(n):
     """FP64 operations per cell-update of the reference algorithm on the n^3
     periodic box: its exact count (tests/golden/flop_counts.json, from the
@@ -520,12 +549,9 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = measured_peak_hbm()
     stage_ms = ms_mixed / args.steps / 3.0
     achieved = B_ALG_3D["mixed"] * N / (stage_ms / 1e3) / 1e9
-    traffic = None  # DRAM bytes of one stage (recon + face + update) from the committed ncu summary
-    tfile = os.path.join(ROOT, "profiles", "rk_stage_box128_mixed_full.md")
-    if os.path.exists(tfile):
-        for line in open(tfile):
-            if line.startswith(f"traffic_bytes_per_stage_{n}:"):
-                traffic = float(line.split(":")[1].split()[0])
+    # DRAM bytes of one stage of the path in use, from its committed ncu summary
+    stage_kernel, summary = STAGE_PATHS[stage_path(fused["enabled"], fkind["march"], cellf["enabled"])]
+    traffic = stage_traffic(summary, n)
 
     batch = batch_measure(args, barrier) if args.batch_cases > 0 else None
     plate = plate_measure(args) if args.plate_steps > 0 and rank == 0 else None
@@ -561,12 +587,12 @@ def run_ours(args, world, rank, local):
             "sweep": sweep,
             "plate": plate,
             "jfnk": jfnk,
-            "roofline": {"bound": "hbm", "kernel": "rk_stage (recon + face + update kernels of one stage)",
+            "roofline": {"bound": "hbm", "kernel": stage_kernel,
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "bytes_per_cell_update": B_ALG_3D["mixed"],
                          "traffic": traffic, "traffic_per_cell_update": traffic / N if traffic else None,
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage "
-                                           "at 128^3, scaled by 8 (profiles/rk_stage_box128_mixed_full.md)"},
+                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage "
+                                            f"at 128^3, scaled by 8 (profiles/{summary})") if traffic else None},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 8 * nc * N,
                     "d2h_bytes_per_step": 8 * nc * N, "steps": e2e_steps},

@@ -79,3 +79,21 @@ def test_reference_arm_runs_on_rank_zero_only():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_roofline_block_follows_the_stage_path_in_use():
+    """The roofline names the RK stage the autotuner chose and takes that stage's
+    DRAM traffic from its own committed ncu summary."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.stage_path(False, False, False) == "three_kernel"
+    assert bench.stage_path(False, True, True) == "cell_flux"
+    assert bench.stage_path(True, True, False) == "march"
+    assert bench.stage_path(True, False, False) == "tile"
+    k3, s3 = bench.STAGE_PATHS["three_kernel"]
+    km, sm = bench.STAGE_PATHS["march"]
+    t3, tm = bench.stage_traffic(s3, 256), bench.stage_traffic(sm, 256)
+    assert t3 == 8 * bench.stage_traffic(s3, 128) and tm == 8 * bench.stage_traffic(sm, 128)
+    n = 256 ** 3
+    assert 700 < t3 / n < 900 and 250 < tm / n < 320  # B per cell-update: three kernels vs one marching kernel
+    assert bench.stage_traffic(s3, 64) is None and bench.stage_traffic(None, 256) is None
