@@ -2,6 +2,7 @@
 every grid the structured generators write qualifies, batches of them too,
 and anything else is refused with a reason."""
 import numpy as np
+import pytest
 
 from ibis_gb300 import Batch, Simulation, grids
 from tests.cases import case
@@ -58,3 +59,22 @@ def test_plane_marching_kernel_eligibility():
     assert not k["march_eligible"] and "three-dimensional" in k["reason"]
     g, c, _ = case("plate")
     assert "viscous" in Simulation(c, g).fused_kind()["reason"]
+
+
+def test_fused_kind_rejects_bad_arguments_on_the_host():
+    """ibisgb_set_fused_kind checks its arguments and the eligibility of the
+    plane-marching kernel before touching a GPU."""
+    from ibis_gb300._lib import IbisgbError
+    g, c, _ = case("ramp")
+    sim = Simulation(c, g)
+    for kind, planes in ((2, 0), (-2, 0), (0, -1)):
+        with pytest.raises(IbisgbError) as e:
+            sim.set_fused_kind(kind, planes)
+        assert e.value.code == -5, (kind, planes)
+    with pytest.raises(IbisgbError) as e:
+        sim.set_fused_kind(1, 0)  # a 2-D grid: the plane-marching kernel does not apply
+    assert e.value.code == -5 and "three-dimensional" in str(e.value)
+    g, c, _ = case("box", n=6)
+    with pytest.raises(IbisgbError) as e:
+        Simulation(c, g).set_fused_kind(1, 16)
+    assert "multiples of 4" in str(e.value)
