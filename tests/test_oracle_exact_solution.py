@@ -21,6 +21,14 @@
    theta-beta-M relation and the normal-shock jumps of the Mach number normal to
    the shock.  At 128 x 64 the mean errors are 0.07-0.11%.
 
+3. Sod's shock tube (left rho = 1, p = 1; right rho = 0.125, p = 0.1; at rest,
+   gamma = 1.4) to t = 0.2 with the default numerics, one row of cells between
+   slip walls: against the exact Riemann solution (Toro's iterative solver for
+   the star pressure, written here from the published method), the L1 errors
+   fall as the cells shrink (order about 0.8 with the discontinuities) and the
+   star state p* = 0.30313, u* = 0.92745 is reproduced between the rarefaction
+   and the contact.
+
 The GPU builds equal the oracle (tests/test_residual_gpu.py,
 tests/test_ramp_full_gpu.py), so they inherit these checks."""
 import math
@@ -160,3 +168,93 @@ def test_compression_ramp_matches_the_oblique_shock():
     for q in exact:
         assert np.mean(np.abs(got[q] / exact[q] - 1)) <= 3e-3, q
     assert float(np.degrees(np.mean(np.arctan2(vy, vx)))) == pytest.approx(15.0, abs=0.02)
+
+
+GAMMA = 1.4
+
+
+def _f_side(p, rk, pk, ak):
+    """Toro's pressure function of one side: a shock for p > pk, a rarefaction otherwise."""
+    if p > pk:
+        A, B = 2 / ((GAMMA + 1) * rk), (GAMMA - 1) / (GAMMA + 1) * pk
+        return (p - pk) * math.sqrt(A / (p + B))
+    return 2 * ak / (GAMMA - 1) * ((p / pk) ** ((GAMMA - 1) / (2 * GAMMA)) - 1)
+
+
+def riemann_star(left, right):
+    """Star pressure and velocity: the root of f_L(p) + f_R(p) + (u_R - u_L), monotone in p."""
+    (rl, ul, pl), (rr, ur, pr) = left, right
+    al, ar = math.sqrt(GAMMA * pl / rl), math.sqrt(GAMMA * pr / rr)
+    lo, hi = 1e-12, 10 * max(pl, pr)
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (lo, mid) if _f_side(mid, rl, pl, al) + _f_side(mid, rr, pr, ar) + (ur - ul) > 0 else (mid, hi)
+    ps = 0.5 * (lo + hi)
+    return ps, 0.5 * (ul + ur) + 0.5 * (_f_side(ps, rr, pr, ar) - _f_side(ps, rl, pl, al))
+
+
+def riemann_exact(left, right, s):
+    """Exact solution (rho, u, p) of the Riemann problem at x/t = s (Toro, ch. 4)."""
+    (rl, ul, pl), (rr, ur, pr) = left, right
+    al, ar = math.sqrt(GAMMA * pl / rl), math.sqrt(GAMMA * pr / rr)
+    ps, us = riemann_star(left, right)
+    g1, g2 = (GAMMA - 1) / (GAMMA + 1), (GAMMA - 1) / (2 * GAMMA)
+    if s <= us:
+        if ps > pl:  # left shock
+            S = ul - al * math.sqrt((GAMMA + 1) / (2 * GAMMA) * ps / pl + g2)
+            return (rl, ul, pl) if s < S else (rl * (ps / pl + g1) / (g1 * ps / pl + 1), us, ps)
+        if s < ul - al:
+            return rl, ul, pl
+        if s > us - al * (ps / pl) ** g2:
+            return rl * (ps / pl) ** (1 / GAMMA), us, ps
+        u = 2 / (GAMMA + 1) * (al + (GAMMA - 1) / 2 * ul + s)
+        c = 2 / (GAMMA + 1) * (al + (GAMMA - 1) / 2 * (ul - s))
+        return rl * (c / al) ** (2 / (GAMMA - 1)), u, pl * (c / al) ** (2 * GAMMA / (GAMMA - 1))
+    if ps > pr:  # right shock
+        S = ur + ar * math.sqrt((GAMMA + 1) / (2 * GAMMA) * ps / pr + g2)
+        return (rr, ur, pr) if s > S else (rr * (ps / pr + g1) / (g1 * ps / pr + 1), us, ps)
+    if s > ur + ar:
+        return rr, ur, pr
+    if s < us + ar * (ps / pr) ** g2:
+        return rr * (ps / pr) ** (1 / GAMMA), us, ps
+    u = 2 / (GAMMA + 1) * (-ar + (GAMMA - 1) / 2 * ur + s)
+    c = 2 / (GAMMA + 1) * (ar - (GAMMA - 1) / 2 * (ur - s))
+    return rr * (c / ar) ** (2 / (GAMMA - 1)), u, pr * (c / ar) ** (2 * GAMMA / (GAMMA - 1))
+
+
+def sod(ni, tend=0.2):
+    x = np.linspace(0.0, 1.0, ni + 1)
+    X = np.repeat(x[:, None], 2, 1)
+    Y = np.repeat(np.array([0.0, 1.0 / ni])[None, :], ni + 1, 0)
+    g = grids.structured_2d(X, Y)
+    b = {"west": grids.supersonic_outflow(), "east": grids.supersonic_outflow(),
+         "south": grids.slip_wall(), "north": grids.slip_wall()}
+    c = grids.make_config(2, b, gas=grids.ideal_gas(1.0),
+                          solver=grids.runge_kutta(cfl=0.5, max_step=100000, max_time=tend))
+    o = Oracle(c, g)
+    xc = 0.5 * (x[1:] + x[:-1])
+    rho, p = np.where(xc < 0.5, 1.0, 0.125), np.where(xc < 0.5, 1.0, 0.1)
+    o.set_initial_condition(p / rho, p, np.zeros(ni), np.zeros(ni))  # R = 1: T = p / rho
+    o.rk_initialise()
+    t = 0.0
+    for _ in range(1000):
+        t = o.rk_steps(20)["t"]
+        if t >= tend * (1 - 1e-12):
+            break
+    assert t == pytest.approx(tend, rel=1e-12) and o.count_bad_cells() == 0
+    ex = np.array([riemann_exact((1.0, 0.0, 1.0), (0.125, 0.0, 0.1), (xx - 0.5) / t) for xx in xc])
+    pr = o.primitives()[:, :o.N]  # rho, p, T, e, vx, vy, vz
+    l1 = {q: float(np.mean(np.abs(pr[k] - ex[:, j]))) for q, k, j in (("rho", 0, 0), ("u", 4, 1), ("p", 1, 2))}
+    star = (xc > 0.55) & (xc < 0.65)  # between the rarefaction's tail (0.486) and the contact (0.685)
+    return l1, float(pr[1][star].mean()), float(pr[4][star].mean())
+
+
+def test_sod_shock_tube_matches_the_exact_riemann_solution():
+    ps, us = riemann_star((1.0, 0.0, 1.0), (0.125, 0.0, 0.1))
+    assert ps == pytest.approx(0.30313, abs=1e-5) and us == pytest.approx(0.92745, abs=1e-5)
+    coarse, _, _ = sod(200)
+    fine, p_star, u_star = sod(400)
+    for q in ("rho", "u", "p"):
+        assert fine[q] <= 3e-3, fine
+        assert fine[q] <= coarse[q] / 1.5, (q, coarse, fine)
+    assert p_star == pytest.approx(ps, rel=2e-3) and u_star == pytest.approx(us, rel=2e-3)
