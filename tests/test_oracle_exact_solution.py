@@ -231,7 +231,7 @@ def riemann_exact(left, right, s):
     return rr * (c / ar) ** (2 / (GAMMA - 1)), u, pr * (c / ar) ** (2 * GAMMA / (GAMMA - 1))
 
 
-def sod(ni, tend=0.2):
+def sod(ni, tend=0.2, **kw):
     x = np.linspace(0.0, 1.0, ni + 1)
     X = np.repeat(x[:, None], 2, 1)
     Y = np.repeat(np.array([0.0, 1.0 / ni])[None, :], ni + 1, 0)
@@ -239,7 +239,7 @@ def sod(ni, tend=0.2):
     b = {"west": grids.supersonic_outflow(), "east": grids.supersonic_outflow(),
          "south": grids.slip_wall(), "north": grids.slip_wall()}
     c = grids.make_config(2, b, gas=grids.ideal_gas(1.0),
-                          solver=grids.runge_kutta(cfl=0.5, max_step=100000, max_time=tend))
+                          solver=grids.runge_kutta(cfl=0.5, max_step=100000, max_time=tend), **kw)
     o = Oracle(c, g)
     xc = 0.5 * (x[1:] + x[:-1])
     rho, p = np.where(xc < 0.5, 1.0, 0.125), np.where(xc < 0.5, 1.0, 0.1)
@@ -267,6 +267,19 @@ def test_sod_shock_tube_matches_the_exact_riemann_solution():
         assert fine[q] <= 3e-3, fine
         assert fine[q] <= coarse[q] / 1.5, (q, coarse, fine)
     assert p_star == pytest.approx(ps, rel=2e-3) and u_star == pytest.approx(us, rel=2e-3)
+
+
+@pytest.mark.parametrize("kw", [{"flux": "ausmdv"}, {"flux": "ldfss2"}, {"flux": "rusanov"}, {"thermo": "rho_p"},
+                                {"thermo": "rho_T"}, {"thermo": "p_T"}],
+                         ids=lambda kw: "-".join(f"{k}={v}" for k, v in kw.items()))
+def test_sod_shock_tube_with_every_flux_and_thermo_pair(kw):
+    """Every flux calculator and interpolated thermodynamic pair reproduces the exact
+    Riemann solution (at 400 cells the L1 density errors are 1.3e-3, Rusanov, the
+    most diffusive, 2.0e-3)."""
+    l1, p_star, u_star = sod(400, **kw)
+    assert l1["rho"] <= 2.5e-3 and l1["u"] <= 4e-3 and l1["p"] <= 1.6e-3, l1
+    ps, us = riemann_star((1.0, 0.0, 1.0), (0.125, 0.0, 0.1))
+    assert p_star == pytest.approx(ps, rel=5e-3) and u_star == pytest.approx(us, rel=5e-3)
 
 
 def extruded_ramp(ni, nj, **kw):
