@@ -38,6 +38,16 @@
    sign that rounding picked, and the limiter drops the cell to first order in
    one layer and not the other (v_z reaches 5e-4 of |v| in the shock cells).
 
+5. The structure of a normal shock in air (Mach 2 at 300 K, Sutherland
+   viscosity, Prandtl number 3/4) on one row of cells between slip walls, with
+   the Rankine-Hugoniot downstream pressure at a subsonic outflow.  At Pr = 3/4
+   the total enthalpy is constant through the shock (Becker's integral, for any
+   mu(T)), and the exact Navier-Stokes profile follows from the momentum
+   equation (4/3) mu(T) du/dx = m (u - u1) + p - p1, with T and p functions of u,
+   integrated here.  This checks the viscous stress, the heat flux and the
+   Sutherland transport.  The velocity error within five shock thicknesses is
+   1.0% of the jump at 3 cells per thickness and 0.39% at 5.
+
 The GPU builds equal the oracle (tests/test_residual_gpu.py,
 tests/test_ramp_full_gpu.py), so they inherit these checks."""
 import math
@@ -325,3 +335,75 @@ def test_extruded_ramp_in_3d_matches_the_oblique_shock():
 def test_extruded_ramp_keeps_z_symmetry_at_first_order():
     pr, _, _, inf = extruded_ramp(32, 16, order=1)
     assert np.abs(pr[6]).max() <= 1e-12 * inf["vx"]
+
+
+def viscous_shock(cells_per_thickness_x40):
+    """The Mach 2 normal shock on 40 exact shock thicknesses, run for one
+    flow-through time from the Rankine-Hugoniot step; returns the largest
+    velocity error within five thicknesses of the shock (a fraction of the
+    jump), the shock position (a fraction of the domain) and the outflow
+    temperature with its Rankine-Hugoniot value."""
+    integrate = pytest.importorskip("scipy.integrate")
+    R, g = 287.0, 1.4
+    cp = g * R / (g - 1)
+    mu0, T0, Ts = 1.716e-5, 273.0, 110.0
+    mu = lambda T: mu0 * (T / T0) ** 1.5 * (T0 + Ts) / (T + Ts)  # noqa: E731  (Sutherland)
+    M1, T1, p1 = 2.0, 300.0, 101325.0
+    rho1 = p1 / (R * T1)
+    u1 = M1 * math.sqrt(g * R * T1)
+    p2 = p1 * (1 + 2 * g / (g + 1) * (M1 ** 2 - 1))
+    r21 = (g + 1) * M1 ** 2 / ((g - 1) * M1 ** 2 + 2)
+    u2, T2 = u1 / r21, p2 / (rho1 * r21 * R)
+    m, h0 = rho1 * u1, cp * T1 + 0.5 * u1 ** 2
+    Tu = lambda u: (h0 - 0.5 * u * u) / cp  # noqa: E731  (constant total enthalpy)
+
+    def dudx(x, y):
+        u = y[0]
+        return [(m * (u - u1) + m * R * Tu(u) / u - p1) * 3.0 / (4.0 * mu(Tu(u)))]
+
+    um = 0.5 * (u1 + u2)
+    fw = integrate.solve_ivp(dudx, [0, 5e-6], [um], rtol=1e-10, atol=1e-12, dense_output=True, max_step=1e-9)
+    bw = integrate.solve_ivp(dudx, [0, -5e-6], [um], rtol=1e-10, atol=1e-12, dense_output=True, max_step=1e-9)
+
+    def u_exact(x):
+        return np.where(x >= 0, fw.sol(np.clip(x, 0, 5e-6))[0], bw.sol(np.clip(x, -5e-6, 0))[0])
+
+    xs = np.linspace(-1e-6, 1e-6, 2001)
+    delta = (u1 - u2) / np.abs(np.gradient(u_exact(xs), xs)).max()  # maximum-slope thickness
+    L, ni = 40 * delta, cells_per_thickness_x40
+    x = np.linspace(0.0, L, ni + 1)
+    X = np.repeat(x[:, None], 2, 1)
+    Y = np.repeat(np.array([0.0, L / ni])[None, :], ni + 1, 0)
+    gas = grids.ideal_gas(R)
+    b = {"west": grids.supersonic_inflow(grids.flow_state(gas, T1, p1, u1, 0.0)), "east": grids.subsonic_outflow(p2),
+         "south": grids.slip_wall(), "north": grids.slip_wall()}
+    tmax = L / u2
+    c = grids.make_config(2, b, gas=gas, viscous=True, Pr=0.75,
+                          solver=grids.runge_kutta(cfl=0.5, max_step=10_000_000, max_time=tmax))
+    o = Oracle(c, grids.structured_2d(X, Y))
+    xc = 0.5 * (x[1:] + x[:-1])
+    up = xc < 0.5 * L
+    o.set_initial_condition(np.where(up, T1, T2), np.where(up, p1, p2), np.where(up, u1, u2), np.zeros(ni))
+    o.rk_initialise()
+    t = 0.0
+    for _ in range(2000):
+        t = o.rk_steps(200)["t"]
+        if t >= tmax * (1 - 1e-12):
+            break
+    assert t >= tmax * (1 - 1e-12) and o.count_bad_cells() == 0
+    pr = o.primitives()[:, :o.N]
+    u = pr[4]
+    k = int(np.argmax(u < um))
+    xm = xc[k - 1] + (um - u[k - 1]) * (xc[k] - xc[k - 1]) / (u[k] - u[k - 1])
+    inner = np.abs(xc - xm) < 5 * delta
+    err = float(np.abs(u - u_exact(xc - xm))[inner].max() / (u1 - u2))
+    return err, xm / L, float(pr[2][-1]), T2
+
+
+def test_viscous_shock_structure_matches_the_navier_stokes_profile():
+    coarse, _, _, _ = viscous_shock(120)
+    fine, pos, T_out, T2 = viscous_shock(200)
+    assert fine <= 6e-3, fine
+    assert coarse / fine >= 2.0, (coarse, fine)  # about second order (3 -> 5 cells per thickness)
+    assert abs(pos - 0.5) <= 0.01
+    assert T_out == pytest.approx(T2, rel=1e-6)
