@@ -4,9 +4,11 @@
 // caching allocator (PyTorch's pool can hold nearly all of HBM, so a raw
 // cudaMalloc next to it can fail), and time loops that must not stall, since
 // cudaMalloc/cudaFree synchronize the device.  For them this file provides
-// ibisgb_l2_norms_noalloc: the same deterministic two-pass reduction as
-// ibisgb_l2_norms, with its per-block partial sums in a fixed file-scope
-// __device__ array instead of a context buffer.
+// ibisgb_l2_norms_noalloc: a deterministic two-pass reduction (a fixed
+// summation order per call, so equal inputs give equal bits; equal to
+// ibisgb_l2_norms to rounding, since that one sums in another order), with
+// its per-block partial sums in a fixed file-scope __device__ array instead
+// of a context buffer.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -64,24 +66,54 @@ __global__ void k_norm_final(const double* partials, int nblocks, double* out) {
     for (int j = 0; j < 6; j++) out[j] = sqrt(s[j]);
 }
 
-// Device address of g_norm_partials, looked up once per device with that device current.
+// Device address of g_norm_partials, looked up with the device current, once
+// per device and context: after a cudaDeviceReset (or any other end of the
+// primary context) the module is loaded again, possibly at another address, so
+// the cached address is keyed on the context it was looked up in.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-double* g_scratch[kMaxDevices] = {};
+struct Scratch {
+    void* ctx;
+    double* addr;
+};
+Scratch g_scratch[kMaxDevices] = {};
+
+typedef int (*CtxGetCurrentFn)(void**);  // cuCtxGetCurrent(CUcontext*), CUresult 0 = success
+
+cudaError_t current_context(void** ctx) {
+    static CtxGetCurrentFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
+        fn = (CtxGetCurrentFn)p;
+    }
+    *ctx = nullptr;
+    return fn(ctx) == 0 ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
 
 cudaError_t scratch_for_current_device(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    void* ctx = nullptr;
+    e = current_context(&ctx);
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch[dev]) {
+    if (!ctx || !g_scratch[dev].addr || g_scratch[dev].ctx != ctx) {
+        // the lookup also makes the device's primary context current when no
+        // context is yet, so the context is read again after it
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_norm_partials);
         if (e != cudaSuccess) return e;
-        g_scratch[dev] = (double*)p;
+        e = current_context(&ctx);
+        if (e != cudaSuccess) return e;
+        g_scratch[dev] = Scratch{ctx, (double*)p};
     }
-    *out = g_scratch[dev];
+    *out = g_scratch[dev].addr;
     return cudaSuccess;
 }
 

@@ -46,6 +46,13 @@ extern "C" {
 #define IBISGB_F64 0
 #define IBISGB_MIXED 1
 #define IBISGB_F64_EXACT 2
+/* MIXED_GRAD: least-squares gradients and Barth-Jespersen limiters in float, on
+ * neighbour values and face offsets taken relative to the cell's own value and
+ * centroid in double (float rounds only these increments); face states,
+ * fluxes, accumulation, update and inversion in double.  For long runs through
+ * shock transients, where the float states and fluxes of MIXED drift beyond
+ * 1e-6 of the FP64 solution. */
+#define IBISGB_MIXED_GRAD 3
 
 typedef struct ibisgb_ctx ibisgb_ctx;
 
@@ -411,8 +418,12 @@ int ibisgb_batch_status(ibisgb_ctx* ctx, ibisgb_rk_status* per_case);
  * not stall on the device synchronization of cudaMalloc/cudaFree.
  * num_cells above IBISGB_NOALLOC_MAX_CELLS, or n_conserved other than 4 or 5,
  * are rejected with IBISGB_ERR_ARG; errors are read with ibisgb_last_error(NULL).
- * The first call on a device looks up the scratch array's device address with
- * that device current: make that first call before any stream capture.  All
+ * The norms are a deterministic two-pass sum (the same bits for the same
+ * input); they equal ibisgb_l2_norms's to rounding, not bit for bit, because
+ * the two sum the cells in different orders.
+ * The first call on a device (and the first after the device's context was
+ * reset) looks up the scratch array's device address with that device
+ * current: make that first call before any stream capture.  All
  * calls share the one scratch array (each call writes every slot it reads), so
  * calls whose work overlaps on the GPU race: serialize them. */
 int ibisgb_l2_norms_noalloc(const double* dudt_device, int64_t num_cells, int32_t n_conserved,
