@@ -453,7 +453,9 @@ def run_reference(args, world, rank):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": headline_config(args.n, world),
+            "config": dict(headline_config(args.n, world), measured_cells_per_gpu=n ** 3,
+                           measured_workload=f"the same box at {n}^3 (bounded CPU sample; the rate is per "
+                                             f"cell-update, so it compares with the {args.n}^3 line)"),
             "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": num_threads(),
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,

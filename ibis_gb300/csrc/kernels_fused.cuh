@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(FusedTile<DIM>::kThreads, DIM == 3 ? 2 : 3)
 #pragma unroll
         for (int q = 0; q < NV; q++) phi[q] = 1.f;
         if (prm.limiter) {
-            // Barth-Jespersen (limiter.cpp:119-159) in the two-division form of k_recon
+            // Barth-Jespersen (limiter.cpp:23-63) in the two-division form of k_recon
             float tpos[NV], tneg[NV];
 #pragma unroll
             for (int q = 0; q < NV; q++) { tpos[q] = 0.f; tneg[q] = 0.f; }

@@ -272,7 +272,7 @@ __device__ __forceinline__ void march_gradients(const MarchCtx& m, const DevView
         const float dxm = fg[4 * SF + skm] - xi, dym = fg[5 * SF + skm] - yi, dzm = fg[6 * SF + skm] - zi;
         const float dxp = fg[4 * SF + skp] - xi, dyp = fg[5 * SF + skp] - yi, dzp = fg[6 * SF + skp] - zi;
         if (prm.limiter) {
-            // Barth-Jespersen (limiter.cpp:119-159) in the two-division form of k_recon
+            // Barth-Jespersen (limiter.cpp:23-63) in the two-division form of k_recon
             float tpos[5], tneg[5];
 #pragma unroll
             for (int q = 0; q < 5; q++) { tpos[q] = 0.f; tneg[q] = 0.f; }

@@ -419,7 +419,7 @@ static void lsq_gradient(const Grid<T>& g, const std::vector<T>& values,
     }
 }
 
-// BarthJespersen::calculate_limiters, limiter.cpp:119-159
+// BarthJespersen::calculate_limiters, limiter.cpp:23-63
 template <typename T>
 static void barth_jespersen(const Grid<T>& g, const std::vector<T>& values,
                             const std::vector<std::array<T, 3>>& grad, double eps,

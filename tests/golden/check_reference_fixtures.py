@@ -59,6 +59,8 @@ def same(grid, path):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {os.path.basename(sys.argv[0])} <path of an ibis checkout>")
+    ref = sys.argv[1]
     same(grids.unit_square_3x3(), os.path.join(ref, "src/grid/test/grid.su2"))
     same(grids.unit_cube_3x3x3(), os.path.join(ref, "src/grid/test/cube.su2"))
