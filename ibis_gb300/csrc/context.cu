@@ -177,12 +177,14 @@ struct ibisgb_ctx {
     StateBufs s64, s32;
     std::vector<double> ic_prims;  // host IC primitives (7 x NT), kept until the first update
     bool have_state = false;
-    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
     // launch variants of recon / face / update per precision (autotuned)
-    int var[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    bool tuned[3] = {false, false, false};
-    double tune_ms[3][3][kNumVariants] = {};
-    static int gidx(int prec) { return prec == IBISGB_MIXED ? 1 : (prec == IBISGB_F64_EXACT ? 2 : 0); }
+    int var[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    bool tuned[4] = {false, false, false, false};
+    double tune_ms[4][3][kNumVariants] = {};
+    static int gidx(int prec) {
+        return prec == IBISGB_MIXED ? 1 : (prec == IBISGB_F64_EXACT ? 2 : (prec == IBISGB_MIXED_GRAD ? 3 : 0));
+    }
 
     // Fused stage on structured blocks (mixed build, inviscid, second order).
     // The mixed primitives live in two buffers that the fused stages alternate
@@ -637,6 +639,7 @@ struct ibisgb_ctx {
     KernelOps ops(int prec) const {
         if (prec == IBISGB_MIXED) return kernels_mixed();
         if (prec == IBISGB_F64_EXACT) return kernels_f64_exact();
+        if (prec == IBISGB_MIXED_GRAD) return kernels_mixed_grad();
         return kernels_f64();
     }
 
@@ -1892,7 +1895,7 @@ int ibisgb_get_stream(ibisgb_ctx* ctx, void** stream) {
 int ibisgb_kernel_times(ibisgb_ctx* ctx, int32_t precision, int32_t reps, double out[4]) {
     if (!ctx || !out || reps < 0) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         ctx->kernel_times(precision, reps, out);
     });
 }
@@ -1900,7 +1903,7 @@ int ibisgb_kernel_times(ibisgb_ctx* ctx, int32_t precision, int32_t reps, double
 int ibisgb_residual_device(ibisgb_ctx* ctx, int32_t precision, double* dudt_device, void* stream) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         cudaStream_t user = (cudaStream_t)stream;
         if (user && user != ctx->stream) {  // order the context stream after the caller's work
             cudaEvent_t ev;
@@ -1920,7 +1923,7 @@ int ibisgb_residual_device(ibisgb_ctx* ctx, int32_t precision, double* dudt_devi
 int ibisgb_residual(ibisgb_ctx* ctx, int32_t precision, double* dudt) {
     if (!ctx || !dudt) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         const size_t bytes = sizeof(double) * ctx->nc() * ctx->mesh.N;
         ctx->out.alloc(bytes);
         ctx->residual(precision, ctx->out.as<double>(), true);
@@ -1951,7 +1954,7 @@ int ibisgb_count_bad_cells(ibisgb_ctx* ctx, int64_t* n) {
 int ibisgb_rk_run(ibisgb_ctx* ctx, int32_t precision, int64_t n_steps, ibisgb_rk_status* status) {
     if (!ctx || n_steps < 0) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         ctx->rk_run(precision, n_steps, status);
     });
 }
@@ -2128,7 +2131,7 @@ int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_
 int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         ctx->steady_initialise(precision);
     });
 }
@@ -2147,7 +2150,7 @@ int ibisgb_steady_norms(ibisgb_ctx* ctx, double norms[6], double initial[6]) {
 int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status* status) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         ctx->newton_step(precision, status);
     });
 }
@@ -2155,7 +2158,7 @@ int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status*
 int ibisgb_autotune(ibisgb_ctx* ctx, int32_t precision, int32_t variants[3], double* times_ms) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         ctx->autotune(precision);
         const int gi = ibisgb_ctx::gidx(precision);
         for (int k = 0; k < 3; k++) {
@@ -2169,7 +2172,7 @@ int ibisgb_autotune(ibisgb_ctx* ctx, int32_t precision, int32_t variants[3], dou
 int ibisgb_set_launch_variants(ibisgb_ctx* ctx, int32_t precision, const int32_t variants[3]) {
     if (!ctx || !variants) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 2) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
         int w[3] = {variants[0], variants[1], variants[2]};
         ctx->set_variants(precision, w);
     });

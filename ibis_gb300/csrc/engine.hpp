@@ -170,6 +170,7 @@ struct KernelOps {
 KernelOps kernels_f64();
 KernelOps kernels_f64_exact();
 KernelOps kernels_mixed();
+KernelOps kernels_mixed_grad();
 
 // precision-independent kernels (kernels_common.cu)
 // Fused Runge-Kutta stage on structured blocks (mixed build, inviscid, second

@@ -214,15 +214,29 @@ __global__ void __launch_bounds__(kBlock) k_ghost_fill(DevView v, FvParams prm) 
 
 // ---------------------------------------------------------------------------
 // k_recon: gradients (WLSGradient::compute_gradients, gradient.h:65-116) and
-// Barth-Jespersen limiters (limiter.cpp:119-159) of every valid cell.
+// Barth-Jespersen limiters (limiter.cpp:23-63) of every valid cell.
 // ---------------------------------------------------------------------------
 // The float build stores limiter-scaled gradients (phi * grad) instead of
 // gradients and limiters, packed per cell: the DIM components of each
 // reconstructed variable in turn (15 floats in 3-D, 8 in 2-D) in a 16-float
 // slot that the face kernel reads as four (two) 128-bit loads per side, instead
 // of 20 (12) scattered values.
+// A translation unit that defines IBISGB_FLOAT_GRADIENTS to 1 builds the
+// MIXED_GRAD family: float gradients and limiters (packed as above) over double
+// primitives, geometry, face states and fluxes.
+#ifndef IBISGB_FLOAT_GRADIENTS
+#define IBISGB_FLOAT_GRADIENTS 0
+#endif
 template <class P, bool EXACT>
-constexpr bool prescaled_gradients() { return !EXACT && sizeof(P) == sizeof(float); }
+constexpr bool prescaled_gradients() { return !EXACT && (sizeof(P) == sizeof(float) || IBISGB_FLOAT_GRADIENTS); }
+// float gradient arithmetic over double primitives and geometry (MIXED_GRAD):
+// every neighbour value and face offset enters the float arithmetic relative to
+// the cell's own value and centroid, formed in double, so that float rounds
+// the increments, not the values they are added to
+template <class R, class P, bool EXACT>
+constexpr bool relative_float_gradients() {
+    return !EXACT && sizeof(R) == sizeof(float) && sizeof(P) == sizeof(double);
+}
 constexpr int kPackedGrad = 16;  // floats per cell of the packed gradients
 
 template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
@@ -242,7 +256,10 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
     const bool visc = prm.viscous != 0;
     const bool lim = reconstruct && prm.limiter;
 
+    constexpr bool REL = relative_float_gradients<R, P, EXACT>();
     R xi = (R)cc[i], yi = (R)cc[NT + i], zi = DIM == 3 ? (R)cc[2 * NT + i] : R(0.0);
+    double xid = 0.0, yid = 0.0, zid = 0.0;
+    if constexpr (REL) { xid = (double)cc[i]; yid = (double)cc[NT + i]; zid = DIM == 3 ? (double)cc[2 * NT + i] : 0.0; }
     R r11 = R(1.0), r12 = R(0.0), r22 = R(1.0), r13 = R(0.0), r23 = R(0.0), r33 = R(1.0), beta = R(0.0);
     if (EXACT) {
         r11 = (R)rr[i]; r12 = (R)rr[N + i]; r22 = (R)rr[2 * N + i];
@@ -250,18 +267,33 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
         beta = (r12 * r23 - r13 * r23) / (r11 * r22);
     }
 
+    // REL: ui = 0 and every neighbour value is taken relative to the cell's (uid)
     R ui[NV], gx[NV], gy[NV], gz[NV], umin[NV], umax[NV];
+    double uid[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) {
-        ui[q] = (R)pr[vidx[q] * NT + i];
+        if constexpr (REL) {
+            uid[q] = (double)pr[vidx[q] * NT + i];
+            ui[q] = R(0.0);
+        } else {
+            uid[q] = 0.0;
+            ui[q] = (R)pr[vidx[q] * NT + i];
+        }
         gx[q] = R(0.0); gy[q] = R(0.0); gz[q] = R(0.0);
         umin[q] = ui[q]; umax[q] = ui[q];
     }
     constexpr int NW = DIM == 3 ? 4 : 3;  // viscous: T, vx, vy[, vz]
     R wi[NW], hx[NW], hy[NW], hz[NW];
+    double wid[NW];
 #pragma unroll
     for (int q = 0; q < NW; q++) {
-        wi[q] = (R)pr[visc_prim(q) * NT + i];
+        if constexpr (REL) {
+            wid[q] = (double)pr[visc_prim(q) * NT + i];
+            wi[q] = R(0.0);
+        } else {
+            wid[q] = 0.0;
+            wi[q] = (R)pr[visc_prim(q) * NT + i];
+        }
         hx[q] = R(0.0); hy[q] = R(0.0); hz[q] = R(0.0);
     }
 
@@ -288,7 +320,9 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
         if (reconstruct) {
 #pragma unroll
             for (int q = 0; q < NV; q++) {
-                R un = (R)pr[vidx[q] * NT + nb];
+                R un;
+                if constexpr (REL) un = (R)((double)pr[vidx[q] * NT + nb] - uid[q]);
+                else un = (R)pr[vidx[q] * NT + nb];
                 R du = un - ui[q];
                 gx[q] += w1 * du; gy[q] += w2 * du;
                 if (DIM == 3) gz[q] += w3 * du;
@@ -300,7 +334,10 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
             const bool ghost = nb >= N;
 #pragma unroll
             for (int q = 0; q < NW; q++) {
-                R un = ghost ? (R)vg[(1 + q) * G + (nb - N)] : (R)pr[visc_prim(q) * NT + nb];
+                R un;
+                if constexpr (REL)
+                    un = (R)((ghost ? (double)vg[(1 + q) * G + (nb - N)] : (double)pr[visc_prim(q) * NT + nb]) - wid[q]);
+                else un = ghost ? (R)vg[(1 + q) * G + (nb - N)] : (R)pr[visc_prim(q) * NT + nb];
                 R du = un - wi[q];
                 hx[q] += w1 * du; hy[q] += w2 * du;
                 if (DIM == 3) hz[q] += w3 * du;
@@ -318,11 +355,15 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
         if (lim) {
             const R eps = par<R>(prm.eps, prm.feps);
             if (EXACT || v.branches) {
-                // face by face, as limiter.cpp:141-156, recording the branch taken
+                // face by face, as limiter.cpp:46-60, recording the branch taken
                 for (int s = 0; s < nf; s++) {
                     const int f = v.cell_face[s * N + i];
                     R dx = (R)fcen[f] - xi, dy = (R)fcen[F + f] - yi;
                     R dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+                    if constexpr (REL) {
+                        dx = (R)((double)fcen[f] - xid); dy = (R)((double)fcen[F + f] - yid);
+                        dz = DIM == 3 ? (R)((double)fcen[2 * F + f] - zid) : R(0.0);
+                    }
 #pragma unroll
                     for (int q = 0; q < NV; q++) {
                         R d2 = DIM == 3 ? gx[q] * dx + gy[q] * dy + gz[q] * dz : gx[q] * dx + gy[q] * dy;
@@ -351,8 +392,13 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                         dz = DIM == 3 ? (R)D[(2 * MF + s) * N + i] : R(0.0);
                     } else {
                         const int f = v.cell_face[s * N + i];
-                        dx = (R)fcen[f] - xi; dy = (R)fcen[F + f] - yi;
-                        dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+                        if constexpr (REL) {
+                            dx = (R)((double)fcen[f] - xid); dy = (R)((double)fcen[F + f] - yid);
+                            dz = DIM == 3 ? (R)((double)fcen[2 * F + f] - zid) : R(0.0);
+                        } else {
+                            dx = (R)fcen[f] - xi; dy = (R)fcen[F + f] - yi;
+                            dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
+                        }
                     }
 #pragma unroll
                     for (int q = 0; q < NV; q++) {
@@ -620,10 +666,13 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
                     const float4 t = src[k];
                     pk[4 * k] = t.x; pk[4 * k + 1] = t.y; pk[4 * k + 2] = t.z; pk[4 * k + 3] = t.w;
                 }
+                // the increment (phi grad) . d in float; with double face states
+                // (MIXED_GRAD) it is added to the double cell value
+                const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
                 auto rec = [&](R val, int w) {
-                    R sgr = DIM == 3 ? (R)pk[3 * w] * dx + (R)pk[3 * w + 1] * dy + (R)pk[3 * w + 2] * dz
-                                     : (R)pk[2 * w] * dx + (R)pk[2 * w + 1] * dy;
-                    return val + sgr;
+                    float sgr = DIM == 3 ? pk[3 * w] * fdx + pk[3 * w + 1] * fdy + pk[3 * w + 2] * fdz
+                                         : pk[2 * w] * fdx + pk[2 * w + 1] * fdy;
+                    return val + (R)sgr;
                 };
                 q[ia] = rec(q[ia], 0);
                 q[ib] = rec(q[ib], 1);
@@ -1218,7 +1267,9 @@ __global__ void __launch_bounds__(kBlock) k_local_dt(DevView v, FvParams prm) {
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
-template <class R, class P, class Gm, bool EXACT>
+// RR: arithmetic of the gradient/limiter kernel when it differs from the face
+// kernel's R (the MIXED_GRAD family: float gradients, double fluxes).
+template <class R, class P, class Gm, bool EXACT, class RR = R>
 struct Launch {
     static void ghost_fill(const DevView& v, const FvParams& p, cudaStream_t s) {
         if (v.G > 0) k_ghost_fill<P, Gm><<<blocks_for(v.G), kBlock, 0, s>>>(v, p);
@@ -1230,8 +1281,8 @@ struct Launch {
     static void recon_v(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {
         constexpr int BS = kVariantThreads[V], MB = kVariantMinBlocks[V];
         const unsigned g = (unsigned)((v.N + BS - 1) / BS);
-        if (v.dim == 3) k_recon<R, P, Gm, 3, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
-        else k_recon<R, P, Gm, 2, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
+        if (v.dim == 3) k_recon<RR, P, Gm, 3, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
+        else k_recon<RR, P, Gm, 2, EXACT, BS, MB><<<g, BS, 0, s>>>(v, p, reco);
     }
     template <int V>
     static void face_v(const DevView& v, const FvParams& p, bool reco, cudaStream_t s) {

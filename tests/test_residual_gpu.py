@@ -7,6 +7,8 @@ tests/cases.py:gross_flux_scale):
     pow(x, 2.0)): CUDA's and glibc's pow may differ in the last bit, <= 1e-14.
   * f64 (FMA contraction allowed): <= 1e-12.
   * mixed (float reconstruction/flux, double accumulation): <= 2e-5.
+  * mixed_grad (float gradients/limiters on relative values, double face
+    states and fluxes): <= 1e-6 (measured 7e-9 to 3e-7).
 Limiter branch selection must be identical in f64_exact; in f64 it may differ
 in at most 1% of the cells, where FMA rounding flips a projection that is zero
 to rounding or an exact tie between two faces.
@@ -92,6 +94,9 @@ def test_residual_parity(name, kw):
 
     r = sim.compute_dudt("mixed")
     assert per_cell_rel_err(r, r_ref, scale).max() <= 2e-5
+
+    r = sim.compute_dudt("mixed_grad")
+    assert per_cell_rel_err(r, r_ref, scale).max() <= 1e-6
 
 
 @pytest.mark.parametrize("name", ["ramp", "plate", "box"])
