@@ -1309,6 +1309,7 @@ void Sim<T>::init_rk(const Json& sc) {  // runge_kutta.cpp:21-80
     rk.max_time = sc.at("max_time").as_double();
     rk.plot_frequency = sc.at("plot_frequency").as_double();
     rk.dt_init = sc.at("dt_init").as_double();
+    rk.aliased_stages = sc.contains("stage_derivatives") && sc.at("stage_derivatives").as_string() == "aliased";
     size_t NT = grid.N + grid.G;
     k.assign(rk.tab.stages(), Conserved<T>(NT, grid.dim));
     k_tmp = Conserved<T>(NT, grid.dim);
@@ -1353,19 +1354,20 @@ void Sim<T>::rk_estimate_dt() {  // runge_kutta.cpp:108-119
 
 template <typename T>
 void Sim<T>::rk_take_step() {  // runge_kutta.cpp:131-203
-    fv.compute_dudt(fs, grid, k[0], gas, tp);
+    auto K = [&](size_t i) -> Conserved<T>& { return k[rk.aliased_stages ? 0 : i]; };
+    fv.compute_dudt(fs, grid, K(0), gas, tp);
     rk_estimate_dt();
     double dt = rk.dt;
     for (size_t i = 1; i < rk.tab.stages(); i++) {
-        axpy_into(U, k_tmp, k[0], rk.tab.A(i, 0) * dt);
+        axpy_into(U, k_tmp, K(0), rk.tab.A(i, 0) * dt);
         for (size_t j = 1; j < i; j++) {
             if (rk.tab.A(i, j) < 1e-14) continue;
-            axpy_inplace(k_tmp, k[j], rk.tab.A(i, j) * dt);
+            axpy_inplace(k_tmp, K(j), rk.tab.A(i, j) * dt);
         }
         conserved_to_primatives(k_tmp, fs_tmp, gas);
-        fv.compute_dudt(fs_tmp, grid, k[i], gas, tp);
+        fv.compute_dudt(fs_tmp, grid, K(i), gas, tp);
     }
-    for (size_t i = 0; i < rk.tab.stages(); i++) axpy_inplace(U, k[i], rk.tab.b[i] * dt);
+    for (size_t i = 0; i < rk.tab.stages(); i++) axpy_inplace(U, K(i), rk.tab.b[i] * dt);
     conserved_to_primatives(U, fs, gas);
     rk.t += dt;
     rk.time_since_last_plot += dt;

@@ -394,6 +394,13 @@ struct Tableau {
 struct RkState {
     Tableau tab;
     double cfl = 0.5, max_time = 1e300, plot_frequency = -1.0, dt_init = -1.0;
+    // The stage derivatives of the reference's RungeKutta share one array: it
+    // builds them as copies of one ConservedQuantities (runge_kutta.cpp:47-48),
+    // and copies of a Kokkos View alias its storage, so every stage reads the
+    // derivative the previous stage wrote.  "stage_derivatives": "aliased" in
+    // the solver block reproduces that; the default keeps one array per stage
+    // (the tableau as written).
+    bool aliased_stages = false;
     double t = 0.0, dt = 0.0, stable_dt = 0.0, time_since_last_plot = 0.0;
     // linear CFL schedule (cfl.cpp:101-127) when non-empty
     std::vector<double> cfl_times, cfl_values;

@@ -11,6 +11,8 @@
 //   * create_mirror_view of a host View is the View itself.
 //   * subview(v, ALL, j) / (i, ALL) / pair ranges give LayoutStride Views.
 //   * the default layout of the host space is LayoutRight.
+//   * inside parallel_for / parallel_reduce, copies and subviews of Views are
+//     untracked (no reference count), as Kokkos does in parallel dispatch.
 //   * parallel_reduce with Sum / Min reducers starts from
 //     reduction_identity<T>::sum() / ::min() (user-specialisable) and joins
 //     partial results with += / min.  The OpenMP space partitions the range
@@ -116,6 +118,19 @@ constexpr ALL_t ALL{};
 
 // ---------------------------------------------------------------- View
 namespace impl {
+// Inside a parallel dispatch, View copies and subviews are not reference
+// counted (Kokkos turns allocation tracking off there as well): they are
+// temporaries of one iteration, and the Views they come from are held by the
+// dispatched functor.
+inline bool& untracked() {
+    static thread_local bool u = false;
+    return u;
+}
+struct UntrackedScope {
+    bool old;
+    UntrackedScope() : old(untracked()) { untracked() = true; }
+    ~UntrackedScope() { untracked() = old; }
+};
 template <class D>
 struct data_traits;
 template <class T>
@@ -196,6 +211,21 @@ public:
     static constexpr unsigned rank_dynamic = traits::static_n1 ? 1 : traits::rank;
 
     View() = default;
+    View(const View& o) : alloc_(impl::untracked() ? nullptr : o.alloc_), ptr_(o.ptr_), label_() {
+        ext_[0] = o.ext_[0]; ext_[1] = o.ext_[1];
+        str_[0] = o.str_[0]; str_[1] = o.str_[1];
+        if (!impl::untracked()) label_ = o.label_;
+    }
+    View& operator=(const View& o) {
+        if (this != &o) {
+            alloc_ = impl::untracked() ? nullptr : o.alloc_;
+            ptr_ = o.ptr_;
+            ext_[0] = o.ext_[0]; ext_[1] = o.ext_[1];
+            str_[0] = o.str_[0]; str_[1] = o.str_[1];
+            if (!impl::untracked()) label_ = o.label_;
+        }
+        return *this;
+    }
 
     explicit View(const std::string& label, size_t n0 = 0, size_t n1 = 0) : label_(label) {
         allocate(n0, traits::static_n1 ? traits::static_n1 : (rank == 2 ? n1 : 1));
@@ -216,7 +246,8 @@ public:
                                        std::is_convertible_v<typename impl::data_traits<D2>::value_type*,
                                                              value_type*>>>
     View(const View<D2, P2...>& o)
-        : alloc_(o.impl_alloc()), ptr_(o.data()), label_(o.label()) {
+        : alloc_(impl::untracked() ? nullptr : o.impl_alloc()), ptr_(o.data()),
+          label_(impl::untracked() ? std::string() : o.label()) {
         ext_[0] = o.extent(0);
         ext_[1] = rank == 2 ? o.extent(1) : 1;
         str_[0] = o.stride(0);
@@ -224,8 +255,9 @@ public:
     }
 
     // a strided View (what subview builds)
-    View(std::shared_ptr<void> alloc, pointer_type p, const size_t ext[2], const size_t str[2], const std::string& label)
-        : alloc_(std::move(alloc)), ptr_(p), label_(label) {
+    View(const std::shared_ptr<void>& alloc, pointer_type p, const size_t ext[2], const size_t str[2],
+         const std::string& label)
+        : alloc_(impl::untracked() ? nullptr : alloc), ptr_(p), label_(impl::untracked() ? std::string() : label) {
         ext_[0] = ext[0]; ext_[1] = ext[1];
         str_[0] = str[0]; str_[1] = str[1];
     }
@@ -405,9 +437,14 @@ template <class F>
 void run_for(Range r, const F& f) {
 #ifdef IBIS_REF_OPENMP
     const long long b = (long long)r.b, e = (long long)r.e;
-#pragma omp parallel for schedule(static)
-    for (long long i = b; i < e; i++) f((size_t)i);
+#pragma omp parallel
+    {
+        UntrackedScope scope;
+#pragma omp for schedule(static)
+        for (long long i = b; i < e; i++) f((size_t)i);
+    }
 #else
+    UntrackedScope scope;
     for (size_t i = r.b; i < r.e; i++) f(i);
 #endif
 }
@@ -473,6 +510,7 @@ void run_reduce(Range r, const F& f, Red red) {
     std::vector<T> part(nt, Red::init());
 #pragma omp parallel num_threads(nt)
     {
+        UntrackedScope scope;
         const int t = omp_get_thread_num(), n = omp_get_num_threads();
         const size_t len = r.e - r.b, chunk = (len + n - 1) / n;
         const size_t b = r.b + std::min(len, chunk * t), e = r.b + std::min(len, chunk * (t + 1));
@@ -485,7 +523,10 @@ void run_reduce(Range r, const F& f, Red red) {
     red.ref = out;
 #else
     T acc = Red::init();
-    for (size_t i = r.b; i < r.e; i++) f(i, acc);
+    {
+        UntrackedScope scope;
+        for (size_t i = r.b; i < r.e; i++) f(i, acc);
+    }
     red.ref = acc;
 #endif
 }
