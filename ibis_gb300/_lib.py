@@ -16,7 +16,7 @@ ERRORS = {
     -4: "IBISGB_ERR_BAD_CELLS", -5: "IBISGB_ERR_ARG", -6: "IBISGB_ERR_TIMEOUT",
     -7: "IBISGB_ERR_STATE",
 }
-PRECISION = {"f64": 0, "mixed": 1, "f64_exact": 2, "mixed_grad": 3}
+PRECISION = {"f64": 0, "mixed": 1, "f64_exact": 2, "mixed_grad": 3, "mixed_ff": 4}
 
 
 class IbisgbError(RuntimeError):

@@ -37,6 +37,7 @@ UNITS = {
     "kernels_f64.cu": "nvcc",
     "kernels_mixed.cu": "nvcc-fast",
     "kernels_grad.cu": "nvcc",
+    "kernels_ff.cu": "nvcc-fast",
     "kernels_exact.cu": "nvcc-nofma",
     "noalloc.cu": "nvcc",
     "kernels_tangent.cu": "nvcc-nofma",

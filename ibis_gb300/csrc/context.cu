@@ -75,6 +75,7 @@ void upload(DBuf& b, const std::vector<T>& v, cudaStream_t s) {
 struct StateBufs {
     DBuf cc, r, face, lsqw, lsqd;                  // geometry
     DBuf prim, vghost, grad, phi, vgrad, flux;     // state and intermediates
+    DBuf prim_lo, cc_lo, face_lo, flux_lo;         // float-float build: lo companions of the float arrays
     bool geometry = false;
     bool prims_current = false;
 };
@@ -174,16 +175,23 @@ struct ibisgb_ctx {
     DBuf cell_face, cell_nbr, outsign, nfaces, left, right, ghost_src, ghost_face, ghost_bound,
         bounds, gfix, feed_off, feed_ghost, vol, inv_vol, inv_vol2;
     DBuf U, k, vsig, ctl, l2, out, branches;
-    StateBufs s64, s32;
+    StateBufs s64, s32, sff;
     std::vector<double> ic_prims;  // host IC primitives (7 x NT), kept until the first update
     bool have_state = false;
-    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool k_alias = false;  // stage derivatives share slot 0 (the reference's RungeKutta)
+    cudaGraphExec_t graph[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // launch variants of recon / face / update per precision (autotuned)
-    int var[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    bool tuned[4] = {false, false, false, false};
-    double tune_ms[4][3][kNumVariants] = {};
+    int var[5][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    bool tuned[5] = {false, false, false, false, false};
+    double tune_ms[5][3][kNumVariants] = {};
     static int gidx(int prec) {
-        return prec == IBISGB_MIXED ? 1 : (prec == IBISGB_F64_EXACT ? 2 : (prec == IBISGB_MIXED_GRAD ? 3 : 0));
+        switch (prec) {
+            case IBISGB_MIXED: return 1;
+            case IBISGB_F64_EXACT: return 2;
+            case IBISGB_MIXED_GRAD: return 3;
+            case IBISGB_MIXED_FF: return 4;
+            default: return 0;
+        }
     }
 
     // Fused stage on structured blocks (mixed build, inviscid, second order).
@@ -288,6 +296,11 @@ struct ibisgb_ctx {
             prm.fdelta = (float)prm.delta; prm.fmu0 = (float)prm.mu0; prm.fT0 = (float)prm.T0;
             prm.fTs = (float)prm.Ts; prm.fPr = (float)prm.Pr; prm.inv_Cv = 1.0 / prm.Cv;
             prm.finv_Cv = (float)prm.inv_Cv;
+            auto lo = [](double d, float f) { return (float)(d - (double)f); };
+            prm.loR = lo(prm.R, prm.fR); prm.loCv = lo(prm.Cv, prm.fCv); prm.loCp = lo(prm.Cp, prm.fCp);
+            prm.logamma = lo(prm.gamma, prm.fgamma); prm.logR = lo(prm.gamma * prm.R, prm.fgR);
+            prm.lodelta = lo(prm.delta, prm.fdelta); prm.lomu0 = lo(prm.mu0, prm.fmu0);
+            prm.loT0 = lo(prm.T0, prm.fT0); prm.loTs = lo(prm.Ts, prm.fTs); prm.loPr = lo(prm.Pr, prm.fPr);
             const Json& solver = config.at("solver");
             if (solver.at("name").as_string() == "runge_kutta") parse_rk(solver);
             if (solver.at("name").as_string() == "steady_state") parse_steady(solver);
@@ -328,6 +341,15 @@ struct ibisgb_ctx {
         c.max_time = sc.at("max_time").as_double();
         c.plot_frequency = sc.at("plot_frequency").as_double();
         dt_init = sc.at("dt_init").as_double();
+        // extension: "stage_derivatives": "aliased" reproduces the reference's
+        // RungeKutta, whose stage derivatives are copies of one Kokkos View and so
+        // share one array (runge_kutta.cpp:47-48); "separate" (the default) keeps
+        // one array per stage, as the tableau is written
+        if (sc.contains("stage_derivatives")) {
+            const std::string sd = sc.at("stage_derivatives").as_string();
+            if (sd != "aliased" && sd != "separate") throw ConfigError("stage_derivatives must be aliased or separate");
+            k_alias = sd == "aliased";
+        }
         rk_configured = true;
     }
 
@@ -449,9 +471,11 @@ struct ibisgb_ctx {
             if (!same_scheme(cs[0]->prm, c.prm))
                 throw ConfigError("case " + std::to_string(i) +
                                   ": cases of a batch must share flux, reconstruction, gas and transport settings");
-            if (!c.rk_configured || !cs[0]->rk_configured || !same_tableau(cs[0]->ctl_host, c.ctl_host))
+            if (!c.rk_configured || !cs[0]->rk_configured || !same_tableau(cs[0]->ctl_host, c.ctl_host) ||
+                c.k_alias != cs[0]->k_alias)
                 throw ConfigError("case " + std::to_string(i) +
-                                  ": cases of a batch must use runge_kutta with the same Butcher tableau");
+                                  ": cases of a batch must use runge_kutta with the same Butcher tableau and "
+                                  "stage_derivatives");
             parts.push_back(&c.mesh);
         }
         const ibisgb_ctx& a = *cs[0];
@@ -460,6 +484,7 @@ struct ibisgb_ctx {
         rk_configured = true;
         ctl_host = a.ctl_host;
         dt_init = a.dt_init;
+        k_alias = a.k_alias;
         std::vector<int64_t> bound_off;
         try {
             merge_meshes(parts, mesh, cell_off, ghost_off, face_off, bound_off);
@@ -593,8 +618,24 @@ struct ibisgb_ctx {
     }
 
     template <class Gm>
-    void upload_geometry(StateBufs& s) {
+    void upload_geometry(StateBufs& s, bool with_lo = false) {
         if (s.geometry) return;
+        if (with_lo) {  // what the float copies of the geometry leave out
+            const int64_t NT = mesh.NT(), F = mesh.F;
+            auto lo = [](double d) { return (float)(d - (double)(float)d); };
+            std::vector<float> cl(3 * NT), fl(13 * F);
+            for (int64_t c = 0; c < NT; c++) {
+                cl[c] = lo(mesh.ccx[c]); cl[NT + c] = lo(mesh.ccy[c]); cl[2 * NT + c] = lo(mesh.ccz[c]);
+            }
+            const std::vector<double>* fa[13] = {&mesh.nx, &mesh.ny, &mesh.nz, &mesh.t1x, &mesh.t1y, &mesh.t1z,
+                                                 &mesh.t2x, &mesh.t2y, &mesh.t2z, &mesh.fcx, &mesh.fcy, &mesh.fcz,
+                                                 &mesh.area};
+            for (int q = 0; q < 13; q++)
+                for (int64_t f = 0; f < F; f++) fl[q * F + f] = lo((*fa[q])[f]);
+            upload(s.cc_lo, cl, stream); upload(s.face_lo, fl, stream);
+            s.prim_lo.alloc(sizeof(float) * 7 * NT);
+            s.flux_lo.alloc(sizeof(float) * nc() * F);
+        }
         const int64_t N = mesh.N, NT = mesh.NT(), F = mesh.F;
         std::vector<Gm> cc(3 * NT), r(6 * N, Gm(0)), fc(13 * F);
         for (int64_t c = 0; c < NT; c++) { cc[c] = (Gm)mesh.ccx[c]; cc[NT + c] = (Gm)mesh.ccy[c]; cc[2 * NT + c] = (Gm)mesh.ccz[c]; }
@@ -635,11 +676,15 @@ struct ibisgb_ctx {
     }
 
     static bool is_mixed(int prec) { return prec == IBISGB_MIXED; }
-    StateBufs& bufs(int prec) { return is_mixed(prec) ? s32 : s64; }
+    static bool is_ff(int prec) { return prec == IBISGB_MIXED_FF; }
+    // float state and geometry arrays (MIXED, and MIXED_FF with its lo companions)
+    static bool float_storage(int prec) { return prec == IBISGB_MIXED || prec == IBISGB_MIXED_FF; }
+    StateBufs& bufs(int prec) { return is_mixed(prec) ? s32 : (is_ff(prec) ? sff : s64); }
     KernelOps ops(int prec) const {
         if (prec == IBISGB_MIXED) return kernels_mixed();
         if (prec == IBISGB_F64_EXACT) return kernels_f64_exact();
         if (prec == IBISGB_MIXED_GRAD) return kernels_mixed_grad();
+        if (prec == IBISGB_MIXED_FF) return kernels_mixed_ff();
         return kernels_f64();
     }
 
@@ -660,7 +705,10 @@ struct ibisgb_ctx {
         v.prim = (is_mixed(prec) && prim_cur) ? prim_alt.p : s.prim.p;
         v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
+        v.prim_lo = s.prim_lo.as<float>(); v.cc_lo = s.cc_lo.as<float>();
+        v.face_lo = s.face_lo.as<float>(); v.flux_lo = s.flux_lo.as<float>();
         v.U = U.as<double>(); v.k = k.as<double>(); v.ctl = ctl.as<StepCtl>();
+        v.k_alias = k_alias ? 1 : 0;
         v.case_of = n_cases > 1 ? case_of.as<int>() : nullptr;
         v.n_cases = n_cases;
         v.branches = nullptr;
@@ -671,15 +719,24 @@ struct ibisgb_ctx {
     void ensure_prims(int prec) {
         ensure_device();
         if (!have_state) throw StateError("no initial condition: call ibisgb_set_primitives first");
-        if (is_mixed(prec)) upload_geometry<float>(s32); else upload_geometry<double>(s64);
+        if (is_mixed(prec)) upload_geometry<float>(s32);
+        else if (is_ff(prec)) upload_geometry<float>(sff, true);
+        else upload_geometry<double>(s64);
         StateBufs& s = bufs(prec);
         if (s.prims_current) return;
         DevView v = view(prec);
         if (!ic_prims.empty()) {
             const int64_t NT = mesh.NT();
-            if (is_mixed(prec)) {
+            if (float_storage(prec)) {
                 std::vector<float> f(ic_prims.begin(), ic_prims.end());
                 CUDA_OK(cudaMemcpyAsync(v.prim, f.data(), sizeof(float) * 7 * NT, cudaMemcpyHostToDevice, stream));
+                if (is_ff(prec)) {
+                    std::vector<float> lo(f.size());
+                    for (size_t q = 0; q < f.size(); q++) lo[q] = (float)(ic_prims[q] - (double)f[q]);
+                    CUDA_OK(cudaMemcpyAsync(v.prim_lo, lo.data(), sizeof(float) * 7 * NT, cudaMemcpyHostToDevice,
+                                            stream));
+                    CUDA_OK(cudaStreamSynchronize(stream));
+                }
                 CUDA_OK(cudaStreamSynchronize(stream));
             } else {
                 CUDA_OK(cudaMemcpyAsync(v.prim, ic_prims.data(), sizeof(double) * 7 * NT, cudaMemcpyHostToDevice, stream));
@@ -695,8 +752,9 @@ struct ibisgb_ctx {
     // prec < 0: the conserved state changed outside a kernel build (no prims current)
     void state_changed(int prec) {
         ic_prims.clear();
-        s64.prims_current = prec >= 0 && !is_mixed(prec);
+        s64.prims_current = prec >= 0 && !float_storage(prec);
         s32.prims_current = prec >= 0 && is_mixed(prec);
+        sff.prims_current = prec >= 0 && is_ff(prec);
     }
 
     void set_primitives(const double* T, const double* p, const double* vx, const double* vy, const double* vz) {
@@ -792,6 +850,7 @@ struct ibisgb_ctx {
         if (fused_elig >= 0) return fused_elig == 1;
         fused_elig = 0;
         if (prm.viscous) fused_why = "viscous fluxes take the generic kernels";
+        else if (k_alias) fused_why = "aliased stage derivatives take the generic kernels";
         else if (prm.cflux) fused_why = "constant-flux boundaries take the generic kernels";
         else if (prm.order != 2) fused_why = "first-order reconstruction takes the generic kernels";
         else {
@@ -895,7 +954,7 @@ struct ibisgb_ctx {
     void* mixed_prim(int which) { return which ? prim_alt.p : s32.prim.p; }
 
     bool cell_eligible() const {
-        return rk_configured && !prm.viscous && !prm.cflux && kernels_mixed().cell_update != nullptr;
+        return rk_configured && !prm.viscous && !prm.cflux && !k_alias && kernels_mixed().cell_update != nullptr;
     }
     std::string cell_why() const {
         if (!rk_configured) return "the solver is not runge_kutta";
@@ -1427,12 +1486,16 @@ struct ibisgb_ctx {
             };
             // The update kernel is timed in its first-stage Runge-Kutta mode (it also forms
             // and commits the next stage state); the primitives it overwrites are restored.
-            const size_t pbytes = (is_mixed(prec) ? sizeof(float) : sizeof(double)) * 7 * mesh.NT();
-            const size_t gbytes = (is_mixed(prec) ? sizeof(float) : sizeof(double)) * 5 * mesh.G;
-            tune_save.alloc(pbytes + gbytes + 16);
+            const size_t pbytes = (float_storage(prec) ? sizeof(float) : sizeof(double)) * 7 * mesh.NT();
+            const size_t gbytes = (float_storage(prec) ? sizeof(float) : sizeof(double)) * 5 * mesh.G;
+            const size_t lbytes = is_ff(prec) ? sizeof(float) * 7 * mesh.NT() : 0;
+            tune_save.alloc(pbytes + gbytes + lbytes + 16);
             CUDA_OK(cudaMemcpyAsync(tune_save.p, v.prim, pbytes, cudaMemcpyDeviceToDevice, stream));
             if (gbytes)
                 CUDA_OK(cudaMemcpyAsync((char*)tune_save.p + pbytes, v.vghost, gbytes, cudaMemcpyDeviceToDevice, stream));
+            if (lbytes)
+                CUDA_OK(cudaMemcpyAsync((char*)tune_save.p + pbytes + gbytes, v.prim_lo, lbytes,
+                                        cudaMemcpyDeviceToDevice, stream));
             auto launch_k = [&](int k, int w) {
                 if (k == 0) o.recon(v, prm, reco, w, stream);
                 else if (k == 1) o.face_flux(v, prm, reco, w, stream);
@@ -1456,6 +1519,9 @@ struct ibisgb_ctx {
             CUDA_OK(cudaMemcpyAsync(v.prim, tune_save.p, pbytes, cudaMemcpyDeviceToDevice, stream));
             if (gbytes)
                 CUDA_OK(cudaMemcpyAsync(v.vghost, (char*)tune_save.p + pbytes, gbytes, cudaMemcpyDeviceToDevice, stream));
+            if (lbytes)
+                CUDA_OK(cudaMemcpyAsync(v.prim_lo, (char*)tune_save.p + pbytes + gbytes, lbytes,
+                                        cudaMemcpyDeviceToDevice, stream));
             if (is_mixed(prec)) {
                 generic_ms = tune_ms[gi][0][vr[0]] + tune_ms[gi][1][vr[1]] + tune_ms[gi][2][vr[2]];
                 fused_ms = 0.0;
@@ -1895,7 +1961,7 @@ int ibisgb_get_stream(ibisgb_ctx* ctx, void** stream) {
 int ibisgb_kernel_times(ibisgb_ctx* ctx, int32_t precision, int32_t reps, double out[4]) {
     if (!ctx || !out || reps < 0) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         ctx->kernel_times(precision, reps, out);
     });
 }
@@ -1903,7 +1969,7 @@ int ibisgb_kernel_times(ibisgb_ctx* ctx, int32_t precision, int32_t reps, double
 int ibisgb_residual_device(ibisgb_ctx* ctx, int32_t precision, double* dudt_device, void* stream) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         cudaStream_t user = (cudaStream_t)stream;
         if (user && user != ctx->stream) {  // order the context stream after the caller's work
             cudaEvent_t ev;
@@ -1923,7 +1989,7 @@ int ibisgb_residual_device(ibisgb_ctx* ctx, int32_t precision, double* dudt_devi
 int ibisgb_residual(ibisgb_ctx* ctx, int32_t precision, double* dudt) {
     if (!ctx || !dudt) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         const size_t bytes = sizeof(double) * ctx->nc() * ctx->mesh.N;
         ctx->out.alloc(bytes);
         ctx->residual(precision, ctx->out.as<double>(), true);
@@ -1954,7 +2020,7 @@ int ibisgb_count_bad_cells(ibisgb_ctx* ctx, int64_t* n) {
 int ibisgb_rk_run(ibisgb_ctx* ctx, int32_t precision, int64_t n_steps, ibisgb_rk_status* status) {
     if (!ctx || n_steps < 0) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         ctx->rk_run(precision, n_steps, status);
     });
 }
@@ -2131,7 +2197,7 @@ int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_
 int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         ctx->steady_initialise(precision);
     });
 }
@@ -2150,7 +2216,7 @@ int ibisgb_steady_norms(ibisgb_ctx* ctx, double norms[6], double initial[6]) {
 int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status* status) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         ctx->newton_step(precision, status);
     });
 }
@@ -2158,7 +2224,7 @@ int ibisgb_newton_step(ibisgb_ctx* ctx, int32_t precision, ibisgb_newton_status*
 int ibisgb_autotune(ibisgb_ctx* ctx, int32_t precision, int32_t variants[3], double* times_ms) {
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         ctx->autotune(precision);
         const int gi = ibisgb_ctx::gidx(precision);
         for (int k = 0; k < 3; k++) {
@@ -2172,7 +2238,7 @@ int ibisgb_autotune(ibisgb_ctx* ctx, int32_t precision, int32_t variants[3], dou
 int ibisgb_set_launch_variants(ibisgb_ctx* ctx, int32_t precision, const int32_t variants[3]) {
     if (!ctx || !variants) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
-        if (precision < 0 || precision > 3) throw ArgError("unknown precision");
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         int w[3] = {variants[0], variants[1], variants[2]};
         ctx->set_variants(precision, w);
     });

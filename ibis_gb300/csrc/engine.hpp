@@ -62,6 +62,9 @@ struct FvParams {
     // float copies for the float kernels (rounded on the host, so that the
     // device does no double->float conversions) and host-side reciprocals
     float fR, fCv, fCp, fgamma, fgR, feps, fdelta, fmu0, fT0, fTs, fPr, finv_Cv;
+    // what the float copies leave out (the double minus its float copy, rounded to
+    // float): float-float kernels take each constant as the pair (f*, lo*)
+    float loR, loCv, loCp, logamma, logR, lodelta, lomu0, loT0, loTs, loPr;
     double inv_Cv;
 };
 
@@ -120,9 +123,17 @@ struct DevView {
     void* phi;     // [5][N]: their limiter values
     void* vgrad;   // [4*3][N]: gradients of T, vx, vy, vz for the viscous flux
     void* flux;    // [nc][F]
+    // float-float build (MIXED_FF) only, else null: what the float arrays above
+    // leave out of each double value (value - float copy, rounded to float), so
+    // that prim + prim_lo etc. hold the value to about 48 bits
+    float* prim_lo;        // [7][NT]
+    const float* cc_lo;    // [3][NT]
+    const float* face_lo;  // [13][F]
+    float* flux_lo;        // [nc][F]
     double* vsig;  // [F]: viscous time-step signal (gamma/rho)(mu/Pr) per face
     double* U;     // [nc][N]
     double* k;     // [stages][nc][N]
+    int k_alias;   // 1: every stage derivative in slot 0 (the reference's aliased stages)
     StepCtl* ctl;            // one control block per case
     const int* case_of;      // case of each valid cell (batched ensembles), or null for one case
     int n_cases;
@@ -171,6 +182,7 @@ KernelOps kernels_f64();
 KernelOps kernels_f64_exact();
 KernelOps kernels_mixed();
 KernelOps kernels_mixed_grad();
+KernelOps kernels_mixed_ff();
 
 // precision-independent kernels (kernels_common.cu)
 // Fused Runge-Kutta stage on structured blocks (mixed build, inviscid, second

@@ -22,6 +22,8 @@
 //                                                      runge_kutta.cpp:131-203]
 #pragma once
 
+#include <type_traits>
+
 #include "numerics.cuh"
 
 namespace ibisgb {
@@ -50,6 +52,18 @@ using State64 = StateT<double>;
 
 IBISGB_HD double real_of(double x) { return x; }
 IBISGB_HD double real_of(float x) { return (double)x; }
+IBISGB_HD double real_of(const FF& x) { return ff_to_double(x); }
+IBISGB_HD float to_float(double x) { return (float)x; }
+IBISGB_HD float to_float(float x) { return x; }
+IBISGB_HD float to_float(const FF& x) { return x.hi; }
+
+// A translation unit that defines IBISGB_FLOAT_FLOAT to 1 builds the MIXED_FF
+// family: the float state and geometry arrays plus their lo companions
+// (DevView::prim_lo ...), face states and fluxes in float-float arithmetic.
+#ifndef IBISGB_FLOAT_FLOAT
+#define IBISGB_FLOAT_FLOAT 0
+#endif
+constexpr bool kFFBuild = IBISGB_FLOAT_FLOAT != 0;
 
 // primitive index of viscous variable q (0 T, 1 vx, 2 vy, 3 vz)
 IBISGB_HD int visc_prim(int q) { return q == 0 ? 2 : 3 + q; }
@@ -84,6 +98,33 @@ __device__ __forceinline__ float d2f(double x) {
     return __uint_as_float(((hi & 0x80000000u) | ((ex - 896u) << 23)) + m + up);
 }
 
+// A double as a float-float pair on the integer pipe: hi as d2f, lo the exact
+// remainder x - hi (the 29 dropped significand bits less the rounding carry,
+// at most 28 bits) rounded to float by an int->float conversion and moved to
+// its binade by an exponent addition.  Zero takes a bit test; tiny and
+// non-finite inputs take the conversion instructions, in a call.
+__device__ __noinline__ FF d2ff_by_instruction(double x) {
+    const float h = __double2float_rn(x);
+    return FF(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ FF d2ff(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ex = (hi >> 20) & 0x7FFu;
+    if (ex == 0u && (hi & 0xFFFFFu) == 0u && lo == 0u) return FF(__uint_as_float(hi & 0x80000000u), 0.f);  // +-0
+    // |x| outside [2^-74, 2^128): hi out of float range, or lo possibly subnormal
+    if (ex - 949u > 201u) return d2ff_by_instruction(x);
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1FFFFFFFu;
+    const unsigned up = (rem > 0x10000000u) | ((rem == 0x10000000u) & m);
+    const float h = __uint_as_float(((hi & 0x80000000u) | ((ex - 896u) << 23)) + m + up);
+    int d = (int)rem - (int)(up << 29);
+    if (d == 0) return FF(h, 0.f);
+    if (hi >> 31) d = -d;
+    // d * 2^(ex - 1075): the conversion is exact to 24 bits, the scaling exact (normal result)
+    const int fb = __float_as_int(__int2float_rn(d));
+    return FF(h, __int_as_float(fb + ((int)ex - 1075) * (1 << 23)));
+}
+
 // A value in the storage type P of the state arrays: for the float build the
 // integer-pipe conversion (bit for bit the instruction's), else a cast.
 template <class P, class S>
@@ -95,10 +136,16 @@ __device__ __forceinline__ P to_storage(S x) {
 // ---------------------------------------------------------------------------
 // Ghost-cell actions on one ghost (boundary.cpp:9-400), in double.
 // ---------------------------------------------------------------------------
+// face_lo (float-float build, else null): what the float geometry leaves out,
+// so that the normal and tangents the actions use are hi + lo in double
 template <class S, class Gm>
 __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const StateT<S>& src,
                               const Gm* face, int F, int f, const FvParams& prm, const double* gfix, int G,
-                              int g) {
+                              int g, const float* face_lo = nullptr) {
+    auto geo = [&](int k) -> S {
+        if (face_lo) return S((double)face[k * F + f] + (double)face_lo[k * F + f]);
+        return S(face[k * F + f]);
+    };
     for (int a = 0; a < n; a++) {
         const Action& A = acts[a];
         switch (A.kind) {
@@ -113,9 +160,9 @@ __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const St
             case aReflectNormal: {
                 gh.T = src.T; gh.p = src.p; gh.rho = src.rho; gh.e = src.e;
                 S x = src.vx, y = src.vy, z = src.vz;
-                S nx = S(face[f]), ny = S(face[F + f]), nz = S(face[2 * F + f]);
-                S t1x = S(face[3 * F + f]), t1y = S(face[4 * F + f]), t1z = S(face[5 * F + f]);
-                S t2x = S(face[6 * F + f]), t2y = S(face[7 * F + f]), t2z = S(face[8 * F + f]);
+                S nx = geo(0), ny = geo(1), nz = geo(2);
+                S t1x = geo(3), t1y = geo(4), t1z = geo(5);
+                S t2x = geo(6), t2y = geo(7), t2z = geo(8);
                 S xs = -(x * nx + y * ny + z * nz);
                 S ys = x * t1x + y * t1y + z * t1z;
                 S zs = x * t2x + y * t2y + z * t2z;
@@ -137,7 +184,7 @@ __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const St
                 break;
             }
             case aSubsonicInflow: {
-                S nx = S(face[f]), ny = S(face[F + f]), nz = S(face[2 * F + f]);
+                S nx = geo(0), ny = geo(1), nz = geo(2);
                 S vc = nx * (S(A.fs[4]) - src.vx) + ny * (S(A.fs[5]) - src.vy) + nz * (S(A.fs[6]) - src.vz);
                 S sos = d_sqrt<S>(S(prm.gamma) * S(prm.R) * src.T);
                 S rho_ref = src.rho;
@@ -155,7 +202,7 @@ __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const St
                 break;
             }
             case aSubsonicOutflow: {
-                S nx = S(face[f]), ny = S(face[F + f]), nz = S(face[2 * F + f]);
+                S nx = geo(0), ny = geo(1), nz = geo(2);
                 S p_face = S(A.value);
                 S rho_ref = src.rho, p_ref = src.p;
                 S sos = d_sqrt<S>(S(prm.gamma) * S(prm.R) * src.T);
@@ -183,14 +230,24 @@ __device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const S
     const Gm* face = (const Gm*)v.face;
     int f = v.ghost_face[g];
     StateT<S> gh = src;
-    apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm, v.gfix, v.G, g);
+    apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm, v.gfix, v.G, g, v.face_lo);
     P* pr = (P*)v.prim;
     const int NT = v.NT, id = v.N + g;
-    pr[id] = to_storage<P>(gh.rho); pr[NT + id] = to_storage<P>(gh.p); pr[2 * NT + id] = to_storage<P>(gh.T);
-    pr[3 * NT + id] = to_storage<P>(gh.e); pr[4 * NT + id] = to_storage<P>(gh.vx);
-    pr[5 * NT + id] = to_storage<P>(gh.vy); pr[6 * NT + id] = to_storage<P>(gh.vz);
+    if constexpr (kFFBuild && sizeof(P) == sizeof(float) && !kIsDual<S>) {
+        const double w[7] = {gh.rho, gh.p, gh.T, gh.e, gh.vx, gh.vy, gh.vz};
+#pragma unroll
+        for (int k = 0; k < 7; k++) {
+            const FF x = d2ff(w[k]);
+            pr[k * NT + id] = x.hi;
+            v.prim_lo[k * NT + id] = x.lo;
+        }
+    } else {
+        pr[id] = to_storage<P>(gh.rho); pr[NT + id] = to_storage<P>(gh.p); pr[2 * NT + id] = to_storage<P>(gh.T);
+        pr[3 * NT + id] = to_storage<P>(gh.e); pr[4 * NT + id] = to_storage<P>(gh.vx);
+        pr[5 * NT + id] = to_storage<P>(gh.vy); pr[6 * NT + id] = to_storage<P>(gh.vz);
+    }
     if (prm.viscous) {
-        apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm, v.gfix, v.G, g);
+        apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm, v.gfix, v.G, g, v.face_lo);
         P* vg = (P*)v.vghost;
         vg[g] = to_storage<P>(gh.p); vg[v.G + g] = to_storage<P>(gh.T); vg[2 * v.G + g] = to_storage<P>(gh.vx);
         vg[3 * v.G + g] = to_storage<P>(gh.vy); vg[4 * v.G + g] = to_storage<P>(gh.vz);
@@ -201,6 +258,11 @@ template <class P, class S>
 __device__ StateT<S> load_state(const DevView& v, int c) {
     const P* pr = (const P*)v.prim;
     const int NT = v.NT;
+    if constexpr (kFFBuild && sizeof(P) == sizeof(float) && !kIsDual<S>) {
+        const float* lo = v.prim_lo;
+        auto g = [&](int k) { return S((double)pr[k * NT + c] + (double)lo[k * NT + c]); };
+        return StateT<S>{g(0), g(1), g(2), g(3), g(4), g(5), g(6)};
+    }
     return StateT<S>{S(pr[c]), S(pr[NT + c]), S(pr[2 * NT + c]), S(pr[3 * NT + c]),
                      S(pr[4 * NT + c]), S(pr[5 * NT + c]), S(pr[6 * NT + c])};
 }
@@ -237,6 +299,12 @@ template <class R, class P, bool EXACT>
 constexpr bool relative_float_gradients() {
     return !EXACT && sizeof(R) == sizeof(float) && sizeof(P) == sizeof(double);
 }
+// the same for the float-float build: the differences are (hi - hi) + (lo - lo)
+// of the float arrays and their lo companions
+template <class R, class P, bool EXACT>
+constexpr bool relative_ff_gradients() {
+    return kFFBuild && !EXACT && sizeof(R) == sizeof(float) && sizeof(P) == sizeof(float);
+}
 constexpr int kPackedGrad = 16;  // floats per cell of the packed gradients
 
 template <class R, class P, class Gm, int DIM, bool EXACT, int BS = kBlock, int MINB = 1>
@@ -257,6 +325,8 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
     const bool lim = reconstruct && prm.limiter;
 
     constexpr bool REL = relative_float_gradients<R, P, EXACT>();
+    constexpr bool RELF = relative_ff_gradients<R, P, EXACT>();
+    const float* plo = v.prim_lo;
     R xi = (R)cc[i], yi = (R)cc[NT + i], zi = DIM == 3 ? (R)cc[2 * NT + i] : R(0.0);
     double xid = 0.0, yid = 0.0, zid = 0.0;
     if constexpr (REL) { xid = (double)cc[i]; yid = (double)cc[NT + i]; zid = DIM == 3 ? (double)cc[2 * NT + i] : 0.0; }
@@ -270,10 +340,17 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
     // REL: ui = 0 and every neighbour value is taken relative to the cell's (uid)
     R ui[NV], gx[NV], gy[NV], gz[NV], umin[NV], umax[NV];
     double uid[NV];
+    float uhi[NV], ulo[NV];  // RELF: the cell's own value as hi + lo
 #pragma unroll
     for (int q = 0; q < NV; q++) {
+        uhi[q] = 0.f; ulo[q] = 0.f;
         if constexpr (REL) {
             uid[q] = (double)pr[vidx[q] * NT + i];
+            ui[q] = R(0.0);
+        } else if constexpr (RELF) {
+            uid[q] = 0.0;
+            uhi[q] = (float)pr[vidx[q] * NT + i];
+            ulo[q] = plo[vidx[q] * NT + i];
             ui[q] = R(0.0);
         } else {
             uid[q] = 0.0;
@@ -285,10 +362,17 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
     constexpr int NW = DIM == 3 ? 4 : 3;  // viscous: T, vx, vy[, vz]
     R wi[NW], hx[NW], hy[NW], hz[NW];
     double wid[NW];
+    float whi[NW], wlo[NW];
 #pragma unroll
     for (int q = 0; q < NW; q++) {
+        whi[q] = 0.f; wlo[q] = 0.f;
         if constexpr (REL) {
             wid[q] = (double)pr[visc_prim(q) * NT + i];
+            wi[q] = R(0.0);
+        } else if constexpr (RELF) {
+            wid[q] = 0.0;
+            whi[q] = (float)pr[visc_prim(q) * NT + i];
+            wlo[q] = plo[visc_prim(q) * NT + i];
             wi[q] = R(0.0);
         } else {
             wid[q] = 0.0;
@@ -322,6 +406,8 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
             for (int q = 0; q < NV; q++) {
                 R un;
                 if constexpr (REL) un = (R)((double)pr[vidx[q] * NT + nb] - uid[q]);
+                else if constexpr (RELF)
+                    un = ((float)pr[vidx[q] * NT + nb] - uhi[q]) + (plo[vidx[q] * NT + nb] - ulo[q]);
                 else un = (R)pr[vidx[q] * NT + nb];
                 R du = un - ui[q];
                 gx[q] += w1 * du; gy[q] += w2 * du;
@@ -337,6 +423,9 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                 R un;
                 if constexpr (REL)
                     un = (R)((ghost ? (double)vg[(1 + q) * G + (nb - N)] : (double)pr[visc_prim(q) * NT + nb]) - wid[q]);
+                else if constexpr (RELF)  // the pre-viscous ghost values are floats
+                    un = ghost ? ((float)vg[(1 + q) * G + (nb - N)] - whi[q]) - wlo[q]
+                               : ((float)pr[visc_prim(q) * NT + nb] - whi[q]) + (plo[visc_prim(q) * NT + nb] - wlo[q]);
                 else un = ghost ? (R)vg[(1 + q) * G + (nb - N)] : (R)pr[visc_prim(q) * NT + nb];
                 R du = un - wi[q];
                 hx[q] += w1 * du; hy[q] += w2 * du;
@@ -502,7 +591,7 @@ __device__ __forceinline__ void convective_flux(const FvParams& prm, const Gas<R
     switch (prm.flux) {
         case kHanel: flux_hanel<R, DIM>(L, Rt, gm, Fl); break;
         case kAusmdv: flux_ausmdv<R, DIM>(L, Rt, gm, Fl); break;
-        case kLdfss2: flux_ldfss2<R, DIM, EXACT>(L, Rt, gm, par<R>(prm.delta, prm.fdelta), Fl); break;
+        case kLdfss2: flux_ldfss2<R, DIM, EXACT>(L, Rt, gm, par<R>(prm.delta, prm.fdelta, prm.lodelta), Fl); break;
         default: flux_rusanov<R, DIM>(L, Rt, gm, Fl); break;
     }
     R px = Fl[1], py = Fl[2], pz = DIM == 3 ? Fl[3] : R(0.0);
@@ -585,8 +674,9 @@ __device__ __forceinline__ void viscous_face(const FvParams& prm, const Gas<R>& 
     R vx = R(0.5) * (sl[2] + sr[2]);
     R vy = R(0.5) * (sl[3] + sr[3]);
     R vz = DIM == 3 ? R(0.5) * (sl[4] + sr[4]) : R(0.0);
-    mu = sutherland<R, EXACT>(T, par<R>(prm.mu0, prm.fmu0), par<R>(prm.T0, prm.fT0), par<R>(prm.Ts, prm.fTs));
-    k = gm.Cp * mu / par<R>(prm.Pr, prm.fPr);
+    mu = sutherland<R, EXACT>(T, par<R>(prm.mu0, prm.fmu0, prm.lomu0), par<R>(prm.T0, prm.fT0, prm.loT0),
+                             par<R>(prm.Ts, prm.fTs, prm.loTs));
+    k = gm.Cp * mu / par<R>(prm.Pr, prm.fPr, prm.loPr);
     R lambda = R(-2.0 / 3.0) * mu;
     const R *gT = g[0], *gx = g[1], *gy = g[2], *gz = g[3];
     R bulk = lambda * (gx[0] + gy[1] + gz[2]);
@@ -619,7 +709,21 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
     const P* gr = (const P*)v.grad;
     const P* ph = (const P*)v.phi;
     const Gas<R> gm(prm);
-    const R nx = (R)fg[f], ny = (R)fg[F + f], nz = DIM == 3 ? (R)fg[2 * F + f] : R(0.0);
+    // float-float build: every geometry and state value as its float plus its lo companion
+    constexpr bool FFR = kFFBuild && std::is_same_v<R, FF>;
+    auto geo = [&](int k) -> R {
+        if constexpr (FFR) return FF((float)fg[k * F + f], v.face_lo[k * F + f]);
+        else return (R)fg[k * F + f];
+    };
+    auto cen = [&](int k, int c) -> R {
+        if constexpr (FFR) return FF((float)cc[k * NT + c], v.cc_lo[k * NT + c]);
+        else return (R)cc[k * NT + c];
+    };
+    auto prim = [&](int k, int c) -> R {
+        if constexpr (FFR) return FF((float)pr[k * NT + c], v.prim_lo[k * NT + c]);
+        else return (R)pr[k * NT + c];
+    };
+    const R nx = geo(0), ny = geo(1), nz = DIM == 3 ? geo(2) : R(0.0);
     R t1x, t1y, t1z, t2x, t2y, t2z;
     if constexpr (!EXACT && sizeof(R) == sizeof(float) && DIM == 3) {
         // The float build rotates into a frame built from n (any orthonormal
@@ -636,11 +740,11 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
         t2y = nz * t1x - nx * t1z;
         t2z = nx * t1y - ny * t1x;
     } else {
-        t1x = (R)fg[3 * F + f]; t1y = (R)fg[4 * F + f]; t1z = DIM == 3 ? (R)fg[5 * F + f] : R(0.0);
-        t2x = DIM == 3 ? (R)fg[6 * F + f] : R(0.0); t2y = DIM == 3 ? (R)fg[7 * F + f] : R(0.0);
-        t2z = (R)fg[8 * F + f];
+        t1x = geo(3); t1y = geo(4); t1z = DIM == 3 ? geo(5) : R(0.0);
+        t2x = DIM == 3 ? geo(6) : R(0.0); t2y = DIM == 3 ? geo(7) : R(0.0);
+        t2z = geo(8);
     }
-    const R fx = (R)fg[9 * F + f], fy = (R)fg[10 * F + f], fz = DIM == 3 ? (R)fg[11 * F + f] : R(0.0);
+    const R fx = geo(9), fy = geo(10), fz = DIM == 3 ? geo(11) : R(0.0);
     int ia, ib;
     thermo_vars(prm.thermo, ia, ib);
     const int cells[2] = {v.left[f], v.right[f]};
@@ -654,9 +758,9 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
 #pragma unroll
         for (int k = 0; k < 7; k++)
             q[k] = (DIM == 2 && k == 6) || (reconstruct && k < 4 && k != ia && k != ib) ? R(0.0)
-                                                                                    : (R)pr[k * NT + c];
+                                                                                    : prim(k, c);
         if (reconstruct && c < N) {
-            R dx = fx - (R)cc[c], dy = fy - (R)cc[NT + c], dz = DIM == 3 ? fz - (R)cc[2 * NT + c] : R(0.0);
+            R dx = fx - cen(0, c), dy = fy - cen(1, c), dz = DIM == 3 ? fz - cen(2, c) : R(0.0);
             if constexpr (prescaled_gradients<P, EXACT>()) {
                 // packed limiter-scaled gradients: q_f = q + (phi grad) . d
                 const float4* src = (const float4*)v.grad + (size_t)c * (kPackedGrad / 4);
@@ -668,7 +772,7 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
                 }
                 // the increment (phi grad) . d in float; with double face states
                 // (MIXED_GRAD) it is added to the double cell value
-                const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+                const float fdx = to_float(dx), fdy = to_float(dy), fdz = to_float(dz);
                 auto rec = [&](R val, int w) {
                     float sgr = DIM == 3 ? pk[3 * w] * fdx + pk[3 * w + 1] * fdy + pk[3 * w + 2] * fdz
                                          : pk[2 * w] * fdx + pk[2 * w + 1] * fdy;
@@ -723,9 +827,16 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
         const P* vgd = (const P*)v.vgrad;
         const P* vgh = (const P*)v.vghost;
         // visc states of both sides (ghost: pre-viscous values): p, T, vx, vy, vz
+        constexpr bool FFR = kFFBuild && std::is_same_v<R, FF>;
         auto vstate = [&](int c, int k) -> R {
             if (c >= N) return (R)vgh[k * G + (c - N)];
-            return (R)pr[(k == 0 ? 1 : visc_prim(k - 1)) * NT + c];
+            const int idx = (k == 0 ? 1 : visc_prim(k - 1)) * NT + c;
+            if constexpr (FFR) return FF((float)pr[idx], v.prim_lo[idx]);
+            else return (R)pr[idx];
+        };
+        auto cen = [&](int k, int c) -> R {
+            if constexpr (FFR) return FF((float)cc[k * NT + c], v.cc_lo[k * NT + c]);
+            else return (R)cc[k * NT + c];
         };
         R sl[5], sr[5], gl[12], grr[12];
 #pragma unroll
@@ -736,8 +847,8 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
         for (int k = 0; k < 12; k++) { gl[k] = (R)vgd[k * N + gl_c]; grr[k] = (R)vgd[k * N + gr_c]; }
         R ex = R(0.0), ey = R(0.0), ez = R(0.0);
         if (interior) {
-            ex = (R)cc[r] - (R)cc[l]; ey = (R)cc[NT + r] - (R)cc[NT + l];
-            ez = DIM == 3 ? (R)cc[2 * NT + r] - (R)cc[2 * NT + l] : R(0.0);
+            ex = cen(0, r) - cen(0, l); ey = cen(1, r) - cen(1, l);
+            ez = DIM == 3 ? cen(2, r) - cen(2, l) : R(0.0);
         }
         R vt[4], rho, mu, k;
         viscous_face<R, DIM, EXACT>(prm, gm, interior, sl, sr, gl, grr, ex, ey, ez, nx, ny, nz, vt, rho, mu, k);
@@ -751,11 +862,20 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
         v.vsig[f] = (prm.gamma / real_of(rho)) * (mud / Prf);
     }
     P* fo = (P*)v.flux;
-    fo[f] = (P)Fg[0];
-    fo[F + f] = (P)mx;
-    fo[2 * F + f] = (P)my;
-    if (DIM == 3) fo[3 * F + f] = (P)mz;
-    fo[(DIM + 1) * F + f] = (P)en;
+    if constexpr (kFFBuild && std::is_same_v<R, FF>) {  // hi into the flux array, lo into its companion
+        float* flo = v.flux_lo;
+        fo[f] = Fg[0].hi; flo[f] = Fg[0].lo;
+        fo[F + f] = mx.hi; flo[F + f] = mx.lo;
+        fo[2 * F + f] = my.hi; flo[2 * F + f] = my.lo;
+        if (DIM == 3) { fo[3 * F + f] = mz.hi; flo[3 * F + f] = mz.lo; }
+        fo[(DIM + 1) * F + f] = en.hi; flo[(DIM + 1) * F + f] = en.lo;
+    } else {
+        fo[f] = (P)Fg[0];
+        fo[F + f] = (P)mx;
+        fo[2 * F + f] = (P)my;
+        if (DIM == 3) fo[3 * F + f] = (P)mz;
+        fo[(DIM + 1) * F + f] = (P)en;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -810,6 +930,32 @@ __device__ Committed<P> commit_state(const DevView& v, const FvParams& prm, int 
     // conserved_to_primatives in double (primative_conserved_conversion.cpp:4-23); the fast
     // paths replace the divisions by one reciprocal (the FP64 pipe is GB300's scarcest unit)
     double rho = u[0], vx, vy, vz, e, T;
+    if constexpr (kFFBuild && sizeof(P) == sizeof(float)) {
+        // float-float build: the inversion in double as the mixed build, T and p in
+        // double too, each primitive stored as float + lo (integer-pipe split)
+        const double ir = recip_newton1_fseed(rho);
+        vx = u[1] * ir;
+        vy = u[2] * ir;
+        vz = DIM == 3 ? u[3] * ir : 0.0;
+        double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
+        e = u[DIM + 1] * ir - ke;
+        T = e * prm.inv_Cv;
+        const double p = rho * prm.R * T;
+        const double w[7] = {rho, p, T, e, vx, vy, vz};
+        float* pr = (float*)v.prim;
+        const int NT = v.NT;
+        float hs[7];
+#pragma unroll
+        for (int k = 0; k < 7; k++) {
+            const FF x = (DIM == 2 && k == 6) ? FF(0.f, 0.f) : d2ff(w[k]);
+            hs[k] = x.hi;
+            pr[k * NT + i] = x.hi;
+            v.prim_lo[k * NT + i] = x.lo;
+        }
+        const State64 s{rho, p, T, e, vx, vy, vz};
+        for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
+        return Committed<P>{rho, (P)hs[2], (P)hs[4], (P)hs[5], (P)hs[6]};
+    }
     if (!EXACT && sizeof(P) == sizeof(float)) {
         // Mixed build: rho, v and e = E/rho - |v|^2/2 in double (the cancellation of
         // strong expansions happens there); T = e/Cv and p = rho R T are products of
@@ -860,6 +1006,11 @@ __device__ Committed<P> commit_state(const DevView& v, const FvParams& prm, int 
     for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
     return Committed<P>{rho, (P)T, (P)vx, (P)vy, (P)vz};
 }
+
+// Storage slot of stage j's derivative: its own, or, when the stages alias
+// (the reference's RungeKutta, whose stage derivatives share one array), slot 0
+// for every stage, which then always holds the latest derivative.
+IBISGB_HD int kslot(const DevView& v, int j) { return v.k_alias ? 0 : j; }
 
 // control block of the case cell i belongs to
 IBISGB_HD StepCtl* ctl_of(const DevView& v, int i) { return v.case_of ? v.ctl + v.case_of[i] : v.ctl; }
@@ -926,7 +1077,35 @@ __device__ double cell_local_dt(const DevView& v, const FvParams& prm, int i, P 
     const int nf = v.nfaces[i];
     double src = 0.0, srv = 0.0;
     const double vol = v.vol[i];
-    if (sizeof(P) == sizeof(float)) {
+    if constexpr (kFFBuild && sizeof(P) == sizeof(float)) {
+        // float-float build: the state this thread just committed (hi + lo) and the
+        // geometry as hi + lo, the signal in float-float arithmetic
+        const float* pr = (const float*)v.prim;
+        const float* lo = v.prim_lo;
+        const int NT = v.NT;
+        const FF vx(pr[4 * NT + i], lo[4 * NT + i]), vy(pr[5 * NT + i], lo[5 * NT + i]);
+        const FF vz = DIM == 3 ? FF(pr[6 * NT + i], lo[6 * NT + i]) : FF(0.f);
+        const FF a = ff_sqrt(FF(prm.fgR, prm.logR) * FF(pr[2 * NT + i], lo[2 * NT + i]));
+        FF sf(0.f);
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const float* fl = v.face_lo;
+            auto geo = [&](int k) { return FF((float)fg[k * F + f], fl[k * F + f]); };
+            FF dot = vx * geo(0) + vy * geo(1);
+            if (DIM == 3) dot = dot + vz * geo(2);
+            const FF A = geo(12);
+            sf = sf + (ff_abs(dot) + a) * A;
+            if (prm.viscous) {
+                const double Ad = ff_to_double(A);
+                srv += v.vsig[f] * Ad * Ad / vol;
+            }
+        }
+        if (!prm.viscous) {
+            const FF lf = d2ff(vol) / sf;
+            return lf.hi > 0.f ? ff_to_double(lf) : 1.0e308 * 10.0;
+        }
+        src = ff_to_double(sf);
+    } else if (sizeof(P) == sizeof(float)) {
         const float vx = (float)pvx, vy = (float)pvy;
         const float vz = DIM == 3 ? (float)pvz : 0.f;
         const float a = sqrtf(prm.fgR * (float)pT);
@@ -1025,7 +1204,7 @@ __device__ __forceinline__ double update_tail(const DevView& v, const FvParams& 
             const double c = ctl->ca[ns][j];
 #pragma unroll
             for (int q = 0; q < NC; q++) {
-                double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
+                double kj = j == stage ? ks[q] : v.k[((size_t)kslot(v, j) * NC + q) * N + i];
                 u[q] += kj * c;
             }
         }
@@ -1038,7 +1217,7 @@ __device__ __forceinline__ double update_tail(const DevView& v, const FvParams& 
             if (j == stage) continue;
             const double c = ctl->cb[j];
 #pragma unroll
-            for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
+            for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)kslot(v, j) * NC + q) * N + i] * c;
         }
         const double c = ctl->cb[stage] * iv;
 #pragma unroll
@@ -1048,7 +1227,7 @@ __device__ __forceinline__ double update_tail(const DevView& v, const FvParams& 
             const double c = ctl->cb[j];
 #pragma unroll
             for (int q = 0; q < NC; q++) {
-                double kj = j == stage ? ks[q] : v.k[((size_t)j * NC + q) * N + i];
+                double kj = j == stage ? ks[q] : v.k[((size_t)kslot(v, j) * NC + q) * N + i];
                 u[q] += kj * c;
             }
         }
@@ -1075,7 +1254,7 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
     double ks[NC];
     // Mixed, last stage of a multi-stage step: the stage derivative is never read
     // again, so it is not stored and its float pair goes straight into the update.
-    const bool fold = sizeof(P) == sizeof(float) && mode == 3 && stage > 0 && !out_rm;
+    const bool fold = sizeof(P) == sizeof(float) && mode == 3 && stage > 0 && !out_rm && !v.k_alias;
     float hi[NC], lo[NC];
     double iv = 0.0;
     if (sizeof(P) == sizeof(float)) {
@@ -1086,9 +1265,22 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
         for (int q = 0; q < NC; q++) { hi[q] = 0.f; lo[q] = 0.f; }
         for (int s = 0; s < nf; s++) {
             const int f = v.cell_face[s * N + i];
-            const float a = -(float)area[f] * (float)v.outsign[s * N + i];
+            const float sg = (float)v.outsign[s * N + i];
+            const float a = -(float)area[f] * sg;
+            if constexpr (kFFBuild) {
+                // float-float flux times float-float area: hi*a, lo*a and hi*a_lo
+                const float alo = -v.face_lo[12 * F + f] * sg;
 #pragma unroll
-            for (int q = 0; q < NC; q++) pair_acc(hi[q], lo[q], (float)fl[q * F + f], a);
+                for (int q = 0; q < NC; q++) {
+                    const float x = (float)fl[q * F + f];
+                    pair_acc(hi[q], lo[q], x, a);
+                    pair_acc(hi[q], lo[q], v.flux_lo[q * F + f], a);
+                    pair_acc(hi[q], lo[q], x, alo);
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < NC; q++) pair_acc(hi[q], lo[q], (float)fl[q * F + f], a);
+            }
         }
         if (fold) {
             iv = v.inv_vol[i];
@@ -1118,7 +1310,7 @@ __device__ __forceinline__ double update_cell(const DevView& v, const FvParams& 
         }
     }
     if (!fold) {
-        double* kk = v.k + (size_t)stage * NC * N;
+        double* kk = v.k + (size_t)kslot(v, stage) * NC * N;
 #pragma unroll
         for (int q = 0; q < NC; q++) {
             kk[q * N + i] = ks[q];
@@ -1172,7 +1364,7 @@ __global__ void __launch_bounds__(BS, MINB) k_cell_update(DevView v, FvParams pr
         const double iv = fold ? v.inv_vol[i] : 0.0;
         if (!fold) {
             const float2 ivp = v.inv_vol2[i];
-            double* kk = v.k + (size_t)stage * NC * N;
+            double* kk = v.k + (size_t)kslot(v, stage) * NC * N;
 #pragma unroll
             for (int q = 0; q < NC; q++) {
                 ks[q] = pair_scale(hi[q], lo[q], ivp);
@@ -1212,7 +1404,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(DevView v, FvParams prm) {
     for (int j = 0; j < ctl->stages; j++) {
         const double c = ctl->cb[j];
 #pragma unroll
-        for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
+        for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)kslot(v, j) * NC + q) * N + i] * c;
     }
 #pragma unroll
     for (int q = 0; q < NC; q++) v.U[q * N + i] = u[q];
@@ -1235,7 +1427,7 @@ __global__ void __launch_bounds__(kBlock) k_combine(DevView v, FvParams prm, int
         if (!((ctl->a_used[stage] >> j) & 1u)) continue;
         const double c = ctl->ca[stage][j];
 #pragma unroll
-        for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)j * NC + q) * N + i] * c;
+        for (int q = 0; q < NC; q++) u[q] += v.k[((size_t)kslot(v, j) * NC + q) * N + i] * c;
     }
     commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
 }
@@ -1389,7 +1581,7 @@ struct Launch {
     }
     static KernelOps ops() {
         return KernelOps{&ghost_fill, &recon, &face_flux, &update, &combine, &prims_from_U, &local_dt,
-                         &finalize, sizeof(P) == sizeof(float) && !EXACT ? &cell_update : nullptr};
+                         &finalize, sizeof(P) == sizeof(float) && !EXACT && !kFFBuild ? &cell_update : nullptr};
     }
 };
 

@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(FusedTile<DIM>::kThreads, DIM == 3 ? 2 : 3)
         double ks[NC];
         if (!fold) {
             const float2 ivp = v.inv_vol2[i];
-            double* kk = v.k + (size_t)stage * NC * N;
+            double* kk = v.k + (size_t)kslot(v, stage) * NC * N;
 #pragma unroll
             for (int q = 0; q < NC; q++) {
                 ks[q] = pair_scale(hi[q], lo[q], ivp);

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "engine.hpp"
+#include "ff.cuh"
 
 namespace ibisgb {
 
@@ -34,22 +35,37 @@ template <> IBISGB_HD float d_floor<float>(float x) { return floorf(x); }
 template <class R> IBISGB_HD R d_copysign(R m, R s);
 template <> IBISGB_HD double d_copysign<double>(double m, double s) { return copysign(m, s); }
 template <> IBISGB_HD float d_copysign<float>(float m, float s) { return copysignf(m, s); }
+template <> IBISGB_HD FF d_sqrt<FF>(FF x) { return ff_sqrt(x); }
+template <> IBISGB_HD FF d_abs<FF>(FF x) { return ff_abs(x); }
+template <> IBISGB_HD FF d_floor<FF>(FF x) { return ff_floor(x); }
+template <> IBISGB_HD FF d_copysign<FF>(FF m, FF s) { return ff_copysign(m, s); }
+// the powers the float-float kernels meet (b^2 in LDFSS2, b^1.5 in Sutherland's
+// law) in float-float; any other power through double
+template <> IBISGB_HD FF d_pow<FF>(FF b, FF e) {
+    if (e.hi == 2.f && e.lo == 0.f) return b * b;
+    if (e.hi == 1.5f && e.lo == 0.f) return b * ff_sqrt(b);
+    const double r = pow(ff_to_double(b), ff_to_double(e));
+    const float h = (float)r;
+    return FF(h, (float)(r - (double)h));
+}
 // Kokkos::min / max semantics (ties keep the first operand)
 template <class R> IBISGB_HD R d_min(R a, R b) { return (b < a) ? b : a; }
 template <class R> IBISGB_HD R d_max(R a, R b) { return (a < b) ? b : a; }
 
 // A parameter in the arithmetic of the kernel: the double value, or its float
 // copy prepared on the host for float kernels.
-template <class R> IBISGB_HD R par(double d, float) { return R(d); }
-template <> IBISGB_HD float par<float>(double, float f) { return f; }
+// Float-float kernels take the float copy plus what it leaves out (lo).
+template <class R> IBISGB_HD R par(double d, float, float = 0.f) { return R(d); }
+template <> IBISGB_HD float par<float>(double, float f, float) { return f; }
+template <> IBISGB_HD FF par<FF>(double, float f, float lo) { return FF(f, lo); }
 
 // Gas constants in the arithmetic of the kernel.
 template <class R>
 struct Gas {
     R R_, Cv, Cp, gamma, gR;  // gR = gamma * R, as in speed_of_sound_ (gas_model.h:27-30)
     IBISGB_HD explicit Gas(const FvParams& p)
-        : R_(par<R>(p.R, p.fR)), Cv(par<R>(p.Cv, p.fCv)), Cp(par<R>(p.Cp, p.fCp)),
-          gamma(par<R>(p.gamma, p.fgamma)), gR(par<R>(p.gamma * p.R, p.fgR)) {}
+        : R_(par<R>(p.R, p.fR, p.loR)), Cv(par<R>(p.Cv, p.fCv, p.loCv)), Cp(par<R>(p.Cp, p.fCp, p.loCp)),
+          gamma(par<R>(p.gamma, p.fgamma, p.logamma)), gR(par<R>(p.gamma * p.R, p.fgR, p.logR)) {}
     IBISGB_HD R sound(R T) const { return d_sqrt<R>(gR * T); }
 };
 

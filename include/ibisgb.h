@@ -53,6 +53,15 @@ extern "C" {
  * shock transients, where the float states and fluxes of MIXED drift beyond
  * 1e-6 of the FP64 solution. */
 #define IBISGB_MIXED_GRAD 3
+/* MIXED_FF: the float arrays of MIXED plus, for every state, geometry and flux
+ * value, the float remainder that the float copy leaves out (value = hi + lo,
+ * about 48 bits).  Gradients and limiters in float on cell-relative values;
+ * face states, thermo closure, flux calculators and the local time step in
+ * float-float arithmetic on the FP32 pipe (an FP64-like result without GB300's
+ * narrow FP64 pipe); ghost actions with the normals as hi + lo; fluxes summed
+ * as float pairs; update and inversion in double.  For long runs through shock
+ * transients at MIXED-like speed. */
+#define IBISGB_MIXED_FF 4
 
 typedef struct ibisgb_ctx ibisgb_ctx;
 

@@ -26,7 +26,7 @@ def _ensemble(short_case=None):
     return sims, b
 
 
-@pytest.mark.parametrize("precision", ["f64_exact", "f64", "mixed"])
+@pytest.mark.parametrize("precision", ["f64_exact", "f64", "mixed", "mixed_grad", "mixed_ff"])
 def test_batch_residual_equals_cases(precision):
     sims, b = _ensemble()
     r = b.compute_dudt(precision)
@@ -34,7 +34,7 @@ def test_batch_residual_equals_cases(precision):
         assert np.array_equal(rb, s.compute_dudt(precision))
 
 
-@pytest.mark.parametrize("precision", ["f64_exact", "mixed"])
+@pytest.mark.parametrize("precision", ["f64_exact", "mixed", "mixed_ff"])
 def test_batch_rk_steps_equal_cases(precision):
     steps = 8
     sims, b = _ensemble(short_case=2)

@@ -53,7 +53,7 @@ def test_exact_build_matches_the_oracle_bit_for_bit(ramp):
 
 
 @pytest.mark.parametrize("precision,tol_rho,tol", [("f64", 1e-12, 1e-12), ("mixed", 5e-5, 1e-3),
-                                                   ("mixed_grad", 1e-6, 1e-6)])
+                                                   ("mixed_grad", 1e-6, 1e-6), ("mixed_ff", 1e-6, 1e-6)])
 def test_fast_builds_stay_close_to_the_oracle(ramp, precision, tol_rho, tol):
     g, c, ic, o, U_ref = ramp
     st, U = _run(g, c, ic, precision)
