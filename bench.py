@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-cases", type=int, default=64, help="ramp cases of the batched ensemble (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=200, help="timed RK steps of the batched ensemble")
+    ap.add_argument("--batch-accuracy-steps", type=int, default=2000,
+                    help="RK steps of the ensemble's accuracy leg (every precision against FP64; 0: skip)")
+    ap.add_argument("--adjoint-check", type=int, default=1,
+                    help="adjoint gradient vs central differences on the 512x256 steady ramp (0: skip)")
     ap.add_argument("--seq-steps", type=int, default=40, help="timed RK steps per case, one case at a time")
     ap.add_argument("--variants", default="",
                     help="launch variants recon,face,update of the mixed build instead of autotuning (profiling)")
@@ -256,6 +260,26 @@ def batch_measure(args, barrier):
     rho_f64 = batch.split(batch.conserved()[:, 0].copy())
     errs = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(rho_mixed, rho_f64)]
 
+    # accuracy over the configured run length: every precision for
+    # args.batch_accuracy_steps steps against the FP64 path, per case; the FP64
+    # path without fused multiply-adds shows how far rounding alone moves a case
+    acc = None
+    if args.batch_accuracy_steps > 0:
+        n_acc = args.batch_accuracy_steps
+        rho_acc, rate_acc = {}, {}
+        for prec in ("f64", "f64_exact", "mixed", "mixed_ff"):
+            batch.set_primitives(*ic_all)
+            if prec == "mixed_ff":
+                batch.autotune(prec)
+                batch.set_primitives(*ic_all)
+            sa = batch.take_steps(n_acc, prec)
+            rate_acc[prec] = cells * 3.0 * n_acc / (sa["device_ms"] / 1e3) / 1e6
+            rho_acc[prec] = batch.split(batch.conserved()[:, 0].copy())
+        acc = {"steps": n_acc, "batched_rate": rate_acc}
+        for prec in ("f64_exact", "mixed", "mixed_ff"):
+            e = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(rho_acc[prec], rho_acc["f64"])]
+            acc[prec] = {"max": max(e), "median": float(np.median(e)), "cases_above_1e-6": int(sum(x > 1e-6 for x in e))}
+
     # sequential: one case at a time, each with its own context and graph
     for s, ic in zip(sims, ics):
         s.set_primitives(*ic)
@@ -283,7 +307,8 @@ def batch_measure(args, barrier):
             "speedup": (upd_b / (ms_b / 1e3)) / (upd_s / wall_s),
             "speedup_vs_device_only": (upd_b / (ms_b / 1e3)) / (upd_s / (dev_ms / 1e3)),
             "rho_rel_l2_err_mixed_vs_f64": {"max": max(errs), "median": float(np.median(errs)),
-                                            "steps": args.warmup + args.batch_steps}}
+                                            "steps": args.warmup + args.batch_steps},
+            "accuracy": acc}
 
 
 def sweep_measure(args):
@@ -523,6 +548,18 @@ def run_ours(args, world, rank, local):
     l2_err = float(np.linalg.norm(rho_mixed - rho_f64) / np.linalg.norm(rho_f64))
     max_err = float(np.abs(rho_mixed - rho_f64).max() / np.abs(rho_f64).max())
 
+    # --- the float-float path (MIXED_FF) over the same steps from the same state
+    sim.set_primitives(*ic)
+    tune_ff = sim.autotune("mixed_ff")
+    sim.take_steps(args.warmup, "mixed_ff")
+    barrier()
+    stff = sim.take_steps(args.steps, "mixed_ff")
+    barrier()
+    ms_ff = max_over_ranks_(stff["device_ms"])
+    rho_ff = sim.conserved()[:, 0]
+    value_ff = whole_job_rate(N, world, 3, args.steps, ms_ff / 1e3)
+    l2_err_ff = float(np.linalg.norm(rho_ff - rho_f64) / np.linalg.norm(rho_f64))
+
     # --- kernel breakdown of one residual evaluation (CUDA events on the context stream)
     kt = sim.kernel_times("mixed", reps=5)
 
@@ -559,6 +596,17 @@ def run_ours(args, world, rank, local):
     plate = plate_measure(args) if args.plate_steps > 0 and rank == 0 else None
     sweep = sweep_measure(args) if args.sweep and rank == 0 else None
     jfnk = jfnk_measure(args) if args.newton_steps > 0 and rank == 0 else None
+    if jfnk is not None and args.adjoint_check:
+        from ibis_gb300.adjoint import gradient_check
+        t_adj = time.perf_counter()
+        gc = gradient_check(512, 256, seed=0, order=1, step=1e-6)
+        jfnk["adjoint_gradient_check"] = {
+            "workload": "512x256 Hicks-Henne ramp, first order, Mach and 16 bumps from seed 0; adjoint gradient of "
+                        "the ramp pressure force vs central differences (step 1e-6) of re-converged states",
+            "relative_errors": {"mach": gc["relative_errors"][0],
+                                **{f"bump_{k}": e for k, e in enumerate(gc["relative_errors"][1:])}},
+            "max_relative_error": max(gc["relative_errors"]),
+            "base_relative_residual": gc["base_relative_residual"], "seconds": time.perf_counter() - t_adj}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -579,6 +627,10 @@ def run_ours(args, world, rank, local):
                     "fp64_roofline": fp64_roofline(value_f64, n, clk.summary()["sm_mhz"] or 2070.0)},
             "accuracy": {"rho_rel_l2_err_mixed_vs_f64": l2_err, "rho_rel_max_err_mixed_vs_f64": max_err,
                          "steps": args.warmup + args.steps},
+            "mixed_ff": {"value": value_ff, "ms_per_step": ms_ff / args.steps, "speedup_vs_f64": value_ff / value_f64,
+                         "rho_rel_l2_err_vs_f64": l2_err_ff, "autotune": tune_ff["variants"],
+                         "arithmetic": "float-float (FP32 pipe) gradients, limiters, face states and fluxes; "
+                                       "f64 accumulate/update"},
             "kernel_ms": {k: round(v, 4) for k, v in kt.items()},
             "autotune": {"variants_table": Simulation.launch_variants(), "mixed": tune_mixed, "f64": tune_f64,
                          "fused_stage": dict({k: fused[k] for k in ("enabled", "fused_ms", "generic_ms")},

@@ -119,3 +119,78 @@ def shape_sensitivity(make_sim, bumps: np.ndarray, U: np.ndarray, lam: np.ndarra
     dJ = (vals[0][0] - vals[1][0]) / (2 * h)
     dR = (vals[0][1] - vals[1][1]) / (2 * h)
     return float(dJ + np.sum(lam * dR))
+
+
+def converge(sim: Simulation, precision: str = "f64", rel_tol: float | None = 1e-12, abs_tol: float | None = None,
+             max_steps: int = 400):
+    """Newton-Krylov steps until the global residual norm is below abs_tol, or,
+    without abs_tol, the relative residual below rel_tol; returns the history."""
+    sim.steady_initialise(precision)
+    hist = []
+    for _ in range(max_steps):
+        st = sim.newton_step(precision)
+        hist.append(st)
+        r = st["residual_norms"][0]
+        if not np.isfinite(r):
+            break
+        if abs_tol is not None and r <= abs_tol:
+            break
+        if abs_tol is None and st["relative_residual"] <= rel_tol:
+            break
+    return hist
+
+
+def gradient_check(ni: int = 512, nj: int = 256, seed: int = 0, order: int = 1, step: float = 1e-6,
+                   tol: float = 1e-12, n_bumps: int = 16) -> dict:
+    """The pressure force on the ramp (x >= 0.2) of the Hicks-Henne ramp case
+    (grids.ramp_bump_case, 15 degrees; Mach U[1.5, 3] and n_bumps amplitudes
+    U[-0.002, 0.002] m from `seed`, as the benchmark draws them): its adjoint
+    gradient with respect to the Mach number and every amplitude, and central
+    differences (step `step`) of the force between states re-converged at the
+    perturbed parameters, each started from the base state and converged to the
+    same absolute residual (tol times the cold start's initial residual)."""
+    from . import grids
+    rng = np.random.default_rng(seed)
+    mach = float(rng.uniform(1.5, 3.0))
+    bumps = rng.uniform(-0.002, 0.002, n_bumps)
+    cfl = {"type": "residual_based", "growth_threshold": 1.0, "power": 1.5, "start_cfl": 5.0, "max_cfl": 1e12}
+    solver = grids.steady_state(cfl=cfl, max_iters=30, tol=1e-3, max_steps=1000)
+    force = {"tag": "wall", "x_min": 0.2}
+
+    def make(m, b):
+        g, c, inf = grids.ramp_bump_case(ni, nj, mach=m, bumps=b, solver=solver, order=order)
+        s = Simulation(c, g)
+        n = s.num_cells
+        s.set_primitives(np.full(n, inf["T"]), np.full(n, inf["p"]), np.full(n, inf["vx"]), np.full(n, inf["vy"]))
+        return s
+
+    base = make(mach, bumps)
+    h0 = converge(base, rel_tol=tol)
+    abs_tol = tol * h0[0]["initial_norms"][0]
+    U0 = base.conserved()
+    J0, dJdU = wall_force(base, **force)
+    lam, ah = solve_adjoint(base, dJdU, tol=1e-12)
+    grads = [mach_sensitivity(base, lam)]
+    grads += [shape_sensitivity(lambda b: make(mach, b), bumps, U0, lam, k, h=1e-7, **force) for k in range(n_bumps)]
+
+    newton = []
+
+    def J_at(m, b):
+        s = make(m, b)
+        s.set_conserved(U0)
+        h = converge(s, abs_tol=abs_tol)
+        newton.append(len(h))
+        return wall_force(s, **force)[0]
+
+    fds = [(J_at(mach + step, bumps) - J_at(mach - step, bumps)) / (2 * step)]
+    for k in range(n_bumps):
+        bp, bm = bumps.copy(), bumps.copy()
+        bp[k] += step
+        bm[k] -= step
+        fds.append((J_at(mach, bp) - J_at(mach, bm)) / (2 * step))
+    rel = [abs(g - f) / abs(f) for g, f in zip(grads, fds)]
+    return {"grid": f"{ni}x{nj}", "order": order, "mach": mach, "force": J0, "step": step,
+            "base_newton_steps": len(h0), "base_relative_residual": h0[-1]["relative_residual"],
+            "adjoint_steps": len(ah), "adjoint_residual": ah[-1]["residual_norm"],
+            "gradient": grads, "central_differences": fds, "relative_errors": rel,
+            "newton_steps_per_perturbed_solve": newton}

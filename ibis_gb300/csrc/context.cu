@@ -76,6 +76,7 @@ struct StateBufs {
     DBuf cc, r, face, lsqw, lsqd;                  // geometry
     DBuf prim, vghost, grad, phi, vgrad, flux;     // state and intermediates
     DBuf prim_lo, cc_lo, face_lo, flux_lo;         // float-float build: lo companions of the float arrays
+    DBuf lsqw_lo, lsqd_lo, grad_lo;
     bool geometry = false;
     bool prims_current = false;
 };
@@ -635,6 +636,12 @@ struct ibisgb_ctx {
             upload(s.cc_lo, cl, stream); upload(s.face_lo, fl, stream);
             s.prim_lo.alloc(sizeof(float) * 7 * NT);
             s.flux_lo.alloc(sizeof(float) * nc() * F);
+            s.grad_lo.alloc(sizeof(float) * 16 * mesh.N);
+            if (!mesh.lsqw.empty()) {
+                std::vector<float> wl(mesh.lsqw.size());
+                for (size_t q = 0; q < wl.size(); q++) wl[q] = lo(mesh.lsqw[q]);
+                upload(s.lsqw_lo, wl, stream);
+            }
         }
         const int64_t N = mesh.N, NT = mesh.NT(), F = mesh.F;
         std::vector<Gm> cc(3 * NT), r(6 * N, Gm(0)), fc(13 * F);
@@ -657,12 +664,18 @@ struct ibisgb_ctx {
             std::vector<Gm> d(3 * MF * N, Gm(0));
             const std::vector<double>* fcs[3] = {&mesh.fcx, &mesh.fcy, &mesh.fcz};
             const std::vector<double>* ccs[3] = {&mesh.ccx, &mesh.ccy, &mesh.ccz};
+            std::vector<float> dl(with_lo ? 3 * MF * N : 0, 0.f);
             for (int64_t c = 0; c < N; c++)
                 for (int64_t k = 0; k < mesh.nfaces[c]; k++) {
                     const int64_t f = mesh.cell_face[c * MF + k];
-                    for (int a = 0; a < 3; a++) d[(a * MF + k) * N + c] = (Gm)((*fcs[a])[f] - (*ccs[a])[c]);
+                    for (int a = 0; a < 3; a++) {
+                        const double x = (*fcs[a])[f] - (*ccs[a])[c];
+                        d[(a * MF + k) * N + c] = (Gm)x;
+                        if (with_lo) dl[(a * MF + k) * N + c] = (float)(x - (double)(float)x);
+                    }
                 }
             upload(s.lsqd, d, stream);
+            if (with_lo) upload(s.lsqd_lo, dl, stream);
         }
         size_t P = sizeof(Gm);
         s.prim.alloc(P * 7 * NT);
@@ -707,6 +720,7 @@ struct ibisgb_ctx {
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
         v.prim_lo = s.prim_lo.as<float>(); v.cc_lo = s.cc_lo.as<float>();
         v.face_lo = s.face_lo.as<float>(); v.flux_lo = s.flux_lo.as<float>();
+        v.lsqw_lo = s.lsqw_lo.as<float>(); v.lsqd_lo = s.lsqd_lo.as<float>(); v.grad_lo = s.grad_lo.as<float>();
         v.U = U.as<double>(); v.k = k.as<double>(); v.ctl = ctl.as<StepCtl>();
         v.k_alias = k_alias ? 1 : 0;
         v.case_of = n_cases > 1 ? case_of.as<int>() : nullptr;

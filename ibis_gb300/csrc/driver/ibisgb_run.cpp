@@ -9,7 +9,7 @@
 // log/gmres_diagnostics.dat (steady state).  The work goes through the C ABI of
 // libibisgb.so only.
 //
-//   ibisgb-run [--precision f64|mixed|f64_exact] [--case DIR]
+//   ibisgb-run [--precision f64|mixed|mixed_ff|mixed_grad|f64_exact] [--case DIR]
 //
 // Exit status: 0 on success, 1 when a step fails or leaves bad cells (as
 // Solver::solve), 2 for unreadable input or a refused configuration.
@@ -106,6 +106,8 @@ class Case {
         if (precision == "f64") prec_ = IBISGB_F64;
         else if (precision == "mixed") prec_ = IBISGB_MIXED;
         else if (precision == "f64_exact") prec_ = IBISGB_F64_EXACT;
+        else if (precision == "mixed_grad") prec_ = IBISGB_MIXED_GRAD;
+        else if (precision == "mixed_ff") prec_ = IBISGB_MIXED_FF;
         else throw Failure{2, "unknown precision " + precision};
         text_ = read_text("config/config.json");
         try {
@@ -334,7 +336,7 @@ int main(int argc, char** argv) {
         if (s == "--precision" && a + 1 < argc) precision = argv[++a];
         else if (s == "--case" && a + 1 < argc) dir = argv[++a];
         else {
-            std::fprintf(stderr, "usage: ibisgb-run [--precision f64|mixed|f64_exact] [--case DIR]\n");
+            std::fprintf(stderr, "usage: ibisgb-run [--precision f64|mixed|mixed_ff|mixed_grad|f64_exact] [--case DIR]\n");
             return 2;
         }
     }

@@ -130,6 +130,9 @@ struct DevView {
     const float* cc_lo;    // [3][NT]
     const float* face_lo;  // [13][F]
     float* flux_lo;        // [nc][F]
+    const float* lsqw_lo;  // [3][MF][N]
+    const float* lsqd_lo;  // [3][MF][N]
+    float* grad_lo;        // [N][16]: lo parts of the packed limiter-scaled gradients
     double* vsig;  // [F]: viscous time-step signal (gamma/rho)(mu/Pr) per face
     double* U;     // [nc][N]
     double* k;     // [stages][nc][N]

@@ -56,6 +56,12 @@ IBISGB_HD double real_of(const FF& x) { return ff_to_double(x); }
 IBISGB_HD float to_float(double x) { return (float)x; }
 IBISGB_HD float to_float(float x) { return x; }
 IBISGB_HD float to_float(const FF& x) { return x.hi; }
+// a value of arithmetic R stored as P (a float-float value keeps its hi part)
+template <class P, class R>
+IBISGB_HD P narrow(const R& x) {
+    if constexpr (std::is_same_v<R, FF>) return (P)x.hi;
+    else return (P)x;
+}
 
 // A translation unit that defines IBISGB_FLOAT_FLOAT to 1 builds the MIXED_FF
 // family: the float state and geometry arrays plus their lo companions
@@ -123,6 +129,13 @@ __device__ __forceinline__ FF d2ff(double x) {
     // d * 2^(ex - 1075): the conversion is exact to 24 bits, the scaling exact (normal result)
     const int fb = __float_as_int(__int2float_rn(d));
     return FF(h, __int_as_float(fb + ((int)ex - 1075) * (1 << 23)));
+}
+
+// (ah + al) - (bh + bl) as a float-float value: the float difference exactly
+// (TwoSum), then the difference of the remainders
+__device__ __forceinline__ FF ff_diff(float ah, float al, float bh, float bl) {
+    const FF d = ff_two_sum(ah, -bh);
+    return ff_fast_two_sum(d.hi, __fadd_rn(d.lo, __fsub_rn(al, bl)));
 }
 
 // A value in the storage type P of the state arrays: for the float build the
@@ -303,7 +316,7 @@ constexpr bool relative_float_gradients() {
 // of the float arrays and their lo companions
 template <class R, class P, bool EXACT>
 constexpr bool relative_ff_gradients() {
-    return kFFBuild && !EXACT && sizeof(R) == sizeof(float) && sizeof(P) == sizeof(float);
+    return kFFBuild && !EXACT && sizeof(P) == sizeof(float) && (sizeof(R) == sizeof(float) || std::is_same_v<R, FF>);
 }
 constexpr int kPackedGrad = 16;  // floats per cell of the packed gradients
 
@@ -326,6 +339,9 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
 
     constexpr bool REL = relative_float_gradients<R, P, EXACT>();
     constexpr bool RELF = relative_ff_gradients<R, P, EXACT>();
+    // float-float gradients and limiters (MIXED_FF): weights, offsets and the
+    // packed output carry their lo companions too
+    constexpr bool FFG = RELF && std::is_same_v<R, FF>;
     const float* plo = v.prim_lo;
     R xi = (R)cc[i], yi = (R)cc[NT + i], zi = DIM == 3 ? (R)cc[2 * NT + i] : R(0.0);
     double xid = 0.0, yid = 0.0, zid = 0.0;
@@ -386,7 +402,12 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
     const int MF = v.MF;
     auto slot = [&](int s, int nb) {
         R w1, w2, w3;
-        if (!EXACT) {  // weights precomputed on the host from the same formulas
+        if constexpr (FFG) {
+            const float* Wl = v.lsqw_lo;
+            w1 = FF((float)W[s * N + i], Wl[s * N + i]);
+            w2 = FF((float)W[(MF + s) * N + i], Wl[(MF + s) * N + i]);
+            w3 = DIM == 3 ? FF((float)W[(2 * MF + s) * N + i], Wl[(2 * MF + s) * N + i]) : FF(0.f);
+        } else if (!EXACT) {  // weights precomputed on the host from the same formulas
             w1 = (R)W[s * N + i];
             w2 = (R)W[(MF + s) * N + i];
             w3 = DIM == 3 ? (R)W[(2 * MF + s) * N + i] : R(0.0);
@@ -406,6 +427,8 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
             for (int q = 0; q < NV; q++) {
                 R un;
                 if constexpr (REL) un = (R)((double)pr[vidx[q] * NT + nb] - uid[q]);
+                else if constexpr (FFG)
+                    un = ff_diff((float)pr[vidx[q] * NT + nb], plo[vidx[q] * NT + nb], uhi[q], ulo[q]);
                 else if constexpr (RELF)
                     un = ((float)pr[vidx[q] * NT + nb] - uhi[q]) + (plo[vidx[q] * NT + nb] - ulo[q]);
                 else un = (R)pr[vidx[q] * NT + nb];
@@ -423,6 +446,9 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                 R un;
                 if constexpr (REL)
                     un = (R)((ghost ? (double)vg[(1 + q) * G + (nb - N)] : (double)pr[visc_prim(q) * NT + nb]) - wid[q]);
+                else if constexpr (FFG)  // the pre-viscous ghost values are floats
+                    un = ghost ? ff_diff((float)vg[(1 + q) * G + (nb - N)], 0.f, whi[q], wlo[q])
+                               : ff_diff((float)pr[visc_prim(q) * NT + nb], plo[visc_prim(q) * NT + nb], whi[q], wlo[q]);
                 else if constexpr (RELF)  // the pre-viscous ghost values are floats
                     un = ghost ? ((float)vg[(1 + q) * G + (nb - N)] - whi[q]) - wlo[q]
                                : ((float)pr[visc_prim(q) * NT + nb] - whi[q]) + (plo[visc_prim(q) * NT + nb] - wlo[q]);
@@ -444,12 +470,25 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
         if (lim) {
             const R eps = par<R>(prm.eps, prm.feps);
             if (EXACT || v.branches) {
-                // face by face, as limiter.cpp:46-60, recording the branch taken
+                // face by face, as limiter.cpp:46-60, recording the branch taken; the
+                // fast builds take the face offsets as their two-division form below
+                // does (per slot where stored), so recording changes no value
+                const Gm* D = (const Gm*)v.lsqd;
                 for (int s = 0; s < nf; s++) {
                     const int f = v.cell_face[s * N + i];
                     R dx = (R)fcen[f] - xi, dy = (R)fcen[F + f] - yi;
                     R dz = DIM == 3 ? (R)fcen[2 * F + f] - zi : R(0.0);
-                    if constexpr (REL) {
+                    if (!EXACT && D) {
+                        if constexpr (FFG) {
+                            const float* Dl = v.lsqd_lo;
+                            dx = FF((float)D[s * N + i], Dl[s * N + i]);
+                            dy = FF((float)D[(MF + s) * N + i], Dl[(MF + s) * N + i]);
+                            dz = DIM == 3 ? FF((float)D[(2 * MF + s) * N + i], Dl[(2 * MF + s) * N + i]) : FF(0.f);
+                        } else {
+                            dx = (R)D[s * N + i]; dy = (R)D[(MF + s) * N + i];
+                            dz = DIM == 3 ? (R)D[(2 * MF + s) * N + i] : R(0.0);
+                        }
+                    } else if constexpr (REL) {
                         dx = (R)((double)fcen[f] - xid); dy = (R)((double)fcen[F + f] - yid);
                         dz = DIM == 3 ? (R)((double)fcen[2 * F + f] - zid) : R(0.0);
                     }
@@ -477,8 +516,15 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                 for (int s = 0; s < nf; s++) {
                     R dx, dy, dz;
                     if (D) {  // face offsets stored per slot
-                        dx = (R)D[s * N + i]; dy = (R)D[(MF + s) * N + i];
-                        dz = DIM == 3 ? (R)D[(2 * MF + s) * N + i] : R(0.0);
+                        if constexpr (FFG) {
+                            const float* Dl = v.lsqd_lo;
+                            dx = FF((float)D[s * N + i], Dl[s * N + i]);
+                            dy = FF((float)D[(MF + s) * N + i], Dl[(MF + s) * N + i]);
+                            dz = DIM == 3 ? FF((float)D[(2 * MF + s) * N + i], Dl[(2 * MF + s) * N + i]) : FF(0.f);
+                        } else {
+                            dx = (R)D[s * N + i]; dy = (R)D[(MF + s) * N + i];
+                            dz = DIM == 3 ? (R)D[(2 * MF + s) * N + i] : R(0.0);
+                        }
                     } else {
                         const int f = v.cell_face[s * N + i];
                         if constexpr (REL) {
@@ -502,7 +548,7 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                     if (tneg[q] < R(0.0)) phi[q] = d_min(phi[q], (umin[q] - ui[q]) / (tneg[q] - eps));
                 }
             }
-            if (!prescaled_gradients<P, EXACT>()) {
+            if constexpr (!prescaled_gradients<P, EXACT>()) {
                 P* pout = (P*)v.phi;
 #pragma unroll
                 for (int q = 0; q < NV; q++) pout[q * N + i] = (P)phi[q];
@@ -512,7 +558,28 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                 for (int q = 0; q < 5; q++) v.branches[i * 5 + q] = q < NV ? code[q] : 0u;
             }
         }
-        if constexpr (prescaled_gradients<P, EXACT>()) {
+        if constexpr (FFG) {
+            float pk[kPackedGrad], pl[kPackedGrad];
+#pragma unroll
+            for (int k = 0; k < kPackedGrad; k++) { pk[k] = 0.f; pl[k] = 0.f; }
+#pragma unroll
+            for (int q = 0; q < NV; q++) {
+                const FF a = gx[q] * phi[q], b = gy[q] * phi[q];
+                pk[DIM * q] = a.hi; pl[DIM * q] = a.lo;
+                pk[DIM * q + 1] = b.hi; pl[DIM * q + 1] = b.lo;
+                if (DIM == 3) {
+                    const FF c = gz[q] * phi[q];
+                    pk[DIM * q + 2] = c.hi; pl[DIM * q + 2] = c.lo;
+                }
+            }
+            float4* dst = (float4*)v.grad + (size_t)i * (kPackedGrad / 4);
+            float4* dlo = (float4*)v.grad_lo + (size_t)i * (kPackedGrad / 4);
+#pragma unroll
+            for (int k = 0; k < (DIM == 3 ? 4 : 2); k++) {
+                dst[k] = make_float4(pk[4 * k], pk[4 * k + 1], pk[4 * k + 2], pk[4 * k + 3]);
+                dlo[k] = make_float4(pl[4 * k], pl[4 * k + 1], pl[4 * k + 2], pl[4 * k + 3]);
+            }
+        } else if constexpr (prescaled_gradients<P, EXACT>()) {
             float pk[kPackedGrad];
 #pragma unroll
             for (int k = 0; k < kPackedGrad; k++) pk[k] = 0.f;
@@ -539,9 +606,9 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
         P* hout = (P*)v.vgrad;
 #pragma unroll
         for (int q = 0; q < NW; q++) {
-            hout[(3 * q) * N + i] = (P)hx[q];
-            hout[(3 * q + 1) * N + i] = (P)hy[q];
-            hout[(3 * q + 2) * N + i] = (P)hz[q];
+            hout[(3 * q) * N + i] = narrow<P>(hx[q]);
+            hout[(3 * q + 1) * N + i] = narrow<P>(hy[q]);
+            hout[(3 * q + 2) * N + i] = narrow<P>(hz[q]);
         }
     }
 }
@@ -771,12 +838,29 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
                     pk[4 * k] = t.x; pk[4 * k + 1] = t.y; pk[4 * k + 2] = t.z; pk[4 * k + 3] = t.w;
                 }
                 // the increment (phi grad) . d in float; with double face states
-                // (MIXED_GRAD) it is added to the double cell value
+                // (MIXED_GRAD) it is added to the double cell value; the float-float
+                // build forms it in float-float from the packed gradients' lo parts
                 const float fdx = to_float(dx), fdy = to_float(dy), fdz = to_float(dz);
-                auto rec = [&](R val, int w) {
-                    float sgr = DIM == 3 ? pk[3 * w] * fdx + pk[3 * w + 1] * fdy + pk[3 * w + 2] * fdz
-                                         : pk[2 * w] * fdx + pk[2 * w + 1] * fdy;
-                    return val + (R)sgr;
+                float pl[kPackedGrad];
+                if constexpr (FFR) {
+                    const float4* slo = (const float4*)v.grad_lo + (size_t)c * (kPackedGrad / 4);
+#pragma unroll
+                    for (int k = 0; k < (DIM == 3 ? 4 : 2); k++) {
+                        const float4 t = slo[k];
+                        pl[4 * k] = t.x; pl[4 * k + 1] = t.y; pl[4 * k + 2] = t.z; pl[4 * k + 3] = t.w;
+                    }
+                }
+                auto rec = [&](R val, int w) -> R {
+                    if constexpr (FFR) {
+                        auto g = [&](int k) { return FF(pk[k], pl[k]); };
+                        const FF sgr = DIM == 3 ? g(3 * w) * dx + g(3 * w + 1) * dy + g(3 * w + 2) * dz
+                                                : g(2 * w) * dx + g(2 * w + 1) * dy;
+                        return val + sgr;
+                    } else {
+                        float sgr = DIM == 3 ? pk[3 * w] * fdx + pk[3 * w + 1] * fdy + pk[3 * w + 2] * fdz
+                                             : pk[2 * w] * fdx + pk[2 * w + 1] * fdy;
+                        return val + (R)sgr;
+                    }
                 };
                 q[ia] = rec(q[ia], 0);
                 q[ib] = rec(q[ib], 1);

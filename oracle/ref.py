@@ -12,6 +12,7 @@ import ctypes as C
 import json
 import os
 import subprocess
+import sys
 import tempfile
 
 import numpy as np
@@ -69,6 +70,7 @@ def lib(kind: str = "serial"):
     L.ref_ss_step.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_longlong)]
     L.ref_ss_conserved.argtypes = [C.c_void_p, _dp]
+    L.ref_run_case.argtypes = [C.c_char_p]
     _libs[kind] = L
     return L
 
@@ -199,6 +201,29 @@ class RefSteadyState:
         out = np.zeros(N * nc)
         _check(self.L, self.L.ref_ss_conserved(self.h, out))
         return out.reshape(N, nc)
+
+
+def run_case(case_dir: str, kind: str = "serial") -> int:
+    """The reference's own driver (make_solver + Solver::solve) on a case
+    directory, as `ibis run` runs it; returns solve()'s result (0: done)."""
+    L = lib(kind)
+    rc = L.ref_run_case(case_dir.encode())
+    if rc < 0:
+        _check(L, rc)
+    return rc
+
+
+def run_prep(case_dir: str, checkout: str) -> None:
+    """The reference's unchanged prep step (src/ibis/ibis/commands/prep/prep.py,
+    main(job.py, share)) in case_dir, with its pybind11 module built here
+    (Makefile.ref pyapi); run in a child process, as `ibis prep` runs it in its
+    own interpreter."""
+    code = ("import sys\n"
+            f"sys.path[:0] = [{os.path.join(checkout, 'src/ibis/ibis/commands')!r}, "
+            f"{os.path.join(checkout, 'src/ibis/ibis/commands/prep')!r}, {REF_DIR!r}]\n"
+            "import prep\n"
+            f"prep.main('job.py', {os.path.join(checkout, 'share')!r})\n")
+    subprocess.run([sys.executable, "-c", code], cwd=case_dir, check=True, capture_output=True, text=True)
 
 
 def run_doctests(timeout: float = 600.0) -> subprocess.CompletedProcess:

@@ -304,6 +304,21 @@ int ref_rk_sizes(void* hp, long long* out) {
     });
 }
 
+// The reference's own driver on a case directory: make_solver + Solver::solve
+// (solver.cpp:18-85), reading config/, io/grid/0000 and io/flow/0000 and writing
+// io/flow/NNNN, io/flow/flows and log/ as `ibis run` does.  Returns solve()'s result.
+int ref_run_case(const char* case_dir) {
+    int result = -1;
+    const int rc = guarded([&] {
+        in_dir(case_dir, [&] {
+            json config = read_json("config/config.json");
+            std::unique_ptr<Solver> solver = make_solver(config, "io/grid", "io/flow");
+            result = solver->solve();
+        });
+    });
+    return rc != 0 ? rc : result;
+}
+
 // ------------------------------------------------------------------ steady state
 struct SsCase {
     std::string dir;
