@@ -76,7 +76,7 @@ struct StateBufs {
     DBuf cc, r, face, lsqw, lsqd;                  // geometry
     DBuf prim, vghost, grad, phi, vgrad, flux;     // state and intermediates
     DBuf prim_lo, cc_lo, face_lo, flux_lo;         // float-float build: lo companions of the float arrays
-    DBuf lsqw_lo, lsqd_lo, grad_lo;
+    DBuf lsqw_lo, lsqd_lo, grad_lo, vgrad_lo, vghost_lo;
     bool geometry = false;
     bool prims_current = false;
 };
@@ -637,6 +637,8 @@ struct ibisgb_ctx {
             s.prim_lo.alloc(sizeof(float) * 7 * NT);
             s.flux_lo.alloc(sizeof(float) * nc() * F);
             s.grad_lo.alloc(sizeof(float) * 16 * mesh.N);
+            s.vgrad_lo.alloc(sizeof(float) * 12 * mesh.N);
+            s.vghost_lo.alloc(sizeof(float) * 5 * std::max<int64_t>(mesh.G, 1));
             if (!mesh.lsqw.empty()) {
                 std::vector<float> wl(mesh.lsqw.size());
                 for (size_t q = 0; q < wl.size(); q++) wl[q] = lo(mesh.lsqw[q]);
@@ -721,6 +723,7 @@ struct ibisgb_ctx {
         v.prim_lo = s.prim_lo.as<float>(); v.cc_lo = s.cc_lo.as<float>();
         v.face_lo = s.face_lo.as<float>(); v.flux_lo = s.flux_lo.as<float>();
         v.lsqw_lo = s.lsqw_lo.as<float>(); v.lsqd_lo = s.lsqd_lo.as<float>(); v.grad_lo = s.grad_lo.as<float>();
+        v.vgrad_lo = s.vgrad_lo.as<float>(); v.vghost_lo = s.vghost_lo.as<float>();
         v.U = U.as<double>(); v.k = k.as<double>(); v.ctl = ctl.as<StepCtl>();
         v.k_alias = k_alias ? 1 : 0;
         v.case_of = n_cases > 1 ? case_of.as<int>() : nullptr;
@@ -1503,12 +1506,16 @@ struct ibisgb_ctx {
             const size_t pbytes = (float_storage(prec) ? sizeof(float) : sizeof(double)) * 7 * mesh.NT();
             const size_t gbytes = (float_storage(prec) ? sizeof(float) : sizeof(double)) * 5 * mesh.G;
             const size_t lbytes = is_ff(prec) ? sizeof(float) * 7 * mesh.NT() : 0;
-            tune_save.alloc(pbytes + gbytes + lbytes + 16);
+            const size_t vlbytes = is_ff(prec) ? sizeof(float) * 5 * mesh.G : 0;
+            tune_save.alloc(pbytes + gbytes + lbytes + vlbytes + 16);
             CUDA_OK(cudaMemcpyAsync(tune_save.p, v.prim, pbytes, cudaMemcpyDeviceToDevice, stream));
             if (gbytes)
                 CUDA_OK(cudaMemcpyAsync((char*)tune_save.p + pbytes, v.vghost, gbytes, cudaMemcpyDeviceToDevice, stream));
             if (lbytes)
                 CUDA_OK(cudaMemcpyAsync((char*)tune_save.p + pbytes + gbytes, v.prim_lo, lbytes,
+                                        cudaMemcpyDeviceToDevice, stream));
+            if (vlbytes)
+                CUDA_OK(cudaMemcpyAsync((char*)tune_save.p + pbytes + gbytes + lbytes, v.vghost_lo, vlbytes,
                                         cudaMemcpyDeviceToDevice, stream));
             auto launch_k = [&](int k, int w) {
                 if (k == 0) o.recon(v, prm, reco, w, stream);
@@ -1535,6 +1542,9 @@ struct ibisgb_ctx {
                 CUDA_OK(cudaMemcpyAsync(v.vghost, (char*)tune_save.p + pbytes, gbytes, cudaMemcpyDeviceToDevice, stream));
             if (lbytes)
                 CUDA_OK(cudaMemcpyAsync(v.prim_lo, (char*)tune_save.p + pbytes + gbytes, lbytes,
+                                        cudaMemcpyDeviceToDevice, stream));
+            if (vlbytes)
+                CUDA_OK(cudaMemcpyAsync(v.vghost_lo, (char*)tune_save.p + pbytes + gbytes + lbytes, vlbytes,
                                         cudaMemcpyDeviceToDevice, stream));
             if (is_mixed(prec)) {
                 generic_ms = tune_ms[gi][0][vr[0]] + tune_ms[gi][1][vr[1]] + tune_ms[gi][2][vr[2]];

@@ -133,6 +133,8 @@ struct DevView {
     const float* lsqw_lo;  // [3][MF][N]
     const float* lsqd_lo;  // [3][MF][N]
     float* grad_lo;        // [N][16]: lo parts of the packed limiter-scaled gradients
+    float* vgrad_lo;       // [4*3][N]: lo parts of the viscous gradients
+    float* vghost_lo;      // [5][G]: lo parts of the pre-viscous ghost values
     double* vsig;  // [F]: viscous time-step signal (gamma/rho)(mu/Pr) per face
     double* U;     // [nc][N]
     double* k;     // [stages][nc][N]

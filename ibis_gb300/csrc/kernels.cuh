@@ -262,8 +262,18 @@ __device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const S
     if (prm.viscous) {
         apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm, v.gfix, v.G, g, v.face_lo);
         P* vg = (P*)v.vghost;
-        vg[g] = to_storage<P>(gh.p); vg[v.G + g] = to_storage<P>(gh.T); vg[2 * v.G + g] = to_storage<P>(gh.vx);
-        vg[3 * v.G + g] = to_storage<P>(gh.vy); vg[4 * v.G + g] = to_storage<P>(gh.vz);
+        if constexpr (kFFBuild && sizeof(P) == sizeof(float) && !kIsDual<S>) {
+            const double w[5] = {gh.p, gh.T, gh.vx, gh.vy, gh.vz};
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                const FF x = d2ff(w[k]);
+                vg[k * v.G + g] = x.hi;
+                v.vghost_lo[k * v.G + g] = x.lo;
+            }
+        } else {
+            vg[g] = to_storage<P>(gh.p); vg[v.G + g] = to_storage<P>(gh.T); vg[2 * v.G + g] = to_storage<P>(gh.vx);
+            vg[3 * v.G + g] = to_storage<P>(gh.vy); vg[4 * v.G + g] = to_storage<P>(gh.vz);
+        }
     }
 }
 
@@ -447,7 +457,7 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                 if constexpr (REL)
                     un = (R)((ghost ? (double)vg[(1 + q) * G + (nb - N)] : (double)pr[visc_prim(q) * NT + nb]) - wid[q]);
                 else if constexpr (FFG)  // the pre-viscous ghost values are floats
-                    un = ghost ? ff_diff((float)vg[(1 + q) * G + (nb - N)], 0.f, whi[q], wlo[q])
+                    un = ghost ? ff_diff((float)vg[(1 + q) * G + (nb - N)], v.vghost_lo[(1 + q) * G + (nb - N)], whi[q], wlo[q])
                                : ff_diff((float)pr[visc_prim(q) * NT + nb], plo[visc_prim(q) * NT + nb], whi[q], wlo[q]);
                 else if constexpr (RELF)  // the pre-viscous ghost values are floats
                     un = ghost ? ((float)vg[(1 + q) * G + (nb - N)] - whi[q]) - wlo[q]
@@ -609,6 +619,11 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
             hout[(3 * q) * N + i] = narrow<P>(hx[q]);
             hout[(3 * q + 1) * N + i] = narrow<P>(hy[q]);
             hout[(3 * q + 2) * N + i] = narrow<P>(hz[q]);
+            if constexpr (FFG) {
+                v.vgrad_lo[(3 * q) * N + i] = hx[q].lo;
+                v.vgrad_lo[(3 * q + 1) * N + i] = hy[q].lo;
+                v.vgrad_lo[(3 * q + 2) * N + i] = hz[q].lo;
+            }
         }
     }
 }
@@ -913,7 +928,10 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
         // visc states of both sides (ghost: pre-viscous values): p, T, vx, vy, vz
         constexpr bool FFR = kFFBuild && std::is_same_v<R, FF>;
         auto vstate = [&](int c, int k) -> R {
-            if (c >= N) return (R)vgh[k * G + (c - N)];
+            if (c >= N) {
+                if constexpr (FFR) return FF((float)vgh[k * G + (c - N)], v.vghost_lo[k * G + (c - N)]);
+                else return (R)vgh[k * G + (c - N)];
+            }
             const int idx = (k == 0 ? 1 : visc_prim(k - 1)) * NT + c;
             if constexpr (FFR) return FF((float)pr[idx], v.prim_lo[idx]);
             else return (R)pr[idx];
@@ -928,7 +946,15 @@ __global__ void __launch_bounds__(BS, MINB) k_face(DevView v, FvParams prm, int 
         const bool interior = lv && rv;
         const int gl_c = interior ? l : (lv ? l : r), gr_c = interior ? r : gl_c;
 #pragma unroll
-        for (int k = 0; k < 12; k++) { gl[k] = (R)vgd[k * N + gl_c]; grr[k] = (R)vgd[k * N + gr_c]; }
+        for (int k = 0; k < 12; k++) {
+            if constexpr (FFR) {
+                gl[k] = FF((float)vgd[k * N + gl_c], v.vgrad_lo[k * N + gl_c]);
+                grr[k] = FF((float)vgd[k * N + gr_c], v.vgrad_lo[k * N + gr_c]);
+            } else {
+                gl[k] = (R)vgd[k * N + gl_c];
+                grr[k] = (R)vgd[k * N + gr_c];
+            }
+        }
         R ex = R(0.0), ey = R(0.0), ez = R(0.0);
         if (interior) {
             ex = cen(0, r) - cen(0, l); ey = cen(1, r) - cen(1, l);

@@ -322,7 +322,7 @@ class Simulation:
         return {"relative_residual": st.relative_residual, "residual_norms": list(st.residual_norms),
                 "gmres_iterations": st.gmres_iterations, "gmres_converged": bool(st.gmres_converged),
                 "gmres_residual": st.gmres_residual, "dt_star": st.dt_star, "cfl": st.cfl,
-                "step": st.step}
+                "step": st.step, "initial_norms": list(st.initial_norms)}
 
     def L2_norms(self) -> np.ndarray:
         """global, mass, momentum_x, momentum_y, momentum_z, energy of the first-stage residual."""
