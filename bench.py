@@ -478,9 +478,11 @@ def run_reference(args, world, rank):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(headline_config(args.n, world), measured_cells_per_gpu=n ** 3,
-                           measured_workload=f"the same box at {n}^3 (bounded CPU sample; the rate is per "
-                                             f"cell-update, so it compares with the {args.n}^3 line)"),
+            "config": dict(headline_config(args.n, world),
+                           workload=f"3-D Euler periodic box measured at {n}^3 on the host cores (a bounded "
+                                    f"CPU sample of the {args.n}^3 residual-throughput case: ssp-rk3, Hanel, "
+                                    f"2nd-order MUSCL + Barth-Jespersen, rho_u; the rate is per cell-update)",
+                           measured_cells_per_gpu=n ** 3),
             "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": num_threads(),
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
@@ -606,7 +608,8 @@ def run_ours(args, world, rank, local):
             "relative_errors": {"mach": gc["relative_errors"][0],
                                 **{f"bump_{k}": e for k, e in enumerate(gc["relative_errors"][1:])}},
             "max_relative_error": max(gc["relative_errors"]),
-            "base_relative_residual": gc["base_relative_residual"], "seconds": time.perf_counter() - t_adj}
+            "base_relative_residual": gc["base_relative_residual"], "adjoint_steps": gc["adjoint_steps"],
+            "adjoint_relative_residual": gc["adjoint_relative_residual"], "seconds": time.perf_counter() - t_adj}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -40,7 +40,7 @@ class NewtonStatus(C.Structure):
 
 class AdjointStatus(C.Structure):
     _fields_ = [("residual_norm", C.c_double), ("gmres_iterations", C.c_int32), ("gmres_converged", C.c_int32),
-                ("gmres_residual", C.c_double), ("dt_star", C.c_double)]
+                ("gmres_residual", C.c_double), ("dt_star", C.c_double), ("scaled_residual_norm", C.c_double)]
 
 
 class RkStatus(C.Structure):
@@ -84,6 +84,7 @@ def load(build_if_missing: bool = True):
     L.ibisgb_rk_run.argtypes = [_P, C.c_int32, C.c_int64, C.POINTER(RkStatus)]
     L.ibisgb_l2_norms.argtypes = [_P, _P]
     L.ibisgb_get_dump.argtypes = [_P, C.c_int32, _P, C.c_int64]
+    L.ibisgb_numbering.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.ibisgb_synchronize.argtypes = [_P]
     L.ibisgb_set_conserved.argtypes = [_P, _P]
     L.ibisgb_set_conserved_device.argtypes = [_P, _P, _P]

@@ -292,6 +292,14 @@ struct ibisgb_ctx {
             if (grid.contains("motion") && grid.at("motion").contains("enabled") &&
                 grid.at("motion").at("enabled").as_bool())
                 throw ConfigError("moving grids are not supported");
+            renumber_mode = 0;
+            if (grid.contains("renumber")) {  // not a reference key: the internal cell order
+                const std::string r = grid.at("renumber").as_string();
+                if (r == "auto") renumber_mode = 0;
+                else if (r == "rcm") renumber_mode = 1;
+                else if (r == "none") renumber_mode = 2;
+                else throw ConfigError("grid.renumber must be auto, rcm or none");
+            }
             prm.fR = (float)prm.R; prm.fCv = (float)prm.Cv; prm.fCp = (float)prm.Cp;
             prm.fgamma = (float)prm.gamma; prm.fgR = prm.fgamma * prm.fR; prm.feps = (float)prm.eps;
             prm.fdelta = (float)prm.delta; prm.fmu0 = (float)prm.mu0; prm.fT0 = (float)prm.T0;
@@ -422,6 +430,7 @@ struct ibisgb_ctx {
         std::vector<BoundarySpec> specs = boundary_specs();
         build_mesh(in, specs, prm.viscous || prm.order > 1, mesh);
         check_index_range();
+        choose_numbering();
         // the fast kernels visit at most 6 face slots per cell in 3-D, 4 in 2-D (the
         // most faces of any element type the reference reads)
         if (mesh.MF > (in.dim == 3 ? 6 : 4)) throw ConfigError("a cell has more faces than any supported element");
@@ -453,6 +462,105 @@ struct ibisgb_ctx {
             }
             bounds_host.push_back(d);
         }
+    }
+
+    // ----- internal cell / face numbering ---------------------------------------
+    // The device arrays are in an internal order (reverse Cuthill-McKee of the
+    // cell graph, faces by their lower then higher cell) when that shortens the
+    // cell graph's bandwidth; every array and id that crosses the ABI stays in the
+    // reference's numbering (grid.h:113-133).  Per-cell and per-face arithmetic and
+    // summation orders are unchanged, so the results are the same bits.
+    int renumber_mode = 0;  // 0 auto, 1 rcm, 2 none
+    MeshNumbering num;
+    int64_t bandwidth_ref = 0, bandwidth_internal = 0;
+    DBuf d_cell_to_new, d_cell_to_ref, map_a, map_b;
+    bool renumbered() const { return num.active(); }
+
+    void choose_numbering() {
+        bandwidth_ref = bandwidth_internal = cell_bandwidth(mesh);
+        if (renumber_mode == 2 || mesh.N < 2) return;
+        if (renumber_mode == 0) {  // auto: unstructured grids only (quad / hex blocks keep their lattice)
+            bool all_lattice = true;
+            for (int64_t c = 0; c < mesh.N && all_lattice; c++)
+                all_lattice = mesh.cell_kind[c] == (mesh.dim == 2 ? kQuad : kHex);
+            if (all_lattice) return;
+        }
+        std::vector<int64_t> order = rcm_cell_order(mesh);
+        Mesh trial = mesh;
+        MeshNumbering tn;
+        renumber_mesh(trial, order, tn);
+        const int64_t bw = cell_bandwidth(trial);
+        if (renumber_mode == 0 && 2 * bw > bandwidth_ref) return;  // auto: only for a 2x shorter bandwidth
+        mesh = std::move(trial);
+        num = std::move(tn);
+        bandwidth_internal = bw;
+    }
+
+    void ensure_maps() {
+        if (!renumbered() || d_cell_to_new.p) return;
+        const int64_t N = mesh.N;
+        std::vector<int32_t> a(N), b(N);
+        for (int64_t i = 0; i < N; i++) {
+            a[i] = (int32_t)num.cell_ref_of_new[i];
+            b[i] = (int32_t)num.cell_new_of_ref[i];
+        }
+        d_cell_to_new.alloc(sizeof(int32_t) * N);
+        d_cell_to_ref.alloc(sizeof(int32_t) * N);
+        CUDA_OK(cudaMemcpyAsync(d_cell_to_new.p, a.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
+        CUDA_OK(cudaMemcpyAsync(d_cell_to_ref.p, b.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+    }
+    // device rows (N x w): reference numbering -> internal (to_internal) or back
+    void map_rows_device(const double* src, double* dst, int w, bool to_internal) {
+        ensure_maps();
+        launch_gather_rows(dst, src, (to_internal ? d_cell_to_new : d_cell_to_ref).as<int32_t>(), (int)mesh.N, w,
+                           stream);
+        CUDA_OK(cudaGetLastError());
+    }
+    // host per-cell values (N x w rows) between the numberings
+    template <class T>
+    void map_rows_host(const T* src, T* dst, int w, bool to_internal) const {
+        const auto& m = to_internal ? num.cell_ref_of_new : num.cell_new_of_ref;
+        for (int64_t i = 0; i < mesh.N; i++)
+            for (int q = 0; q < w; q++) dst[i * w + q] = src[m[i] * w + q];
+    }
+    int64_t cell_id_to_ref(int64_t c) const {
+        return (renumbered() && c >= 0 && c < mesh.N) ? num.cell_ref_of_new[c] : c;
+    }
+    int64_t face_id_to_ref(int64_t f) const { return (renumbered() && f >= 0) ? num.face_ref_of_new[f] : f; }
+
+    // the residual / tangent / adjoint entry points on rows in the reference numbering
+    void residual_rows(int prec, double* out_rows) {
+        if (!renumbered()) return residual(prec, out_rows, true);
+        map_b.alloc(sizeof(double) * nvars());
+        residual(prec, map_b.as<double>(), true);
+        map_rows_device(map_b.as<double>(), out_rows, nc(), false);
+    }
+    void jvp_rows(const double* v, double* out_rows, double inv_dt_star, bool reconstruct) {
+        if (!renumbered()) return jvp(v, out_rows, inv_dt_star, reconstruct);
+        map_a.alloc(sizeof(double) * nvars());
+        map_b.alloc(sizeof(double) * nvars());
+        map_rows_device(v, map_a.as<double>(), nc(), true);
+        jvp(map_a.as<double>(), map_b.as<double>(), inv_dt_star, reconstruct);
+        map_rows_device(map_b.as<double>(), out_rows, nc(), false);
+    }
+    void vjp_rows(const double* w, double* out_rows, double* ghost_out, bool reconstruct) {
+        if (!renumbered()) return vjp(w, out_rows, ghost_out, reconstruct);
+        map_a.alloc(sizeof(double) * nvars());
+        map_b.alloc(sizeof(double) * nvars());
+        map_rows_device(w, map_a.as<double>(), nc(), true);
+        vjp(map_a.as<double>(), map_b.as<double>(), ghost_out, reconstruct);  // ghost ids are not renumbered
+        map_rows_device(map_b.as<double>(), out_rows, nc(), false);
+    }
+    void adjoint_step_rows(const double* g, double* lam, double cfl, ibisgb_adjoint_status* st) {
+        if (!renumbered()) return adjoint_step(g, lam, cfl, st);
+        map_a.alloc(sizeof(double) * nvars());
+        map_b.alloc(sizeof(double) * nvars());
+        map_rows_device(g, map_a.as<double>(), nc(), true);
+        map_rows_device(lam, map_b.as<double>(), nc(), true);
+        adjoint_step(map_a.as<double>(), map_b.as<double>(), cfl, st);
+        map_rows_device(map_b.as<double>(), lam, nc(), false);
+        CUDA_OK(cudaStreamSynchronize(stream));
     }
 
     void check_index_range() const {
@@ -493,6 +601,26 @@ struct ibisgb_ctx {
             throw ConfigError(e.what());
         }
         check_index_range();
+        bandwidth_ref = bandwidth_internal = 0;
+        bool any = false;
+        for (int i = 0; i < n; i++) any = any || cs[i]->num.active();
+        if (any) {  // each case's numbering at its offsets (merge_meshes keeps the cases' own orders)
+            num.cell_ref_of_new.resize(mesh.N);
+            num.cell_new_of_ref.resize(mesh.N);
+            num.face_ref_of_new.resize(mesh.F);
+            num.face_new_of_ref.resize(mesh.F);
+            for (int i = 0; i < n; i++) {
+                const MeshNumbering& ci = cs[i]->num;
+                for (int64_t c = 0; c < cell_off[i + 1] - cell_off[i]; c++) {
+                    num.cell_ref_of_new[cell_off[i] + c] = cell_off[i] + (ci.active() ? ci.cell_ref_of_new[c] : c);
+                    num.cell_new_of_ref[cell_off[i] + c] = cell_off[i] + (ci.active() ? ci.cell_new_of_ref[c] : c);
+                }
+                for (int64_t f = 0; f < face_off[i + 1] - face_off[i]; f++) {
+                    num.face_ref_of_new[face_off[i] + f] = face_off[i] + (ci.active() ? ci.face_ref_of_new[f] : f);
+                    num.face_new_of_ref[face_off[i] + f] = face_off[i] + (ci.active() ? ci.face_new_of_ref[f] : f);
+                }
+            }
+        }
         prm.cflux = 0;
         for (int i = 0; i < n; i++) {
             // profile tables of case i follow those of the cases before it
@@ -1401,40 +1529,70 @@ struct ibisgb_ctx {
     }
 
     // One pseudo-time step of the steady adjoint J^T lambda + g = 0 (J = dR/dU at
-    // the current state): r = J^T lambda + g, GMRES on (I/dt* - J^T) d = r with
-    // the steady solver's settings, lambda += d.  The continuation converges
+    // the current state): r = J^T lambda + g, GMRES on S (I/dt* - J^T) S^-1 y = S r
+    // with the steady solver's settings, lambda += S^-1 y.  S scales each conserved
+    // variable to its RMS over the cells (density and energy; sqrt of their product
+    // for the momenta): density and energy differ by ~1e5, and GMRES on the
+    // unscaled operator stagnates on the energy rows.  The continuation converges
     // wherever the forward pseudo-time iteration does (J^T has J's spectrum) and
-    // becomes one linear solve as the CFL grows.
-    DBuf adj_r, adj_d, adj_norm;
+    // becomes restarted GMRES on the scaled J^T as the CFL grows.
+    DBuf adj_r, adj_d, adj_t, adj_norm;
     void adjoint_step(const double* g, double* lam, double cfl, ibisgb_adjoint_status* out) {
         if (n_cases > 1) throw StateError("steady-state solves run one case per context, not on a batch");
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
         const Steady& st = steady;
         const size_t n = nvars();
+        const int ncv = nc();
         ensure_krylov(st.max_iters);
         adj_r.alloc(sizeof(double) * n);
         adj_d.alloc(sizeof(double) * n);
-        adj_norm.alloc(sizeof(double) * 2);
+        adj_t.alloc(sizeof(double) * n);
+        adj_norm.alloc(sizeof(double) * 8);
         double* r = adj_r.as<double>();
         double* d = adj_d.as<double>();
+        double* t = adj_t.as<double>();
+        double* nrm = adj_norm.as<double>();
+        // RMS of each conserved variable (U is one array per variable)
+        const int64_t N = mesh.N;
+        for (int q = 0; q < ncv; q++)
+            launch_dot(U.as<double>() + q * N, U.as<double>() + q * N, N, kpart.as<double>(), nrm + 2 + q, true,
+                       stream);
         vjp(lam, r, nullptr, true);
         launch_axpby(r, g, (long long)n, 1.0, 1.0, stream);  // r = J^T lambda + g
-        launch_dot(r, r, (long long)n, kpart.as<double>(), adj_norm.as<double>(), true, stream);
-        double rnorm = 0.0;
-        CUDA_OK(cudaMemcpyAsync(&rnorm, adj_norm.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        launch_dot(r, r, (long long)n, kpart.as<double>(), nrm, true, stream);
+        double hn[8] = {};
+        CUDA_OK(cudaMemcpyAsync(hn, nrm, sizeof(double) * (2 + ncv), cudaMemcpyDeviceToHost, stream));
+        CUDA_OK(cudaStreamSynchronize(stream));
+        const double rnorm = hn[0];
+        const double inv_sqrt_n = 1.0 / std::sqrt((double)N);
+        const double rho_s = hn[2] * inv_sqrt_n, e_s = hn[2 + ncv - 1] * inv_sqrt_n;
+        if (!(rho_s > 0.0) || !(e_s > 0.0)) throw StateError("adjoint scaling: the state has no density or energy");
+        RowScale sc{}, isc{};
+        for (int q = 0; q < ncv; q++) {
+            sc.s[q] = (q == 0) ? rho_s : (q == ncv - 1) ? e_s : std::sqrt(rho_s * e_s);
+            isc.s[q] = 1.0 / sc.s[q];
+        }
+        launch_scale_rows(r, r, (long long)n, ncv, sc, stream);  // S r
+        launch_dot(r, r, (long long)n, kpart.as<double>(), nrm + 1, true, stream);
+        double srnorm = 0.0;
+        CUDA_OK(cudaMemcpyAsync(&srnorm, nrm + 1, sizeof(double), cudaMemcpyDeviceToHost, stream));
         const double stable = estimate_dt(IBISGB_F64);  // synchronizes the stream
         const double dt_star = cfl * stable, inv = 1.0 / dt_star;
         CUDA_OK(cudaMemsetAsync(d, 0, sizeof(double) * n, stream));
-        auto A = [&](const double* x, double* y) {
-            vjp(x, y, nullptr, true);
-            launch_axpby(y, x, (long long)n, inv, -1.0, stream);  // y = x / dt* - J^T x
+        auto A = [&](const double* x, double* y) {  // y = S (I/dt* - J^T) S^-1 x
+            launch_scale_rows(t, x, (long long)n, ncv, isc, stream);
+            vjp(t, y, nullptr, true);
+            launch_axpby(y, t, (long long)n, inv, -1.0, stream);
+            launch_scale_rows(y, y, (long long)n, ncv, sc, stream);
         };
         GmresOut res = gmres(A, r, d, st.max_iters, st.tol, kv.as<double>(), nullptr, nullptr);
+        launch_scale_rows(d, d, (long long)n, ncv, isc, stream);
         launch_axpby(lam, d, (long long)n, 1.0, 1.0, stream);
         CUDA_OK(cudaGetLastError());
         CUDA_OK(cudaStreamSynchronize(stream));
         if (out) {
             out->residual_norm = rnorm;
+            out->scaled_residual_norm = srnorm;
             out->gmres_iterations = res.iters;
             out->gmres_converged = res.success ? 1 : 0;
             out->gmres_residual = res.residual;
@@ -1736,17 +1894,24 @@ struct ibisgb_ctx {
         ensure_device();
         const int64_t N = mesh.N;
         const size_t bytes = sizeof(double) * nc() * N;
+        // rows in the reference numbering -> the internal one (renumbered grids)
+        auto internal_rows = [&](const double* r) {
+            if (!renumbered()) return r;
+            map_a.alloc(bytes);
+            map_rows_device(r, map_a.as<double>(), nc(), true);
+            return (const double*)map_a.as<double>();
+        };
         if (device) {
-            launch_rows_to_soa(rows, U.as<double>(), (int)N, nc(), stream);
+            launch_rows_to_soa(internal_rows(rows), U.as<double>(), (int)N, nc(), stream);
         } else if (const void* d = mapped_host(rows)) {
             // pinned host rows: the layout kernel reads them in place (one pass, all SMs)
-            launch_rows_to_soa((const double*)d, U.as<double>(), (int)N, nc(), stream);
+            launch_rows_to_soa(internal_rows((const double*)d), U.as<double>(), (int)N, nc(), stream);
             CUDA_OK(cudaGetLastError());
             CUDA_OK(cudaStreamSynchronize(stream));  // the caller may reuse its buffer on return
         } else {
             out.alloc(bytes);
             CUDA_OK(cudaMemcpyAsync(out.p, rows, bytes, cudaMemcpyHostToDevice, stream));
-            launch_rows_to_soa(out.as<double>(), U.as<double>(), (int)N, nc(), stream);
+            launch_rows_to_soa(internal_rows(out.as<double>()), U.as<double>(), (int)N, nc(), stream);
         }
         CUDA_OK(cudaGetLastError());
         if (!have_state) reset_rk();
@@ -1760,6 +1925,16 @@ struct ibisgb_ctx {
         if (!have_state) throw StateError("no initial condition");
         const int64_t N = mesh.N;
         const size_t bytes = sizeof(double) * nc() * N;
+        if (renumbered()) {  // internal rows, then gathered into the reference numbering
+            map_a.alloc(bytes);
+            out.alloc(bytes);
+            launch_soa_to_rows(U.as<double>(), map_a.as<double>(), (int)N, nc(), stream);
+            void* d = mapped_host(rows);
+            map_rows_device(map_a.as<double>(), d ? (double*)d : out.as<double>(), nc(), false);
+            if (!d) CUDA_OK(cudaMemcpyAsync(rows, out.p, bytes, cudaMemcpyDeviceToHost, stream));
+            CUDA_OK(cudaStreamSynchronize(stream));
+            return;
+        }
         if (void* d = mapped_host(rows)) {
             // pinned host rows: the layout kernel writes them in place
             launch_soa_to_rows(U.as<double>(), (double*)d, (int)N, nc(), stream);
@@ -1932,7 +2107,20 @@ int ibisgb_get_sizes(const ibisgb_ctx* ctx, ibisgb_sizes* out) {
 int ibisgb_set_primitives(ibisgb_ctx* ctx, const double* T, const double* p, const double* vx,
                           const double* vy, const double* vz) {
     if (!ctx) return IBISGB_ERR_ARG;
-    return guarded(ctx, [&] { ctx->set_primitives(T, p, vx, vy, vz); });
+    return guarded(ctx, [&] {
+        if (!ctx->renumbered()) return ctx->set_primitives(T, p, vx, vy, vz);
+        const double* in[5] = {T, p, vx, vy, vz};
+        std::vector<double> mapped[5];
+        const double* pp[5];
+        for (int q = 0; q < 5; q++) {
+            pp[q] = nullptr;
+            if (!in[q]) continue;
+            mapped[q].resize(ctx->mesh.N);
+            ctx->map_rows_host(in[q], mapped[q].data(), 1, true);
+            pp[q] = mapped[q].data();
+        }
+        ctx->set_primitives(pp[0], pp[1], pp[2], pp[3], pp[4]);
+    });
 }
 
 int ibisgb_get_primitives(ibisgb_ctx* ctx, double* rho, double* p, double* T, double* e, double* vx,
@@ -1940,7 +2128,18 @@ int ibisgb_get_primitives(ibisgb_ctx* ctx, double* rho, double* p, double* T, do
     if (!ctx) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
         double* o[7] = {rho, p, T, e, vx, vy, vz};
-        ctx->get_primitives(o);
+        if (!ctx->renumbered()) return ctx->get_primitives(o);
+        std::vector<double> internal[7];
+        double* io[7];
+        for (int q = 0; q < 7; q++) {
+            io[q] = nullptr;
+            if (!o[q]) continue;
+            internal[q].resize(ctx->mesh.N);
+            io[q] = internal[q].data();
+        }
+        ctx->get_primitives(io);
+        for (int q = 0; q < 7; q++)
+            if (o[q]) ctx->map_rows_host(io[q], o[q], 1, false);
     });
 }
 
@@ -2000,12 +2199,12 @@ int ibisgb_residual_device(ibisgb_ctx* ctx, int32_t precision, double* dudt_devi
             CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
             CUDA_OK(cudaEventRecord(ev, user));
             CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
-            ctx->residual(precision, dudt_device, true);
+            ctx->residual_rows(precision, dudt_device);
             CUDA_OK(cudaEventRecord(ev, ctx->stream));
             CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
             CUDA_OK(cudaEventDestroy(ev));
         } else {
-            ctx->residual(precision, dudt_device, true);
+            ctx->residual_rows(precision, dudt_device);
         }
     });
 }
@@ -2016,7 +2215,7 @@ int ibisgb_residual(ibisgb_ctx* ctx, int32_t precision, double* dudt) {
         if (precision < 0 || precision > 4) throw ArgError("unknown precision");
         const size_t bytes = sizeof(double) * ctx->nc() * ctx->mesh.N;
         ctx->out.alloc(bytes);
-        ctx->residual(precision, ctx->out.as<double>(), true);
+        ctx->residual_rows(precision, ctx->out.as<double>());
         CUDA_OK(cudaMemcpyAsync(dudt, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
@@ -2065,15 +2264,25 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
     return guarded(ctx, [&] {
         const Mesh& m = ctx->mesh;
         const int64_t N = m.N, F = m.F, G = m.G, MF = m.MF, NT = m.NT();
+        const int nc = ctx->nc();
+        // the dump in the internal numbering first, then (renumbered grids) in the reference's
+        std::vector<unsigned char> raw;
         auto put = [&](const void* src, size_t n) {
             if ((int64_t)n > bytes) throw ArgError("dump buffer too small");
-            std::memcpy(buf, src, n);
+            raw.assign((const unsigned char*)src, (const unsigned char*)src + n);
         };
         auto dev = [&](const void* src, size_t n) {
             if ((int64_t)n > bytes) throw ArgError("dump buffer too small");
             if (!src) throw StateError("nothing to dump yet");
-            CUDA_OK(cudaMemcpyAsync(buf, src, n, cudaMemcpyDeviceToHost, ctx->stream));
+            raw.resize(n);
+            CUDA_OK(cudaMemcpyAsync(raw.data(), src, n, cudaMemcpyDeviceToHost, ctx->stream));
             CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        };
+        auto face_rows = [&](const auto& soa_host) {  // SoA face values -> F x nc rows
+            std::vector<double> o(soa_host.size());
+            for (int64_t f = 0; f < F; f++)
+                for (int q = 0; q < nc; q++) o[f * nc + q] = soa_host[q * F + f];
+            put(o.data(), sizeof(double) * o.size());
         };
         switch (which) {
             case 0: put(m.left.data(), sizeof(int64_t) * F); break;
@@ -2107,34 +2316,92 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
                 break;
             }
             case 10: {
-                std::vector<double> soa(ctx->nc() * F);
-                dev(ctx->s64.flux.p, 0);
+                if (!ctx->s64.flux.p) throw StateError("nothing to dump yet");
+                std::vector<double> soa(nc * F);
                 CUDA_OK(cudaMemcpyAsync(soa.data(), ctx->s64.flux.p, sizeof(double) * soa.size(),
                                         cudaMemcpyDeviceToHost, ctx->stream));
                 CUDA_OK(cudaStreamSynchronize(ctx->stream));
-                std::vector<double> o(soa.size());
-                for (int64_t f = 0; f < F; f++)
-                    for (int q = 0; q < ctx->nc(); q++) o[f * ctx->nc() + q] = soa[q * F + f];
-                put(o.data(), sizeof(double) * o.size());
+                face_rows(soa);
                 break;
             }
             case 13: {  // face fluxes of the last mixed-precision residual / stage
-                std::vector<float> soa(ctx->nc() * F);
-                dev(ctx->s32.flux.p, 0);
+                if (!ctx->s32.flux.p) throw StateError("nothing to dump yet");
+                std::vector<float> soa(nc * F);
                 CUDA_OK(cudaMemcpyAsync(soa.data(), ctx->s32.flux.p, sizeof(float) * soa.size(),
                                         cudaMemcpyDeviceToHost, ctx->stream));
                 CUDA_OK(cudaStreamSynchronize(ctx->stream));
-                std::vector<double> o(soa.size());
-                for (int64_t f = 0; f < F; f++)
-                    for (int q = 0; q < ctx->nc(); q++) o[f * ctx->nc() + q] = soa[q * F + f];
-                put(o.data(), sizeof(double) * o.size());
+                face_rows(soa);
                 break;
             }
             case 11: put(m.ghost_face.data(), sizeof(int64_t) * G); break;
             case 12: put(m.ghost_bound.data(), sizeof(int64_t) * G); break;
+            case 14: {  // the reference id of each internal cell
+                std::vector<int64_t> o(N);
+                for (int64_t c = 0; c < N; c++) o[c] = ctx->cell_id_to_ref(c);
+                put(o.data(), sizeof(int64_t) * N);
+                break;
+            }
+            case 15: {  // the reference id of each internal face
+                std::vector<int64_t> o(F);
+                for (int64_t f = 0; f < F; f++) o[f] = ctx->face_id_to_ref(f);
+                put(o.data(), sizeof(int64_t) * F);
+                break;
+            }
             default: throw ArgError("unknown dump");
         }
+        if (!ctx->renumbered() || which == 14 || which == 15) {
+            std::memcpy(buf, raw.data(), raw.size());
+            return;
+        }
+        const MeshNumbering& nm = ctx->num;
+        // rows of w elements of T over n items (cells or faces), reordered to the reference
+        // numbering, the values of id arrays mapped by `val`
+        auto reorder = [&](auto tag, int64_t n, int64_t w, const std::vector<int64_t>& new_of_ref, int64_t blocks,
+                           int64_t block_stride, auto val) {
+            using T = decltype(tag);
+            const T* in = (const T*)raw.data();
+            T* out = (T*)buf;
+            std::memcpy(buf, raw.data(), raw.size());  // anything outside the reordered rows (ghosts) as is
+            for (int64_t b = 0; b < blocks; b++)
+                for (int64_t r = 0; r < n; r++)
+                    for (int64_t k = 0; k < w; k++)
+                        out[b * block_stride + r * w + k] = val(in[b * block_stride + new_of_ref[r] * w + k]);
+        };
+        auto same = [](auto x) { return x; };
+        auto cell_val = [&](int64_t c) { return ctx->cell_id_to_ref(c); };
+        auto face_val = [&](int64_t f) { return ctx->face_id_to_ref(f); };
+        switch (which) {
+            case 0: case 1: reorder(int64_t{}, F, 1, nm.face_new_of_ref, 1, 0, cell_val); break;
+            case 2: reorder(int64_t{}, N, MF, nm.cell_new_of_ref, 1, 0, face_val); break;
+            case 3: reorder(int32_t{}, N, MF, nm.cell_new_of_ref, 1, 0, same); break;
+            case 4: reorder(int64_t{}, N, MF, nm.cell_new_of_ref, 1, 0, cell_val); break;
+            case 5: {
+                const int64_t* in = (const int64_t*)raw.data();
+                for (int64_t g = 0; g < G; g++) ((int64_t*)buf)[g] = cell_val(in[g]);
+                break;
+            }
+            case 6: reorder(double{}, F, 1, nm.face_new_of_ref, 13, F, same); break;
+            case 7: reorder(double{}, N, 1, nm.cell_new_of_ref, 4, NT, same); break;
+            case 8: reorder(uint32_t{}, N, 5, nm.cell_new_of_ref, 1, 0, same); break;
+            case 9: reorder(double{}, N, 1, nm.cell_new_of_ref, 5, N, same); break;
+            case 10: case 13: reorder(double{}, F, nc, nm.face_new_of_ref, 1, 0, same); break;
+            case 11: {
+                const int64_t* in = (const int64_t*)raw.data();
+                for (int64_t g = 0; g < G; g++) ((int64_t*)buf)[g] = face_val(in[g]);
+                break;
+            }
+            default: std::memcpy(buf, raw.data(), raw.size());  // 12: per ghost, ghost ids are not renumbered
+        }
     });
+}
+
+int ibisgb_numbering(const ibisgb_ctx* ctx, int32_t* renumbered, int64_t* bandwidth_reference,
+                     int64_t* bandwidth_internal) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    if (renumbered) *renumbered = ctx->renumbered() ? 1 : 0;
+    if (bandwidth_reference) *bandwidth_reference = ctx->bandwidth_ref;
+    if (bandwidth_internal) *bandwidth_internal = ctx->bandwidth_internal;
+    return IBISGB_OK;
 }
 
 int ibisgb_jvp_device(ibisgb_ctx* ctx, const double* v_device, double* out_device, double inv_dt_star,
@@ -2149,7 +2416,7 @@ int ibisgb_jvp_device(ibisgb_ctx* ctx, const double* v_device, double* out_devic
             CUDA_OK(cudaEventRecord(ev, user));
             CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
         }
-        ctx->jvp(v_device, out_device, inv_dt_star, allow_reconstruction != 0);
+        ctx->jvp_rows(v_device, out_device, inv_dt_star, allow_reconstruction != 0);
         if (ev) {
             CUDA_OK(cudaEventRecord(ev, ctx->stream));
             CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
@@ -2166,7 +2433,7 @@ int ibisgb_jvp(ibisgb_ctx* ctx, const double* v, double* out, double inv_dt_star
         const size_t n = ctx->nvars();
         ctx->ensure_krylov(1);
         CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, v, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-        ctx->jvp(ctx->kr0.as<double>(), ctx->kw.as<double>(), inv_dt_star, allow_reconstruction != 0);
+        ctx->jvp_rows(ctx->kr0.as<double>(), ctx->kw.as<double>(), inv_dt_star, allow_reconstruction != 0);
         CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
@@ -2184,7 +2451,7 @@ int ibisgb_vjp_device(ibisgb_ctx* ctx, const double* w_device, double* out_devic
             CUDA_OK(cudaEventRecord(ev, user));
             CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
         }
-        ctx->vjp(w_device, out_device, ghost_out_device, allow_reconstruction != 0);
+        ctx->vjp_rows(w_device, out_device, ghost_out_device, allow_reconstruction != 0);
         if (ev) {
             CUDA_OK(cudaEventRecord(ev, ctx->stream));
             CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
@@ -2202,8 +2469,8 @@ int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out,
         ctx->ensure_krylov(1);
         ctx->adj_gout.alloc(sizeof(double) * std::max(ng, (size_t)1));
         CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, w, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-        ctx->vjp(ctx->kr0.as<double>(), ctx->kw.as<double>(), ghost_out ? ctx->adj_gout.as<double>() : nullptr,
-                 allow_reconstruction != 0);
+        ctx->vjp_rows(ctx->kr0.as<double>(), ctx->kw.as<double>(), ghost_out ? ctx->adj_gout.as<double>() : nullptr,
+                      allow_reconstruction != 0);
         CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
         if (ghost_out && ng)
             CUDA_OK(cudaMemcpyAsync(ghost_out, ctx->adj_gout.p, sizeof(double) * ng, cudaMemcpyDeviceToHost,
@@ -2215,7 +2482,7 @@ int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out,
 int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_device, double cfl,
                         ibisgb_adjoint_status* status) {
     if (!ctx || !g_device || !lambda_device || !(cfl > 0.0)) return IBISGB_ERR_ARG;
-    return guarded(ctx, [&] { ctx->adjoint_step(g_device, lambda_device, cfl, status); });
+    return guarded(ctx, [&] { ctx->adjoint_step_rows(g_device, lambda_device, cfl, status); });
 }
 
 int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision) {

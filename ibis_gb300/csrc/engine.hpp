@@ -255,6 +255,9 @@ void launch_tangent(const DevView& v, const FvParams& p, const double* vt, doubl
 void set_thread_error(const std::string& msg);
 
 // row-major (N x nc) <-> slot-major ([nc][N]) conserved state
+struct RowScale { double s[5]; };
+void launch_scale_rows(double* out, const double* in, long long n, int nc, const RowScale& sc, cudaStream_t s);
+void launch_gather_rows(double* dst, const double* src, const int32_t* map, int N, int w, cudaStream_t s);
 void launch_rows_to_soa(const double* rows, double* soa, int N, int nc, cudaStream_t s);
 void launch_soa_to_rows(const double* soa, double* rows, int N, int nc, cudaStream_t s);
 

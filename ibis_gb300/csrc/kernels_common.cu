@@ -174,6 +174,21 @@ __global__ void k_axpby(double* y, const double* x, long long n, double a, doubl
         y[i] = a * x[i] + b * y[i];
 }
 
+// out[i * nc + q] = in[i * nc + q] * s[q]  (per-variable scaling of row vectors)
+__global__ void k_scale_rows(double* out, const double* in, long long n, int nc, RowScale sc) {
+    for (long long i = (long long)blockIdx.x * kRB + threadIdx.x; i < n; i += (long long)gridDim.x * kRB)
+        out[i] = in[i] * sc.s[i % nc];
+}
+
+// dst[i * w + q] = src[map[i] * w + q]   (rows between two cell numberings)
+__global__ void k_gather_rows(double* dst, const double* src, const int32_t* map, int N, int w) {
+    const long long n = (long long)N * w;
+    for (long long t = (long long)blockIdx.x * kRB + threadIdx.x; t < n; t += (long long)gridDim.x * kRB) {
+        const long long i = t / w;
+        dst[t] = src[(long long)map[i] * w + (t - i * w)];
+    }
+}
+
 // U[q][i] += dU[i * nc + q]   (Jfnk::apply_update_, jfnk.cpp:63-76)
 __global__ void k_add_rows(double* U, const double* dU, int N, int nc) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,6 +217,12 @@ void launch_gemv_add(double* x, const double* V, long long n, int m, const doubl
 }
 void launch_axpby(double* y, const double* x, long long n, double a, double b, cudaStream_t s) {
     k_axpby<<<kDotBlocks, kRB, 0, s>>>(y, x, n, a, b);
+}
+void launch_scale_rows(double* out, const double* in, long long n, int nc, const RowScale& sc, cudaStream_t s) {
+    k_scale_rows<<<kDotBlocks, kRB, 0, s>>>(out, in, n, nc, sc);
+}
+void launch_gather_rows(double* dst, const double* src, const int32_t* map, int N, int w, cudaStream_t s) {
+    k_gather_rows<<<kDotBlocks, kRB, 0, s>>>(dst, src, map, N, w);
 }
 void launch_add_rows(double* U, const double* dU, int N, int nc, cudaStream_t s) {
     long long n = (long long)N * nc;

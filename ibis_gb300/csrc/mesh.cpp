@@ -599,3 +599,154 @@ void merge_meshes(const std::vector<const Mesh*>& parts, Mesh& out, std::vector<
 }
 
 }  // namespace ibisgb
+
+namespace ibisgb {
+
+// Reverse Cuthill-McKee order of the valid cells over their interior-face
+// graph: each connected component breadth-first from a pseudo-peripheral cell
+// (the far end of a breadth-first sweep from a cell of least degree),
+// neighbours queued by increasing degree, the whole order reversed.
+std::vector<int64_t> rcm_cell_order(const Mesh& m) {
+    const int64_t N = m.N;
+    const int MF = m.MF;
+    std::vector<int32_t> deg(N, 0);
+    for (int64_t c = 0; c < N; c++)
+        for (int k = 0; k < MF; k++) {
+            const int64_t nb = m.cell_nbr[c * MF + k];
+            if (nb >= 0 && nb < N) deg[c]++;
+        }
+    std::vector<int64_t> order;
+    order.reserve(N);
+    std::vector<char> seen(N, 0);
+    std::vector<int64_t> level(N, -1), nbrs;
+    auto bfs_far = [&](int64_t s) {  // the last cell of a breadth-first sweep (on a scratch level array)
+        std::vector<int64_t> q{s};
+        level[s] = 0;
+        int64_t last = s;
+        for (size_t h = 0; h < q.size(); h++) {
+            const int64_t c = q[h];
+            last = c;
+            for (int k = 0; k < MF; k++) {
+                const int64_t nb = m.cell_nbr[c * MF + k];
+                if (nb < 0 || nb >= N || level[nb] >= 0) continue;
+                level[nb] = level[c] + 1;
+                q.push_back(nb);
+            }
+        }
+        for (int64_t c : q) level[c] = -1;
+        return last;
+    };
+    std::vector<int64_t> by_degree(N);
+    for (int64_t c = 0; c < N; c++) by_degree[c] = c;
+    std::stable_sort(by_degree.begin(), by_degree.end(), [&](int64_t a, int64_t b) { return deg[a] < deg[b]; });
+    for (int64_t s0 : by_degree) {
+        if (seen[s0]) continue;
+        const int64_t s = bfs_far(bfs_far(s0));
+        const size_t head0 = order.size();
+        order.push_back(s);
+        seen[s] = 1;
+        for (size_t h = head0; h < order.size(); h++) {
+            const int64_t c = order[h];
+            nbrs.clear();
+            for (int k = 0; k < MF; k++) {
+                const int64_t nb = m.cell_nbr[c * MF + k];
+                if (nb >= 0 && nb < N && !seen[nb]) {
+                    seen[nb] = 1;
+                    nbrs.push_back(nb);
+                }
+            }
+            std::stable_sort(nbrs.begin(), nbrs.end(), [&](int64_t a, int64_t b) { return deg[a] < deg[b]; });
+            order.insert(order.end(), nbrs.begin(), nbrs.end());
+        }
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
+// Bandwidth of the valid-cell graph: the largest |i - j| over interior faces.
+int64_t cell_bandwidth(const Mesh& m) {
+    int64_t b = 0;
+    for (int64_t f = 0; f < m.F; f++)
+        if (m.left[f] >= 0 && m.left[f] < m.N && m.right[f] >= 0 && m.right[f] < m.N)
+            b = std::max<int64_t>(b, std::llabs(m.left[f] - m.right[f]));
+    return b;
+}
+
+void renumber_mesh(Mesh& m, const std::vector<int64_t>& cell_ref_of_new, MeshNumbering& num) {
+    const int64_t N = m.N, F = m.F, G = m.G;
+    const int MF = m.MF;
+    num.cell_ref_of_new = cell_ref_of_new;
+    num.cell_new_of_ref.assign(N, -1);
+    for (int64_t c = 0; c < N; c++) num.cell_new_of_ref[cell_ref_of_new[c]] = c;
+    auto cnew = [&](int64_t c) { return c >= 0 && c < N ? num.cell_new_of_ref[c] : c; };  // ghosts keep their ids
+    // faces by their lower, then higher, new cell id
+    std::vector<int64_t> fo(F);
+    for (int64_t f = 0; f < F; f++) fo[f] = f;
+    auto key = [&](int64_t f) {
+        const int64_t a = cnew(m.left[f]), b = cnew(m.right[f]);
+        return std::make_pair(std::min(a, b), std::max(a, b));
+    };
+    std::stable_sort(fo.begin(), fo.end(), [&](int64_t x, int64_t y) { return key(x) < key(y); });
+    num.face_ref_of_new = fo;
+    num.face_new_of_ref.assign(F, -1);
+    for (int64_t f = 0; f < F; f++) num.face_new_of_ref[fo[f]] = f;
+    auto fnew = [&](int64_t f) { return f >= 0 ? num.face_new_of_ref[f] : f; };
+
+    // faces
+    {
+        std::vector<int8_t> kind(F);
+        std::vector<int64_t> off(1, 0), vtx, l(F), r(F);
+        std::vector<double>* g[13] = {&m.nx, &m.ny, &m.nz, &m.t1x, &m.t1y, &m.t1z, &m.t2x, &m.t2y, &m.t2z,
+                                      &m.fcx, &m.fcy, &m.fcz, &m.area};
+        std::vector<std::vector<double>> gn(13, std::vector<double>(F));
+        for (int64_t f = 0; f < F; f++) {
+            const int64_t o = fo[f];
+            kind[f] = m.face_kind[o];
+            vtx.insert(vtx.end(), m.face_vtx.begin() + m.face_vtx_off[o], m.face_vtx.begin() + m.face_vtx_off[o + 1]);
+            off.push_back((int64_t)vtx.size());
+            l[f] = cnew(m.left[o]);
+            r[f] = cnew(m.right[o]);
+            for (int q = 0; q < 13; q++) gn[q][f] = (*g[q])[o];
+        }
+        m.face_kind.swap(kind); m.face_vtx_off.swap(off); m.face_vtx.swap(vtx); m.left.swap(l); m.right.swap(r);
+        for (int q = 0; q < 13; q++) g[q]->swap(gn[q]);
+    }
+    // cells (slot order within a cell is kept: it is the reference's summation order)
+    {
+        std::vector<int8_t> kind(N), osg((size_t)N * MF);
+        std::vector<int64_t> off(1, 0), vtx, cf((size_t)N * MF), cn((size_t)N * MF);
+        std::vector<int32_t> nf(N);
+        std::vector<double> cx(m.ccx), cy(m.ccy), cz(m.ccz), vol(m.volume), rr(m.r.size()), w(m.lsqw.size());
+        for (int64_t c = 0; c < N; c++) {
+            const int64_t o = cell_ref_of_new[c];
+            kind[c] = m.cell_kind[o];
+            vtx.insert(vtx.end(), m.cell_vtx.begin() + m.cell_vtx_off[o], m.cell_vtx.begin() + m.cell_vtx_off[o + 1]);
+            off.push_back((int64_t)vtx.size());
+            nf[c] = m.nfaces[o];
+            for (int k = 0; k < MF; k++) {
+                cf[c * MF + k] = fnew(m.cell_face[o * MF + k]);
+                cn[c * MF + k] = cnew(m.cell_nbr[o * MF + k]);
+                osg[c * MF + k] = m.outsign[o * MF + k];
+            }
+            cx[c] = m.ccx[o]; cy[c] = m.ccy[o]; cz[c] = m.ccz[o]; vol[c] = m.volume[o];
+            if (!m.r.empty())
+                for (int q = 0; q < 6; q++) rr[c * 6 + q] = m.r[o * 6 + q];
+            if (!m.lsqw.empty())
+                for (int a = 0; a < 3; a++)
+                    for (int k = 0; k < MF; k++) w[((size_t)a * MF + k) * N + c] = m.lsqw[((size_t)a * MF + k) * N + o];
+        }
+        m.cell_kind.swap(kind); m.cell_vtx_off.swap(off); m.cell_vtx.swap(vtx); m.nfaces.swap(nf);
+        m.cell_face.swap(cf); m.cell_nbr.swap(cn); m.outsign.swap(osg);
+        m.ccx.swap(cx); m.ccy.swap(cy); m.ccz.swap(cz); m.volume.swap(vol);
+        m.r.swap(rr); m.lsqw.swap(w);
+    }
+    // boundaries and ghosts (ghost ids are unchanged)
+    for (auto& bf : m.bound_faces)
+        for (auto& f : bf) f = fnew(f);
+    for (int64_t g = 0; g < G; g++) {
+        m.ghost_face[g] = fnew(m.ghost_face[g]);
+        m.ghost_src[g] = cnew(m.ghost_src[g]);
+    }
+}
+
+}  // namespace ibisgb

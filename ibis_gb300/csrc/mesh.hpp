@@ -89,6 +89,23 @@ struct Mesh {
 void build_mesh(const GridInput& in, const std::vector<BoundarySpec>& bounds, bool need_lsq,
                 Mesh& m);
 
+// An internal numbering of cells and faces and its map to the reference's
+// (each vector maps an id of one numbering to the other).
+struct MeshNumbering {
+    std::vector<int64_t> cell_new_of_ref, cell_ref_of_new, face_new_of_ref, face_ref_of_new;
+    bool active() const { return !cell_ref_of_new.empty(); }
+};
+
+// Reverse Cuthill-McKee order of the valid cells (their reference ids in the
+// new order) and the bandwidth of the valid-cell graph.
+std::vector<int64_t> rcm_cell_order(const Mesh& m);
+int64_t cell_bandwidth(const Mesh& m);
+
+// Renumbers the valid cells (cell_ref_of_new: the reference id of each new id)
+// and the faces (by their lower, then higher, new cell id) of a built mesh in
+// place, keeping each cell's face slots in order and the ghost ids; fills num.
+void renumber_mesh(Mesh& m, const std::vector<int64_t>& cell_ref_of_new, MeshNumbering& num);
+
 // Concatenation of independent cases (batched ensembles): valid cells of all
 // cases first, in case order, then all ghost cells; faces and boundaries in
 // case order.  The offset vectors get one entry per case plus the total.

@@ -170,6 +170,34 @@ def tetrahedralize(g: Su2Grid) -> Su2Grid:
     return _grid_from_cells(g, [VTK_TETRA] * len(cells), cells, _split_marker_quads(g, faces))
 
 
+def shuffle_cells(g: Su2Grid, seed: int = 0) -> Su2Grid:
+    """The same grid with its cells listed in a seeded random order (as some
+    unstructured generators write them); vertices and markers unchanged."""
+    perm = np.random.default_rng(seed).permutation(g.num_cells)
+    lens = (g.cell_offsets[1:] - g.cell_offsets[:-1])[perm]
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    idx = np.arange(off[-1]) - np.repeat(off[:-1], lens) + np.repeat(g.cell_offsets[:-1][perm], lens)
+    out = copy.copy(g)
+    out.cell_conn = g.cell_conn[idx]
+    out.cell_types = g.cell_types[perm]
+    out.cell_offsets = off
+    return out
+
+
+def tet_channel_case(n: int, shuffle_seed: int | None = None, **kw):
+    """A 3-D channel of n^3 hexahedra split into 6 n^3 tetrahedra (optionally listed
+    in shuffled order): supersonic inflow (west, Mach ~2 at 300 K, 1e5 Pa, slightly
+    oblique) and outflow (east), slip walls elsewhere.  Returns (grid, config, inflow)."""
+    gas = ideal_gas(287.0)
+    inflow = flow_state(gas, 300.0, 1e5, 700.0, 30.0, 20.0)
+    g = tetrahedralize(box_3d(n))
+    if shuffle_seed is not None:
+        g = shuffle_cells(g, shuffle_seed)
+    b = {"west": supersonic_inflow(inflow), "east": supersonic_outflow(), "south": slip_wall(),
+         "north": slip_wall(), "bottom": slip_wall(), "top": slip_wall()}
+    return g, make_config(3, b, gas=gas, **kw), inflow
+
+
 def prisms_3d(g: Su2Grid) -> Su2Grid:
     """Each hexahedron as two wedges (triangular prisms) split by its v0-v2 / v4-v6
     diagonal plane; the bottom and top boundary quads split to match."""

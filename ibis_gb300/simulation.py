@@ -31,7 +31,7 @@ DUMPS = {"left": (0, np.int64), "right": (1, np.int64), "cell_faces": (2, np.int
          "face_geometry": (6, np.float64), "cell_geometry": (7, np.float64),
          "limiter_branches": (8, np.uint32), "limiters": (9, np.float64),
          "face_flux": (10, np.float64), "ghost_face": (11, np.int64), "ghost_boundary": (12, np.int64),
-         "face_flux_mixed": (13, np.float64)}
+         "face_flux_mixed": (13, np.float64), "cell_order": (14, np.int64), "face_order": (15, np.int64)}
 
 
 def _ptr(a: np.ndarray):
@@ -307,9 +307,9 @@ class Simulation:
         st = AdjointStatus()
         self._call("ibisgb_adjoint_step", C.c_void_p(g.data_ptr()), C.c_void_p(lam.data_ptr()), float(cfl),
                    C.byref(st))
-        return {"residual_norm": st.residual_norm, "gmres_iterations": st.gmres_iterations,
-                "gmres_converged": bool(st.gmres_converged), "gmres_residual": st.gmres_residual,
-                "dt_star": st.dt_star}
+        return {"residual_norm": st.residual_norm, "scaled_residual_norm": st.scaled_residual_norm,
+                "gmres_iterations": st.gmres_iterations, "gmres_converged": bool(st.gmres_converged),
+                "gmres_residual": st.gmres_residual, "dt_star": st.dt_star}
 
     def steady_initialise(self, precision: str = "f64"):
         """Jfnk::initialise: residual and initial norms at the current state."""
@@ -334,6 +334,13 @@ class Simulation:
         self._call("ibisgb_synchronize")
 
     # ---------------------------------------------------------------- dumps
+    def numbering(self) -> dict:
+        """Whether the device arrays use an internal (reverse Cuthill-McKee) order,
+        and the cell graph's bandwidth in the reference's and the internal order."""
+        r, b0, b1 = C.c_int32(), C.c_int64(), C.c_int64()
+        self._call("ibisgb_numbering", C.byref(r), C.byref(b0), C.byref(b1))
+        return {"renumbered": bool(r.value), "bandwidth_reference": b0.value, "bandwidth_internal": b1.value}
+
     def dump(self, name: str) -> np.ndarray:
         which, dt = DUMPS[name]
         N, F, G, MF, NT, nc = (self.num_cells, self.num_faces, self.num_ghost_cells, self.max_faces,
@@ -342,7 +349,7 @@ class Simulation:
                  "neighbours": (N, MF), "ghost_source": (G,), "face_geometry": (13, F),
                  "cell_geometry": (4, NT), "limiter_branches": (N, 5), "limiters": (5, N),
                  "face_flux": (F, nc), "ghost_face": (G,), "ghost_boundary": (G,),
-                 "face_flux_mixed": (F, nc)}[name]
+                 "face_flux_mixed": (F, nc), "cell_order": (N,), "face_order": (F,)}[name]
         out = np.empty(shape, dt)
         self._call("ibisgb_get_dump", which, _ptr(out), out.nbytes)
         return out

@@ -197,8 +197,22 @@ int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]);
  * 10 face fluxes of the last residual (double F x n_conserved),
  * 11 boundary face of each ghost cell (int64 G), 12 boundary (index in sorted
  * tag order) of each ghost cell (int64 G), 13 face fluxes of the last MIXED
- * residual evaluation (double F x n_conserved, from the float fluxes). */
+ * residual evaluation (double F x n_conserved, from the float fluxes),
+ * 14 the reference id of each internal cell (int64 N), 15 the reference id of
+ * each internal face (int64 F). */
 int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
+
+/* The device arrays' cell and face order.  The grid's optional "renumber" key
+ * ("auto" when absent, "rcm", "none"; not a reference key) selects it: "rcm"
+ * orders the valid cells by reverse Cuthill-McKee over the interior-face graph
+ * and the faces by their lower, then higher, cell; "auto" does so for grids with
+ * cells other than quadrilaterals (2-D) or hexahedra (3-D) when that at least
+ * halves the cell graph's bandwidth (max |left - right| over interior faces).
+ * Every array and id that crosses this ABI stays in the reference's numbering
+ * (grid.h:113-133); each cell's face slots and every summation keep their order,
+ * so results do not depend on the numbering.  Ghost cells keep their ids. */
+int ibisgb_numbering(const ibisgb_ctx* ctx, int32_t* renumbered, int64_t* bandwidth_reference,
+                     int64_t* bandwidth_internal);
 
 /* Result of one Newton step of the steady solver. */
 typedef struct {
@@ -253,15 +267,20 @@ typedef struct {
     int32_t gmres_converged;
     double gmres_residual;  /* |g_k| / beta of the last GMRES iteration */
     double dt_star;         /* cfl * stable dt of the current state */
+    double scaled_residual_norm;  /* |S (J^T lambda + g)| before the step (S below) */
 } ibisgb_adjoint_status;
 
 /* One step of the discrete adjoint of the steady problem, J^T lambda = -g with
  * J = dR/dU at the current (converged) state and g = dObjective/dU (device
  * vectors, N x n_conserved rows): r = J^T lambda + g, then GMRES on
- * (I/dt* - J^T) d = r (dt* = cfl * the stable time step; GMRES length and
- * tolerance from the config's steady solver, or 50 and 1e-2) and lambda += d,
- * in place.  The transposed counterpart of ibisgb_newton_step; no counterpart
- * in the reference.  Iterate with a growing cfl until residual_norm is small.
+ * S (I/dt* - J^T) S^-1 y = S r and lambda += S^-1 y, in place (dt* = cfl * the
+ * stable time step; GMRES length and tolerance from the config's steady solver,
+ * or 50 and 1e-2).  S is diagonal per conserved variable: the RMS over the cells
+ * of density and total energy, sqrt(RMS density * RMS energy) for the momenta --
+ * the conserved variables differ by ~1e5 in magnitude, and unscaled GMRES
+ * stagnates on that spread.  The transposed counterpart of ibisgb_newton_step; no
+ * counterpart in the reference.  Iterate with a growing cfl until
+ * scaled_residual_norm is small.
  * With lambda, dObjective/dp = dObjective/dp|_U + lambda . dR/dp for any
  * parameter p of the boundary states (through ibisgb_vjp's ghost adjoint) or of
  * the grid. */

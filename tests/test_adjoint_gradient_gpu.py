@@ -44,7 +44,8 @@ def test_force_gradient_matches_central_differences():
     J, dJdU = wall_force(sim, **FORCE)
     assert J > 0
     lam, hist = solve_adjoint(sim, dJdU, tol=1e-13)
-    assert hist[-1]["residual_norm"] <= 1e-13 * np.linalg.norm(dJdU), [h["residual_norm"] for h in hist]
+    assert hist[-1]["scaled_residual_norm"] <= 1e-13 * hist[0]["scaled_residual_norm"], \
+        [h["scaled_residual_norm"] for h in hist]
     # Mach
     dM = mach_sensitivity(sim, lam)
     h = 1e-6 * M0
