@@ -16,6 +16,7 @@ the data path); the time is the max over ranks.
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import math
 import os
@@ -63,6 +64,13 @@ def parse():
                     help="per-cell flux path (face fluxes recomputed inside the update kernel): let the "
                          "autotuner choose, force, or disable")
     ap.add_argument("--plate-steps", type=int, default=300, help="RK steps of the flat-plate accuracy case (0: skip)")
+    ap.add_argument("--renumber-n", type=int, default=56,
+                    help="hexahedra per side of the tetrahedral channel of the renumbering leg (6 n^3 cells; 0: skip)")
+    ap.add_argument("--renumber-steps", type=int, default=20, help="timed RK steps per ordering of that leg")
+    ap.add_argument("--renumber-orders", default="as_generated,shuffled,shuffled_rcm",
+                    help="orderings of that leg (comma separated)")
+    ap.add_argument("--renumber-only", action="store_true",
+                    help="run only the renumbering leg and print its JSON (for profiling its kernels)")
     ap.add_argument("--newton-steps", type=int, default=25, help="Newton steps of the ramp JFNK case (0: skip)")
     ap.add_argument("--first-order-max-steps", type=int, default=400,
                     help="Newton step limit of the first-order ramp's time-to-1e-10 run")
@@ -368,6 +376,42 @@ def plate_measure(args):
     return out
 
 
+def renumber_measure(args):
+    """Cell order and throughput on an unstructured grid: the 3-D tetrahedral
+    channel of 6 n^3 cells (grids.tet_channel_case: supersonic in/out, slip walls;
+    second order, Hanel, Barth-Jespersen, mixed build) in three orders -- as
+    generated (hexahedron by hexahedron), the cells shuffled (seeded), and the
+    shuffled grid renumbered by reverse Cuthill-McKee inside the context -- with
+    the cell graph's bandwidth and the RK-step throughput of each."""
+    from ibis_gb300 import Simulation, grids
+    n = args.renumber_n
+    g0, c, inf = grids.tet_channel_case(n)
+    gs = grids.shuffle_cells(g0, 0)
+    rng = np.random.default_rng(7)
+    N = g0.num_cells
+    st = [np.full(N, inf[k]) * (1.0 + 0.02 * rng.standard_normal(N)) for k in ("T", "p", "vx", "vy", "vz")]
+    out = {"workload": f"tetrahedral channel {N} cells (6 x {n}^3), ssp-rk3, Hanel, MUSCL + Barth-Jespersen, "
+                       f"mixed build, {args.renumber_steps} timed steps per ordering", "cells": N,
+           "unit": "Mcell-updates/s"}
+    perm = np.random.default_rng(0).permutation(N)  # shuffle_cells(g0, 0): cell k is cell perm[k] of g0
+    for name, grid, mode in (("as_generated", g0, "none"), ("shuffled", gs, "none"), ("shuffled_rcm", gs, "rcm")):
+        if name not in args.renumber_orders.split(","):
+            continue
+        cc = copy.deepcopy(c)
+        cc["grid"]["renumber"] = mode
+        sim = Simulation(cc, grid)
+        sim.set_primitives(*(st if grid is g0 else [a[perm] for a in st]))
+        if args.variants:  # fixed launch variants (no autotuning launches)
+            sim.set_launch_variants("mixed", *(int(x) for x in args.variants.split(",")))
+        sim.take_steps(3, "mixed")
+        r = sim.take_steps(args.renumber_steps, "mixed")
+        info = sim.numbering()
+        out[name] = {"value": N * 3.0 * args.renumber_steps / (r["device_ms"] / 1e3) / 1e6,
+                     "renumbered": info["renumbered"], "bandwidth_reference": info["bandwidth_reference"],
+                     "bandwidth_internal": info["bandwidth_internal"]}
+    return out
+
+
 def jfnk_measure(args):
     """Steady Jacobian-free Newton-Krylov on the Hicks-Henne ramp (512 x 256,
     15 degrees, 16 bump amplitudes U[-0.002, 0.002] m and inflow Mach U[1.5, 3]
@@ -596,6 +640,7 @@ def run_ours(args, world, rank, local):
 
     batch = batch_measure(args, barrier) if args.batch_cases > 0 else None
     plate = plate_measure(args) if args.plate_steps > 0 and rank == 0 else None
+    renum = renumber_measure(args) if args.renumber_n > 0 and rank == 0 else None
     sweep = sweep_measure(args) if args.sweep and rank == 0 else None
     jfnk = jfnk_measure(args) if args.newton_steps > 0 and rank == 0 else None
     if jfnk is not None and args.adjoint_check:
@@ -643,6 +688,7 @@ def run_ours(args, world, rank, local):
             "batch": batch,
             "sweep": sweep,
             "plate": plate,
+            "renumber": renum,
             "jfnk": jfnk,
             "roofline": {"bound": "hbm", "kernel": stage_kernel,
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -669,6 +715,11 @@ def main():
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.renumber_only:
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(local)
+            print(json.dumps({"renumber": renumber_measure(args)}), flush=True)
     else:
         run_ours(args, world, rank, local)
 

@@ -95,6 +95,8 @@ def load(build_if_missing: bool = True):
     L.ibisgb_jvp_device.argtypes = [_P, _P, _P, C.c_double, C.c_int32, _P]
     L.ibisgb_vjp.argtypes = [_P, _P, _P, _P, C.c_int32]
     L.ibisgb_vjp_device.argtypes = [_P, _P, _P, _P, C.c_int32, _P]
+    L.ibisgb_vjp_geometry.argtypes = [_P, _P, _P, _P, C.c_int32]
+    L.ibisgb_vjp_geometry_device.argtypes = [_P, _P, _P, _P, C.c_int32, _P]
     L.ibisgb_adjoint_step.argtypes = [_P, _P, _P, C.c_double, C.POINTER(AdjointStatus)]
     L.ibisgb_steady_initialise.argtypes = [_P, C.c_int32]
     L.ibisgb_newton_step.argtypes = [_P, C.c_int32, C.POINTER(NewtonStatus)]

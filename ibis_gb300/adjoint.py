@@ -13,8 +13,10 @@ the engine's tangent / adjoint kernels:
   (ibisgb_adjoint_step, pseudo-time continuation on the device);
 * dJ/dM = lambda . dR/dM through the inflow ghost cells (ibisgb_vjp's ghost
   adjoint; the inflow ghost velocity is M a at fixed T and p);
-* dJ/dalpha_k = dJ/dalpha_k|_U + lambda . dR/dalpha_k|_U, the partials at
-  fixed U by central differences of the residual and of J on perturbed grids.
+* dJ/dalpha_k = dJ/dalpha_k|_U + lambda . dR/dalpha_k|_U: lambda^T dR/dgeometry
+  from the engine's geometry adjoint (ibisgb_vjp_geometry), chained to the
+  vertex displacement of each Hicks-Henne bump through the complex-step
+  derivative of the grid geometry (ibis_gb300.geometry).
 """
 from __future__ import annotations
 
@@ -30,35 +32,41 @@ def _bound_index(sim: Simulation, tag: str) -> int:
     return tags.index(tag)
 
 
-def wall_force(sim: Simulation, tag: str = "wall", x_min: float | None = None, component: int = 1):
-    """(J, dJ/dU) of the pressure force on boundary `tag` (faces with centre x >= x_min)."""
-    gas = sim.config["gas_model"]
-    k = gas["R"] / gas["Cv"]
+def _wall_faces(sim: Simulation, tag: str):
     sel = sim.dump("ghost_boundary") == _bound_index(sim, tag)
-    faces = sim.dump("ghost_face")[sel]
-    cells = sim.dump("ghost_source")[sel]
-    fg = sim.dump("face_geometry")
+    return sim.dump("ghost_face")[sel], sim.dump("ghost_source")[sel]
+
+
+def _force(sim: Simulation, U, fg, faces, cells, x_min, component):
+    """J = sum p_c A_f (-n_out)[component] over the wall faces (fg may be complex)."""
+    k = sim.config["gas_model"]["R"] / sim.config["gas_model"]["Cv"]
     n = fg[0:3, faces]
-    area = fg[12, faces]
     left = sim.dump("left")[faces]
     n_out = np.where(left == cells, n, -n)
-    wgt = area * (-n_out[component])
+    wgt = fg[12, faces] * (-n_out[component])
     if x_min is not None:
-        wgt = np.where(fg[9, faces] >= x_min, wgt, 0.0)
-    U = sim.conserved()
+        wgt = np.where(fg[9, faces].real >= x_min, wgt, 0.0)
     dim = sim.dim
-    rho = U[cells, 0]
-    m = U[cells, 1:dim + 1]
-    E = U[cells, dim + 1]
+    rho, m, E = U[cells, 0], U[cells, 1:dim + 1], U[cells, dim + 1]
     m2 = (m * m).sum(axis=1)
     p = k * (E - 0.5 * m2 / rho)
-    J = float(np.sum(wgt * p))
+    return np.sum(wgt * p), wgt, k
+
+
+def wall_force(sim: Simulation, tag: str = "wall", x_min: float | None = None, component: int = 1):
+    """(J, dJ/dU) of the pressure force on boundary `tag` (faces with centre x >= x_min)."""
+    faces, cells = _wall_faces(sim, tag)
+    U = sim.conserved()
+    J, wgt, k = _force(sim, U, sim.dump("face_geometry"), faces, cells, x_min, component)
+    dim = sim.dim
+    rho, m = U[cells, 0], U[cells, 1:dim + 1]
+    m2 = (m * m).sum(axis=1)
     dJ = np.zeros_like(U)
     np.add.at(dJ[:, 0], cells, wgt * k * 0.5 * m2 / (rho * rho))
     for d in range(dim):
         np.add.at(dJ[:, 1 + d], cells, -wgt * k * m[:, d] / rho)
     np.add.at(dJ[:, dim + 1], cells, wgt * k)
-    return J, dJ
+    return float(J), dJ
 
 
 def steady_solve(sim: Simulation, tol: float = 1e-10, max_steps: int = 200, precision: str = "f64_exact"):
@@ -105,10 +113,29 @@ def mach_sensitivity(sim: Simulation, lam: np.ndarray, tag: str = "inflow", flow
     return float(np.sum(gadj[sel, 4]) * a * math.cos(th) + np.sum(gadj[sel, 5]) * a * math.sin(th))
 
 
-def shape_sensitivity(make_sim, bumps: np.ndarray, U: np.ndarray, lam: np.ndarray, k: int, h: float = 1e-7,
-                      **force_kw) -> float:
-    """dJ/dalpha_k|_U + lambda . dR/dalpha_k|_U, both by central differences on
-    grids rebuilt with bump k moved by +-h (make_sim(bumps) -> Simulation)."""
+def shape_gradient(sim: Simulation, grid, lam: np.ndarray, dxyz: np.ndarray, tag: str = "wall",
+                   x_min: float | None = None, component: int = 1, topology=None, geometry_adjoint=None) -> float:
+    """dJ/dalpha = dJ/dalpha|_U + lambda . dR/dalpha|_U for the vertex displacement
+    dxyz per unit alpha (num_vertices x 3): the engine's geometry adjoint
+    lambda^T dR/dgeometry (ibisgb_vjp_geometry, one evaluation serves every
+    parameter; pass it as geometry_adjoint to reuse it) contracted with the
+    complex-step derivative of the grid geometry (ibis_gb300.geometry), plus the
+    force's own dependence on the wall faces' areas and normals."""
+    from .geometry import GridTopology
+    topo = topology or GridTopology(sim, grid)
+    fb, cb = geometry_adjoint if geometry_adjoint is not None else sim.geometry_adjoint(lam)
+    h = 1e-30
+    fz, cz = topo.geometry(np.asarray(grid.xyz, np.float64) + 1j * h * np.asarray(dxyz, np.float64))
+    faces, cells = _wall_faces(sim, tag)
+    Jz, _, _ = _force(sim, sim.conserved(), fz, faces, cells, x_min, component)
+    return float(Jz.imag / h + np.sum(fb * fz.imag / h) + np.sum(cb * cz.imag / h))
+
+
+def shape_sensitivity_fd(make_sim, bumps: np.ndarray, U: np.ndarray, lam: np.ndarray, k: int, h: float = 1e-7,
+                         **force_kw) -> float:
+    """The same derivative for bump k by central differences at fixed U of the
+    residual and of J on grids rebuilt with bump k moved by +-h (make_sim(bumps)
+    -> Simulation); a check of shape_gradient."""
     vals = []
     for sgn in (1.0, -1.0):
         b = np.array(bumps, np.float64)
@@ -121,6 +148,19 @@ def shape_sensitivity(make_sim, bumps: np.ndarray, U: np.ndarray, lam: np.ndarra
     dJ = (vals[0][0] - vals[1][0]) / (2 * h)
     dR = (vals[0][1] - vals[1][1]) / (2 * h)
     return float(dJ + np.sum(lam * dR))
+
+
+def bump_displacements(ni: int, nj: int, n_bumps: int = 16, **kw) -> list:
+    """Vertex displacement of the Hicks-Henne ramp grid per unit amplitude of each
+    bump (grids.ramp_2d_bumps is linear in the amplitudes)."""
+    from . import grids
+    base = grids.ramp_2d(ni, nj, **kw).xyz
+    out = []
+    for k in range(n_bumps):
+        e = np.zeros(n_bumps)
+        e[k] = 1.0
+        out.append(grids.ramp_2d_bumps(ni, nj, bumps=e, **kw).xyz - base)
+    return out
 
 
 def converge(sim: Simulation, precision: str = "f64", rel_tol: float | None = 1e-12, abs_tol: float | None = None,
@@ -173,7 +213,12 @@ def gradient_check(ni: int = 512, nj: int = 256, seed: int = 0, order: int = 1, 
     J0, dJdU = wall_force(base, **force)
     lam, ah = solve_adjoint(base, dJdU, tol=1e-10)
     grads = [mach_sensitivity(base, lam)]
-    grads += [shape_sensitivity(lambda b: make(mach, b), bumps, U0, lam, k, h=1e-7, **force) for k in range(n_bumps)]
+    from .geometry import GridTopology
+    grid = grids.ramp_2d_bumps(ni, nj, bumps=bumps)
+    topo = GridTopology(base, grid)
+    gadj = base.geometry_adjoint(lam)
+    grads += [shape_gradient(base, grid, lam, dx, topology=topo, geometry_adjoint=gadj, **force)
+              for dx in bump_displacements(ni, nj, n_bumps)]
 
     newton = []
 

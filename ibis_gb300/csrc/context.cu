@@ -1328,6 +1328,60 @@ struct ibisgb_ctx {
         CUDA_OK(cudaGetLastError());
     }
 
+    // w^T dR/dgeometry: face rows (13 x F: n, t1, t2, centre, area) and cell rows
+    // (4 x (N+G): centroid, volume), internal numbering
+    DBuf geo_fcb, geo_vb, geo_nbc;
+    void vjp_geometry(const double* w_dev, double* face_out, double* cell_out, bool reconstruct) {
+        if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
+        if (prm.viscous || prm.cflux)
+            throw ConfigError("the geometry adjoint covers inviscid residuals without constant-flux boundaries");
+        DevView v = tangent_view();
+        ensure_adjoint();
+        const int64_t N = mesh.N, F = mesh.F, MF = mesh.MF;
+        geo_fcb.alloc(sizeof(double) * 6 * F);
+        geo_vb.alloc(sizeof(double) * 2 * F);
+        geo_nbc.alloc(sizeof(double) * 3 * MF * std::max<int64_t>(N, 1));
+        AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
+                     adj_back.as<signed char>(), adj_qv.as<double>(), adj_qg.as<double>(), adj_gav.as<double>()};
+        a.geo_face = face_out;
+        a.geo_cell = cell_out;
+        a.geo_fcb = geo_fcb.as<double>();
+        a.geo_vb = geo_vb.as<double>();
+        a.geo_nbc = geo_nbc.as<double>();
+        launch_adjoint_geometry(v, prm, w_dev, reconstruct && prm.order == 2, a, stream);
+        CUDA_OK(cudaGetLastError());
+    }
+    // the same on rows and geometry arrays in the reference numbering
+    DBuf map_fg, map_cg, d_face_to_ref, geo_out_face, geo_out_cell;
+    void vjp_geometry_rows(const double* w, double* face_out, double* cell_out, bool reconstruct) {
+        if (!renumbered()) return vjp_geometry(w, face_out, cell_out, reconstruct);
+        const int64_t N = mesh.N, F = mesh.F, NT = mesh.NT();
+        if (!d_face_to_ref.p) {
+            std::vector<int32_t> fm(F);
+            for (int64_t f = 0; f < F; f++) fm[f] = (int32_t)num.face_new_of_ref[f];
+            d_face_to_ref.alloc(sizeof(int32_t) * F);
+            CUDA_OK(cudaMemcpyAsync(d_face_to_ref.p, fm.data(), sizeof(int32_t) * F, cudaMemcpyHostToDevice, stream));
+            CUDA_OK(cudaStreamSynchronize(stream));
+        }
+        map_a.alloc(sizeof(double) * nvars());
+        map_fg.alloc(sizeof(double) * 13 * F);
+        map_cg.alloc(sizeof(double) * 4 * NT);
+        map_rows_device(w, map_a.as<double>(), nc(), true);
+        vjp_geometry(map_a.as<double>(), map_fg.as<double>(), map_cg.as<double>(), reconstruct);
+        ensure_maps();
+        for (int r = 0; r < 13; r++)
+            launch_gather_rows(face_out + r * F, map_fg.as<double>() + r * F, d_face_to_ref.as<int32_t>(), (int)F, 1,
+                               stream);
+        for (int r = 0; r < 4; r++) {
+            launch_gather_rows(cell_out + r * NT, map_cg.as<double>() + r * NT, d_cell_to_ref.as<int32_t>(), (int)N,
+                               1, stream);
+            if (NT > N)
+                CUDA_OK(cudaMemcpyAsync(cell_out + r * NT + N, map_cg.as<double>() + r * NT + N,
+                                        sizeof(double) * (NT - N), cudaMemcpyDeviceToDevice, stream));
+        }
+        CUDA_OK(cudaGetLastError());
+    }
+
     size_t nvars() const { return (size_t)mesh.N * nc(); }
 
     void ensure_krylov(int m) {
@@ -2341,6 +2395,15 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
                 put(o.data(), sizeof(int64_t) * N);
                 break;
             }
+            case 16: {  // the vertices of each face (int64 F x 4, -1 padded)
+                if ((int64_t)m.face_vtx_off.size() != F + 1) throw StateError("a batch keeps no face vertices");
+                std::vector<int64_t> o(4 * F, -1);
+                for (int64_t f = 0; f < F; f++)
+                    for (int64_t j = m.face_vtx_off[f], k = 0; j < m.face_vtx_off[f + 1] && k < 4; j++, k++)
+                        o[4 * f + k] = m.face_vtx[j];
+                put(o.data(), sizeof(int64_t) * 4 * F);
+                break;
+            }
             case 15: {  // the reference id of each internal face
                 std::vector<int64_t> o(F);
                 for (int64_t f = 0; f < F; f++) o[f] = ctx->face_id_to_ref(f);
@@ -2385,6 +2448,7 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
             case 8: reorder(uint32_t{}, N, 5, nm.cell_new_of_ref, 1, 0, same); break;
             case 9: reorder(double{}, N, 1, nm.cell_new_of_ref, 5, N, same); break;
             case 10: case 13: reorder(double{}, F, nc, nm.face_new_of_ref, 1, 0, same); break;
+            case 16: reorder(int64_t{}, F, 4, nm.face_new_of_ref, 1, 0, same); break;
             case 11: {
                 const int64_t* in = (const int64_t*)raw.data();
                 for (int64_t g = 0; g < G; g++) ((int64_t*)buf)[g] = face_val(in[g]);
@@ -2475,6 +2539,47 @@ int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out,
         if (ghost_out && ng)
             CUDA_OK(cudaMemcpyAsync(ghost_out, ctx->adj_gout.p, sizeof(double) * ng, cudaMemcpyDeviceToHost,
                                     ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ibisgb_vjp_geometry_device(ibisgb_ctx* ctx, const double* w_device, double* face_out_device,
+                               double* cell_out_device, int32_t allow_reconstruction, void* stream) {
+    if (!ctx || !w_device || !face_out_device || !cell_out_device) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        ctx->ensure_device();
+        if (user && user != ctx->stream) {
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+        }
+        ctx->vjp_geometry_rows(w_device, face_out_device, cell_out_device, allow_reconstruction != 0);
+        if (ev) {
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        }
+    });
+}
+
+int ibisgb_vjp_geometry(ibisgb_ctx* ctx, const double* w, double* face_out, double* cell_out,
+                        int32_t allow_reconstruction) {
+    if (!ctx || !w || !face_out || !cell_out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_device();
+        const size_t n = ctx->nvars(), nf = 13 * (size_t)ctx->mesh.F, ncl = 4 * (size_t)ctx->mesh.NT();
+        ctx->ensure_krylov(1);
+        ctx->geo_out_face.alloc(sizeof(double) * nf);
+        ctx->geo_out_cell.alloc(sizeof(double) * ncl);
+        CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, w, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->vjp_geometry_rows(ctx->kr0.as<double>(), ctx->geo_out_face.as<double>(), ctx->geo_out_cell.as<double>(),
+                               allow_reconstruction != 0);
+        CUDA_OK(cudaMemcpyAsync(face_out, ctx->geo_out_face.p, sizeof(double) * nf, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        CUDA_OK(cudaMemcpyAsync(cell_out, ctx->geo_out_cell.p, sizeof(double) * ncl, cudaMemcpyDeviceToHost,
+                                ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
 }

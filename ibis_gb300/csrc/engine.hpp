@@ -227,11 +227,22 @@ struct AdjScratch {
     double* qv;               // [2][5][F] viscous: adjoints of the sides' p, T, v (valid sides)
     double* qg;               // [2][12][F] viscous: adjoints of the sides' viscous gradients
     double* gav;              // [5][G]    viscous: adjoints of the ghosts' pre-viscous p, T, v
+    // geometry adjoint (ibisgb_vjp_geometry; null for the state-only product)
+    double* geo_face = nullptr;  // [13][F]   out: n, t1, t2, face centre, area
+    double* geo_cell = nullptr;  // [4][N+G]  out: centroid, volume (ghost rows: centroid only)
+    double* geo_fcb = nullptr;   // [2][3][F] face-centre adjoint from each side's cell
+    double* geo_vb = nullptr;    // [2][F]    volume adjoint of each side's cell from the face
+    double* geo_nbc = nullptr;   // [3][MF][N] centroid adjoint each cell sends to the neighbour of slot s
 };
 // out = (dR/dU)^T w for w, out of N x nc rows; ghost_out (optional, G x 7 rows):
 // the adjoint of every ghost cell's primitives (rho, p, T, e, v).
 void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool reconstruct, const AdjScratch& a,
                     double* out, double* ghost_out, cudaStream_t s);
+// The adjoint of the residual with respect to the grid geometry, w^T dR/dgeom, into
+// a.geo_face / a.geo_cell (inviscid residuals without constant-flux boundaries;
+// the least-squares factors are differentiated through the centroids).
+void launch_adjoint_geometry(const DevView& v, const FvParams& p, const double* w, bool reconstruct,
+                             const AdjScratch& a, cudaStream_t s);
 
 void launch_dt_finalize(StepCtl* ctl, int n_cases, cudaStream_t s);
 void launch_reset_dt(StepCtl* ctl, int n_cases, cudaStream_t s);

@@ -156,7 +156,8 @@ __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const St
                               const Gm* face, int F, int f, const FvParams& prm, const double* gfix, int G,
                               int g, const float* face_lo = nullptr) {
     auto geo = [&](int k) -> S {
-        if (face_lo) return S((double)face[k * F + f] + (double)face_lo[k * F + f]);
+        if constexpr (std::is_arithmetic<Gm>::value)  // (a dual geometry, for its adjoint, has no lo part)
+            if (face_lo) return S((double)face[k * F + f] + (double)face_lo[k * F + f]);
         return S(face[k * F + f]);
     };
     for (int a = 0; a < n; a++) {

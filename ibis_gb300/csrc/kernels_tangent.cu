@@ -177,6 +177,49 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
             else ga[(size_t)in[k] * G + (c - N)] = acc;
         }
     }
+    if (a.geo_face) {
+        // geometry: each normal / tangent component read by the flux (one dual seed
+        // each, 2-D reads n_x, n_y, t1_x, t1_y, t2_z), the area (R is linear in it) and
+        // the volume of each valid side (R_c = -(1/V_c) sum outsign A F)
+        constexpr int kRead[9] = {0, 1, 3, 4, 8, 2, 5, 6, 7};
+        constexpr int NG = DIM == 3 ? 9 : 5;
+        double gbar[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, Fr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int jj = 0; jj < NG; jj++) {
+            const int j = kRead[jj];
+            DualA gd[9];
+            for (int k = 0; k < 9; k++) {
+                const bool unread = DIM == 2 && (k == 2 || k == 5 || k == 6 || k == 7);
+                gd[k] = DualA(unread ? 0.0 : fg[k * F + f], k == j ? 1.0 : 0.0);
+            }
+            DualA qd[2][7];
+            for (int s2 = 0; s2 < 2; s2++)
+                for (int m = 0; m < 7; m++) qd[s2][m] = DualA(qv[s2][m]);
+            FaceSide<DualA> S[2];
+            for (int s2 = 0; s2 < 2; s2++)
+                side_state<DualA, DIM, true>(prm.thermo, gm, reconstruct, qd[s2], gd[0], gd[1], gd[2], gd[3], gd[4],
+                                             gd[5], gd[6], gd[7], gd[8], S[s2]);
+            DualA Fd[5];
+            convective_flux<DualA, DIM, true>(prm, gm, S[0], S[1], gd[0], gd[1], gd[2], gd[3], gd[4], gd[5], gd[6],
+                                              gd[7], gd[8], Fd);
+            double acc = 0.0;
+            for (int q = 0; q < 5; q++) acc += fb[q] * Fd[q].du;
+            gbar[j] = acc;
+            if (jj == 0)
+                for (int q = 0; q < 5; q++) Fr[q] = Fd[q].re;
+        }
+        for (int k = 0; k < 9; k++) a.geo_face[(size_t)k * F + f] = gbar[k];
+        double ab = 0.0;
+        for (int q = 0; q < 5; q++) ab += fb[q] * Fr[q];
+        a.geo_face[(size_t)12 * F + f] = ab / A;
+        for (int side = 0; side < 2; side++) {
+            const int c = cells[side];
+            if (c >= N) continue;
+            const double V = v.vol[c], sc = (side == 0 ? -A : A) / V;
+            double wf = 0.0;
+            for (int q = 0; q < NC; q++) wf += w[(size_t)c * NC + q] * Fr[q == NC - 1 ? 4 : q];
+            a.geo_vb[(size_t)side * F + f] = -sc / V * wf;
+        }
+    }
     if (!prm.viscous) return;
     // viscous terms (subtracted from the flux): states p, T, v of both sides and
     // the viscous gradients of the valid cells, one dual seed each
@@ -236,6 +279,38 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
             if (c < N && (interior || side == (l < N ? 0 : 1))) b = eval(1, side, k);
             a.qg[(size_t)(side * 12 + k) * F + f] = b;
         }
+    }
+}
+
+// Least-squares weights of every face slot of a cell from its neighbours'
+// centroid offsets d[s] = x_nb(s) - x_i, on a dual scalar: the factors r of
+// WLSGradient::compute_weights (gradient.h:119-162) and the per-neighbour weights
+// of compute_gradients (gradient.h:89-107), as the mesh builder forms them.
+template <int DIM>
+__device__ void lsq_weights(const DualA (&d)[6][3], int nf, DualA (&w)[6][3]) {
+    const DualA one(1.0);
+    DualA sxx(0.0), sxy(0.0), sxz(0.0), syy(0.0), syz(0.0), szz(0.0);
+    for (int s = 0; s < nf; s++) {
+        sxx += d[s][0] * d[s][0]; sxy += d[s][0] * d[s][1]; syy += d[s][1] * d[s][1];
+        if (DIM == 3) { sxz += d[s][0] * d[s][2]; syz += d[s][1] * d[s][2]; szz += d[s][2] * d[s][2]; }
+    }
+    const DualA r11 = dual_sqrt(sxx);
+    const DualA r12 = one / r11 * sxy;
+    const DualA r22 = dual_sqrt(syy - r12 * r12);
+    DualA r13(0.0), r23(0.0), r33(1.0);
+    if (DIM == 3) {
+        r13 = one / r11 * sxz;
+        r23 = one / r22 * (syz - r12 / r11 * sxz);
+        r33 = dual_sqrt(szz - (r13 * r13 + r23 * r23));
+    }
+    const DualA beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+    for (int s = 0; s < nf; s++) {
+        const DualA a1 = d[s][0] / (r11 * r11);
+        const DualA a2 = one / (r22 * r22) * (d[s][1] - r12 / r11 * d[s][0]);
+        const DualA a3 = DIM == 3 ? one / (r33 * r33) * (d[s][2] - r23 / r22 * d[s][1] + beta * d[s][0]) : DualA(0.0);
+        w[s][0] = a1 - r12 / r11 * a2 + beta * a3;
+        w[s][1] = a2 - r23 / r22 * a3;
+        w[s][2] = a3;
     }
 }
 
@@ -311,6 +386,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
             }
         }
     }
+    const bool geo = a.geo_cell != nullptr;
+    if (geo) {  // the cell's volume, from its faces
+        double vbar = 0.0;
+        for (int s = 0; s < nf; s++)
+            vbar += a.geo_vb[(size_t)(v.outsign[s * N + i] > 0 ? 0 : 1) * F + v.cell_face[s * N + i]];
+        a.geo_cell[(size_t)3 * NT + i] = vbar;
+    }
     if (!reconstruct) {
         for (int s = 0; s < nf; s++) {
             const int f = v.cell_face[s * N + i];
@@ -330,6 +412,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
             gb[k][d] = 0.0;
         }
     }
+    // face-centre adjoint by slot (dx = x_f - x_i enters the reconstruction and the limiter)
+    double fcs[6][3];
+    for (int s = 0; s < 6; s++) fcs[s][0] = fcs[s][1] = fcs[s][2] = 0.0;
     // reconstruction q_f = q + phi (g . dx) on every face of the cell
     for (int s = 0; s < nf; s++) {
         const int f = v.cell_face[s * N + i];
@@ -342,6 +427,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
             phib[k] += b * sgr;
             gb[k][0] += b * phi[k] * dx; gb[k][1] += b * phi[k] * dy;
             if (DIM == 3) gb[k][2] += b * phi[k] * dz;
+            if (geo) {
+                const double c = b * phi[k];
+                fcs[s][0] += c * g[k][0]; fcs[s][1] += c * g[k][1];
+                if (DIM == 3) fcs[s][2] += c * g[k][2];
+            }
         }
     }
     // the min / max arguments
@@ -389,6 +479,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
             const double tb = d2b * (double)sg * (t < 0.0 ? -1.0 : 1.0);
             gb[k][0] += tb * dx; gb[k][1] += tb * dy;
             if (DIM == 3) gb[k][2] += tb * dz;
+            if (geo) {
+                fcs[win][0] += tb * g[k][0]; fcs[win][1] += tb * g[k][1];
+                if (DIM == 3) fcs[win][2] += tb * g[k][2];
+            }
             // delta = u_ext - u_i: the extreme is the cell itself (no net term) or a neighbour
             ext[k] = sg > 0 ? amax[k] : amin[k];
             if (ext[k] >= 0) { extb[k] = db; pb[in[k]] -= db; }
@@ -408,6 +502,46 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
         }
     }
     for (int m = 0; m < 7; m++) self[(size_t)m * N + i] = pb[m];
+    if (!geo) return;
+    // the least-squares weights' adjoint, taken through the centroid offsets
+    double ccs[3] = {0.0, 0.0, 0.0};
+    double wb[6][3];
+    DualA dd[6][3];
+    for (int s = 0; s < nf; s++) {
+        const int nb = v.cell_nbr[s * N + i];
+        wb[s][0] = wb[s][1] = wb[s][2] = 0.0;
+        for (int k = 0; k < NV; k++) {
+            const double du = pr[in[k] * NT + nb].re - ui[k];
+            for (int d = 0; d < 3; d++) wb[s][d] += gb[k][d] * du;
+        }
+        dd[s][0] = DualA(cc[nb] - xi);
+        dd[s][1] = DualA(cc[NT + nb] - yi);
+        dd[s][2] = DualA(DIM == 3 ? cc[2 * NT + nb] - zi : 0.0);
+    }
+    for (int sj = 0; sj < nf; sj++) {
+        const int nb = v.cell_nbr[sj * N + i];
+        for (int sd = 0; sd < DIM; sd++) {
+            dd[sj][sd].du = 1.0;
+            DualA wd[6][3];
+            lsq_weights<DIM>(dd, nf, wd);
+            dd[sj][sd].du = 0.0;
+            double acc = 0.0;
+            for (int s = 0; s < nf; s++)
+                for (int d = 0; d < DIM; d++) acc += wb[s][d] * wd[s][d].du;
+            ccs[sd] -= acc;
+            if (nb < N) a.geo_nbc[((size_t)sd * MF + sj) * N + i] = acc;
+            else a.geo_cell[(size_t)sd * NT + nb] += acc;  // a ghost's only valid cell
+        }
+    }
+    for (int s = 0; s < nf; s++) {
+        const int f = v.cell_face[s * N + i];
+        const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
+        for (int d = 0; d < 3; d++) {
+            a.geo_fcb[((size_t)side * 3 + d) * F + f] = fcs[s][d];
+            ccs[d] -= fcs[s][d];
+        }
+    }
+    for (int d = 0; d < 3; d++) a.geo_cell[(size_t)d * NT + i] = ccs[d];
 }
 
 // Pass 3, per valid cell: the primitive adjoint (own part, what its valid
@@ -429,13 +563,18 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
     for (int m = 0; m < 7; m++) pb[m] = self[(size_t)m * N + i];
     if (reconstruct || prm.viscous) {
         const int nf = v.nfaces[i];
+        double cb[3] = {0.0, 0.0, 0.0};
         for (int s = 0; s < nf; s++) {
             const int nb = v.cell_nbr[s * N + i];
             if (nb >= N) continue;
             const int bs = back[s * N + i];
             if (bs < 0) continue;  // no face back to this cell (cannot happen on a conforming grid)
             for (int m = 0; m < 7; m++) pb[m] += nba[((size_t)m * MF + bs) * N + nb];
+            if (a.geo_cell && reconstruct)
+                for (int d = 0; d < 3; d++) cb[d] += a.geo_nbc[((size_t)d * MF + bs) * N + nb];
         }
+        if (a.geo_cell && reconstruct)
+            for (int d = 0; d < 3; d++) a.geo_cell[(size_t)d * NT + i] += cb[d];
     }
     // ghosts filled from this cell (fill_ghost's pre-reconstruction actions)
     const double* fg = (const double*)v.face;
@@ -450,6 +589,26 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
         double gvb[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         if (prm.viscous)
             for (int q = 0; q < 5; q++) gvb[q] = a.gav[(size_t)q * G + g];
+        if (a.geo_face) {  // the ghost's dependence on its face's frame (slip-wall reflection)
+            constexpr int kRead[9] = {0, 1, 3, 4, 8, 2, 5, 6, 7};
+            constexpr int NG = DIM == 3 ? 9 : 5;
+            StateT<DualA> src{DualA(pr[i].re), DualA(pr[NT + i].re), DualA(pr[2 * NT + i].re),
+                              DualA(pr[3 * NT + i].re), DualA(pr[4 * NT + i].re), DualA(pr[5 * NT + i].re),
+                              DualA(pr[6 * NT + i].re)};
+            for (int jj = 0; jj < NG; jj++) {
+                const int j = kRead[jj];
+                DualA gl[9];
+                for (int k = 0; k < 9; k++) {
+                    const bool unread = DIM == 2 && (k == 2 || k == 5 || k == 6 || k == 7);
+                    gl[k] = DualA(unread ? 0.0 : fg[k * v.F + f], k == j ? 1.0 : 0.0);
+                }
+                StateT<DualA> gh = src;
+                apply_actions<DualA, DualA>(B.pre, B.n_pre, gh, src, gl, 1, 0, prm, v.gfix, G, g);
+                a.geo_face[(size_t)j * v.F + f] += gb[0] * gh.rho.du + gb[1] * gh.p.du + gb[2] * gh.T.du +
+                                                   gb[3] * gh.e.du + gb[4] * gh.vx.du + gb[5] * gh.vy.du +
+                                                   gb[6] * gh.vz.du;
+            }
+        }
         for (int m = 0; m < 7; m++) {
             double sv[7];
             for (int q = 0; q < 7; q++) sv[q] = pr[q * NT + i].re;
@@ -467,6 +626,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
             }
         }
     }
+    if (!out) return;
     // conserved_to_primatives (primative_conserved_conversion.cpp:4-23), one seed per component
     for (int j = 0; j < NC; j++) {
         DualA u[NC];
@@ -484,7 +644,39 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
     }
 }
 
+// Face centres: the two side cells' reconstruction / limiter terms.
+__global__ void __launch_bounds__(kBlock) k_adj_geo_face(int F, AdjScratch a) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    for (int d = 0; d < 3; d++)
+        a.geo_face[(size_t)(9 + d) * F + f] = a.geo_fcb[(size_t)d * F + f] + a.geo_fcb[(size_t)(3 + d) * F + f];
+}
+
 }  // namespace k_tan
+
+void launch_adjoint_geometry(const DevView& v, const FvParams& p, const double* w, bool reconstruct,
+                             const AdjScratch& a, cudaStream_t s) {
+    using namespace k_tan;
+    const unsigned bn = blocks_for(v.N), bf = blocks_for(v.F);
+    if (v.G > 0) cudaMemsetAsync(a.ga, 0, sizeof(double) * 7 * v.G, s);
+    cudaMemsetAsync(a.geo_cell, 0, sizeof(double) * 4 * (size_t)v.NT, s);
+    cudaMemsetAsync(a.geo_fcb, 0, sizeof(double) * 6 * (size_t)v.F, s);
+    cudaMemsetAsync(a.geo_vb, 0, sizeof(double) * 2 * (size_t)v.F, s);
+    if (v.dim == 3) {
+        k_tan_prims<3><<<bn, kBlock, 0, s>>>(v, p, nullptr);
+        if (reconstruct) k_recon<Dual, Dual, double, 3, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        k_adj_face<3><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a);
+        k_adj_cell<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a);
+        k_adj_final<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a, nullptr, nullptr);
+    } else {
+        k_tan_prims<2><<<bn, kBlock, 0, s>>>(v, p, nullptr);
+        if (reconstruct) k_recon<Dual, Dual, double, 2, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        k_adj_face<2><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a);
+        k_adj_cell<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a);
+        k_adj_final<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a, nullptr, nullptr);
+    }
+    k_adj_geo_face<<<bf, kBlock, 0, s>>>(v.F, a);
+}
 
 void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool reconstruct, const AdjScratch& a,
                     double* out, double* ghost_out, cudaStream_t s) {

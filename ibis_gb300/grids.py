@@ -172,7 +172,8 @@ def tetrahedralize(g: Su2Grid) -> Su2Grid:
 
 def shuffle_cells(g: Su2Grid, seed: int = 0) -> Su2Grid:
     """The same grid with its cells listed in a seeded random order (as some
-    unstructured generators write them); vertices and markers unchanged."""
+    unstructured generators write them); vertices and markers unchanged.  Cell k
+    of the result is cell perm[k] of g, perm = np.random.default_rng(seed).permutation(num_cells)."""
     perm = np.random.default_rng(seed).permutation(g.num_cells)
     lens = (g.cell_offsets[1:] - g.cell_offsets[:-1])[perm]
     off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)

@@ -31,7 +31,8 @@ DUMPS = {"left": (0, np.int64), "right": (1, np.int64), "cell_faces": (2, np.int
          "face_geometry": (6, np.float64), "cell_geometry": (7, np.float64),
          "limiter_branches": (8, np.uint32), "limiters": (9, np.float64),
          "face_flux": (10, np.float64), "ghost_face": (11, np.int64), "ghost_boundary": (12, np.int64),
-         "face_flux_mixed": (13, np.float64), "cell_order": (14, np.int64), "face_order": (15, np.int64)}
+         "face_flux_mixed": (13, np.float64), "cell_order": (14, np.int64), "face_order": (15, np.int64),
+         "face_vertices": (16, np.int64)}
 
 
 def _ptr(a: np.ndarray):
@@ -285,6 +286,19 @@ class Simulation:
         out = out.reshape(self.num_cells, self.n_conserved)
         return (out, g) if ghosts else out
 
+    def geometry_adjoint(self, w, allow_reconstruction: bool = True):
+        """w^T dR/dgeometry (ibisgb_vjp_geometry) for w of shape (N, n_conserved):
+        (face, cell) with face (13, F) = adjoints of n, t1, t2, face centre, area
+        (the rows of dump("face_geometry")) and cell (4, N+G) = adjoints of the
+        centroids and volumes (the rows of dump("cell_geometry"))."""
+        w = np.ascontiguousarray(w, np.float64).reshape(-1)
+        if w.size != self.num_cells * self.n_conserved:
+            raise ValueError("w has the wrong size")
+        face = np.empty((13, self.num_faces))
+        cell = np.empty((4, self.num_cells + self.num_ghost_cells))
+        self._call("ibisgb_vjp_geometry", _ptr(w), _ptr(face), _ptr(cell), int(allow_reconstruction))
+        return face, cell
+
     def vector_jacobian_product_into(self, w, out, ghost_out=None, allow_reconstruction: bool = True,
                                      stream=None):
         """Device version for contiguous float64 CUDA tensors (N, n_conserved); ghost_out (G, 7) optional."""
@@ -349,7 +363,7 @@ class Simulation:
                  "neighbours": (N, MF), "ghost_source": (G,), "face_geometry": (13, F),
                  "cell_geometry": (4, NT), "limiter_branches": (N, 5), "limiters": (5, N),
                  "face_flux": (F, nc), "ghost_face": (G,), "ghost_boundary": (G,),
-                 "face_flux_mixed": (F, nc), "cell_order": (N,), "face_order": (F,)}[name]
+                 "face_flux_mixed": (F, nc), "cell_order": (N,), "face_order": (F,), "face_vertices": (F, 4)}[name]
         out = np.empty(shape, dt)
         self._call("ibisgb_get_dump", which, _ptr(out), out.nbytes)
         return out

@@ -199,7 +199,8 @@ int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]);
  * tag order) of each ghost cell (int64 G), 13 face fluxes of the last MIXED
  * residual evaluation (double F x n_conserved, from the float fluxes),
  * 14 the reference id of each internal cell (int64 N), 15 the reference id of
- * each internal face (int64 F). */
+ * each internal face (int64 F), 16 the vertices of each face (int64 F x 4, -1
+ * padded; the grid's vertex ids). */
 int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
 
 /* The device arrays' cell and face order.  The grid's optional "renumber" key
@@ -259,6 +260,24 @@ int ibisgb_vjp_device(ibisgb_ctx* ctx, const double* w_device, double* out_devic
 
 /* As ibisgb_vjp_device with host vectors (ghost_out: G x 7, may be NULL). */
 int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out, int32_t allow_reconstruction);
+
+/* The adjoint of the residual with respect to the grid geometry at the current
+ * state: for w (N x n_conserved rows), w^T dR/dgeom into face_out (13 x F: the
+ * face normal, tangents t1 and t2, centre and area, the layout of dump 6) and
+ * cell_out (4 x (N+G): centroid and volume, the layout of dump 7; ghost rows hold
+ * the ghost centroids' adjoint, ghost volumes are not inputs).  Covers what the
+ * inviscid residual reads: the face frame in the flux rotation and in the
+ * slip-wall ghost reflection (ghost_cells.cpp / boundary.cpp), areas and volumes
+ * in the surface integral (finite_volume.cpp:220-255), face centres and centroids
+ * in the reconstruction and the Barth-Jespersen limiter (limiter.cpp:23-63) and
+ * the centroids (ghosts included) through the least-squares factors
+ * (gradient.h:89-162).  2-D grids have no n_z, t1_z, t2_x, t2_y inputs (rows 0).
+ * Viscous residuals and constant-flux boundaries: IBISGB_ERR_CONFIG.  No
+ * counterpart in the reference. */
+int ibisgb_vjp_geometry_device(ibisgb_ctx* ctx, const double* w_device, double* face_out_device,
+                               double* cell_out_device, int32_t allow_reconstruction, void* stream);
+int ibisgb_vjp_geometry(ibisgb_ctx* ctx, const double* w, double* face_out, double* cell_out,
+                        int32_t allow_reconstruction);
 
 /* Result of one pseudo-time step of the steady adjoint. */
 typedef struct {

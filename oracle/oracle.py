@@ -65,6 +65,7 @@ def lib():
         L.orc_get_conserved.argtypes = [C.c_void_p, _dp]
         L.orc_steady_initialise.argtypes = [C.c_void_p]
         L.orc_jvp.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int]
+        L.orc_geometry_jvp.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int]
         L.orc_steady_rhs.argtypes = [C.c_void_p, _dp]
         L.orc_steady_steps.argtypes = [C.c_void_p, C.c_int, _dp]
         L.orc_steady_conserved.argtypes = [C.c_void_p, _dp]
@@ -232,6 +233,16 @@ class Oracle:
         self._check(lib().orc_jvp(self.h, np.ascontiguousarray(v, np.float64).reshape(-1), out,
                                   float(dt_star), int(allow_reconstruction)))
         return out
+
+    def geometry_jvp(self, dface, dcell, allow_reconstruction=True):
+        """dR/dgeometry . (dface, dcell) at the current steady state by the reference's
+        dual numbers seeded in the geometry (dface 13 x F, dcell 4 x (N+G), the
+        layouts of the face / cell geometry dumps); returns N x n_conserved."""
+        out = np.zeros(self.N * self.nc)
+        self._check(lib().orc_geometry_jvp(self.h, np.ascontiguousarray(dface, np.float64).reshape(-1),
+                                           np.ascontiguousarray(dcell, np.float64).reshape(-1), out,
+                                           int(allow_reconstruction)))
+        return out.reshape(self.N, self.nc)
 
     def steady_rhs(self):
         out = np.zeros(self.N * self.nc)

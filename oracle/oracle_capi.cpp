@@ -371,6 +371,44 @@ int orc_jvp(void* hp, const double* v, double* out, double dt_star, int allow_re
     GUARD_END(h, -1)
 }
 
+// Directional derivative of the residual at the steady simulation's current state
+// along a perturbation of the grid geometry: dface (13 x F: n, t1, t2, face
+// centre, area) and dcell (4 x (N+G): centroid, volume) seeded into the dual
+// parts of the Grid<Dual> arrays; the least-squares factors are recomputed from
+// the dual centroids (gradient.h:119-162), so they carry the centroids'
+// perturbation.  The geometry's dual parts are cleared afterwards.
+int orc_geometry_jvp(void* hp, const double* dface, const double* dcell, double* out, int allow_reconstruction) {
+    Handle* h = (Handle*)hp;
+    GUARD_BEGIN
+    Steady& st = *h->steady;
+    Sim<Dual>& s = *st.sim;
+    Grid<Dual>& g = s.grid;
+    std::vector<Dual>* fa[13] = {&g.nx, &g.ny, &g.nz, &g.t1x, &g.t1y, &g.t1z, &g.t2x, &g.t2y, &g.t2z,
+                                 &g.cx, &g.cy, &g.cz, &g.area};
+    std::vector<Dual>* ca[4] = {&g.ccx, &g.ccy, &g.ccz, &g.volume};
+    const size_t NT = g.N + g.G;
+    auto seed = [&](bool on) {
+        for (int k = 0; k < 13; k++)
+            for (size_t f = 0; f < g.F; f++) (*fa[k])[f].du = on ? dface[k * g.F + f] : 0.0;
+        for (int k = 0; k < 4; k++)
+            for (size_t c = 0; c < NT; c++) (*ca[k])[c].du = on ? dcell[k * NT + c] : 0.0;
+        if (!g.r.empty()) g.compute_gradient_weights();
+    };
+    seed(true);
+    size_t nc = g.dim + 2;
+    for (size_t c = 0; c < g.N; c++)
+        for (size_t q = 0; q < nc; q++) {
+            st.cq_tmp.q[c * nc + q].re = s.U.q[c * nc + q].re;
+            st.cq_tmp.q[c * nc + q].du = 0.0;
+        }
+    conserved_to_primatives(st.cq_tmp, st.fs_tmp, s.gas);
+    s.fv.compute_dudt(st.fs_tmp, g, st.residuals, s.gas, s.tp, allow_reconstruction != 0);
+    for (size_t i = 0; i < g.N * nc; i++) out[i] = st.residuals.q[i].du;
+    seed(false);
+    return 0;
+    GUARD_END(h, -1)
+}
+
 // real residual of the steady simulation at its current state (N x nc)
 int orc_steady_rhs(void* hp, double* out) {
     Handle* h = (Handle*)hp;

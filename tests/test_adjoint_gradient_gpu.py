@@ -1,6 +1,7 @@
 """Discrete-adjoint gradient of the integrated ramp pressure force (the Hicks-
 Henne ramp of the 512 x 256 steady-state case, on a reduced grid) with respect to the inflow Mach
-number and two bump amplitudes, against central differences of the force
+number and the bump amplitudes (the shape terms through the geometry adjoint
+kernels), against central differences of the force
 between steady states re-converged at perturbed parameters (relative 1e-5).
 A 10-degree ramp with second-order (unlimited) reconstruction on a grid small
 enough (12 x 6 cells, 288 unknowns) for one GMRES cycle of 300 to solve each
@@ -12,7 +13,8 @@ import numpy as np
 import pytest
 
 from ibis_gb300 import Simulation, grids
-from ibis_gb300.adjoint import mach_sensitivity, shape_sensitivity, solve_adjoint, steady_solve, wall_force
+from ibis_gb300.adjoint import (bump_displacements, mach_sensitivity, shape_gradient, shape_sensitivity_fd,
+                                solve_adjoint, steady_solve, wall_force)
 
 pytestmark = pytest.mark.gpu
 
@@ -51,12 +53,19 @@ def test_force_gradient_matches_central_differences():
     h = 1e-6 * M0
     fd = (wall_force(solved(mach=M0 + h), **FORCE)[0] - wall_force(solved(mach=M0 - h), **FORCE)[0]) / (2 * h)
     assert abs(dM - fd) <= 1e-5 * abs(fd), (dM, fd)
-    # two bumps
+    # every bump through the geometry adjoint; two of them against re-converged
+    # central differences, all against central differences of R and J at fixed U
     U = sim.conserved()
+    grid = grids.ramp_2d_bumps(NI, NJ, angle_deg=10.0, bumps=B0)
+    gadj = sim.geometry_adjoint(lam)
+    disp = bump_displacements(NI, NJ, angle_deg=10.0)
+    grads = [shape_gradient(sim, grid, lam, d, geometry_adjoint=gadj, **FORCE) for d in disp]
+    for k in range(len(B0)):
+        fdu = shape_sensitivity_fd(lambda b: make(bumps=b), B0, U, lam, k, h=1e-7, **FORCE)
+        assert abs(grads[k] - fdu) <= 1e-5 * max(abs(fdu), 1e-3 * max(abs(x) for x in grads)), (k, grads[k], fdu)
     for k in (4, 11):
-        da = shape_sensitivity(lambda b: make(bumps=b), B0, U, lam, k, h=1e-7, **FORCE)
         b_p, b_m = B0.copy(), B0.copy()
         b_p[k] += 1e-7
         b_m[k] -= 1e-7
         fd = (wall_force(solved(bumps=b_p), **FORCE)[0] - wall_force(solved(bumps=b_m), **FORCE)[0]) / 2e-7
-        assert abs(da - fd) <= 1e-5 * abs(fd), (k, da, fd)
+        assert abs(grads[k] - fd) <= 1e-5 * abs(fd), (k, grads[k], fd)
