@@ -10,10 +10,18 @@ differentiable function of the conserved state, with the hand-written tangent
 The forward pass evaluates the residual in the FP64_EXACT build (the
 reference's operation order), so the backward pass is the exact transpose of
 the derivative of what forward returned.  Both run on the current CUDA stream.
+
+Every call goes through the pybind11 module _ibisgb_py (csrc/python/ibisgb_py.cpp),
+the sibling of the reference's python_api module, which hands the tensors'
+device pointers and the current stream to the C ABI.
 """
 from __future__ import annotations
 
 import torch
+
+from . import _ibisgb_py as _py  # built by ibis_gb300.build; the import fails loudly when it is missing
+
+_F64_EXACT = 2
 
 
 class Residual(torch.autograd.Function):
@@ -22,10 +30,9 @@ class Residual(torch.autograd.Function):
         if U.dtype != torch.float64 or not U.is_cuda:
             raise TypeError("U must be a float64 CUDA tensor")
         U = U.contiguous()
-        stream = torch.cuda.current_stream()
-        sim.set_conserved_into(U, stream=stream)
+        _py.set_conserved(sim, U)
         out = torch.empty_like(U)
-        sim.compute_dudt_into(out, "f64_exact", stream=stream)
+        _py.residual(sim, _F64_EXACT, out)
         ctx.sim = sim
         ctx.save_for_backward(U)
         ctx.save_for_forward(U)
@@ -35,21 +42,19 @@ class Residual(torch.autograd.Function):
     def backward(ctx, grad_out):
         (U,) = ctx.saved_tensors
         sim = ctx.sim
-        stream = torch.cuda.current_stream()
-        sim.set_conserved_into(U, stream=stream)  # linearise at the forward state
+        _py.set_conserved(sim, U)  # linearise at the forward state
         g = torch.empty_like(U)
-        sim.vector_jacobian_product_into(grad_out.contiguous(), g, stream=stream)
+        _py.vjp(sim, grad_out.contiguous(), g)
         return g, None
 
     @staticmethod
     def jvp(ctx, dU, _):
         (U,) = ctx.saved_tensors
         sim = ctx.sim
-        stream = torch.cuda.current_stream()
-        sim.set_conserved_into(U, stream=stream)
+        _py.set_conserved(sim, U)
         out = torch.empty_like(U)
-        sim.matrix_vector_product_into(dU.contiguous(), out, inv_dt_star=0.0, stream=stream)
-        return -out  # matrix_vector_product gives inv_dt v - J v
+        _py.jvp(sim, dU.contiguous(), out, 0.0)
+        return -out  # the product is inv_dt v - J v
 
 
 def residual(sim, U):
@@ -90,18 +95,16 @@ def _rk_step(sim, U, dt, a, b):
 
 
 def residual_raw(sim, U):
-    stream = torch.cuda.current_stream()
-    sim.set_conserved_into(U.contiguous(), stream=stream)
+    _py.set_conserved(sim, U.contiguous())
     out = torch.empty_like(U)
-    sim.compute_dudt_into(out, "f64_exact", stream=stream)
+    _py.residual(sim, _F64_EXACT, out)
     return out
 
 
 def _vjp_raw(sim, U, w):
-    stream = torch.cuda.current_stream()
-    sim.set_conserved_into(U.contiguous(), stream=stream)
+    _py.set_conserved(sim, U.contiguous())
     out = torch.empty_like(U)
-    sim.vector_jacobian_product_into(w.contiguous(), out, stream=stream)
+    _py.vjp(sim, w.contiguous(), out)
     return out
 
 

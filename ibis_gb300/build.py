@@ -21,6 +21,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libibisgb.so")
 DRIVER = os.path.join(OUT, "ibisgb-run")
+PYMOD_SRC = os.path.join(SRC, "python", "ibisgb_py.cpp")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -103,7 +104,39 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"building ibisgb-run failed:\n{r.stdout}\n{r.stderr}")
+    build_python_module(verbose)
     return LIB
+
+
+def python_module_path() -> str:
+    import sysconfig
+    return os.path.join(HERE, "_ibisgb_py" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_python_module(verbose: bool = False) -> str:
+    """The pybind11 module _ibisgb_py (csrc/python/ibisgb_py.cpp), a client of
+    libibisgb.so, against the pybind11 headers that ship with torch."""
+    import sysconfig
+    import torch
+    mod = python_module_path()
+    inputs = [LIB, PYMOD_SRC, os.path.join(INCLUDE, "ibisgb.h")]
+    if os.path.exists(mod) and os.path.getmtime(mod) >= max(os.path.getmtime(p) for p in inputs):
+        return mod
+    torch_inc = os.path.join(os.path.dirname(torch.__file__), "include")
+    py_inc = sysconfig.get_paths()["include"]
+    if not os.path.exists(os.path.join(py_inc, "Python.h")):
+        print(f"ibis_gb300.build: no Python.h under {py_inc}; _ibisgb_py (torch.autograd bindings) not built",
+              file=sys.stderr)
+        return ""
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-shared", "-fPIC", "-fvisibility=hidden",
+           "-I", INCLUDE, "-I", torch_inc, "-I", py_inc, PYMOD_SRC, "-o", mod,
+           "-L", OUT, "-libisgb", "-Wl,-rpath,$ORIGIN/_build"]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"building the _ibisgb_py module failed:\n{r.stdout}\n{r.stderr}")
+    return mod
 
 
 if __name__ == "__main__":
