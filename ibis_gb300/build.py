@@ -129,7 +129,8 @@ def build_python_module(verbose: bool = False) -> str:
               file=sys.stderr)
         return ""
     cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-shared", "-fPIC", "-fvisibility=hidden",
-           "-I", INCLUDE, "-I", torch_inc, "-I", py_inc, PYMOD_SRC, "-o", mod,
+           "-I", INCLUDE, "-I", torch_inc, "-I", py_inc, "-I", os.path.join(os.path.dirname(os.path.dirname(_nvcc())), "include"),
+           PYMOD_SRC, "-o", mod,
            "-L", OUT, "-libisgb", "-Wl,-rpath,$ORIGIN/_build"]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)

@@ -13,6 +13,8 @@
 #include <stdexcept>
 #include <string>
 
+#include <cuda_runtime_api.h>
+
 #include "ibisgb.h"
 
 namespace py = pybind11;
@@ -37,9 +39,12 @@ void* device_ptr(py::object t, const char* what, int64_t n = 0) {
     return reinterpret_cast<void*>(t.attr("data_ptr")().cast<uintptr_t>());
 }
 
+// the current torch stream as the C ABI's stream argument: the ABI reads NULL as
+// "no ordering", so torch's legacy default stream (handle 0) goes as cudaStreamLegacy
 void* current_stream() {
     py::object s = py::module_::import("torch.cuda").attr("current_stream")();
-    return reinterpret_cast<void*>(s.attr("cuda_stream").cast<uintptr_t>());
+    const uintptr_t h = s.attr("cuda_stream").cast<uintptr_t>();
+    return h ? reinterpret_cast<void*>(h) : (void*)cudaStreamLegacy;
 }
 
 void check(ibisgb_ctx* ctx, int rc) {
