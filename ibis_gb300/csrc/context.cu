@@ -1330,17 +1330,17 @@ struct ibisgb_ctx {
 
     // w^T dR/dgeometry: face rows (13 x F: n, t1, t2, centre, area) and cell rows
     // (4 x (N+G): centroid, volume), internal numbering
-    DBuf geo_fcb, geo_vb, geo_nbc;
+    DBuf geo_fcb, geo_vb, geo_nbc, geo_ceb;
     void vjp_geometry(const double* w_dev, double* face_out, double* cell_out, bool reconstruct) {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
-        if (prm.viscous || prm.cflux)
-            throw ConfigError("the geometry adjoint covers inviscid residuals without constant-flux boundaries");
+        if (prm.cflux) throw ConfigError("the geometry adjoint covers residuals without constant-flux boundaries");
         DevView v = tangent_view();
         ensure_adjoint();
         const int64_t N = mesh.N, F = mesh.F, MF = mesh.MF;
         geo_fcb.alloc(sizeof(double) * 6 * F);
         geo_vb.alloc(sizeof(double) * 2 * F);
         geo_nbc.alloc(sizeof(double) * 3 * MF * std::max<int64_t>(N, 1));
+        geo_ceb.alloc(sizeof(double) * 3 * F);
         AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
                      adj_back.as<signed char>(), adj_qv.as<double>(), adj_qg.as<double>(), adj_gav.as<double>()};
         a.geo_face = face_out;
@@ -1348,6 +1348,7 @@ struct ibisgb_ctx {
         a.geo_fcb = geo_fcb.as<double>();
         a.geo_vb = geo_vb.as<double>();
         a.geo_nbc = geo_nbc.as<double>();
+        a.geo_ceb = geo_ceb.as<double>();
         launch_adjoint_geometry(v, prm, w_dev, reconstruct && prm.order == 2, a, stream);
         CUDA_OK(cudaGetLastError());
     }

@@ -233,14 +233,15 @@ struct AdjScratch {
     double* geo_fcb = nullptr;   // [2][3][F] face-centre adjoint from each side's cell
     double* geo_vb = nullptr;    // [2][F]    volume adjoint of each side's cell from the face
     double* geo_nbc = nullptr;   // [3][MF][N] centroid adjoint each cell sends to the neighbour of slot s
+    double* geo_ceb = nullptr;   // [3][F]    viscous: adjoint of an interior face's centroid offset x_r - x_l
 };
 // out = (dR/dU)^T w for w, out of N x nc rows; ghost_out (optional, G x 7 rows):
 // the adjoint of every ghost cell's primitives (rho, p, T, e, v).
 void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool reconstruct, const AdjScratch& a,
                     double* out, double* ghost_out, cudaStream_t s);
 // The adjoint of the residual with respect to the grid geometry, w^T dR/dgeom, into
-// a.geo_face / a.geo_cell (inviscid residuals without constant-flux boundaries;
-// the least-squares factors are differentiated through the centroids).
+// a.geo_face / a.geo_cell (residuals without constant-flux boundaries; the
+// least-squares factors are differentiated through the centroids).
 void launch_adjoint_geometry(const DevView& v, const FvParams& p, const double* w, bool reconstruct,
                              const AdjScratch& a, cudaStream_t s);
 

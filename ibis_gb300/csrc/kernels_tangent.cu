@@ -177,6 +177,21 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
             else ga[(size_t)in[k] * G + (c - N)] = acc;
         }
     }
+    // the face's total flux (convective less viscous), for the area and volume adjoints
+    double Ft[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    auto finish_geo = [&]() {
+        double ab = 0.0;
+        for (int q = 0; q < 5; q++) ab += fb[q] * Ft[q];
+        a.geo_face[(size_t)12 * F + f] = ab / A;
+        for (int side = 0; side < 2; side++) {
+            const int c = cells[side];
+            if (c >= N) continue;
+            const double V = v.vol[c], sc = (side == 0 ? -A : A) / V;
+            double wf = 0.0;
+            for (int q = 0; q < NC; q++) wf += w[(size_t)c * NC + q] * Ft[q == NC - 1 ? 4 : q];
+            a.geo_vb[(size_t)side * F + f] = -sc / V * wf;
+        }
+    };
     if (a.geo_face) {
         // geometry: each normal / tangent component read by the flux (one dual seed
         // each, 2-D reads n_x, n_y, t1_x, t1_y, t2_z), the area (R is linear in it) and
@@ -208,19 +223,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
                 for (int q = 0; q < 5; q++) Fr[q] = Fd[q].re;
         }
         for (int k = 0; k < 9; k++) a.geo_face[(size_t)k * F + f] = gbar[k];
-        double ab = 0.0;
-        for (int q = 0; q < 5; q++) ab += fb[q] * Fr[q];
-        a.geo_face[(size_t)12 * F + f] = ab / A;
-        for (int side = 0; side < 2; side++) {
-            const int c = cells[side];
-            if (c >= N) continue;
-            const double V = v.vol[c], sc = (side == 0 ? -A : A) / V;
-            double wf = 0.0;
-            for (int q = 0; q < NC; q++) wf += w[(size_t)c * NC + q] * Fr[q == NC - 1 ? 4 : q];
-            a.geo_vb[(size_t)side * F + f] = -sc / V * wf;
-        }
+        for (int q = 0; q < 5; q++) Ft[q] = Fr[q];
     }
-    if (!prm.viscous) return;
+    if (!prm.viscous) {
+        if (a.geo_face) finish_geo();
+        return;
+    }
     // viscous terms (subtracted from the flux): states p, T, v of both sides and
     // the viscous gradients of the valid cells, one dual seed each
     const Dual* pr = (const Dual*)v.prim;
@@ -280,6 +288,28 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
             a.qg[(size_t)(side * 12 + k) * F + f] = b;
         }
     }
+    if (!a.geo_face) return;
+    // geometry of the viscous terms: the normal, the centroid offset e = x_r - x_l
+    // (interior faces) and the terms' own values for the area and volume adjoints
+    auto evalg = [&](int j, double (&re)[4]) {
+        DualA sl[5], sr[5], gl[12], gr[12];
+        for (int q = 0; q < 5; q++) { sl[q] = DualA(sv[0][q]); sr[q] = DualA(sv[1][q]); }
+        for (int q = 0; q < 12; q++) { gl[q] = DualA(gv[0][q]); gr[q] = DualA(gv[1][q]); }
+        const DualA gnx(fg[f], j == 0 ? 1.0 : 0.0), gny(fg[F + f], j == 1 ? 1.0 : 0.0);
+        const DualA gnz(DIM == 3 ? fg[2 * F + f] : 0.0, j == 2 ? 1.0 : 0.0);
+        const DualA gex(ex.re, j == 3 ? 1.0 : 0.0), gey(ey.re, j == 4 ? 1.0 : 0.0), gez(ez.re, j == 5 ? 1.0 : 0.0);
+        DualA out[4], rho, mu, kk;
+        viscous_face<DualA, DIM, true>(prm, gm, interior, sl, sr, gl, gr, gex, gey, gez, gnx, gny, gnz, out, rho, mu,
+                                       kk);
+        for (int m = 0; m < 4; m++) re[m] = out[m].re;
+        return tb[0] * out[0].du + tb[1] * out[1].du + tb[2] * out[2].du + tb[3] * out[3].du;
+    };
+    double vr[4];
+    for (int j = 0; j < (DIM == 3 ? 3 : 2); j++) a.geo_face[(size_t)j * F + f] += evalg(j, vr);
+    for (int d = 0; d < 3; d++)
+        a.geo_ceb[(size_t)d * F + f] = (interior && (DIM == 3 || d < 2)) ? evalg(3 + d, vr) : 0.0;
+    for (int m = 0; m < 4; m++) Ft[1 + m] -= vr[m];  // the terms are subtracted from momentum and energy
+    finish_geo();
 }
 
 // Least-squares weights of every face slot of a cell from its neighbours'
@@ -311,6 +341,40 @@ __device__ void lsq_weights(const DualA (&d)[6][3], int nf, DualA (&w)[6][3]) {
         w[s][0] = a1 - r12 / r11 * a2 + beta * a3;
         w[s][1] = a2 - r23 / r22 * a3;
         w[s][2] = a3;
+    }
+}
+
+// The least-squares weights' adjoint wb (per slot) of valid cell i taken through the
+// centroid offsets: what each valid neighbour's centroid receives goes to
+// a.geo_nbc per slot, a ghost's centroid receives it directly (its only valid
+// cell), and the cell's own centroid adjoint is returned in own[].
+template <int DIM>
+__device__ void lsq_geometry_adjoint(const DevView& v, const AdjScratch& a, int i, int nf, const double (&wb)[6][3],
+                                     double (&own)[3]) {
+    const int N = v.N, NT = v.NT, MF = v.MF;
+    const double* cc = (const double*)v.cc;
+    const double xi = cc[i], yi = cc[NT + i], zi = DIM == 3 ? cc[2 * NT + i] : 0.0;
+    DualA dd[6][3];
+    for (int s = 0; s < nf; s++) {
+        const int nb = v.cell_nbr[s * N + i];
+        dd[s][0] = DualA(cc[nb] - xi);
+        dd[s][1] = DualA(cc[NT + nb] - yi);
+        dd[s][2] = DualA(DIM == 3 ? cc[2 * NT + nb] - zi : 0.0);
+    }
+    for (int sj = 0; sj < nf; sj++) {
+        const int nb = v.cell_nbr[sj * N + i];
+        for (int sd = 0; sd < DIM; sd++) {
+            dd[sj][sd].du = 1.0;
+            DualA wd[6][3];
+            lsq_weights<DIM>(dd, nf, wd);
+            dd[sj][sd].du = 0.0;
+            double acc = 0.0;
+            for (int s = 0; s < nf; s++)
+                for (int d = 0; d < DIM; d++) acc += wb[s][d] * wd[s][d].du;
+            own[sd] -= acc;
+            if (nb < N) a.geo_nbc[((size_t)sd * MF + sj) * N + i] = acc;
+            else a.geo_cell[(size_t)sd * NT + nb] += acc;
+        }
     }
 }
 
@@ -358,12 +422,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
         w2 = a2 - r23 / r22 * a3;
         w3 = a3;
     };
+    constexpr int NW = DIM == 3 ? 4 : 3;
+    double hb[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     if (prm.viscous) {
         // viscous: the faces' adjoints of this cell's p, T, v and of its viscous
         // gradients, then the gradients' least squares reversed onto the neighbours
         // (valid cells' T, v; ghosts' pre-viscous values)
-        constexpr int NW = DIM == 3 ? 4 : 3;
-        double hb[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (int s = 0; s < nf; s++) {
             const int f = v.cell_face[s * N + i];
             const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
@@ -387,17 +451,40 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
         }
     }
     const bool geo = a.geo_cell != nullptr;
-    if (geo) {  // the cell's volume, from its faces
-        double vbar = 0.0;
-        for (int s = 0; s < nf; s++)
-            vbar += a.geo_vb[(size_t)(v.outsign[s * N + i] > 0 ? 0 : 1) * F + v.cell_face[s * N + i]];
+    // the least-squares weights' adjoint per slot (viscous gradients here, the
+    // reconstruction gradients below) and the cell's own centroid adjoint
+    double wb[6][3], ccs[3] = {0.0, 0.0, 0.0};
+    if (geo) {
+        double vbar = 0.0;  // the cell's volume, from its faces
+        for (int s = 0; s < nf; s++) {
+            const int f = v.cell_face[s * N + i];
+            const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
+            vbar += a.geo_vb[(size_t)side * F + f];
+            if (prm.viscous)  // the viscous centroid offset e = x_r - x_l of interior faces
+                for (int d = 0; d < 3; d++) ccs[d] += (side == 0 ? -1.0 : 1.0) * a.geo_ceb[(size_t)d * F + f];
+        }
         a.geo_cell[(size_t)3 * NT + i] = vbar;
+        const Dual* vgh = (const Dual*)v.vghost;
+        for (int s = 0; s < 6; s++) wb[s][0] = wb[s][1] = wb[s][2] = 0.0;
+        if (prm.viscous)
+            for (int s = 0; s < nf; s++) {
+                const int nb = v.cell_nbr[s * N + i];
+                for (int q = 0; q < NW; q++) {
+                    const double wi = pr[visc_prim(q) * NT + i].re;
+                    const double wn = nb >= N ? vgh[(size_t)(1 + q) * G + (nb - N)].re : pr[visc_prim(q) * NT + nb].re;
+                    for (int d = 0; d < 3; d++) wb[s][d] += hb[q][d] * (wn - wi);
+                }
+            }
     }
     if (!reconstruct) {
         for (int s = 0; s < nf; s++) {
             const int f = v.cell_face[s * N + i];
             const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
             for (int k = 0; k < K; k++) pb[in[k]] += qf[(size_t)(side * 6 + k) * F + f];
+        }
+        if (geo) {
+            if (prm.viscous) lsq_geometry_adjoint<DIM>(v, a, i, nf, wb, ccs);
+            for (int d = 0; d < 3; d++) a.geo_cell[(size_t)d * NT + i] = ccs[d];
         }
         for (int m = 0; m < 7; m++) self[(size_t)m * N + i] = pb[m];
         return;
@@ -503,36 +590,15 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
     }
     for (int m = 0; m < 7; m++) self[(size_t)m * N + i] = pb[m];
     if (!geo) return;
-    // the least-squares weights' adjoint, taken through the centroid offsets
-    double ccs[3] = {0.0, 0.0, 0.0};
-    double wb[6][3];
-    DualA dd[6][3];
+    // the reconstruction gradients' part of the least-squares weights' adjoint
     for (int s = 0; s < nf; s++) {
         const int nb = v.cell_nbr[s * N + i];
-        wb[s][0] = wb[s][1] = wb[s][2] = 0.0;
         for (int k = 0; k < NV; k++) {
             const double du = pr[in[k] * NT + nb].re - ui[k];
             for (int d = 0; d < 3; d++) wb[s][d] += gb[k][d] * du;
         }
-        dd[s][0] = DualA(cc[nb] - xi);
-        dd[s][1] = DualA(cc[NT + nb] - yi);
-        dd[s][2] = DualA(DIM == 3 ? cc[2 * NT + nb] - zi : 0.0);
     }
-    for (int sj = 0; sj < nf; sj++) {
-        const int nb = v.cell_nbr[sj * N + i];
-        for (int sd = 0; sd < DIM; sd++) {
-            dd[sj][sd].du = 1.0;
-            DualA wd[6][3];
-            lsq_weights<DIM>(dd, nf, wd);
-            dd[sj][sd].du = 0.0;
-            double acc = 0.0;
-            for (int s = 0; s < nf; s++)
-                for (int d = 0; d < DIM; d++) acc += wb[s][d] * wd[s][d].du;
-            ccs[sd] -= acc;
-            if (nb < N) a.geo_nbc[((size_t)sd * MF + sj) * N + i] = acc;
-            else a.geo_cell[(size_t)sd * NT + nb] += acc;  // a ghost's only valid cell
-        }
-    }
+    lsq_geometry_adjoint<DIM>(v, a, i, nf, wb, ccs);
     for (int s = 0; s < nf; s++) {
         const int f = v.cell_face[s * N + i];
         const int side = v.outsign[s * N + i] > 0 ? 0 : 1;
@@ -570,10 +636,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
             const int bs = back[s * N + i];
             if (bs < 0) continue;  // no face back to this cell (cannot happen on a conforming grid)
             for (int m = 0; m < 7; m++) pb[m] += nba[((size_t)m * MF + bs) * N + nb];
-            if (a.geo_cell && reconstruct)
+            if (a.geo_cell)
                 for (int d = 0; d < 3; d++) cb[d] += a.geo_nbc[((size_t)d * MF + bs) * N + nb];
         }
-        if (a.geo_cell && reconstruct)
+        if (a.geo_cell)
             for (int d = 0; d < 3; d++) a.geo_cell[(size_t)d * NT + i] += cb[d];
     }
     // ghosts filled from this cell (fill_ghost's pre-reconstruction actions)
@@ -604,9 +670,14 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
                 }
                 StateT<DualA> gh = src;
                 apply_actions<DualA, DualA>(B.pre, B.n_pre, gh, src, gl, 1, 0, prm, v.gfix, G, g);
-                a.geo_face[(size_t)j * v.F + f] += gb[0] * gh.rho.du + gb[1] * gh.p.du + gb[2] * gh.T.du +
-                                                   gb[3] * gh.e.du + gb[4] * gh.vx.du + gb[5] * gh.vy.du +
-                                                   gb[6] * gh.vz.du;
+                double d = gb[0] * gh.rho.du + gb[1] * gh.p.du + gb[2] * gh.T.du + gb[3] * gh.e.du +
+                           gb[4] * gh.vx.du + gb[5] * gh.vy.du + gb[6] * gh.vz.du;
+                if (prm.viscous) {  // the pre-viscous actions continue from the pre-reconstruction ghost
+                    apply_actions<DualA, DualA>(B.visc, B.n_visc, gh, src, gl, 1, 0, prm, v.gfix, G, g);
+                    d += gvb[0] * gh.p.du + gvb[1] * gh.T.du + gvb[2] * gh.vx.du + gvb[3] * gh.vy.du +
+                         gvb[4] * gh.vz.du;
+                }
+                a.geo_face[(size_t)j * v.F + f] += d;
             }
         }
         for (int m = 0; m < 7; m++) {
@@ -659,18 +730,19 @@ void launch_adjoint_geometry(const DevView& v, const FvParams& p, const double* 
     using namespace k_tan;
     const unsigned bn = blocks_for(v.N), bf = blocks_for(v.F);
     if (v.G > 0) cudaMemsetAsync(a.ga, 0, sizeof(double) * 7 * v.G, s);
+    if (v.G > 0 && p.viscous) cudaMemsetAsync(a.gav, 0, sizeof(double) * 5 * v.G, s);
     cudaMemsetAsync(a.geo_cell, 0, sizeof(double) * 4 * (size_t)v.NT, s);
     cudaMemsetAsync(a.geo_fcb, 0, sizeof(double) * 6 * (size_t)v.F, s);
     cudaMemsetAsync(a.geo_vb, 0, sizeof(double) * 2 * (size_t)v.F, s);
     if (v.dim == 3) {
         k_tan_prims<3><<<bn, kBlock, 0, s>>>(v, p, nullptr);
-        if (reconstruct) k_recon<Dual, Dual, double, 3, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        if (reconstruct || p.viscous) k_recon<Dual, Dual, double, 3, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
         k_adj_face<3><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a);
         k_adj_cell<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a);
         k_adj_final<3><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a, nullptr, nullptr);
     } else {
         k_tan_prims<2><<<bn, kBlock, 0, s>>>(v, p, nullptr);
-        if (reconstruct) k_recon<Dual, Dual, double, 2, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        if (reconstruct || p.viscous) k_recon<Dual, Dual, double, 2, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
         k_adj_face<2><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a);
         k_adj_cell<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a);
         k_adj_final<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a, nullptr, nullptr);

@@ -271,9 +271,12 @@ int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out,
  * in the surface integral (finite_volume.cpp:220-255), face centres and centroids
  * in the reconstruction and the Barth-Jespersen limiter (limiter.cpp:23-63) and
  * the centroids (ghosts included) through the least-squares factors
- * (gradient.h:89-162).  2-D grids have no n_z, t1_z, t2_x, t2_y inputs (rows 0).
- * Viscous residuals and constant-flux boundaries: IBISGB_ERR_CONFIG.  No
- * counterpart in the reference. */
+ * (gradient.h:89-162), and in viscous residuals the normal and the centroid
+ * offset of the face gradient (viscous_flux.cpp:36-80) and the viscous least
+ * squares.  The boundary-layer profile's ghost states are taken as fixed (their
+ * dependence on the ghost centroid's height is not differentiated).  2-D grids
+ * have no n_z, t1_z, t2_x, t2_y inputs (rows 0).  Constant-flux boundaries:
+ * IBISGB_ERR_CONFIG.  No counterpart in the reference. */
 int ibisgb_vjp_geometry_device(ibisgb_ctx* ctx, const double* w_device, double* face_out_device,
                                double* cell_out_device, int32_t allow_reconstruction, void* stream);
 int ibisgb_vjp_geometry(ibisgb_ctx* ctx, const double* w, double* face_out, double* cell_out,
