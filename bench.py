@@ -628,6 +628,17 @@ def run_ours(args, world, rank, local):
         sim.take_steps(1, "mixed")
         sim.conserved(out=host_out)
     barrier()
+    e2e_seq_s = max_over_ranks_(time.perf_counter() - t0)
+    e2e_seq_value = whole_job_rate(N, world, 3, e2e_steps, e2e_seq_s)
+    # the same jobs through ibisgb_rk_run_host: each step's upload and read-back on
+    # copy streams, overlapping the neighbouring steps' kernels
+    host_out2 = torch.empty((N, nc), dtype=torch.float64, pin_memory=True).numpy()
+    outs = [host_out if j % 2 == 0 else host_out2 for j in range(e2e_steps)]
+    sim.take_steps_host([host_in, host_in], [host_out, host_out2], 1, "mixed")
+    barrier()
+    t0 = time.perf_counter()
+    sim.take_steps_host([host_in] * e2e_steps, outs, 1, "mixed")
+    barrier()
     e2e_s = max_over_ranks_(time.perf_counter() - t0)
     e2e_value = whole_job_rate(N, world, 3, e2e_steps, e2e_s)
 
@@ -698,7 +709,13 @@ def run_ours(args, world, rank, local):
                                             f"at 128^3, scaled by 8 (profiles/{summary})") if traffic else None},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 8 * nc * N,
-                    "d2h_bytes_per_step": 8 * nc * N, "steps": e2e_steps},
+                    "d2h_bytes_per_step": 8 * nc * N, "steps": e2e_steps,
+                    "api": "ibisgb_rk_run_host: per step the state from pinned host rows, one ssp-rk3 step, the "
+                           "new state to pinned host rows; the next step's upload and the previous step's "
+                           "read-back run on copy streams during the step's kernels",
+                    "sequential_value": e2e_seq_value,
+                    "sequential_api": "ibisgb_set_conserved + ibisgb_rk_run + ibisgb_get_conserved per step, "
+                                      "each call synchronous"},
             "gpu_launches": (4 if fused["enabled"] else 7 if cellf["enabled"] else KERNELS_PER_STEP) * args.steps + 2,
             "gpu_launches_note": "kernels of the timed headline call: one graph per step (dt control + 3 fused "
                                  "stages, dt control + 3 x recon/cell-flux update, or dt control + 3 x "

@@ -82,12 +82,14 @@ def steady_solve(sim: Simulation, tol: float = 1e-10, max_steps: int = 200, prec
 
 
 def solve_adjoint(sim: Simulation, dJdU: np.ndarray, tol: float = 1e-10, cfl0: float = 10.0,
-                  growth: float = 4.0, cfl_max: float = 1e12, max_steps: int = 2000):
+                  growth: float = 4.0, cfl_max: float = 1e12, max_steps: int = 2000, krylov: int = 100):
     """lambda with J_R^T lambda = -dJ/dU at the current state, by the device's
-    pseudo-time continuation (the CFL grows geometrically; restarted GMRES on the
-    variable-scaled J^T once it is large) until the scaled residual is below tol
-    of its first value; returns (lambda, history)."""
+    pseudo-time continuation (the CFL grows geometrically; restarted GMRES of
+    `krylov` vectors on the variable-scaled J^T once it is large; 0 keeps the
+    steady solver's length) until the scaled residual is below tol of its first
+    value; returns (lambda, history)."""
     import torch
+    sim.set_adjoint_krylov(krylov)
     g = torch.tensor(np.ascontiguousarray(dJdU), dtype=torch.float64, device="cuda")
     lam = torch.zeros_like(g)
     cfl, hist, first = cfl0, [], None

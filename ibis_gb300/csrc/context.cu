@@ -235,6 +235,10 @@ struct ibisgb_ctx {
             if (g) cudaGraphExecDestroy(g);
         for (auto& g : graph_fused)
             if (g) cudaGraphExecDestroy(g);
+        for (auto& e : pipe_ev)
+            if (e) cudaEventDestroy(e);
+        if (pipe_h2d) cudaStreamDestroy(pipe_h2d);
+        if (pipe_d2h) cudaStreamDestroy(pipe_d2h);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -929,6 +933,7 @@ struct ibisgb_ctx {
         have_state = true;
         s64.prims_current = false;
         s32.prims_current = false;
+        sff.prims_current = false;
         // RungeKutta::initialise: t = 0, dt = dt_init or max (runge_kutta.cpp:82-104)
         reset_rk();
     }
@@ -1183,7 +1188,9 @@ struct ibisgb_ctx {
         }
     }
 
-    void rk_run(int prec, int64_t n, ibisgb_rk_status* st) {
+    // Tuning and the per-step graphs of precision prec; returns whether the fused
+    // (or per-cell flux) stage runs.  The primitives of the current state are made current.
+    bool prepare_rk(int prec) {
         if (!rk_configured) throw ConfigError("config.json solver is not runge_kutta");
         ensure_prims(prec);
         int gi = gidx(prec);
@@ -1214,26 +1221,45 @@ struct ibisgb_ctx {
             CUDA_OK(cudaGraphInstantiate(&graph[gi], g, 0));
             CUDA_OK(cudaGraphDestroy(g));
         }
+        return fused;
+    }
+
+    // n steps on the context stream (the local-dt prologue, then one graph per step)
+    void enqueue_rk(int prec, int64_t n, bool fused) {
         if (!prm.viscous && n > 0) {  // local dt of the current state for the first step
             DevView v = view(prec);
             launch_reset_dt(v.ctl, n_cases, stream);
             ops(prec).local_dt(v, prm, stream);
             CUDA_OK(cudaGetLastError());
         }
-        cudaEvent_t e0, e1;
-        CUDA_OK(cudaEventCreate(&e0));
-        CUDA_OK(cudaEventCreate(&e1));
-        CUDA_OK(cudaEventRecord(e0, stream));
         if (fused) {
             for (int64_t i = 0; i < n; i++) {
                 CUDA_OK(cudaGraphLaunch(graph_fused[prim_cur], stream));
                 prim_cur ^= (ctl_host.stages & 1);
             }
         } else {
+            const int gi = gidx(prec);
             for (int64_t i = 0; i < n; i++) CUDA_OK(cudaGraphLaunch(graph[gi], stream));
         }
-        CUDA_OK(cudaEventRecord(e1, stream));
         state_changed(prec);
+    }
+
+    void rk_run(int prec, int64_t n, ibisgb_rk_status* st) {
+        const bool fused = prepare_rk(prec);
+        cudaEvent_t e0, e1;
+        CUDA_OK(cudaEventCreate(&e0));
+        CUDA_OK(cudaEventCreate(&e1));
+        CUDA_OK(cudaEventRecord(e0, stream));
+        enqueue_rk(prec, n, fused);
+        CUDA_OK(cudaEventRecord(e1, stream));
+        float ms = finish_rk(prec, fused, e0, e1, st);
+        (void)ms;
+    }
+
+    // The step control after the last enqueued step (t, dt, steps, bad cells: a batch
+    // reports its minimum times, maximum steps and total bad cells); throws on bad cells.
+    float finish_rk(int prec, bool fused, cudaEvent_t e0, cudaEvent_t e1, ibisgb_rk_status* st) {
+        (void)prec;
         last_ctl.resize(n_cases);
         CUDA_OK(cudaMemcpyAsync(last_ctl.data(), ctl.p, sizeof(StepCtl) * n_cases, cudaMemcpyDeviceToHost, stream));
         CUDA_OK(cudaStreamSynchronize(stream));
@@ -1256,6 +1282,83 @@ struct ibisgb_ctx {
             st->device_ms = ms;
         }
         if (c.bad_cells > 0) throw std::runtime_error("bad cells");
+        return ms;
+    }
+
+    // n_jobs Runge-Kutta runs from host rows: job j replaces the state by U_in[j],
+    // takes `steps` steps and writes the new state to U_out[j] -- what
+    // set_conserved + rk_run + get_conserved do per job, with job j+1's upload and
+    // job j-1's read-back on two copy streams while job j's steps run (two device
+    // staging buffers each way).  Pinned host rows make the copies asynchronous.
+    DBuf pipe_in[2], pipe_out[2];
+    cudaStream_t pipe_h2d = nullptr, pipe_d2h = nullptr;
+    cudaEvent_t pipe_ev[8] = {};
+    void rk_run_host(int prec, int64_t n_jobs, int64_t steps, const double* const* U_in, double* const* U_out,
+                     ibisgb_rk_status* st) {
+        if (n_jobs <= 0) throw ArgError("n_jobs must be positive");
+        for (int64_t j = 0; j < n_jobs; j++)
+            if (!U_in[j] || !U_out[j]) throw ArgError("a job's host rows are null");
+        ensure_device();
+        if (!have_state) set_conserved(U_in[0]);
+        const bool fused = prepare_rk(prec);
+        const size_t bytes = sizeof(double) * nvars();
+        if (!pipe_h2d) {
+            CUDA_OK(cudaStreamCreateWithFlags(&pipe_h2d, cudaStreamNonBlocking));
+            CUDA_OK(cudaStreamCreateWithFlags(&pipe_d2h, cudaStreamNonBlocking));
+            for (auto& e : pipe_ev) CUDA_OK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        for (int b = 0; b < 2; b++) {
+            pipe_in[b].alloc(bytes);
+            pipe_out[b].alloc(bytes);
+        }
+        if (renumbered()) map_a.alloc(bytes);
+        cudaEvent_t* ev_in = pipe_ev, *ev_used = pipe_ev + 2, *ev_packed = pipe_ev + 4, *ev_read = pipe_ev + 6;
+        cudaEvent_t e0, e1;
+        CUDA_OK(cudaEventCreate(&e0));
+        CUDA_OK(cudaEventCreate(&e1));
+        CUDA_OK(cudaEventRecord(e0, stream));
+        CUDA_OK(cudaStreamWaitEvent(pipe_h2d, e0, 0));
+        CUDA_OK(cudaStreamWaitEvent(pipe_d2h, e0, 0));
+        auto upload = [&](int64_t j) {
+            const int b = (int)(j & 1);
+            if (j >= 2) CUDA_OK(cudaStreamWaitEvent(pipe_h2d, ev_used[b], 0));  // job j-2 consumed buffer b
+            CUDA_OK(cudaMemcpyAsync(pipe_in[b].p, U_in[j], bytes, cudaMemcpyHostToDevice, pipe_h2d));
+            CUDA_OK(cudaEventRecord(ev_in[b], pipe_h2d));
+        };
+        upload(0);
+        for (int64_t j = 0; j < n_jobs; j++) {
+            const int b = (int)(j & 1);
+            if (j + 1 < n_jobs) upload(j + 1);
+            CUDA_OK(cudaStreamWaitEvent(stream, ev_in[b], 0));
+            const double* rows = pipe_in[b].as<double>();
+            if (renumbered()) {
+                map_rows_device(rows, map_a.as<double>(), nc(), true);
+                rows = map_a.as<double>();
+            }
+            launch_rows_to_soa(rows, U.as<double>(), (int)mesh.N, nc(), stream);
+            CUDA_OK(cudaEventRecord(ev_used[b], stream));
+            ic_prims.clear();
+            state_changed(-1);
+            ensure_prims(prec);
+            enqueue_rk(prec, steps, fused);
+            if (j >= 2) CUDA_OK(cudaStreamWaitEvent(stream, ev_read[b], 0));  // job j-2's read-back is done
+            if (renumbered()) {
+                launch_soa_to_rows(U.as<double>(), map_a.as<double>(), (int)mesh.N, nc(), stream);
+                map_rows_device(map_a.as<double>(), pipe_out[b].as<double>(), nc(), false);
+            } else {
+                launch_soa_to_rows(U.as<double>(), pipe_out[b].as<double>(), (int)mesh.N, nc(), stream);
+            }
+            CUDA_OK(cudaGetLastError());
+            CUDA_OK(cudaEventRecord(ev_packed[b], stream));
+            CUDA_OK(cudaStreamWaitEvent(pipe_d2h, ev_packed[b], 0));
+            CUDA_OK(cudaMemcpyAsync(U_out[j], pipe_out[b].p, bytes, cudaMemcpyDeviceToHost, pipe_d2h));
+            CUDA_OK(cudaEventRecord(ev_read[b], pipe_d2h));
+        }
+        CUDA_OK(cudaStreamWaitEvent(stream, ev_read[(n_jobs - 1) & 1], 0));
+        CUDA_OK(cudaEventRecord(e1, stream));
+        finish_rk(prec, fused, e0, e1, st);
+        CUDA_OK(cudaStreamSynchronize(pipe_h2d));
+        CUDA_OK(cudaStreamSynchronize(pipe_d2h));
     }
 
     // ----- tangent (SteadyStateLinearisation::matrix_vector_product) ---------
@@ -1592,13 +1695,15 @@ struct ibisgb_ctx {
     // wherever the forward pseudo-time iteration does (J^T has J's spectrum) and
     // becomes restarted GMRES on the scaled J^T as the CFL grows.
     DBuf adj_r, adj_d, adj_t, adj_norm;
+    int adj_krylov = 0;  // GMRES length of the adjoint step (0: the steady solver's)
     void adjoint_step(const double* g, double* lam, double cfl, ibisgb_adjoint_status* out) {
         if (n_cases > 1) throw StateError("steady-state solves run one case per context, not on a batch");
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
         const Steady& st = steady;
         const size_t n = nvars();
         const int ncv = nc();
-        ensure_krylov(st.max_iters);
+        const int m = adj_krylov > 0 ? adj_krylov : st.max_iters;
+        ensure_krylov(m);
         adj_r.alloc(sizeof(double) * n);
         adj_d.alloc(sizeof(double) * n);
         adj_t.alloc(sizeof(double) * n);
@@ -1640,7 +1745,7 @@ struct ibisgb_ctx {
             launch_axpby(y, t, (long long)n, inv, -1.0, stream);
             launch_scale_rows(y, y, (long long)n, ncv, sc, stream);
         };
-        GmresOut res = gmres(A, r, d, st.max_iters, st.tol, kv.as<double>(), nullptr, nullptr);
+        GmresOut res = gmres(A, r, d, m, st.tol, kv.as<double>(), nullptr, nullptr);
         launch_scale_rows(d, d, (long long)n, ncv, isc, stream);
         launch_axpby(lam, d, (long long)n, 1.0, 1.0, stream);
         CUDA_OK(cudaGetLastError());
@@ -1974,6 +2079,7 @@ struct ibisgb_ctx {
         ic_prims.clear();
         s64.prims_current = false;
         s32.prims_current = false;
+        sff.prims_current = false;
     }
 
     void get_conserved(double* rows) {
@@ -2303,6 +2409,15 @@ int ibisgb_rk_run(ibisgb_ctx* ctx, int32_t precision, int64_t n_steps, ibisgb_rk
     });
 }
 
+int ibisgb_rk_run_host(ibisgb_ctx* ctx, int32_t precision, int64_t n_jobs, int64_t steps_per_job,
+                       const double* const* U_in, double* const* U_out, ibisgb_rk_status* status) {
+    if (!ctx || !U_in || !U_out || n_jobs <= 0 || steps_per_job < 0) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        if (precision < 0 || precision > 4) throw ArgError("unknown precision");
+        ctx->rk_run_host(precision, n_jobs, steps_per_job, U_in, U_out, status);
+    });
+}
+
 int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]) {
     if (!ctx || !out) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
@@ -2589,6 +2704,12 @@ int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_
                         ibisgb_adjoint_status* status) {
     if (!ctx || !g_device || !lambda_device || !(cfl > 0.0)) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] { ctx->adjoint_step_rows(g_device, lambda_device, cfl, status); });
+}
+
+int ibisgb_set_adjoint_krylov(ibisgb_ctx* ctx, int32_t max_iters) {
+    if (!ctx || max_iters < 0 || max_iters > 1000) return IBISGB_ERR_ARG;
+    ctx->adj_krylov = max_iters;
+    return IBISGB_OK;
 }
 
 int ibisgb_steady_initialise(ibisgb_ctx* ctx, int32_t precision) {

@@ -251,6 +251,25 @@ class Simulation:
         return {"t": st.t, "dt": st.dt, "stable_dt": st.stable_dt, "steps": st.steps,
                 "bad_cells": st.bad_cells, "device_ms": st.device_ms}
 
+    def take_steps_host(self, U_in, U_out, steps: int = 1, precision: str = "f64") -> dict:
+        """For each pair (U_in[j], U_out[j]) of host arrays (N, n_conserved): the state
+        from U_in[j], `steps` Runge-Kutta steps, the new state into U_out[j]
+        (ibisgb_rk_run_host: the next upload and the previous read-back overlap the
+        steps when the arrays are pinned).  Returns the last job's status."""
+        arrs_in = [np.ascontiguousarray(a, np.float64) for a in U_in]
+        if len(arrs_in) != len(U_out) or not arrs_in:
+            raise ValueError("U_in and U_out need the same, nonzero number of arrays")
+        shape = (self.num_cells, self.n_conserved)
+        for a in list(arrs_in) + list(U_out):
+            if a.shape != shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"expected contiguous float64 arrays of shape {shape}")
+        pin = (C.c_void_p * len(arrs_in))(*[a.ctypes.data for a in arrs_in])
+        pout = (C.c_void_p * len(U_out))(*[a.ctypes.data for a in U_out])
+        st = RkStatus()
+        self._call("ibisgb_rk_run_host", PRECISION[precision], len(arrs_in), int(steps), pin, pout, C.byref(st))
+        return {"t": st.t, "dt": st.dt, "stable_dt": st.stable_dt, "steps": st.steps,
+                "bad_cells": st.bad_cells, "device_ms": st.device_ms}
+
     # ------------------------------------------------------- steady / JFNK
     def matrix_vector_product(self, v, inv_dt_star: float = 0.0, allow_reconstruction: bool = True):
         """inv_dt_star * v - (dR/dU) v for v of shape (N, n_conserved) (host arrays);
@@ -324,6 +343,10 @@ class Simulation:
         return {"residual_norm": st.residual_norm, "scaled_residual_norm": st.scaled_residual_norm,
                 "gmres_iterations": st.gmres_iterations, "gmres_converged": bool(st.gmres_converged),
                 "gmres_residual": st.gmres_residual, "dt_star": st.dt_star}
+
+    def set_adjoint_krylov(self, max_iters: int) -> None:
+        """GMRES length of adjoint_step (0: the steady solver's max_iters)."""
+        self._call("ibisgb_set_adjoint_krylov", int(max_iters))
 
     def steady_initialise(self, precision: str = "f64"):
         """Jfnk::initialise: residual and initial norms at the current state."""

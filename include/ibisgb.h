@@ -180,6 +180,19 @@ int ibisgb_count_bad_cells(ibisgb_ctx* ctx, int64_t* n);
  * IBISGB_ERR_BAD_CELLS after the first step that leaves bad cells. */
 int ibisgb_rk_run(ibisgb_ctx* ctx, int32_t precision, int64_t n_steps, ibisgb_rk_status* status);
 
+/* n_jobs Runge-Kutta runs between host buffers: job j replaces the state by the
+ * rows U_in[j] (N x n_conserved, reference cell order), takes steps_per_job steps
+ * and writes the new state to U_out[j] -- the same results as
+ * ibisgb_set_conserved + ibisgb_rk_run + ibisgb_get_conserved per job, with job
+ * j+1's upload and job j-1's read-back on copy streams while job j's steps run.
+ * Pinned host buffers (cudaHostAlloc, torch pin_memory) make the copies overlap;
+ * the buffers of a job may be reused once the call returns.  The status is the
+ * last job's (IBISGB_ERR_BAD_CELLS when it left bad cells).  A driver that
+ * advances a stream of states (ensembles kept on the host, sampling, surrogate
+ * training) calls this instead of the three calls per state. */
+int ibisgb_rk_run_host(ibisgb_ctx* ctx, int32_t precision, int64_t n_jobs, int64_t steps_per_job,
+                       const double* const* U_in, double* const* U_out, ibisgb_rk_status* status);
+
 /* L2 norms of the first-stage residual of the last step: global, mass,
  * momentum_x, momentum_y, momentum_z, energy.  Replaces
  * ConservedQuantities<T>::L2_norms (conserved_quantities.cpp:40-69) on k_[0]
@@ -308,6 +321,11 @@ typedef struct {
  * the grid. */
 int ibisgb_adjoint_step(ibisgb_ctx* ctx, const double* g_device, double* lambda_device, double cfl,
                         ibisgb_adjoint_status* status);
+
+/* GMRES length of ibisgb_adjoint_step (1..1000; 0 restores the steady solver's
+ * max_iters).  The adjoint is a linear solve, so a longer Krylov space than the
+ * forward Newton steps' (whose length is the reference's, for parity) pays. */
+int ibisgb_set_adjoint_krylov(ibisgb_ctx* ctx, int32_t max_iters);
 
 /* Residual and initial norms of the steady solver at the current state
  * (Jfnk::initialise, src/solvers/solvers/jfnk.cpp:25-30).  `precision` is the
