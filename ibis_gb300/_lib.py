@@ -97,6 +97,8 @@ def load(build_if_missing: bool = True):
     L.ibisgb_vjp_device.argtypes = [_P, _P, _P, _P, C.c_int32, _P]
     L.ibisgb_vjp_geometry.argtypes = [_P, _P, _P, _P, C.c_int32]
     L.ibisgb_set_adjoint_krylov.argtypes = [_P, C.c_int32]
+    L.ibisgb_jvp_geometry.argtypes = [_P, _P, _P, _P, C.c_int32]
+    L.ibisgb_jvp_geometry_device.argtypes = [_P, _P, _P, _P, C.c_int32, _P]
     L.ibisgb_rk_run_host.argtypes = [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P, _P]
     L.ibisgb_vjp_geometry_device.argtypes = [_P, _P, _P, _P, C.c_int32, _P]
     L.ibisgb_adjoint_step.argtypes = [_P, _P, _P, C.c_double, C.POINTER(AdjointStatus)]

@@ -1455,8 +1455,52 @@ struct ibisgb_ctx {
         launch_adjoint_geometry(v, prm, w_dev, reconstruct && prm.order == 2, a, stream);
         CUDA_OK(cudaGetLastError());
     }
+    // dR/dgeometry . (dface, dcell) (N x nc rows, internal numbering)
+    DBuf gt_face, gt_cc, gt_vol, gt_r;
+    void jvp_geometry(const double* dface, const double* dcell, double* out, bool reconstruct) {
+        if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
+        if (prm.cflux) throw ConfigError("the geometry tangent covers residuals without constant-flux boundaries");
+        DevView v = tangent_view();
+        const int64_t N = mesh.N, F = mesh.F, NT = mesh.NT();
+        const size_t D = 2 * sizeof(double);
+        gt_face.alloc(D * 13 * F);
+        gt_cc.alloc(D * 3 * NT);
+        gt_vol.alloc(D * std::max<int64_t>(N, 1));
+        gt_r.alloc(D * 6 * std::max<int64_t>(N, 1));
+        GeoTangent g{gt_face.p, gt_cc.p, gt_vol.p, gt_r.p};
+        launch_tangent_geometry(v, prm, dface, dcell, reconstruct && prm.order == 2, g, out, stream);
+        CUDA_OK(cudaGetLastError());
+    }
+
     // the same on rows and geometry arrays in the reference numbering
-    DBuf map_fg, map_cg, d_face_to_ref, geo_out_face, geo_out_cell;
+    DBuf map_fg, map_cg, d_face_to_ref, d_face_to_new, geo_out_face, geo_out_cell;
+    void jvp_geometry_rows(const double* dface, const double* dcell, double* out, bool reconstruct) {
+        if (!renumbered()) return jvp_geometry(dface, dcell, out, reconstruct);
+        const int64_t N = mesh.N, F = mesh.F, NT = mesh.NT();
+        if (!d_face_to_new.p) {
+            std::vector<int32_t> fm(F);
+            for (int64_t f = 0; f < F; f++) fm[f] = (int32_t)num.face_ref_of_new[f];
+            d_face_to_new.alloc(sizeof(int32_t) * F);
+            CUDA_OK(cudaMemcpyAsync(d_face_to_new.p, fm.data(), sizeof(int32_t) * F, cudaMemcpyHostToDevice, stream));
+            CUDA_OK(cudaStreamSynchronize(stream));
+        }
+        ensure_maps();
+        map_fg.alloc(sizeof(double) * 13 * F);
+        map_cg.alloc(sizeof(double) * 4 * NT);
+        map_b.alloc(sizeof(double) * nvars());
+        for (int r = 0; r < 13; r++)
+            launch_gather_rows(map_fg.as<double>() + r * F, dface + r * F, d_face_to_new.as<int32_t>(), (int)F, 1,
+                               stream);
+        for (int r = 0; r < 4; r++) {
+            launch_gather_rows(map_cg.as<double>() + r * NT, dcell + r * NT, d_cell_to_new.as<int32_t>(), (int)N, 1,
+                               stream);
+            if (NT > N)
+                CUDA_OK(cudaMemcpyAsync(map_cg.as<double>() + r * NT + N, dcell + r * NT + N,
+                                        sizeof(double) * (NT - N), cudaMemcpyDeviceToDevice, stream));
+        }
+        jvp_geometry(map_fg.as<double>(), map_cg.as<double>(), map_b.as<double>(), reconstruct);
+        map_rows_device(map_b.as<double>(), out, nc(), false);
+    }
     void vjp_geometry_rows(const double* w, double* face_out, double* cell_out, bool reconstruct) {
         if (!renumbered()) return vjp_geometry(w, face_out, cell_out, reconstruct);
         const int64_t N = mesh.N, F = mesh.F, NT = mesh.NT();
@@ -2677,6 +2721,45 @@ int ibisgb_vjp_geometry_device(ibisgb_ctx* ctx, const double* w_device, double* 
             CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
             CUDA_OK(cudaEventDestroy(ev));
         }
+    });
+}
+
+int ibisgb_jvp_geometry_device(ibisgb_ctx* ctx, const double* dface_device, const double* dcell_device,
+                               double* out_device, int32_t allow_reconstruction, void* stream) {
+    if (!ctx || !dface_device || !dcell_device || !out_device) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        ctx->ensure_device();
+        if (user && user != ctx->stream) {
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+        }
+        ctx->jvp_geometry_rows(dface_device, dcell_device, out_device, allow_reconstruction != 0);
+        if (ev) {
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        }
+    });
+}
+
+int ibisgb_jvp_geometry(ibisgb_ctx* ctx, const double* dface, const double* dcell, double* out,
+                        int32_t allow_reconstruction) {
+    if (!ctx || !dface || !dcell || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_device();
+        const size_t n = ctx->nvars(), nf = 13 * (size_t)ctx->mesh.F, ncl = 4 * (size_t)ctx->mesh.NT();
+        ctx->ensure_krylov(1);
+        ctx->geo_out_face.alloc(sizeof(double) * nf);
+        ctx->geo_out_cell.alloc(sizeof(double) * ncl);
+        CUDA_OK(cudaMemcpyAsync(ctx->geo_out_face.p, dface, sizeof(double) * nf, cudaMemcpyHostToDevice, ctx->stream));
+        CUDA_OK(cudaMemcpyAsync(ctx->geo_out_cell.p, dcell, sizeof(double) * ncl, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->jvp_geometry_rows(ctx->geo_out_face.as<double>(), ctx->geo_out_cell.as<double>(), ctx->kw.as<double>(),
+                               allow_reconstruction != 0);
+        CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
 }
 

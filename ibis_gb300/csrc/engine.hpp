@@ -244,6 +244,16 @@ void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool r
 // least-squares factors are differentiated through the centroids).
 void launch_adjoint_geometry(const DevView& v, const FvParams& p, const double* w, bool reconstruct,
                              const AdjScratch& a, cudaStream_t s);
+// The geometry tangent: out = dR/dgeometry . (dface [13][F], dcell [4][N+G]) at the
+// current state, on dual copies of the geometry (each element 2 doubles).
+struct GeoTangent {
+    void* face;  // [13][F]
+    void* cc;    // [3][N+G]
+    void* vol;   // [N]
+    void* r;     // [6][N] least-squares factors
+};
+void launch_tangent_geometry(const DevView& v, const FvParams& p, const double* dface, const double* dcell,
+                             bool reconstruct, const GeoTangent& g, double* out, cudaStream_t s);
 
 void launch_dt_finalize(StepCtl* ctl, int n_cases, cudaStream_t s);
 void launch_reset_dt(StepCtl* ctl, int n_cases, cudaStream_t s);

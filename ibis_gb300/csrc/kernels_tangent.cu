@@ -6,6 +6,8 @@
 // reference's semantics (dual.cuh), so branch choices, limiter selections and
 // flux splittings follow the real part exactly as in ibis.  Compiled with
 // -fmad=false like the exact real path.
+#include <algorithm>
+
 #include "numerics.cuh"
 #include "dual.cuh"
 
@@ -19,7 +21,8 @@ namespace k_tan {
 // from v, rows of N x nc) and the ghosts they feed: conserved_to_primatives in
 // Dual (primative_conserved_conversion.cpp:4-23) followed by the
 // pre-reconstruction / pre-viscous actions, as compute_dudt applies them.
-template <int DIM>
+// Gm = Dual: the geometry is dual too (the geometry tangent's ghost reflection).
+template <int DIM, class Gm = double>
 __global__ void __launch_bounds__(kBlock) k_tan_prims(DevView v, FvParams prm, const double* vt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
@@ -42,7 +45,70 @@ __global__ void __launch_bounds__(kBlock) k_tan_prims(DevView v, FvParams prm, c
     pr[4 * NT + i] = vx; pr[5 * NT + i] = vy; pr[6 * NT + i] = vz;
     const StateT<Dual> s{rho, p, T, e, vx, vy, vz};
     for (int k = v.feed_off[i]; k < v.feed_off[i + 1]; k++)
-        fill_ghost<Dual, double, Dual>(v, prm, v.feed_ghost[k], s);
+        fill_ghost<Dual, Gm, Dual>(v, prm, v.feed_ghost[k], s);
+}
+
+// ---------------------------------------------------------------------------
+// Geometry tangent: dR/dgeometry . d at the current state, the residual kernels
+// run on dual geometry (the face frame, centres and areas, the centroids --
+// ghosts included -- and volumes, seeded with d) and a state of zero tangent; the
+// least-squares factors are formed again from the dual centroids.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_geo_seed(const double* fg, const double* cc, const double* vol,
+                                                     const double* dface, const double* dcell, int F, int NT, int N,
+                                                     Dual* gface, Dual* gcc, Dual* gvol) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 13LL * F) gface[t] = Dual(fg[t], dface[t]);
+    if (t < 3LL * NT) gcc[t] = Dual(cc[t], dcell[t]);
+    if (t < N) gvol[t] = Dual(vol[t], dcell[3LL * NT + t]);
+}
+
+// WLSGradient::compute_weights (gradient.h:119-162) on the dual centroids, in the
+// mesh builder's form (r11 r12 r22 [r13 r23 r33], one array each)
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_geo_r(DevView v, const Dual* gcc, Dual* gr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    const int N = v.N, NT = v.NT;
+    const Dual xi = gcc[i], yi = gcc[NT + i], zi = DIM == 3 ? gcc[2 * NT + i] : Dual(0.0);
+    Dual sxx(0.0), sxy(0.0), sxz(0.0), syy(0.0), syz(0.0), szz(0.0);
+    for (int s = 0; s < v.nfaces[i]; s++) {
+        const int nb = v.cell_nbr[s * N + i];
+        const Dual dx = gcc[nb] - xi, dy = gcc[NT + nb] - yi, dz = DIM == 3 ? gcc[2 * NT + nb] - zi : Dual(0.0);
+        sxx += dx * dx; sxy += dx * dy; sxz += dx * dz;
+        syy += dy * dy; syz += dy * dz; szz += dz * dz;
+    }
+    const Dual one(1.0);
+    const Dual r11 = dual_sqrt(sxx);
+    const Dual r12 = one / r11 * sxy;
+    const Dual r22 = dual_sqrt(syy - r12 * r12);
+    gr[i] = r11; gr[N + i] = r12; gr[2 * N + i] = r22;
+    if (DIM == 3) {
+        const Dual r13 = one / r11 * sxz;
+        const Dual r23 = one / r22 * (syz - r12 / r11 * sxz);
+        gr[3 * N + i] = r13; gr[4 * N + i] = r23; gr[5 * N + i] = dual_sqrt(szz - (r13 * r13 + r23 * r23));
+    }
+}
+
+// out = -(dual part of dU/dt): the surface integral with dual areas and volumes
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_geo_tan_update(DevView v, const Dual* gface, const Dual* gvol,
+                                                           double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    constexpr int NC = DIM + 2;
+    const int N = v.N, F = v.F;
+    const Dual* fl = (const Dual*)v.flux;
+    Dual acc[NC];
+    const int nf = v.nfaces[i];
+    for (int s = 0; s < nf; s++) {
+        const int f = v.cell_face[s * N + i];
+        const Dual a = -gface[12 * F + f] * Dual((double)v.outsign[s * N + i]);
+#pragma unroll
+        for (int q = 0; q < NC; q++) acc[q] += fl[q * F + f] * a;
+    }
+#pragma unroll
+    for (int q = 0; q < NC; q++) out[(size_t)i * NC + q] = (acc[q] / gvol[i]).du;
 }
 
 // Dual surface integral (flux_surface_integral, finite_volume.cpp:220-255) and
@@ -768,6 +834,34 @@ void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool r
         k_adj_face<2><<<bf, kBlock, 0, s>>>(v, p, w, reconstruct, a);
         k_adj_cell<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a);
         k_adj_final<2><<<bn, kBlock, 0, s>>>(v, p, reconstruct, a, out, ghost_out);
+    }
+}
+
+void launch_tangent_geometry(const DevView& v0, const FvParams& p, const double* dface, const double* dcell,
+                             bool reconstruct, const GeoTangent& g, double* out, cudaStream_t s) {
+    using namespace k_tan;
+    const int F = v0.F, NT = v0.NT, N = v0.N;
+    const long long nseed = std::max<long long>(13LL * F, 3LL * NT);
+    k_geo_seed<<<(unsigned)((nseed + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+        (const double*)v0.face, (const double*)v0.cc, v0.vol, dface, dcell, F, NT, N, (Dual*)g.face, (Dual*)g.cc,
+        (Dual*)g.vol);
+    DevView v = v0;
+    v.face = g.face;
+    v.cc = g.cc;
+    v.r = g.r;
+    const unsigned bn = blocks_for(N), bf = blocks_for(F);
+    if (v.dim == 3) {
+        if (reconstruct || p.viscous) k_geo_r<3><<<bn, kBlock, 0, s>>>(v, (const Dual*)g.cc, (Dual*)g.r);
+        k_tan_prims<3, Dual><<<bn, kBlock, 0, s>>>(v, p, nullptr);
+        if (reconstruct || p.viscous) k_recon<Dual, Dual, Dual, 3, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        k_face<Dual, Dual, Dual, 3, true><<<bf, kBlock, 0, s>>>(v, p, reconstruct);
+        k_geo_tan_update<3><<<bn, kBlock, 0, s>>>(v, (const Dual*)g.face, (const Dual*)g.vol, out);
+    } else {
+        if (reconstruct || p.viscous) k_geo_r<2><<<bn, kBlock, 0, s>>>(v, (const Dual*)g.cc, (Dual*)g.r);
+        k_tan_prims<2, Dual><<<bn, kBlock, 0, s>>>(v, p, nullptr);
+        if (reconstruct || p.viscous) k_recon<Dual, Dual, Dual, 2, true><<<bn, kBlock, 0, s>>>(v, p, reconstruct);
+        k_face<Dual, Dual, Dual, 2, true><<<bf, kBlock, 0, s>>>(v, p, reconstruct);
+        k_geo_tan_update<2><<<bn, kBlock, 0, s>>>(v, (const Dual*)g.face, (const Dual*)g.vol, out);
     }
 }
 

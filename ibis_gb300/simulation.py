@@ -305,6 +305,18 @@ class Simulation:
         out = out.reshape(self.num_cells, self.n_conserved)
         return (out, g) if ghosts else out
 
+    def geometry_tangent(self, dface, dcell, allow_reconstruction: bool = True) -> np.ndarray:
+        """dR/dgeometry . (dface, dcell) (ibisgb_jvp_geometry) for dface (13, F) and
+        dcell (4, N+G) in the layouts of the face / cell geometry dumps; returns
+        (N, n_conserved)."""
+        df = np.ascontiguousarray(dface, np.float64)
+        dc = np.ascontiguousarray(dcell, np.float64)
+        if df.shape != (13, self.num_faces) or dc.shape != (4, self.num_cells + self.num_ghost_cells):
+            raise ValueError("dface must be (13, F) and dcell (4, N+G)")
+        out = np.empty((self.num_cells, self.n_conserved))
+        self._call("ibisgb_jvp_geometry", _ptr(df), _ptr(dc), _ptr(out), int(allow_reconstruction))
+        return out
+
     def geometry_adjoint(self, w, allow_reconstruction: bool = True):
         """w^T dR/dgeometry (ibisgb_vjp_geometry) for w of shape (N, n_conserved):
         (face, cell) with face (13, F) = adjoints of n, t1, t2, face centre, area

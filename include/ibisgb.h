@@ -295,6 +295,18 @@ int ibisgb_vjp_geometry_device(ibisgb_ctx* ctx, const double* w_device, double* 
 int ibisgb_vjp_geometry(ibisgb_ctx* ctx, const double* w, double* face_out, double* cell_out,
                         int32_t allow_reconstruction);
 
+/* The geometry tangent, the transpose of ibisgb_vjp_geometry: out (N x
+ * n_conserved rows) = dR/dgeometry . (dface, dcell) at the current state, with
+ * dface (13 x F) and dcell (4 x (N+G)) in the layouts of dumps 6 and 7 (ghost
+ * volumes ignored).  The residual kernels run on dual copies of the geometry,
+ * the least-squares factors formed again from the dual centroids -- the
+ * reference's Dual<T> seeded in GridBlock<Dual>'s geometry.  Constant-flux
+ * boundaries: IBISGB_ERR_CONFIG. */
+int ibisgb_jvp_geometry_device(ibisgb_ctx* ctx, const double* dface_device, const double* dcell_device,
+                               double* out_device, int32_t allow_reconstruction, void* stream);
+int ibisgb_jvp_geometry(ibisgb_ctx* ctx, const double* dface, const double* dcell, double* out,
+                        int32_t allow_reconstruction);
+
 /* Result of one pseudo-time step of the steady adjoint. */
 typedef struct {
     double residual_norm;   /* |J^T lambda + g| before the step */

@@ -1,4 +1,5 @@
-"""The geometry adjoint (ibisgb_vjp_geometry): w^T dR/dgeometry against the
+"""The geometry adjoint (ibisgb_vjp_geometry) and tangent (ibisgb_jvp_geometry):
+w^T dR/dgeometry and dR/dgeometry . d against the
 oracle's dual-number directional derivative of the residual along a random
 perturbation of the geometry (the reference's Dual seeded in the Grid<Dual>
 face frame, centres, areas, centroids -- ghosts included -- and volumes, the
@@ -58,9 +59,15 @@ def test_geometry_adjoint_is_the_transpose_of_the_dual_geometry_derivative(name,
     rhs = float(np.sum(fb * df) + np.sum(cb * dc))
     mag = float(np.sum(np.abs(w * jd)))
     assert abs(lhs - rhs) <= 1e-12 * mag, (lhs, rhs, mag)
+    # the device's own geometry tangent: equal to the oracle's dual derivative, and
+    # the geometry adjoint its transpose
+    jg = sim.geometry_tangent(df, dc)
+    assert np.abs(jg - jd).max() <= 1e-12 * np.abs(jd).max()
+    lhs_g = float(np.sum(w * jg))
+    assert abs(lhs_g - rhs) <= 1e-12 * mag, (lhs_g, rhs, mag)
 
 
-def test_geometry_adjoint_is_independent_of_the_numbering():
+def test_geometry_tangent_and_adjoint_are_independent_of_the_numbering():
     g, c, st = case("tet")
     out = []
     for mode in ("none", "rcm"):
@@ -70,7 +77,8 @@ def test_geometry_adjoint_is_independent_of_the_numbering():
         sim.set_primitives(*st)
         U = sim.conserved()
         w = np.random.default_rng(2).standard_normal(U.shape) / np.abs(U).mean(axis=0)
-        out.append(sim.geometry_adjoint(w))
+        df, dc = perturbation(sim, np.random.default_rng(5))
+        out.append(sim.geometry_adjoint(w) + (sim.geometry_tangent(df, dc),))
     for a, b in zip(out[0], out[1]):
         assert np.allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(a).max())
 
