@@ -122,3 +122,23 @@ def test_batch_of_renumbered_cases_matches_the_cases_alone():
         assert np.array_equal(s.compute_dudt("f64_exact"), r)
     for s, r in zip(sims, b.split(b.dump("cell_geometry")[:, :b.num_cells].T)):
         assert np.array_equal(s.dump("cell_geometry")[:, :s.num_cells].T, r)
+
+
+def test_driver_writes_the_same_flow_files_when_renumbered(tmp_path):
+    import subprocess
+    from ibis_gb300 import build
+    outs = []
+    for mode in ("auto", "none"):
+        g, c, st = case("tet")
+        c = copy.deepcopy(c)
+        c["grid"]["renumber"] = mode
+        c["solver"] = grids.runge_kutta(max_step=5, plot_every_n_steps=5)
+        d = tmp_path / mode
+        grids.write_case(str(d), g, c, *st)
+        r = subprocess.run([build.DRIVER, "--case", str(d), "--precision", "f64_exact"], capture_output=True,
+                           text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        outs.append({n: (d / "io" / "flow" / "0001" / n).read_bytes() for n in ("T", "p", "vx", "vy", "vz")})
+    g, c, _ = case("tet")
+    assert Simulation(c, g).numbering()["renumbered"]  # "auto" renumbers this grid
+    assert outs[0] == outs[1]
