@@ -1224,9 +1224,10 @@ struct ibisgb_ctx {
         return fused;
     }
 
-    // n steps on the context stream (the local-dt prologue, then one graph per step)
-    void enqueue_rk(int prec, int64_t n, bool fused) {
-        if (!prm.viscous && n > 0) {  // local dt of the current state for the first step
+    // n steps on the context stream (the local-dt prologue unless the caller formed
+    // it already, then one graph per step)
+    void enqueue_rk(int prec, int64_t n, bool fused, bool prologue = true) {
+        if (prologue && !prm.viscous && n > 0) {  // local dt of the current state for the first step
             DevView v = view(prec);
             launch_reset_dt(v.ctl, n_cases, stream);
             ops(prec).local_dt(v, prm, stream);
@@ -1330,17 +1331,18 @@ struct ibisgb_ctx {
             const int b = (int)(j & 1);
             if (j + 1 < n_jobs) upload(j + 1);
             CUDA_OK(cudaStreamWaitEvent(stream, ev_in[b], 0));
-            const double* rows = pipe_in[b].as<double>();
-            if (renumbered()) {
-                map_rows_device(rows, map_a.as<double>(), nc(), true);
-                rows = map_a.as<double>();
-            }
-            launch_rows_to_soa(rows, U.as<double>(), (int)mesh.N, nc(), stream);
+            // the state, its primitives and ghosts and the first step's local dt in one pass
+            DevView v = view(prec);
+            const bool with_dt = !prm.viscous && steps > 0;
+            if (with_dt) launch_reset_dt(v.ctl, n_cases, stream);
+            if (renumbered()) ensure_maps();
+            ops(prec).load_state(v, prm, pipe_in[b].as<double>(),
+                                 renumbered() ? d_cell_to_new.as<int32_t>() : nullptr, with_dt ? 1 : 0, stream);
+            CUDA_OK(cudaGetLastError());
             CUDA_OK(cudaEventRecord(ev_used[b], stream));
             ic_prims.clear();
-            state_changed(-1);
-            ensure_prims(prec);
-            enqueue_rk(prec, steps, fused);
+            state_changed(prec);
+            enqueue_rk(prec, steps, fused, false);
             if (j >= 2) CUDA_OK(cudaStreamWaitEvent(stream, ev_read[b], 0));  // job j-2's read-back is done
             if (renumbered()) {
                 launch_soa_to_rows(U.as<double>(), map_a.as<double>(), (int)mesh.N, nc(), stream);

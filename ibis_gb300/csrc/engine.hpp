@@ -181,6 +181,12 @@ struct KernelOps {
     // the new primitives go to prim_out (not the buffer the view reads)
     void (*cell_update)(const DevView&, const FvParams&, bool reconstruct, int mode, int stage, int with_dt,
                         int variant, void* prim_out, cudaStream_t);
+    // U from N x nc device rows (rows[map[i]] for cell i when map is not null), the
+    // primitives and ghosts from it, and (with_dt) the local time step of the new
+    // state min-reduced into the control blocks: the layout pass, prims_from_U and
+    // local_dt in one kernel
+    void (*load_state)(const DevView&, const FvParams&, const double* rows, const int32_t* map, int with_dt,
+                       cudaStream_t);
 };
 
 KernelOps kernels_f64();

@@ -1558,6 +1558,28 @@ __global__ void __launch_bounds__(kBlock) k_prims_from_U(DevView v, FvParams prm
     commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
 }
 
+// U of valid cell i from its row (row map[i] of the rows when map is set), then
+// what k_prims_from_U and (with_dt) k_local_dt do for it, in one pass.
+template <class P, class Gm, int DIM, bool EXACT>
+__global__ void __launch_bounds__(kBlock) k_load_state(DevView v, FvParams prm, const double* rows, const int32_t* map,
+                                                     int with_dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double local = 1.0e308 * 10.0;
+    if (i < v.N) {
+        constexpr int NC = DIM + 2;
+        const long long r = map ? (long long)map[i] : (long long)i;
+        double u[NC];
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
+            u[q] = rows[r * NC + q];
+            v.U[q * v.N + i] = u[q];
+        }
+        const Committed<P> st = commit_state<P, Gm, DIM, EXACT>(v, prm, i, u);
+        if (with_dt) local = cell_local_dt<P, Gm, DIM>(v, prm, i, st.vx, st.vy, st.vz, st.T);
+    }
+    if (with_dt) reduce_local_dt(v, i, local);
+}
+
 // Local CFL time step of each valid cell, min-reduced into ctl->dt_bits.
 template <class P, class Gm, int DIM>
 __global__ void __launch_bounds__(kBlock) k_local_dt(DevView v, FvParams prm) {
@@ -1686,6 +1708,11 @@ struct Launch {
         if (v.dim == 3) k_prims_from_U<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
         else k_prims_from_U<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
     }
+    static void load_state(const DevView& v, const FvParams& p, const double* rows, const int32_t* map, int with_dt,
+                           cudaStream_t s) {
+        if (v.dim == 3) k_load_state<P, Gm, 3, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, rows, map, with_dt);
+        else k_load_state<P, Gm, 2, EXACT><<<blocks_for(v.N), kBlock, 0, s>>>(v, p, rows, map, with_dt);
+    }
     static void local_dt(const DevView& v, const FvParams& p, cudaStream_t s) {
         if (v.dim == 3) k_local_dt<P, Gm, 3><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
         else k_local_dt<P, Gm, 2><<<blocks_for(v.N), kBlock, 0, s>>>(v, p);
@@ -1696,7 +1723,8 @@ struct Launch {
     }
     static KernelOps ops() {
         return KernelOps{&ghost_fill, &recon, &face_flux, &update, &combine, &prims_from_U, &local_dt,
-                         &finalize, sizeof(P) == sizeof(float) && !EXACT && !kFFBuild ? &cell_update : nullptr};
+                         &finalize, sizeof(P) == sizeof(float) && !EXACT && !kFFBuild ? &cell_update : nullptr,
+                         &load_state};
     }
 };
 

@@ -1,7 +1,8 @@
 """ibisgb_rk_run_host: Runge-Kutta runs between host buffers with the next
-upload and the previous read-back on copy streams.  Every job's output must be
-the same bits as set_conserved + rk_run + get_conserved run one job after the
-other (pinned and pageable buffers, renumbered grids, every precision build)."""
+upload and the previous read-back on copy streams, each job's state, primitives
+and first local time step formed in one pass.  Every job's output must be the
+same bits as set_conserved + rk_run + get_conserved run one job after the other
+(pinned and pageable buffers, renumbered grids, viscous, every precision build)."""
 import copy
 
 import numpy as np
@@ -20,7 +21,8 @@ def states(sim, n, seed):
 
 
 @pytest.mark.parametrize("name,prec,pinned", [("ramp", "mixed", True), ("ramp", "f64_exact", False),
-                                              ("tet", "mixed_ff", True), ("box", "f64", True)])
+                                              ("tet", "mixed_ff", True), ("box", "f64", True),
+                                              ("plate", "mixed", True)])
 def test_pipelined_runs_equal_the_calls_one_by_one(name, prec, pinned):
     torch = pytest.importorskip("torch")
     g, c, st = case(name)
