@@ -82,22 +82,30 @@ def steady_solve(sim: Simulation, tol: float = 1e-10, max_steps: int = 200, prec
 
 
 def solve_adjoint(sim: Simulation, dJdU: np.ndarray, tol: float = 1e-10, cfl0: float = 10.0,
-                  growth: float = 4.0, cfl_max: float = 1e12, max_steps: int = 2000, krylov: int = 100):
+                  growth: float = 4.0, cfl_max: float = 1e12, max_steps: int = 2000, krylov: int = 100,
+                  stall_steps: int = 200):
     """lambda with J_R^T lambda = -dJ/dU at the current state, by the device's
     pseudo-time continuation (the CFL grows geometrically; restarted GMRES of
     `krylov` vectors on the variable-scaled J^T once it is large; 0 keeps the
     steady solver's length) until the scaled residual is below tol of its first
-    value; returns (lambda, history)."""
+    value, or has not fallen by 10% in stall_steps steps (its rounding floor);
+    returns (lambda, history)."""
     import torch
     sim.set_adjoint_krylov(krylov)
     g = torch.tensor(np.ascontiguousarray(dJdU), dtype=torch.float64, device="cuda")
     lam = torch.zeros_like(g)
     cfl, hist, first = cfl0, [], None
-    for _ in range(max_steps):
+    best, best_at = math.inf, 0
+    for k in range(max_steps):
         st = sim.adjoint_step(g, lam, cfl)
         hist.append(st)
-        first = st["scaled_residual_norm"] if first is None else first
-        if st["scaled_residual_norm"] <= tol * first or not np.isfinite(st["scaled_residual_norm"]):
+        r = st["scaled_residual_norm"]
+        first = r if first is None else first
+        if r <= tol * first or not np.isfinite(r):
+            break
+        if r < 0.9 * best:
+            best, best_at = r, k
+        elif k - best_at >= stall_steps:  # no 10% gain in stall_steps steps: at the rounding floor
             break
         cfl = min(cfl * growth, cfl_max)
     torch.cuda.synchronize()

@@ -1358,9 +1358,10 @@ struct ibisgb_ctx {
         }
         CUDA_OK(cudaStreamWaitEvent(stream, ev_read[(n_jobs - 1) & 1], 0));
         CUDA_OK(cudaEventRecord(e1, stream));
-        finish_rk(prec, fused, e0, e1, st);
+        // every copy has completed before the call returns, bad cells or not
         CUDA_OK(cudaStreamSynchronize(pipe_h2d));
         CUDA_OK(cudaStreamSynchronize(pipe_d2h));
+        finish_rk(prec, fused, e0, e1, st);
     }
 
     // ----- tangent (SteadyStateLinearisation::matrix_vector_product) ---------
