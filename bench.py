@@ -616,7 +616,7 @@ def run_ours(args, world, rank, local):
     host_out = torch.empty((N, nc), dtype=torch.float64, pin_memory=True).numpy()
     sim.set_primitives(*ic)
     sim.conserved(out=host_in)
-    e2e_steps = max(3, min(10, args.steps))
+    e2e_steps = max(3, args.steps)  # as many steps as the device-timed headline
     for _ in range(2):
         sim.set_conserved(host_in)
         sim.take_steps(1, "mixed")
