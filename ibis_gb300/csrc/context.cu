@@ -1439,7 +1439,6 @@ struct ibisgb_ctx {
     DBuf geo_fcb, geo_vb, geo_nbc, geo_ceb;
     void vjp_geometry(const double* w_dev, double* face_out, double* cell_out, bool reconstruct) {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
-        if (prm.cflux) throw ConfigError("the geometry adjoint covers residuals without constant-flux boundaries");
         DevView v = tangent_view();
         ensure_adjoint();
         const int64_t N = mesh.N, F = mesh.F, MF = mesh.MF;
@@ -1462,7 +1461,6 @@ struct ibisgb_ctx {
     DBuf gt_face, gt_cc, gt_vol, gt_r;
     void jvp_geometry(const double* dface, const double* dcell, double* out, bool reconstruct) {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
-        if (prm.cflux) throw ConfigError("the geometry tangent covers residuals without constant-flux boundaries");
         DevView v = tangent_view();
         const int64_t N = mesh.N, F = mesh.F, NT = mesh.NT();
         const size_t D = 2 * sizeof(double);

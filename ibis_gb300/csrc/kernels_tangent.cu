@@ -282,6 +282,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
             DualA Fd[5];
             convective_flux<DualA, DIM, true>(prm, gm, S[0], S[1], gd[0], gd[1], gd[2], gd[3], gd[4], gd[5], gd[6],
                                               gd[7], gd[8], Fd);
+            if (prm.cflux)  // a constant-flux face: the fixed state's flux through the face's normal
+                if (const BoundDev* B = constant_flux_bound(v, cells[0], cells[1]))
+                    constant_flux<DualA, DIM>(B->cfs, prm.Cv, gd[0], gd[1], gd[2], Fd);
             double acc = 0.0;
             for (int q = 0; q < 5; q++) acc += fb[q] * Fd[q].du;
             gbar[j] = acc;

@@ -288,8 +288,9 @@ int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out,
  * offset of the face gradient (viscous_flux.cpp:36-80) and the viscous least
  * squares.  The boundary-layer profile's ghost states are taken as fixed (their
  * dependence on the ghost centroid's height is not differentiated).  2-D grids
- * have no n_z, t1_z, t2_x, t2_y inputs (rows 0).  Constant-flux boundaries:
- * IBISGB_ERR_CONFIG.  No counterpart in the reference. */
+ * have no n_z, t1_z, t2_x, t2_y inputs (rows 0).  A constant-flux face's flux
+ * depends on the geometry through its normal only.  No counterpart in the
+ * reference. */
 int ibisgb_vjp_geometry_device(ibisgb_ctx* ctx, const double* w_device, double* face_out_device,
                                double* cell_out_device, int32_t allow_reconstruction, void* stream);
 int ibisgb_vjp_geometry(ibisgb_ctx* ctx, const double* w, double* face_out, double* cell_out,
@@ -300,8 +301,7 @@ int ibisgb_vjp_geometry(ibisgb_ctx* ctx, const double* w, double* face_out, doub
  * dface (13 x F) and dcell (4 x (N+G)) in the layouts of dumps 6 and 7 (ghost
  * volumes ignored).  The residual kernels run on dual copies of the geometry,
  * the least-squares factors formed again from the dual centroids -- the
- * reference's Dual<T> seeded in GridBlock<Dual>'s geometry.  Constant-flux
- * boundaries: IBISGB_ERR_CONFIG. */
+ * reference's Dual<T> seeded in GridBlock<Dual>'s geometry. */
 int ibisgb_jvp_geometry_device(ibisgb_ctx* ctx, const double* dface_device, const double* dcell_device,
                                double* out_device, int32_t allow_reconstruction, void* stream);
 int ibisgb_jvp_geometry(ibisgb_ctx* ctx, const double* dface, const double* dcell, double* out,

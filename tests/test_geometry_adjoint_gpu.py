@@ -7,8 +7,8 @@ least-squares factors recomputed from the dual centroids): the dot-product test
 <w, dR/dgeom . d> = <J_geom^T w, d> to 1e-12, on second-order (Barth-Jespersen
 and unlimited) and first-order residuals, inviscid and viscous (the flat
 plate's no-slip wall, subsonic in/outflow with a fixed-temperature wall), 2-D
-and 3-D, every element type, slip walls, supersonic in/out and periodic
-boundaries; and the same result with the grid renumbered internally."""
+and 3-D, every element type, slip walls, supersonic in/out, constant-flux and
+periodic boundaries; and the same result with the grid renumbered internally."""
 import copy
 
 import numpy as np
@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 CASES = [("ramp", {}), ("ramp", {"limiter": "unlimited"}), ("ramp", {"order": 1}), ("ramp", {"flux": "ausmdv"}),
          ("ramp", {"flux": "rusanov"}), ("ramp", {"thermo": "rho_p"}), ("tri", {}), ("tiny2d", {}),
          ("box", {}), ("box_inout", {}), ("tet", {}), ("wedge", {}), ("pyramid", {}),
-         ("plate", {}), ("plate", {"order": 1}), ("subsonic", {})]
+         ("plate", {}), ("plate", {"order": 1}), ("subsonic", {}), ("cflux_ramp", {}), ("cflux_box", {})]
 IDS = ["-".join([n] + [f"{k}={v}" for k, v in kw.items()]) for n, kw in CASES]
 UNREAD_2D = [2, 5, 6, 7, 11]  # n_z, t1_z, t2_x, t2_y, centre z: not inputs of a 2-D residual
 
@@ -81,11 +81,3 @@ def test_geometry_tangent_and_adjoint_are_independent_of_the_numbering():
         out.append(sim.geometry_adjoint(w) + (sim.geometry_tangent(df, dc),))
     for a, b in zip(out[0], out[1]):
         assert np.allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(a).max())
-
-
-def test_constant_flux_boundaries_are_refused():
-    g, c, st = case("cflux_ramp")
-    sim = Simulation(c, g)
-    sim.set_primitives(*st)
-    with pytest.raises(Exception, match="constant-flux"):
-        sim.geometry_adjoint(np.zeros((sim.num_cells, sim.n_conserved)))
