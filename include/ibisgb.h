@@ -286,8 +286,9 @@ int ibisgb_vjp(ibisgb_ctx* ctx, const double* w, double* out, double* ghost_out,
  * the centroids (ghosts included) through the least-squares factors
  * (gradient.h:89-162), and in viscous residuals the normal and the centroid
  * offset of the face gradient (viscous_flux.cpp:36-80) and the viscous least
- * squares.  The boundary-layer profile's ghost states are taken as fixed (their
- * dependence on the ghost centroid's height is not differentiated).  2-D grids
+ * squares.  The boundary-layer profile is evaluated at the ghost centroid's real
+ * height, as the reference's spline (cubic_spline.cpp, on doubles) does under its
+ * dual type, so it carries no geometry derivative.  2-D grids
  * have no n_z, t1_z, t2_x, t2_y inputs (rows 0).  A constant-flux face's flux
  * depends on the geometry through its normal only.  No counterpart in the
  * reference. */

@@ -23,7 +23,8 @@ pytestmark = pytest.mark.gpu
 CASES = [("ramp", {}), ("ramp", {"limiter": "unlimited"}), ("ramp", {"order": 1}), ("ramp", {"flux": "ausmdv"}),
          ("ramp", {"flux": "rusanov"}), ("ramp", {"thermo": "rho_p"}), ("tri", {}), ("tiny2d", {}),
          ("box", {}), ("box_inout", {}), ("tet", {}), ("wedge", {}), ("pyramid", {}),
-         ("plate", {}), ("plate", {"order": 1}), ("subsonic", {}), ("cflux_ramp", {}), ("cflux_box", {})]
+         ("plate", {}), ("plate", {"order": 1}), ("subsonic", {}), ("bl_plate", {}), ("cflux_ramp", {}),
+         ("cflux_box", {})]
 IDS = ["-".join([n] + [f"{k}={v}" for k, v in kw.items()]) for n, kw in CASES]
 UNREAD_2D = [2, 5, 6, 7, 11]  # n_z, t1_z, t2_x, t2_y, centre z: not inputs of a 2-D residual
 
