@@ -80,7 +80,7 @@ IBISGB_HD int visc_prim(int q) { return q == 0 ? 2 : 3 + q; }
 // subnormal floats; doubles outside the normal float range, infinities, NaN --
 // take the instruction, in a function that is called, not inlined, so that no
 // predicated conversion is issued for the common case.  Results are bit for bit
-// the instructions' under this build's flags (checked by ibisgb_check_conversions).
+// the instructions' under the translation unit's compiler flags (checked by ibisgb_check_conversions).
 __device__ __noinline__ double f2d_by_instruction(float x) { return (double)x; }
 __device__ __noinline__ float d2f_by_instruction(double x) { return __double2float_rn(x); }
 
