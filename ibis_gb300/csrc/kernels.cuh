@@ -1068,30 +1068,26 @@ __device__ Committed<P> commit_state(const DevView& v, const FvParams& prm, int 
         return Committed<P>{rho, (P)hs[2], (P)hs[4], (P)hs[5], (P)hs[6]};
     }
     if (!EXACT && sizeof(P) == sizeof(float)) {
-        // Mixed build: rho, v and e = E/rho - |v|^2/2 in float-float on the FP32 pipe
-        // (~48-bit significands: the cancellation of strong expansions keeps 24 bits
-        // more than the float primitives it is rounded to), the conserved values split
-        // on the integer pipe; T = e/Cv and p = rho R T are products of values already
-        // rounded to float, so they are formed in float.  No FP64 operation for
-        // interior cells.
-        const FF rho2 = d2ff(rho);
-        const FF ir = FF(1.f) / rho2;  // a state with rho <= 0 is a bad cell either way
-        const FF vx2 = d2ff(u[1]) * ir, vy2 = d2ff(u[2]) * ir;
-        const FF vz2 = DIM == 3 ? d2ff(u[3]) * ir : FF(0.f);
-        const FF ke2 = (vx2 * vx2 + vy2 * vy2 + vz2 * vz2) * 0.5f;
-        const FF e2 = d2ff(u[DIM + 1]) * ir - ke2;
-        const float rf = rho2.hi, ef = e2.hi;
+        // Mixed build: rho, v and e = E/rho - |v|^2/2 in double (the cancellation of
+        // strong expansions happens there); T = e/Cv and p = rho R T are products of
+        // values already rounded to float, so they are formed in float.
+        const double ir = recip_newton1_fseed(rho);  // a state with rho <= 0 is a bad cell either way
+        vx = u[1] * ir;
+        vy = u[2] * ir;
+        vz = DIM == 3 ? u[3] * ir : 0.0;
+        double ke = 0.5 * (vx * vx + vy * vy + vz * vz);
+        e = u[DIM + 1] * ir - ke;
+        const float rf = d2f(rho), ef = d2f(e);
         const float Tf = ef * prm.finv_Cv;
         const float pf = rf * prm.fR * Tf;
-        const float vxf = vx2.hi, vyf = vy2.hi, vzf = DIM == 3 ? vz2.hi : 0.f;
+        const float vxf = d2f(vx), vyf = d2f(vy), vzf = DIM == 3 ? d2f(vz) : 0.f;
         P* pr = (P*)v.prim;
         const int NT = v.NT;
         pr[i] = (P)rf; pr[NT + i] = (P)pf; pr[2 * NT + i] = (P)Tf; pr[3 * NT + i] = (P)ef;
         pr[4 * NT + i] = (P)vxf; pr[5 * NT + i] = (P)vyf; pr[6 * NT + i] = (P)vzf;
         const int k0 = v.feed_off[i], k1 = v.feed_off[i + 1];
         if (k0 < k1) {  // boundary cells: the ghost actions work on the double state
-            const State64 s{rho, f2d(pf), f2d(Tf), ff_to_double(e2), ff_to_double(vx2), ff_to_double(vy2),
-                            ff_to_double(vz2)};
+            const State64 s{rho, f2d(pf), f2d(Tf), e, vx, vy, vz};
             for (int k = k0; k < k1; k++) fill_ghost<P, Gm>(v, prm, v.feed_ghost[k], s);
         }
         return Committed<P>{rho, (P)Tf, (P)vxf, (P)vyf, (P)vzf};
