@@ -273,8 +273,9 @@ def batch_measure(args, barrier):
     # path without fused multiply-adds shows how far rounding alone moves a case
     acc = None
     if args.batch_accuracy_steps > 0:
+        from ibis_gb300.adjoint import _force, _wall_faces
         n_acc = args.batch_accuracy_steps
-        rho_acc, rate_acc = {}, {}
+        rho_acc, p_acc, U_acc, rate_acc = {}, {}, {}, {}
         for prec in ("f64", "f64_exact", "mixed", "mixed_ff"):
             batch.set_primitives(*ic_all)
             if prec == "mixed_ff":
@@ -282,11 +283,28 @@ def batch_measure(args, barrier):
                 batch.set_primitives(*ic_all)
             sa = batch.take_steps(n_acc, prec)
             rate_acc[prec] = cells * 3.0 * n_acc / (sa["device_ms"] / 1e3) / 1e6
-            rho_acc[prec] = batch.split(batch.conserved()[:, 0].copy())
-        acc = {"steps": n_acc, "batched_rate": rate_acc}
+            U_all = batch.conserved()
+            rho_acc[prec] = batch.split(U_all[:, 0].copy())
+            p_acc[prec] = batch.split(batch.primitives()["p"].copy())
+            U_acc[prec] = batch.split(U_all)
+        # the integrated pressure force on each case's ramp wall (x >= 0.2), from its state
+        walls = [(_wall_faces(sm, "wall"), sm.dump("face_geometry")) for sm in sims]
+
+        def force(prec, j):
+            (faces, wcells), fg = walls[j]
+            return float(_force(sims[j], U_acc[prec][j], fg, faces, wcells, 0.2, 1)[0])
+        acc = {"steps": n_acc, "batched_rate": rate_acc,
+               "errors": "relative to the FP64 build, per case: L2 and max of density and pressure, and the "
+                         "integrated ramp-wall pressure force"}
         for prec in ("f64_exact", "mixed", "mixed_ff"):
             e = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(rho_acc[prec], rho_acc["f64"])]
-            acc[prec] = {"max": max(e), "median": float(np.median(e)), "cases_above_1e-6": int(sum(x > 1e-6 for x in e))}
+            em = [float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(rho_acc[prec], rho_acc["f64"])]
+            ep = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(p_acc[prec], p_acc["f64"])]
+            epm = [float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(p_acc[prec], p_acc["f64"])]
+            ef = [abs(force(prec, j) - force("f64", j)) / abs(force("f64", j)) for j in range(len(sims))]
+            acc[prec] = {"max": max(e), "median": float(np.median(e)), "cases_above_1e-6": int(sum(x > 1e-6 for x in e)),
+                         "rho_max_err_max": max(em), "p_l2_err_max": max(ep), "p_max_err_max": max(epm),
+                         "wall_force_err_max": max(ef), "wall_force_err_median": float(np.median(ef))}
 
     # sequential: one case at a time, each with its own context and graph
     for s, ic in zip(sims, ics):
@@ -579,6 +597,7 @@ def run_ours(args, world, rank, local):
         barrier()
     ms_mixed = max_over_ranks_(st["device_ms"])
     rho_mixed = sim.conserved()[:, 0].copy()
+    p_mixed = sim.primitives()["p"].copy()
     value = whole_job_rate(N, world, 3, args.steps, ms_mixed / 1e3)
 
     # --- plain FP64 path over the same steps from the same state, and its accuracy reference
@@ -590,9 +609,12 @@ def run_ours(args, world, rank, local):
     barrier()
     ms_f64 = max_over_ranks_(st64["device_ms"])
     rho_f64 = sim.conserved()[:, 0]
+    p_f64 = sim.primitives()["p"]
     value_f64 = whole_job_rate(N, world, 3, args.steps, ms_f64 / 1e3)
     l2_err = float(np.linalg.norm(rho_mixed - rho_f64) / np.linalg.norm(rho_f64))
     max_err = float(np.abs(rho_mixed - rho_f64).max() / np.abs(rho_f64).max())
+    p_l2_err = float(np.linalg.norm(p_mixed - p_f64) / np.linalg.norm(p_f64))
+    p_max_err = float(np.abs(p_mixed - p_f64).max() / np.abs(p_f64).max())
 
     # --- the float-float path (MIXED_FF) over the same steps from the same state
     sim.set_primitives(*ic)
@@ -685,6 +707,7 @@ def run_ours(args, world, rank, local):
                     "mixed_speedup": value / value_f64,
                     "fp64_roofline": fp64_roofline(value_f64, n, clk.summary()["sm_mhz"] or 2070.0)},
             "accuracy": {"rho_rel_l2_err_mixed_vs_f64": l2_err, "rho_rel_max_err_mixed_vs_f64": max_err,
+                         "p_rel_l2_err_mixed_vs_f64": p_l2_err, "p_rel_max_err_mixed_vs_f64": p_max_err,
                          "steps": args.warmup + args.steps},
             "mixed_ff": {"value": value_ff, "ms_per_step": ms_ff / args.steps, "speedup_vs_f64": value_ff / value_f64,
                          "rho_rel_l2_err_vs_f64": l2_err_ff, "autotune": tune_ff["variants"],
