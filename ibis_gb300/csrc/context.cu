@@ -314,6 +314,7 @@ struct ibisgb_ctx {
             prm.logamma = lo(prm.gamma, prm.fgamma); prm.logR = lo(prm.gamma * prm.R, prm.fgR);
             prm.lodelta = lo(prm.delta, prm.fdelta); prm.lomu0 = lo(prm.mu0, prm.fmu0);
             prm.loT0 = lo(prm.T0, prm.fT0); prm.loTs = lo(prm.Ts, prm.fTs); prm.loPr = lo(prm.Pr, prm.fPr);
+            prm.loinv_Cv = lo(prm.inv_Cv, prm.finv_Cv);
             const Json& solver = config.at("solver");
             if (solver.at("name").as_string() == "runge_kutta") parse_rk(solver);
             if (solver.at("name").as_string() == "steady_state") parse_steady(solver);

@@ -64,7 +64,7 @@ struct FvParams {
     float fR, fCv, fCp, fgamma, fgR, feps, fdelta, fmu0, fT0, fTs, fPr, finv_Cv;
     // what the float copies leave out (the double minus its float copy, rounded to
     // float): float-float kernels take each constant as the pair (f*, lo*)
-    float loR, loCv, loCp, logamma, logR, lodelta, lomu0, loT0, loTs, loPr;
+    float loR, loCv, loCp, logamma, logR, lodelta, lomu0, loT0, loTs, loPr, loinv_Cv;
     double inv_Cv;
 };
 

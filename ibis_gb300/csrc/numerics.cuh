@@ -5,6 +5,8 @@
 // FMA contraction reproduces ibis bit for bit.
 #pragma once
 
+#include <type_traits>
+
 #include <cuda_runtime.h>
 
 #include "engine.hpp"
@@ -63,9 +65,11 @@ template <> IBISGB_HD FF par<FF>(double, float f, float lo) { return FF(f, lo); 
 template <class R>
 struct Gas {
     R R_, Cv, Cp, gamma, gR;  // gR = gamma * R, as in speed_of_sound_ (gas_model.h:27-30)
+    R iCv;                    // 1 / Cv: the float-float build multiplies by it instead of dividing
     IBISGB_HD explicit Gas(const FvParams& p)
         : R_(par<R>(p.R, p.fR, p.loR)), Cv(par<R>(p.Cv, p.fCv, p.loCv)), Cp(par<R>(p.Cp, p.fCp, p.loCp)),
-          gamma(par<R>(p.gamma, p.fgamma, p.logamma)), gR(par<R>(p.gamma * p.R, p.fgR, p.logR)) {}
+          gamma(par<R>(p.gamma, p.fgamma, p.logamma)), gR(par<R>(p.gamma * p.R, p.fgR, p.logR)),
+          iCv(par<R>(p.inv_Cv, p.finv_Cv, p.loinv_Cv)) {}
     IBISGB_HD R sound(R T) const { return d_sqrt<R>(gR * T); }
 };
 
@@ -91,16 +95,28 @@ IBISGB_HD void flux_hanel(const FaceSide<R>& L, const FaceSide<R>& Rt, const Gas
     R HR = eR + pRrR + keR;
     R pLplus, uLplus;
     if (d_abs(uL) <= aL) {
-        uLplus = R(1.0) / (R(4.0) * aL) * (uL + aL) * (uL + aL);
-        pLplus = pL * uLplus * (R(1.0) / aL * (R(2.0) - uL / aL));
+        if constexpr (std::is_same<R, FF>::value) {  // one reciprocal of a for its three uses
+            const R ia = R(1.f) / aL;
+            uLplus = ia * 0.25f * (uL + aL) * (uL + aL);
+            pLplus = pL * uLplus * (ia * (R(2.0) - uL * ia));
+        } else {
+            uLplus = R(1.0) / (R(4.0) * aL) * (uL + aL) * (uL + aL);
+            pLplus = pL * uLplus * (R(1.0) / aL * (R(2.0) - uL / aL));
+        }
     } else {
         uLplus = R(0.5) * (uL + d_abs(uL));
         pLplus = pL * uLplus * (R(1.0) / uL);
     }
     R pRminus, uRminus;
     if (d_abs(uR) <= aR) {
-        uRminus = R(-1.0) / (R(4.0) * aR) * (uR - aR) * (uR - aR);
-        pRminus = pR * uRminus * (R(1.0) / aR * (R(-2.0) - uR / aR));
+        if constexpr (std::is_same<R, FF>::value) {
+            const R ia = R(1.f) / aR;
+            uRminus = -(ia * 0.25f * (uR - aR) * (uR - aR));
+            pRminus = pR * uRminus * (ia * (R(-2.0) - uR * ia));
+        } else {
+            uRminus = R(-1.0) / (R(4.0) * aR) * (uR - aR) * (uR - aR);
+            pRminus = pR * uRminus * (R(1.0) / aR * (R(-2.0) - uR / aR));
+        }
     } else {
         uRminus = R(0.5) * (uR - d_abs(uR));
         pRminus = pR * uRminus * (R(1.0) / uR);
@@ -250,7 +266,11 @@ template <class R>
 IBISGB_HD void thermo_close(int kind, const Gas<R>& gm, R& rho, R& p, R& T, R& e) {
     switch (kind) {
         case kRhoP: T = p / (rho * gm.R_); e = gm.Cv * T; break;
-        case kRhoU: T = e / gm.Cv; p = rho * gm.R_ * T; break;
+        case kRhoU:
+            if constexpr (std::is_same<R, FF>::value) T = e * gm.iCv;
+            else T = e / gm.Cv;
+            p = rho * gm.R_ * T;
+            break;
         case kRhoT: p = rho * gm.R_ * T; e = gm.Cv * T; break;
         default: rho = p / (gm.R_ * T); e = gm.Cv * T; break;  // p_T
     }
