@@ -84,6 +84,7 @@ def load(build_if_missing: bool = True):
     L.ibisgb_rk_run.argtypes = [_P, C.c_int32, C.c_int64, C.POINTER(RkStatus)]
     L.ibisgb_l2_norms.argtypes = [_P, _P]
     L.ibisgb_get_dump.argtypes = [_P, C.c_int32, _P, C.c_int64]
+    L.ibisgb_set_geometry.argtypes = [_P, _P, _P]
     L.ibisgb_numbering.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.ibisgb_synchronize.argtypes = [_P]
     L.ibisgb_set_conserved.argtypes = [_P, _P]

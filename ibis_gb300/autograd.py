@@ -62,6 +62,66 @@ def residual(sim, U):
     return Residual.apply(U, sim)
 
 
+class ResidualGeometry(torch.autograd.Function):
+    """R(U, face, cell): the residual as a function of the state and of the grid
+    geometry arrays (face: 13 x F normal, tangents, centre, area; cell: 4 x (N+G)
+    centroid, volume -- the layouts of the geometry dumps).  The forward pass
+    installs the geometry (ibisgb_set_geometry, which forms the least-squares
+    factors again); the backward pass is the state and geometry adjoints
+    (ibisgb_vjp / ibisgb_vjp_geometry), forward mode the tangents."""
+
+    @staticmethod
+    def forward(ctx, U, face, cell, sim):
+        for t, name in ((U, "U"), (face, "face"), (cell, "cell")):
+            if t.dtype != torch.float64 or not t.is_cuda:
+                raise TypeError(f"{name} must be a float64 CUDA tensor")
+        sim.set_geometry(face.detach().cpu().numpy(), cell.detach().cpu().numpy())
+        U = U.contiguous()
+        _py.set_conserved(sim, U)
+        out = torch.empty_like(U)
+        _py.residual(sim, _F64_EXACT, out)
+        ctx.sim = sim
+        ctx.save_for_backward(U, face, cell)
+        ctx.save_for_forward(U, face, cell)
+        return out
+
+    @staticmethod
+    def _linearise(ctx):
+        U, face, cell = ctx.saved_tensors
+        ctx.sim.set_geometry(face.detach().cpu().numpy(), cell.detach().cpu().numpy())
+        _py.set_conserved(ctx.sim, U)
+        return U, face, cell
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        U, face, cell = ResidualGeometry._linearise(ctx)
+        w = grad_out.contiguous()
+        gU = torch.empty_like(U)
+        _py.vjp(ctx.sim, w, gU)
+        gf, gc = torch.empty_like(face), torch.empty_like(cell)
+        _py.vjp_geometry(ctx.sim, w, gf, gc)
+        return gU, gf, gc, None
+
+    @staticmethod
+    def jvp(ctx, dU, dface, dcell, _):
+        U, face, cell = ResidualGeometry._linearise(ctx)
+        out = torch.zeros_like(U)
+        if dU is not None:
+            _py.jvp(ctx.sim, dU.contiguous(), out, 0.0)
+            out = -out  # the product is inv_dt v - J v
+        if dface is not None or dcell is not None:
+            g = torch.empty_like(U)
+            _py.jvp_geometry(ctx.sim, (dface if dface is not None else torch.zeros_like(face)).contiguous(),
+                             (dcell if dcell is not None else torch.zeros_like(cell)).contiguous(), g)
+            out = out + g
+        return out
+
+
+def residual_geometry(sim, U, face, cell):
+    """dU/dt of `sim` at state U on the geometry (face, cell), differentiable in all three."""
+    return ResidualGeometry.apply(U, face, cell, sim)
+
+
 def _tableau(sim):
     """The Butcher tableau of the config's Runge-Kutta block: a (strictly lower), b."""
     bt = sim.config["solver"]["butcher_tableau"]

@@ -724,18 +724,7 @@ struct ibisgb_ctx {
         std::vector<int> cur(off.begin(), off.end() - 1);
         for (int64_t g = 0; g < G; g++) fg[cur[gs[g]]++] = (int)g;
         upload(feed_off, off, stream); upload(feed_ghost, fg, stream);
-        std::vector<double> v(mesh.volume.begin(), mesh.volume.begin() + N);
-        upload(vol, v, stream);
-        for (auto& x : v) x = 1.0 / x;
-        upload(inv_vol, v, stream);
-        {  // 1/volume as two floats whose sum is it to ~2^-48 (the mixed build's residual scaling)
-            std::vector<float> p(2 * (size_t)N);
-            for (int64_t c = 0; c < N; c++) {
-                p[2 * c] = (float)v[c];
-                p[2 * c + 1] = (float)(v[c] - (double)p[2 * c]);
-            }
-            upload(inv_vol2, p, stream);
-        }
+        upload_volumes();
         U.alloc(sizeof(double) * nc() * N);
         k.alloc(sizeof(double) * nc() * N * stages());
         vsig.alloc(sizeof(double) * F);
@@ -749,6 +738,49 @@ struct ibisgb_ctx {
         }
         l2.alloc(sizeof(double) * (6 + 6 * 304));
         CUDA_OK(cudaStreamSynchronize(stream));
+    }
+
+    void upload_volumes() {
+        const int64_t N = mesh.N;
+        std::vector<double> v(mesh.volume.begin(), mesh.volume.begin() + N);
+        upload(vol, v, stream);
+        for (auto& x : v) x = 1.0 / x;
+        upload(inv_vol, v, stream);
+        // 1/volume as two floats whose sum is it to ~2^-48 (the mixed build's residual scaling)
+        std::vector<float> p(2 * (size_t)N);
+        for (int64_t c = 0; c < N; c++) {
+            p[2 * c] = (float)v[c];
+            p[2 * c + 1] = (float)(v[c] - (double)p[2 * c]);
+        }
+        upload(inv_vol2, p, stream);
+        CUDA_OK(cudaStreamSynchronize(stream));
+    }
+
+    // Replaces the grid geometry (face rows 13 x F: n, t1, t2, centre, area; cell
+    // rows 4 x (N+G): centroid, volume; the layouts of dumps 6 and 7, reference
+    // numbering) and forms the least-squares factors again from the centroids.
+    // The connectivity and the boundary-layer profile's ghost states stay; the
+    // structured-block stages, which hold their own lattice geometry, are switched off.
+    void set_geometry(const double* face, const double* cell) {
+        if (n_cases > 1) throw StateError("a batch's geometry belongs to its cases");
+        const int64_t N = mesh.N, F = mesh.F, NT = mesh.NT();
+        std::vector<double>* fa[13] = {&mesh.nx, &mesh.ny, &mesh.nz, &mesh.t1x, &mesh.t1y, &mesh.t1z,
+                                       &mesh.t2x, &mesh.t2y, &mesh.t2z, &mesh.fcx, &mesh.fcy, &mesh.fcz, &mesh.area};
+        std::vector<double>* ca[4] = {&mesh.ccx, &mesh.ccy, &mesh.ccz, &mesh.volume};
+        for (int q = 0; q < 13; q++)
+            for (int64_t f = 0; f < F; f++) (*fa[q])[f] = face[q * F + (renumbered() ? num.face_ref_of_new[f] : f)];
+        for (int q = 0; q < 4; q++)
+            for (int64_t c = 0; c < NT; c++) {
+                if (q == 3 && c >= N) continue;  // ghost volumes are not inputs
+                (*ca[q])[c] = cell[q * NT + (c < N ? cell_id_to_ref(c) : c)];
+            }
+        if (!mesh.r.empty()) compute_lsq(mesh);
+        s64.geometry = s32.geometry = sff.geometry = false;
+        s64.prims_current = s32.prims_current = sff.prims_current = false;
+        fused_elig = march_elig = 0;
+        fused_on = false;
+        fused_why = march_why = "the geometry was replaced (ibisgb_set_geometry)";
+        if (uploaded) upload_volumes();
     }
 
     template <class Gm>
@@ -2619,6 +2651,11 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
             default: std::memcpy(buf, raw.data(), raw.size());  // 12: per ghost, ghost ids are not renumbered
         }
     });
+}
+
+int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell) {
+    if (!ctx || !face || !cell) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->set_geometry(face, cell); });
 }
 
 int ibisgb_numbering(const ibisgb_ctx* ctx, int32_t* renumbered, int64_t* bandwidth_reference,

@@ -463,48 +463,55 @@ void build_mesh(const GridInput& in, const std::vector<BoundarySpec>& bounds_in,
     }
 
     // --- least-squares QR factors (gradient.h:119-162)
-    if (need_lsq) {
-        m.r.assign(N * 6, 0.0);
+    if (need_lsq) compute_lsq(m);
+}
+
+// WLSGradient::compute_weights and the per-neighbour weights of compute_gradients
+// (gradient.h:89-162) from the centroids: the r factors per valid cell and the
+// weights per neighbour slot.
+void compute_lsq(Mesh& m) {
+    const int64_t N = m.N;
+    const int MF = m.MF;
+    m.r.assign(N * 6, 0.0);
 #pragma omp parallel for schedule(static)
-        for (int64_t c = 0; c < N; c++) {
-            double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0, szz = 0.0;
-            double xi = m.ccx[c], yi = m.ccy[c], zi = m.ccz[c];
-            for (int k = 0; k < m.nfaces[c]; k++) {
-                int64_t nb = m.cell_nbr[c * MF + k];
-                double dx = m.ccx[nb] - xi, dy = m.ccy[nb] - yi, dz = m.ccz[nb] - zi;
-                sxx += dx * dx; sxy += dx * dy; sxz += dx * dz;
-                syy += dy * dy; syz += dy * dz; szz += dz * dz;
-            }
-            double r11 = std::sqrt(sxx);
-            double r12 = 1.0 / r11 * sxy;
-            double r22 = std::sqrt(syy - r12 * r12);
-            double r13 = 1.0 / r11 * sxz;
-            double r23 = 1.0 / r22 * (syz - r12 / r11 * sxz);
-            double r33 = std::sqrt(szz - (r13 * r13 + r23 * r23));
-            double* rr = &m.r[c * 6];
-            rr[0] = r11; rr[1] = r12; rr[2] = r22;
-            if (m.dim == 3) { rr[3] = r13; rr[4] = r23; rr[5] = r33; }
+    for (int64_t c = 0; c < N; c++) {
+        double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0, szz = 0.0;
+        double xi = m.ccx[c], yi = m.ccy[c], zi = m.ccz[c];
+        for (int k = 0; k < m.nfaces[c]; k++) {
+            int64_t nb = m.cell_nbr[c * MF + k];
+            double dx = m.ccx[nb] - xi, dy = m.ccy[nb] - yi, dz = m.ccz[nb] - zi;
+            sxx += dx * dx; sxy += dx * dy; sxz += dx * dz;
+            syy += dy * dy; syz += dy * dz; szz += dz * dz;
         }
-        // the weights WLSGradient::compute_gradients applies to each neighbour
-        // difference (gradient.h:89-107), stored per neighbour slot
-        m.lsqw.assign(3 * (size_t)MF * N, 0.0);
+        double r11 = std::sqrt(sxx);
+        double r12 = 1.0 / r11 * sxy;
+        double r22 = std::sqrt(syy - r12 * r12);
+        double r13 = 1.0 / r11 * sxz;
+        double r23 = 1.0 / r22 * (syz - r12 / r11 * sxz);
+        double r33 = std::sqrt(szz - (r13 * r13 + r23 * r23));
+        double* rr = &m.r[c * 6];
+        rr[0] = r11; rr[1] = r12; rr[2] = r22;
+        if (m.dim == 3) { rr[3] = r13; rr[4] = r23; rr[5] = r33; }
+    }
+    // the weights WLSGradient::compute_gradients applies to each neighbour
+    // difference (gradient.h:89-107), stored per neighbour slot
+    m.lsqw.assign(3 * (size_t)MF * N, 0.0);
 #pragma omp parallel for schedule(static)
-        for (int64_t c = 0; c < N; c++) {
-            const double* rr = &m.r[c * 6];
-            double r11 = rr[0], r12 = rr[1], r22 = rr[2], r13 = 0.0, r23 = 0.0, r33 = 0.0;
-            if (m.dim == 3) { r13 = rr[3]; r23 = rr[4]; r33 = rr[5]; }
-            double beta = (r12 * r23 - r13 * r23) / (r11 * r22);
-            for (int k = 0; k < m.nfaces[c]; k++) {
-                int64_t nb = m.cell_nbr[c * MF + k];
-                double dx = m.ccx[nb] - m.ccx[c], dy = m.ccy[nb] - m.ccy[c], dz = m.ccz[nb] - m.ccz[c];
-                double a1 = dx / (r11 * r11);
-                double a2 = 1.0 / (r22 * r22) * (dy - r12 / r11 * dx);
-                double a3 = 0.0;
-                if (m.dim == 3) a3 = 1.0 / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx);
-                m.lsqw[(0 * (size_t)MF + k) * N + c] = a1 - r12 / r11 * a2 + beta * a3;
-                m.lsqw[(1 * (size_t)MF + k) * N + c] = a2 - r23 / r22 * a3;
-                m.lsqw[(2 * (size_t)MF + k) * N + c] = a3;
-            }
+    for (int64_t c = 0; c < N; c++) {
+        const double* rr = &m.r[c * 6];
+        double r11 = rr[0], r12 = rr[1], r22 = rr[2], r13 = 0.0, r23 = 0.0, r33 = 0.0;
+        if (m.dim == 3) { r13 = rr[3]; r23 = rr[4]; r33 = rr[5]; }
+        double beta = (r12 * r23 - r13 * r23) / (r11 * r22);
+        for (int k = 0; k < m.nfaces[c]; k++) {
+            int64_t nb = m.cell_nbr[c * MF + k];
+            double dx = m.ccx[nb] - m.ccx[c], dy = m.ccy[nb] - m.ccy[c], dz = m.ccz[nb] - m.ccz[c];
+            double a1 = dx / (r11 * r11);
+            double a2 = 1.0 / (r22 * r22) * (dy - r12 / r11 * dx);
+            double a3 = 0.0;
+            if (m.dim == 3) a3 = 1.0 / (r33 * r33) * (dz - r23 / r22 * dy + beta * dx);
+            m.lsqw[(0 * (size_t)MF + k) * N + c] = a1 - r12 / r11 * a2 + beta * a3;
+            m.lsqw[(1 * (size_t)MF + k) * N + c] = a2 - r23 / r22 * a3;
+            m.lsqw[(2 * (size_t)MF + k) * N + c] = a3;
         }
     }
 }

@@ -89,6 +89,10 @@ struct Mesh {
 void build_mesh(const GridInput& in, const std::vector<BoundarySpec>& bounds, bool need_lsq,
                 Mesh& m);
 
+// The least-squares factors (r, lsqw) of a built mesh from its centroids
+// (WLSGradient::compute_weights / compute_gradients, gradient.h:89-162).
+void compute_lsq(Mesh& m);
+
 // An internal numbering of cells and faces and its map to the reference's
 // (each vector maps an id of one numbering to the other).
 struct MeshNumbering {

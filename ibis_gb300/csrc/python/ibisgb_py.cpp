@@ -120,4 +120,16 @@ PYBIND11_MODULE(_ibisgb_py, m) {
         },
         py::arg("sim"), py::arg("w"), py::arg("face_out"), py::arg("cell_out"), py::arg("allow_reconstruction") = true,
         "face_out (13 x F) and cell_out (4 x (N+G)) = w^T dR/dgeometry.");
+    m.def(
+        "jvp_geometry",
+        [](py::object sim, py::object dface, py::object dcell, py::object out, bool allow_reconstruction) {
+            ibisgb_ctx* c = handle(sim);
+            const Sizes s = sizes(c);
+            const double* df = (const double*)device_ptr(dface, "dface", 13 * s.F);
+            const double* dc = (const double*)device_ptr(dcell, "dcell", 4 * s.NT);
+            double* o = (double*)device_ptr(out, "out", s.n);
+            check(c, ibisgb_jvp_geometry_device(c, df, dc, o, allow_reconstruction ? 1 : 0, current_stream()));
+        },
+        py::arg("sim"), py::arg("dface"), py::arg("dcell"), py::arg("out"), py::arg("allow_reconstruction") = true,
+        "out (N x n_conserved) = dR/dgeometry . (dface, dcell).");
 }

@@ -305,6 +305,15 @@ class Simulation:
         out = out.reshape(self.num_cells, self.n_conserved)
         return (out, g) if ghosts else out
 
+    def set_geometry(self, face, cell) -> None:
+        """Replace the grid geometry (ibisgb_set_geometry): face (13, F) and cell (4, N+G)
+        in the layouts of the face / cell geometry dumps."""
+        f = np.ascontiguousarray(face, np.float64)
+        c = np.ascontiguousarray(cell, np.float64)
+        if f.shape != (13, self.num_faces) or c.shape != (4, self.num_cells + self.num_ghost_cells):
+            raise ValueError("face must be (13, F) and cell (4, N+G)")
+        self._call("ibisgb_set_geometry", _ptr(f), _ptr(c))
+
     def geometry_tangent(self, dface, dcell, allow_reconstruction: bool = True) -> np.ndarray:
         """dR/dgeometry . (dface, dcell) (ibisgb_jvp_geometry) for dface (13, F) and
         dcell (4, N+G) in the layouts of the face / cell geometry dumps; returns

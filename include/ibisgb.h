@@ -216,6 +216,17 @@ int ibisgb_l2_norms(ibisgb_ctx* ctx, double out[6]);
  * padded; the grid's vertex ids). */
 int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
 
+/* Replaces the grid geometry: face (13 x F: normal, tangents t1 and t2, centre,
+ * area) and cell (4 x (N+G): centroid, volume; ghost volumes ignored), host
+ * arrays in the layouts of dumps 6 and 7, reference numbering.  The
+ * least-squares factors are formed again from the centroids; connectivity,
+ * boundary actions and the boundary-layer profile's ghost states are kept, and
+ * the structured-block stages (which hold their own lattice geometry) are
+ * switched off.  With ibisgb_vjp_geometry / ibisgb_jvp_geometry this makes the
+ * residual a differentiable function of the geometry arrays.  No counterpart in
+ * the reference (its GridBlock is built once from the SU2 file). */
+int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell);
+
 /* The device arrays' cell and face order.  The grid's optional "renumber" key
  * ("auto" when absent, "rcm", "none"; not a reference key) selects it: "rcm"
  * orders the valid cells by reverse Cuthill-McKee over the interior-face graph

@@ -149,3 +149,38 @@ def test_unsteady_adjoint_with_checkpoints():
         jm = float((rk_steps(sim, U0 - h * v, dts) * w).sum())
     fd = (jp - jm) / (2 * h)
     assert abs(fd - pred) <= 1e-5 * abs(pred), (fd, pred)
+
+
+def test_torch_autograd_through_the_geometry():
+    """The residual as a function of the state and the geometry arrays
+    (ibis_gb300.autograd.residual_geometry): gradcheck of the state and geometry
+    adjoints against central differences of the residual on geometry installed by
+    ibisgb_set_geometry (the least-squares factors formed again), forward mode
+    against the geometry tangent, both in scaled variables."""
+    torch = pytest.importorskip("torch")
+    from torch.autograd.forward_ad import dual_level, make_dual, unpack_dual
+    from ibis_gb300.autograd import residual_geometry
+    g, c, st = case("ramp", ni=6, nj=3, limiter="unlimited")
+    sim = Simulation(c, g)
+    sim.set_primitives(*st)
+    U0 = torch.tensor(sim.conserved(), dtype=torch.float64, device="cuda")
+    F0 = torch.tensor(sim.dump("face_geometry"), dtype=torch.float64, device="cuda")
+    C0 = torch.tensor(sim.dump("cell_geometry"), dtype=torch.float64, device="cuda")
+    su = U0.abs().mean(dim=0)
+    sf = F0.abs().mean(dim=1, keepdim=True) + 1e-3
+    sc = C0.abs().mean(dim=1, keepdim=True) + 1e-3
+    rs = residual_geometry(sim, U0, F0, C0).abs().mean(dim=0)
+    xu = (U0 / su).clone().requires_grad_(True)
+    xf = (F0 / sf).clone().requires_grad_(True)
+    xc = (C0 / sc).clone().requires_grad_(True)
+    f = lambda a, b, d: residual_geometry(sim, a * su, b * sf, d * sc) / rs  # noqa: E731
+    assert torch.autograd.gradcheck(f, (xu, xf, xc), eps=1e-6, atol=1e-5, rtol=1e-4, nondet_tol=0.0, fast_mode=True)
+    # forward mode: the state and geometry tangents together
+    du, dfc, dcc = torch.randn_like(U0) * su, torch.randn_like(F0) * sf, torch.randn_like(C0) * sc
+    with dual_level():
+        out = residual_geometry(sim, make_dual(U0, du), make_dual(F0, dfc), make_dual(C0, dcc))
+        jt = unpack_dual(out).tangent
+    h = 1e-7
+    fd = (residual_geometry(sim, U0 + h * du, F0 + h * dfc, C0 + h * dcc)
+          - residual_geometry(sim, U0 - h * du, F0 - h * dfc, C0 - h * dcc)) / (2 * h)
+    assert torch.allclose(jt, fd, rtol=1e-5, atol=1e-5 * fd.abs().max().item())

@@ -10,7 +10,7 @@ torch = pytest.importorskip("torch")
 def test_module_exports_and_checks_its_arguments():
     from ibis_gb300 import Simulation, _ibisgb_py as py
     from tests.cases import case
-    for name in ("set_conserved", "residual", "jvp", "vjp", "vjp_geometry"):
+    for name in ("set_conserved", "residual", "jvp", "vjp", "vjp_geometry", "jvp_geometry"):
         assert callable(getattr(py, name)), name
     g, c, st = case("ramp")
     sim = Simulation(c, g)
