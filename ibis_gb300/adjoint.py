@@ -112,15 +112,25 @@ def solve_adjoint(sim: Simulation, dJdU: np.ndarray, tol: float = 1e-10, cfl0: f
     return lam.cpu().numpy(), hist
 
 
-def mach_sensitivity(sim: Simulation, lam: np.ndarray, tag: str = "inflow", flow_angle_deg: float = 0.0) -> float:
-    """lambda . dR/dM: the inflow ghost velocity is M a (cos, sin of the flow angle) at fixed T, p."""
+def inflow_sensitivity(sim: Simulation, lam: np.ndarray, tag: str = "inflow") -> np.ndarray:
+    """lambda . dR/dtheta for boundary `tag`'s inflow parameters theta = (T, p, vx, vy,
+    vz): the flow-state adjoint (ibisgb_vjp_flow_state: every action of the boundary
+    that carries the state, ghost cells and constant-flux faces) chained through
+    rho = p / (R T), energy = Cv T."""
     gas = sim.config["gas_model"]
-    fs = sim.config["grid"]["boundaries"][tag]["pre_reconstruction"][0]["flow_state"]
-    a = math.sqrt(gas["gamma"] * gas["R"] * fs["T"])
-    _, gadj = sim.vector_jacobian_product(lam, ghosts=True)
-    sel = sim.dump("ghost_boundary") == _bound_index(sim, tag)
+    fs = sim.flow_state(tag)
+    g = sim.flow_state_adjoint(lam)[tag]
+    T, p, R = fs["T"], fs["p"], gas["R"]
+    return np.array([g[0] - g[2] * p / (R * T * T) + g[3] * gas["Cv"], g[1] + g[2] / (R * T), g[4], g[5], g[6]])
+
+
+def mach_sensitivity(sim: Simulation, lam: np.ndarray, tag: str = "inflow", flow_angle_deg: float = 0.0) -> float:
+    """lambda . dR/dM: the inflow velocity is M a (cos, sin of the flow angle) at fixed T, p."""
+    gas = sim.config["gas_model"]
+    a = math.sqrt(gas["gamma"] * gas["R"] * sim.flow_state(tag)["T"])
     th = math.radians(flow_angle_deg)
-    return float(np.sum(gadj[sel, 4]) * a * math.cos(th) + np.sum(gadj[sel, 5]) * a * math.sin(th))
+    d = inflow_sensitivity(sim, lam, tag)
+    return float(d[2] * a * math.cos(th) + d[3] * a * math.sin(th))
 
 
 def shape_gradient(sim: Simulation, grid, lam: np.ndarray, dxyz: np.ndarray, tag: str = "wall",

@@ -122,6 +122,66 @@ def residual_geometry(sim, U, face, cell):
     return ResidualGeometry.apply(U, face, cell, sim)
 
 
+def _flow_state_values(sim, theta):
+    """The 7 flow-state entries (T, p, rho, energy, vx, vy, vz) of the inflow
+    parameters theta = (T, p, vx, vy, vz): rho = p / (R T) and energy = Cv T from
+    the ideal gas, as the prep step's FlowState.as_dict (ibis_py_utils.py:32-37)."""
+    gas = sim.config["gas_model"]
+    T, p, vx, vy, vz = (float(x) for x in theta.detach().cpu().tolist())
+    return [T, p, p / (gas["R"] * T), gas["Cv"] * T, vx, vy, vz]
+
+
+class ResidualFlowState(torch.autograd.Function):
+    """R(U, theta): the residual as a function of the state and of the inflow
+    parameters theta = (T, p, vx, vy, vz) of one boundary (float64 tensor of 5;
+    rho and energy follow from T and p through the gas model).  The forward pass
+    installs the flow state on every action of the boundary that carries one
+    (ibisgb_set_flow_state); the backward pass is the state adjoint and the
+    flow-state adjoint (ibisgb_vjp / ibisgb_vjp_flow_state) chained through
+    rho = p / (R T), energy = Cv T."""
+
+    @staticmethod
+    def forward(ctx, U, theta, sim, tag):
+        if U.dtype != torch.float64 or not U.is_cuda:
+            raise TypeError("U must be a float64 CUDA tensor")
+        if theta.numel() != 5:
+            raise ValueError("theta must hold T, p, vx, vy, vz")
+        _py.set_flow_state(sim, tag, _flow_state_values(sim, theta))
+        U = U.contiguous()
+        _py.set_conserved(sim, U)
+        out = torch.empty_like(U)
+        _py.residual(sim, _F64_EXACT, out)
+        ctx.sim, ctx.tag = sim, tag
+        ctx.save_for_backward(U, theta)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        U, theta = ctx.saved_tensors
+        sim = ctx.sim
+        _py.set_flow_state(sim, ctx.tag, _flow_state_values(sim, theta))  # linearise at the forward state
+        _py.set_conserved(sim, U)
+        w = grad_out.contiguous()
+        gU = torch.empty_like(U)
+        _py.vjp(sim, w, gU)
+        tags = sorted(sim.config["grid"]["boundaries"].keys())
+        graw = torch.empty((len(tags), 7), dtype=torch.float64, device=U.device)
+        _py.vjp_flow_state(sim, w, graw)
+        g = graw[tags.index(ctx.tag)].to(theta.device)
+        gas = sim.config["gas_model"]
+        T, p = theta[0].detach(), theta[1].detach()
+        R = gas["R"]
+        gT = g[0] - g[2] * p / (R * T * T) + g[3] * gas["Cv"]
+        gp = g[1] + g[2] / (R * T)
+        return gU, torch.stack([gT, gp, g[4], g[5], g[6]]).reshape(theta.shape), None, None
+
+
+def residual_flow_state(sim, U, theta, tag: str = "inflow"):
+    """dU/dt of `sim` at state U with boundary `tag`'s inflow parameters theta =
+    (T, p, vx, vy, vz), differentiable in U and theta."""
+    return ResidualFlowState.apply(U, theta, sim, tag)
+
+
 def _tableau(sim):
     """The Butcher tableau of the config's Runge-Kutta block: a (strictly lower), b."""
     bt = sim.config["solver"]["butcher_tableau"]

@@ -849,6 +849,7 @@ struct ibisgb_ctx {
         s.vghost.alloc(P * 5 * std::max<int64_t>(mesh.G, 1));
         s.grad.alloc(P * 16 * N);  // 15 x N, or the mixed build's 16 packed floats per cell
         s.phi.alloc(P * 5 * N);
+        if (s.phi.p) CUDA_OK(cudaMemsetAsync(s.phi.p, 0, P * 5 * N, stream));  // 2-D leaves the fifth row unwritten
         s.vgrad.alloc(P * 12 * N);
         s.flux.alloc(P * nc() * F);
         s.geometry = true;
@@ -999,7 +1000,10 @@ struct ibisgb_ctx {
         // compute_dudt applies the pre-reconstruction actions first (finite_volume.cpp:62)
         o.ghost_fill(v, prm, stream);
         if (record_branches && prm.order == 2 && prm.limiter) {
-            branches.alloc(sizeof(unsigned) * 5 * mesh.N);
+            if (!branches.p) {  // a 2-D grid leaves the fifth row unwritten
+                branches.alloc(sizeof(unsigned) * 5 * mesh.N);
+                if (branches.p) CUDA_OK(cudaMemsetAsync(branches.p, 0, sizeof(unsigned) * 5 * mesh.N, stream));
+            }
             v.branches = branches.as<unsigned>();
         }
         bool reco = prm.order == 2;
@@ -1562,6 +1566,77 @@ struct ibisgb_ctx {
                                         sizeof(double) * (NT - N), cudaMemcpyDeviceToDevice, stream));
         }
         CUDA_OK(cudaGetLastError());
+    }
+
+    // The flow state (T, p, rho, energy, vx, vy, vz) of boundary `tag`: every
+    // action that carries one (flow_state_copy, subsonic_inflow before
+    // reconstruction or the viscous gradients, constant_flux after the convective
+    // flux) takes `fs`, as if the config had given it.
+    int bound_index(const char* tag) const {
+        for (size_t b = 0; b < mesh.bounds.size(); b++)
+            if (mesh.bounds[b].tag == tag) return (int)b;
+        throw ArgError(std::string("no boundary ") + tag);
+    }
+    static bool carries_flow_state(const Action& a) { return a.kind == aFlowStateCopy || a.kind == aSubsonicInflow; }
+    bool has_flow_state(const BoundDev& d) const {
+        bool any = d.cflux != 0;
+        for (int k = 0; k < d.n_pre; k++) any |= carries_flow_state(d.pre[k]);
+        for (int k = 0; k < d.n_visc; k++) any |= carries_flow_state(d.visc[k]);
+        return any;
+    }
+    void flow_state(const char* tag, double* fs) const {
+        if (n_cases > 1) throw StateError("a batch's boundary states belong to its cases");
+        const BoundDev& d = bounds_host[bound_index(tag)];
+        for (int k = 0; k < d.n_pre; k++)
+            if (carries_flow_state(d.pre[k])) return (void)std::copy(d.pre[k].fs, d.pre[k].fs + 7, fs);
+        for (int k = 0; k < d.n_visc; k++)
+            if (carries_flow_state(d.visc[k])) return (void)std::copy(d.visc[k].fs, d.visc[k].fs + 7, fs);
+        if (d.cflux) return (void)std::copy(d.cfs, d.cfs + 7, fs);
+        throw ArgError(std::string("boundary ") + tag + " has no flow state");
+    }
+    void set_flow_state(const char* tag, const double* fs) {
+        if (n_cases > 1) throw StateError("a batch's boundary states belong to its cases");
+        for (int k = 0; k < 7; k++)
+            if (!std::isfinite(fs[k])) throw ArgError("flow state entries must be finite");
+        BoundDev& d = bounds_host[bound_index(tag)];
+        if (!has_flow_state(d)) throw ArgError(std::string("boundary ") + tag + " has no flow state");
+        for (int k = 0; k < d.n_pre; k++)
+            if (carries_flow_state(d.pre[k])) std::copy(fs, fs + 7, d.pre[k].fs);
+        for (int k = 0; k < d.n_visc; k++)
+            if (carries_flow_state(d.visc[k])) std::copy(fs, fs + 7, d.visc[k].fs);
+        if (d.cflux) std::copy(fs, fs + 7, d.cfs);
+        s64.prims_current = s32.prims_current = sff.prims_current = false;  // ghosts carry the old state
+        if (uploaded) {
+            upload(bounds, bounds_host, stream);
+            CUDA_OK(cudaStreamSynchronize(stream));
+        }
+    }
+
+    // out (num_boundaries x 7, sorted tag order) = w^T dR/d(flow state of each
+    // boundary), the derivative taken with every action of the boundary that
+    // carries a flow state moving together (set_flow_state's semantics)
+    DBuf fs_ghost;
+    void vjp_flow_state(const double* w_dev, double* out_dev, bool reconstruct) {
+        if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
+        if (n_cases > 1) throw StateError("a batch's boundary states belong to its cases");
+        DevView v = tangent_view();
+        ensure_adjoint();
+        const int64_t G = mesh.G;
+        fs_ghost.alloc(sizeof(double) * 7 * std::max<int64_t>(G, 1));
+        CUDA_OK(cudaMemsetAsync(fs_ghost.p, 0, sizeof(double) * 7 * std::max<int64_t>(G, 1), stream));
+        AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
+                     adj_back.as<signed char>(), adj_qv.as<double>(), adj_qg.as<double>(), adj_gav.as<double>()};
+        a.fs_ghost = fs_ghost.as<double>();
+        launch_adjoint(v, prm, w_dev, reconstruct && prm.order == 2, a, nullptr, nullptr, stream);
+        launch_sum_ghost_rows(fs_ghost.as<double>(), ghost_bound.as<int>(), (int)G, (int)mesh.bounds.size(), out_dev,
+                              stream);
+        CUDA_OK(cudaGetLastError());
+    }
+    void vjp_flow_state_rows(const double* w, double* out_dev, bool reconstruct) {
+        if (!renumbered()) return vjp_flow_state(w, out_dev, reconstruct);
+        map_a.alloc(sizeof(double) * nvars());
+        map_rows_device(w, map_a.as<double>(), nc(), true);
+        vjp_flow_state(map_a.as<double>(), out_dev, reconstruct);  // ghost ids are not renumbered
     }
 
     size_t nvars() const { return (size_t)mesh.N * nc(); }
@@ -2656,6 +2731,53 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
 int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell) {
     if (!ctx || !face || !cell) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] { ctx->set_geometry(face, cell); });
+}
+
+int ibisgb_set_flow_state(ibisgb_ctx* ctx, const char* tag, const double* fs) {
+    if (!ctx || !tag || !fs) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->set_flow_state(tag, fs); });
+}
+
+int ibisgb_get_flow_state(ibisgb_ctx* ctx, const char* tag, double* fs) {
+    if (!ctx || !tag || !fs) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] { ctx->flow_state(tag, fs); });
+}
+
+int ibisgb_vjp_flow_state_device(ibisgb_ctx* ctx, const double* w_device, double* out_device,
+                                 int32_t allow_reconstruction, void* stream) {
+    if (!ctx || !w_device || !out_device) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        ctx->ensure_device();
+        if (user && user != ctx->stream) {
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+        }
+        ctx->vjp_flow_state_rows(w_device, out_device, allow_reconstruction != 0);
+        if (ev) {
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        }
+    });
+}
+
+int ibisgb_vjp_flow_state(ibisgb_ctx* ctx, const double* w, double* out, int32_t allow_reconstruction) {
+    if (!ctx || !w || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_device();
+        const size_t n = ctx->nvars(), nb = 7 * ctx->mesh.bounds.size();
+        ctx->ensure_krylov(1);
+        ctx->geo_out_face.alloc(sizeof(double) * std::max(nb, (size_t)1));
+        CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, w, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->vjp_flow_state_rows(ctx->kr0.as<double>(), ctx->geo_out_face.as<double>(), allow_reconstruction != 0);
+        if (nb)
+            CUDA_OK(cudaMemcpyAsync(out, ctx->geo_out_face.p, sizeof(double) * nb, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
 }
 
 int ibisgb_numbering(const ibisgb_ctx* ctx, int32_t* renumbered, int64_t* bandwidth_reference,

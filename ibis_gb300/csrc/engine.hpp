@@ -240,6 +240,9 @@ struct AdjScratch {
     double* geo_vb = nullptr;    // [2][F]    volume adjoint of each side's cell from the face
     double* geo_nbc = nullptr;   // [3][MF][N] centroid adjoint each cell sends to the neighbour of slot s
     double* geo_ceb = nullptr;   // [3][F]    viscous: adjoint of an interior face's centroid offset x_r - x_l
+    // boundary flow-state adjoint (ibisgb_vjp_flow_state; null otherwise)
+    double* fs_ghost = nullptr;  // [G][7]    out, added to: each ghost's share of w^T dR/d(its boundary's flow
+                                 //           state: T, p, rho, energy, vx, vy, vz)
 };
 // out = (dR/dU)^T w for w, out of N x nc rows; ghost_out (optional, G x 7 rows):
 // the adjoint of every ghost cell's primitives (rho, p, T, e, v).
@@ -250,6 +253,9 @@ void launch_adjoint(const DevView& v, const FvParams& p, const double* w, bool r
 // least-squares factors are differentiated through the centroids).
 void launch_adjoint_geometry(const DevView& v, const FvParams& p, const double* w, bool reconstruct,
                              const AdjScratch& a, cudaStream_t s);
+// out[b * 7 + k] = sum over the ghosts g of boundary b of rows[g * 7 + k] (nb
+// boundaries, G ghosts, ghost_bound per ghost), in a fixed order.
+void launch_sum_ghost_rows(const double* rows, const int* ghost_bound, int G, int nb, double* out, cudaStream_t s);
 // The geometry tangent: out = dR/dgeometry . (dface [13][F], dcell [4][N+G]) at the
 // current state, on dual copies of the geometry (each element 2 doubles).
 struct GeoTangent {

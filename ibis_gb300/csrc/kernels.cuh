@@ -150,22 +150,29 @@ __device__ __forceinline__ P to_storage(S x) {
 // Ghost-cell actions on one ghost (boundary.cpp:9-400), in double.
 // ---------------------------------------------------------------------------
 // face_lo (float-float build, else null): what the float geometry leaves out,
-// so that the normal and tangents the actions use are hi + lo in double
+// so that the normal and tangents the actions use are hi + lo in double.
+// fs_dir (dual S only, else null): a tangent direction of the actions' flow
+// state (T, p, rho, energy, vx, vy, vz), for the derivative with respect to it.
 template <class S, class Gm>
 __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const StateT<S>& src,
                               const Gm* face, int F, int f, const FvParams& prm, const double* gfix, int G,
-                              int g, const float* face_lo = nullptr) {
+                              int g, const float* face_lo = nullptr, const double* fs_dir = nullptr) {
     auto geo = [&](int k) -> S {
         if constexpr (std::is_arithmetic<Gm>::value)  // (a dual geometry, for its adjoint, has no lo part)
             if (face_lo) return S((double)face[k * F + f] + (double)face_lo[k * F + f]);
         return S(face[k * F + f]);
     };
+    auto fsv = [&](const Action& A, int k) -> S {
+        if constexpr (kIsDual<S>)
+            if (fs_dir) return S(A.fs[k], fs_dir[k]);
+        return S(A.fs[k]);
+    };
     for (int a = 0; a < n; a++) {
         const Action& A = acts[a];
         switch (A.kind) {
             case aFlowStateCopy:
-                gh.T = S(A.fs[0]); gh.p = S(A.fs[1]); gh.rho = S(A.fs[2]); gh.e = S(A.fs[3]);
-                gh.vx = S(A.fs[4]); gh.vy = S(A.fs[5]); gh.vz = S(A.fs[6]);
+                gh.T = fsv(A, 0); gh.p = fsv(A, 1); gh.rho = fsv(A, 2); gh.e = fsv(A, 3);
+                gh.vx = fsv(A, 4); gh.vy = fsv(A, 5); gh.vz = fsv(A, 6);
                 break;
             case aInternalCopy:
             case aPeriodicCopy:
@@ -199,15 +206,15 @@ __device__ void apply_actions(const Action* acts, int n, StateT<S>& gh, const St
             }
             case aSubsonicInflow: {
                 S nx = geo(0), ny = geo(1), nz = geo(2);
-                S vc = nx * (S(A.fs[4]) - src.vx) + ny * (S(A.fs[5]) - src.vy) + nz * (S(A.fs[6]) - src.vz);
+                S vc = nx * (fsv(A, 4) - src.vx) + ny * (fsv(A, 5) - src.vy) + nz * (fsv(A, 6) - src.vz);
                 S sos = d_sqrt<S>(S(prm.gamma) * S(prm.R) * src.T);
                 S rho_ref = src.rho;
-                S p_in = S(A.fs[1]);
+                S p_in = fsv(A, 1);
                 S p_face = S(0.5) * (p_in + src.p - rho_ref * sos * vc);
-                S rho_face = S(A.fs[2]) + (p_face - p_in) / sos / sos;
-                S vxf = S(A.fs[4]) - nx * (p_in - p_face) / (rho_ref * sos);
-                S vyf = S(A.fs[5]) - ny * (p_in - p_face) / (rho_ref * sos);
-                S vzf = S(A.fs[6]) - nz * (p_in - p_face) / (rho_ref * sos);
+                S rho_face = fsv(A, 2) + (p_face - p_in) / sos / sos;
+                S vxf = fsv(A, 4) - nx * (p_in - p_face) / (rho_ref * sos);
+                S vyf = fsv(A, 5) - ny * (p_in - p_face) / (rho_ref * sos);
+                S vzf = fsv(A, 6) - nz * (p_in - p_face) / (rho_ref * sos);
                 gh.p = S(2.0) * p_face - src.p;
                 gh.rho = S(2.0) * rho_face - src.rho;
                 gh.T = gh.p / (gh.rho * S(prm.R));
@@ -694,8 +701,8 @@ __device__ __forceinline__ void convective_flux(const FvParams& prm, const Gas<R
 // ConstantFlux::apply (boundary.cpp:404-444) on a fixed grid: the flux of the
 // state fs (T, p, rho, energy, vx, vy, vz) through a face of normal n, in the
 // global frame.  The energy term keeps the reference's vy * n.x.
-template <class R, int DIM>
-__device__ __forceinline__ void constant_flux(const double (&fs)[7], double Cv, R nx, R ny, R nz, R (&out)[5]) {
+template <class R, int DIM, class E = double>
+__device__ __forceinline__ void constant_flux(const E (&fs)[7], double Cv, R nx, R ny, R nz, R (&out)[5]) {
     const R vx = R(fs[4]), vy = R(fs[5]), vz = R(fs[6]), p = R(fs[1]);
     const R u = R(Cv) * R(fs[0]);  // internal_energy: Cv T
     const R mass = R(fs[2]) * (vx * nx + vy * ny + vz * nz);

@@ -264,7 +264,30 @@ __global__ void k_soa_to_rows2(const double* soa, double2* rows, int N, int nc) 
     v.y = soa[(size_t)((e + 1) % nc) * N + (e + 1) / nc];
     rows[t] = v;
 }
+
+// One block per boundary: the ghosts of boundary b, visited in a fixed strided
+// order and summed by a tree, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(256) k_sum_ghost_rows(const double* rows, const int* gb, int G, double* out) {
+    __shared__ double red[7][256];
+    const int b = blockIdx.x, t = threadIdx.x;
+    double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int g = t; g < G; g += 256)
+        if (gb[g] == b)
+            for (int k = 0; k < 7; k++) acc[k] += rows[(size_t)g * 7 + k];
+    for (int k = 0; k < 7; k++) red[k][t] = acc[k];
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (t < h)
+            for (int k = 0; k < 7; k++) red[k][t] += red[k][t + h];
+        __syncthreads();
+    }
+    if (t < 7) out[b * 7 + t] = red[t][0];
+}
 }  // namespace
+
+void launch_sum_ghost_rows(const double* rows, const int* ghost_bound, int G, int nb, double* out, cudaStream_t s) {
+    if (nb > 0) k_sum_ghost_rows<<<(unsigned)nb, 256, 0, s>>>(rows, ghost_bound, G, out);
+}
 
 void launch_rows_to_soa(const double* rows, double* soa, int N, int nc, cudaStream_t s) {
     long long n = (long long)N * nc;

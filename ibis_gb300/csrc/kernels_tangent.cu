@@ -224,6 +224,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
     // a constant-flux face's convective flux does not depend on the state
     const int K = prm.cflux && constant_flux_bound(v, cells[0], cells[1]) ? 0
                                                                            : face_inputs<DIM>(prm.thermo, reconstruct, in);
+    if (K == 0)  // nothing flows back to the valid side's inputs (k_adj_cell reads every slot of every face)
+        for (int side = 0; side < 2; side++)
+            if (cells[side] < N)
+                for (int k = 0; k < 6; k++) qf[(size_t)(side * 6 + k) * F + f] = 0.0;
     for (int side = 0; side < 2; side++) {
         for (int k = 0; k < K; k++) {
             DualA qd[2][7];
@@ -243,6 +247,19 @@ __global__ void __launch_bounds__(kBlock) k_adj_face(DevView v, FvParams prm, co
             else ga[(size_t)in[k] * G + (c - N)] = acc;
         }
     }
+    if (a.fs_ghost && prm.cflux)  // a constant-flux face: the flux of its boundary's fixed state
+        if (const BoundDev* B = constant_flux_bound(v, cells[0], cells[1])) {
+            const int g = (cells[1] >= N ? cells[1] : cells[0]) - N;
+            for (int j = 0; j < 7; j++) {
+                DualA fsd[7];
+                for (int k = 0; k < 7; k++) fsd[k] = DualA(B->cfs[k], k == j ? 1.0 : 0.0);
+                DualA Fd[5];
+                constant_flux<DualA, DIM>(fsd, prm.Cv, nx, ny, nz, Fd);
+                double acc = 0.0;
+                for (int q = 0; q < 5; q++) acc += fb[q] * Fd[q].du;
+                a.fs_ghost[(size_t)g * 7 + j] += acc;
+            }
+        }
     // the face's total flux (convective less viscous), for the area and volume adjoints
     double Ft[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     auto finish_geo = [&]() {
@@ -747,6 +764,33 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(DevView v, FvParams prm, i
                          gvb[4] * gh.vz.du;
                 }
                 a.geo_face[(size_t)j * v.F + f] += d;
+            }
+        }
+        if (a.fs_ghost) {  // the ghost's dependence on its boundary's flow state, one seed per entry
+            bool uses = false;
+            for (int k = 0; k < B.n_pre; k++) uses |= B.pre[k].kind == aFlowStateCopy || B.pre[k].kind == aSubsonicInflow;
+            if (prm.viscous)
+                for (int k = 0; k < B.n_visc; k++)
+                    uses |= B.visc[k].kind == aFlowStateCopy || B.visc[k].kind == aSubsonicInflow;
+            if (uses) {
+                StateT<DualA> src{DualA(pr[i].re), DualA(pr[NT + i].re), DualA(pr[2 * NT + i].re),
+                                  DualA(pr[3 * NT + i].re), DualA(pr[4 * NT + i].re), DualA(pr[5 * NT + i].re),
+                                  DualA(pr[6 * NT + i].re)};
+                for (int j = 0; j < 7; j++) {
+                    double dir[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                    dir[j] = 1.0;
+                    StateT<DualA> gh = src;
+                    apply_actions<DualA, double>(B.pre, B.n_pre, gh, src, fg, v.F, f, prm, v.gfix, G, g, nullptr, dir);
+                    double d = gb[0] * gh.rho.du + gb[1] * gh.p.du + gb[2] * gh.T.du + gb[3] * gh.e.du +
+                               gb[4] * gh.vx.du + gb[5] * gh.vy.du + gb[6] * gh.vz.du;
+                    if (prm.viscous) {
+                        apply_actions<DualA, double>(B.visc, B.n_visc, gh, src, fg, v.F, f, prm, v.gfix, G, g, nullptr,
+                                                     dir);
+                        d += gvb[0] * gh.p.du + gvb[1] * gh.T.du + gvb[2] * gh.vx.du + gvb[3] * gh.vy.du +
+                             gvb[4] * gh.vz.du;
+                    }
+                    a.fs_ghost[(size_t)g * 7 + j] += d;
+                }
             }
         }
         for (int m = 0; m < 7; m++) {

@@ -52,12 +52,13 @@ void check(ibisgb_ctx* ctx, int rc) {
 }
 
 struct Sizes {
-    int64_t n = 0, n_rows = 0, F = 0, NT = 0;
+    int64_t n = 0, n_rows = 0, F = 0, NT = 0, nb = 0;
 };
 Sizes sizes(ibisgb_ctx* ctx) {
     ibisgb_sizes s{};
     check(ctx, ibisgb_get_sizes(ctx, &s));
-    return {s.num_cells * s.n_conserved, s.num_cells, s.num_faces, s.num_cells + s.num_ghost_cells};
+    return {s.num_cells * s.n_conserved, s.num_cells, s.num_faces, s.num_cells + s.num_ghost_cells,
+            s.num_boundaries};
 }
 
 const char* precision_doc =
@@ -132,4 +133,26 @@ PYBIND11_MODULE(_ibisgb_py, m) {
         },
         py::arg("sim"), py::arg("dface"), py::arg("dcell"), py::arg("out"), py::arg("allow_reconstruction") = true,
         "out (N x n_conserved) = dR/dgeometry . (dface, dcell).");
+    m.def(
+        "set_flow_state",
+        [](py::object sim, const std::string& tag, py::sequence fs) {
+            ibisgb_ctx* c = handle(sim);
+            if (py::len(fs) != 7) throw std::invalid_argument("fs must hold 7 values: T, p, rho, energy, vx, vy, vz");
+            double a[7];
+            for (int k = 0; k < 7; k++) a[k] = fs[k].cast<double>();
+            check(c, ibisgb_set_flow_state(c, tag.c_str(), a));
+        },
+        py::arg("sim"), py::arg("tag"), py::arg("fs"),
+        "The flow state (T, p, rho, energy, vx, vy, vz) of every action of boundary tag that carries one.");
+    m.def(
+        "vjp_flow_state",
+        [](py::object sim, py::object w, py::object out, bool allow_reconstruction) {
+            ibisgb_ctx* c = handle(sim);
+            const Sizes s = sizes(c);
+            const double* x = (const double*)device_ptr(w, "w", s.n);
+            double* o = (double*)device_ptr(out, "out", 7 * s.nb);
+            check(c, ibisgb_vjp_flow_state_device(c, x, o, allow_reconstruction ? 1 : 0, current_stream()));
+        },
+        py::arg("sim"), py::arg("w"), py::arg("out"), py::arg("allow_reconstruction") = true,
+        "out (num_boundaries x 7, sorted tag order) = w^T dR/d(each boundary's flow state).");
 }

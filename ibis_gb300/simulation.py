@@ -314,6 +314,39 @@ class Simulation:
             raise ValueError("face must be (13, F) and cell (4, N+G)")
         self._call("ibisgb_set_geometry", _ptr(f), _ptr(c))
 
+    _FS_KEYS = ("T", "p", "rho", "energy", "vx", "vy", "vz")
+
+    def boundary_tags(self) -> list:
+        """The boundary tags in the order the engine numbers them (sorted)."""
+        return sorted(self.config["grid"]["boundaries"].keys())
+
+    def flow_state(self, tag: str) -> dict:
+        """The flow state of boundary `tag` in the engine (ibisgb_get_flow_state), as the
+        config's flow_state object: T, p, rho, energy, vx, vy, vz."""
+        fs = np.empty(7)
+        self._call("ibisgb_get_flow_state", tag.encode(), _ptr(fs))
+        return dict(zip(self._FS_KEYS, (float(x) for x in fs)))
+
+    def set_flow_state(self, tag: str, fs: dict) -> None:
+        """Give every action of boundary `tag` that carries a flow state the state fs
+        (a flow_state object: T, p, rho, energy, vx, vy, vz; ibisgb_set_flow_state).
+        rho and energy are taken as given: build fs with grids.flow_state for a
+        state consistent with the gas model."""
+        a = np.array([float(fs[k]) for k in self._FS_KEYS])
+        self._call("ibisgb_set_flow_state", tag.encode(), _ptr(a))
+
+    def flow_state_adjoint(self, w, allow_reconstruction: bool = True) -> dict:
+        """w^T dR/d(flow state) for w of shape (N, n_conserved) (ibisgb_vjp_flow_state):
+        {tag: array of 7 (T, p, rho, energy, vx, vy, vz)} for every boundary; zeros for
+        boundaries without a flow state."""
+        w = np.ascontiguousarray(w, np.float64).reshape(-1)
+        if w.size != self.num_cells * self.n_conserved:
+            raise ValueError("w has the wrong size")
+        tags = self.boundary_tags()
+        out = np.empty((max(len(tags), 1), 7))
+        self._call("ibisgb_vjp_flow_state", _ptr(w), _ptr(out), int(allow_reconstruction))
+        return {t: out[b].copy() for b, t in enumerate(tags)}
+
     def geometry_tangent(self, dface, dcell, allow_reconstruction: bool = True) -> np.ndarray:
         """dR/dgeometry . (dface, dcell) (ibisgb_jvp_geometry) for dface (13, F) and
         dcell (4, N+G) in the layouts of the face / cell geometry dumps; returns

@@ -227,6 +227,40 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
  * the reference (its GridBlock is built once from the SU2 file). */
 int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell);
 
+/* Replaces the flow state (7 doubles: T, p, rho, energy, vx, vy, vz -- the
+ * "flow_state" object of the config) of boundary `tag`: every action of it that
+ * carries one takes fs, as if the config had given it (FlowStateCopy and
+ * SubsonicInflow, src/finite_volume/finite_volume/boundaries/boundary.cpp:10-12,
+ * 280-282, in the pre-reconstruction and pre-viscous-gradient lists; the
+ * constant_flux flux action, boundary.cpp:404-444).  rho and energy are inputs
+ * as in the config (the reference takes them as given); keep them consistent
+ * with the gas model (rho = p / (R T), energy = Cv T) for a physical state.
+ * IBISGB_ERR_ARG for an unknown tag, a boundary with no flow state or a
+ * non-finite entry; IBISGB_ERR_STATE on a batch (its cases' states are fixed
+ * when it is made).  No counterpart in the reference (its boundary conditions
+ * are built once from the config). */
+int ibisgb_set_flow_state(ibisgb_ctx* ctx, const char* tag, const double* fs);
+
+/* The flow state of boundary `tag` (7 doubles, as ibisgb_set_flow_state). */
+int ibisgb_get_flow_state(ibisgb_ctx* ctx, const char* tag, double* fs);
+
+/* out = w^T dR/d(flow state): for w (N x n_conserved rows), the adjoint of the
+ * residual with respect to each boundary's flow state (num_boundaries x 7, the
+ * boundaries in sorted tag order, the entries as ibisgb_set_flow_state; zero
+ * rows for boundaries without one).  Every action of a boundary that carries a
+ * flow state moves together, ibisgb_set_flow_state's semantics; through the
+ * ghost cells (each ghost's actions differentiated with the flow state seeded,
+ * the viscous ghost values included) and the constant-flux faces.  out_device
+ * is device memory, on `stream` (NULL: the context stream).  The transposed
+ * derivative the steady adjoint needs for inflow parameters: with lambda from
+ * ibisgb_adjoint_step, dObjective/dfs = dObjective/dfs|_U + lambda . dR/dfs.
+ * No counterpart in the reference. */
+int ibisgb_vjp_flow_state_device(ibisgb_ctx* ctx, const double* w_device, double* out_device,
+                                 int32_t allow_reconstruction, void* stream);
+
+/* As ibisgb_vjp_flow_state_device with host vectors. */
+int ibisgb_vjp_flow_state(ibisgb_ctx* ctx, const double* w, double* out, int32_t allow_reconstruction);
+
 /* The device arrays' cell and face order.  The grid's optional "renumber" key
  * ("auto" when absent, "rcm", "none"; not a reference key) selects it: "rcm"
  * orders the valid cells by reverse Cuthill-McKee over the interior-face graph

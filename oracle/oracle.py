@@ -66,6 +66,7 @@ def lib():
         L.orc_steady_initialise.argtypes = [C.c_void_p]
         L.orc_jvp.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int]
         L.orc_geometry_jvp.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int]
+        L.orc_flow_state_jvp.argtypes = [C.c_void_p, C.c_char_p, _dp, _dp, C.c_int]
         L.orc_steady_rhs.argtypes = [C.c_void_p, _dp]
         L.orc_steady_steps.argtypes = [C.c_void_p, C.c_int, _dp]
         L.orc_steady_conserved.argtypes = [C.c_void_p, _dp]
@@ -242,6 +243,15 @@ class Oracle:
         self._check(lib().orc_geometry_jvp(self.h, np.ascontiguousarray(dface, np.float64).reshape(-1),
                                            np.ascontiguousarray(dcell, np.float64).reshape(-1), out,
                                            int(allow_reconstruction)))
+        return out.reshape(self.N, self.nc)
+
+    def flow_state_jvp(self, tag, dfs, allow_reconstruction=True):
+        """dR/dfs . dfs at the current steady state by the reference's dual numbers
+        seeded in boundary `tag`'s flow state (dfs: T, p, rho, energy, vx, vy, vz)
+        on every action of it that carries one; returns N x n_conserved."""
+        out = np.zeros(self.N * self.nc)
+        self._check(lib().orc_flow_state_jvp(self.h, tag.encode(), np.ascontiguousarray(dfs, np.float64).reshape(7),
+                                             out, int(allow_reconstruction)))
         return out.reshape(self.N, self.nc)
 
     def steady_rhs(self):

@@ -1,5 +1,6 @@
 // ORACLE — test infrastructure only. extern "C" surface of the CPU restatement
 // (oracle_core.hpp), loaded by the tests and by the CPU-baseline leg of bench.py.
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -393,6 +394,42 @@ int orc_geometry_jvp(void* hp, const double* dface, const double* dcell, double*
         for (int k = 0; k < 4; k++)
             for (size_t c = 0; c < NT; c++) (*ca[k])[c].du = on ? dcell[k * NT + c] : 0.0;
         if (!g.r.empty()) g.compute_gradient_weights();
+    };
+    seed(true);
+    size_t nc = g.dim + 2;
+    for (size_t c = 0; c < g.N; c++)
+        for (size_t q = 0; q < nc; q++) {
+            st.cq_tmp.q[c * nc + q].re = s.U.q[c * nc + q].re;
+            st.cq_tmp.q[c * nc + q].du = 0.0;
+        }
+    conserved_to_primatives(st.cq_tmp, st.fs_tmp, s.gas);
+    s.fv.compute_dudt(st.fs_tmp, g, st.residuals, s.gas, s.tp, allow_reconstruction != 0);
+    for (size_t i = 0; i < g.N * nc; i++) out[i] = st.residuals.q[i].du;
+    seed(false);
+    return 0;
+    GUARD_END(h, -1)
+}
+
+// Directional derivative of the residual at the steady simulation's current state
+// along a perturbation dfs (T, p, rho, energy, vx, vy, vz) of boundary `tag`'s
+// flow state, seeded into the dual parts of every action of that boundary that
+// carries one (flow_state_copy, subsonic_inflow, constant_flux); cleared afterwards.
+int orc_flow_state_jvp(void* hp, const char* tag, const double* dfs, double* out, int allow_reconstruction) {
+    Handle* h = (Handle*)hp;
+    GUARD_BEGIN
+    Steady& st = *h->steady;
+    Sim<Dual>& s = *st.sim;
+    Grid<Dual>& g = s.grid;
+    const auto& tags = g.boundary_tags;
+    const size_t b = (size_t)(std::find(tags.begin(), tags.end(), std::string(tag)) - tags.begin());
+    if (b == tags.size()) throw std::runtime_error(std::string("no boundary ") + tag);
+    BoundaryCondition& bc = s.fv.bcs[b];
+    auto seed = [&](bool on) {
+        for (auto* list : {&bc.pre_reconstruction, &bc.post_convective_flux, &bc.pre_viscous_grad})
+            for (Action& a : *list)
+                if (a.kind == ActionKind::FlowStateCopy || a.kind == ActionKind::SubsonicInflow ||
+                    a.kind == ActionKind::ConstantFlux)
+                    for (int k = 0; k < 7; k++) a.fs_du[k] = on ? dfs[k] : 0.0;
     };
     seed(true);
     size_t nc = g.dim + 2;

@@ -489,9 +489,10 @@ void FiniteVolume<T>::apply_ghost_actions(const std::vector<Action>& acts, FlowS
             size_t valid = l < N ? l : r;
             switch (a.kind) {
                 case ActionKind::FlowStateCopy:  // boundary.cpp:14-46
-                    fs.temp[ghost] = a.fs[0]; fs.p[ghost] = a.fs[1];
-                    fs.rho[ghost] = a.fs[2]; fs.e[ghost] = a.fs[3];
-                    fs.vx[ghost] = a.fs[4]; fs.vy[ghost] = a.fs[5]; fs.vz[ghost] = a.fs[6];
+                    fs.temp[ghost] = fs_value<T>(a, 0); fs.p[ghost] = fs_value<T>(a, 1);
+                    fs.rho[ghost] = fs_value<T>(a, 2); fs.e[ghost] = fs_value<T>(a, 3);
+                    fs.vx[ghost] = fs_value<T>(a, 4); fs.vy[ghost] = fs_value<T>(a, 5);
+                    fs.vz[ghost] = fs_value<T>(a, 6);
                     break;
                 case ActionKind::InternalCopy:  // boundary.cpp:99-137
                     fs.temp[ghost] = fs.temp[valid]; fs.p[ghost] = fs.p[valid];
@@ -538,16 +539,16 @@ void FiniteVolume<T>::apply_ghost_actions(const std::vector<Action>& acts, FlowS
                 }
                 case ActionKind::SubsonicInflow: {  // boundary.cpp:284-343
                     T nxf = g.nx[f], nyf = g.ny[f], nzf = g.nz[f];
-                    T vc = nxf * (a.fs[4] - fs.vx[valid]) + nyf * (a.fs[5] - fs.vy[valid]) +
-                           nzf * (a.fs[6] - fs.vz[valid]);
+                    const T fvx = fs_value<T>(a, 4), fvy = fs_value<T>(a, 5), fvz = fs_value<T>(a, 6);
+                    T vc = nxf * (fvx - fs.vx[valid]) + nyf * (fvy - fs.vy[valid]) + nzf * (fvz - fs.vz[valid]);
                     T sos = o_sqrt(gas.gamma * gas.R * fs.temp[valid]);
                     T rho_ref = fs.rho[valid];
-                    T p_in = a.fs[1];
+                    T p_in = fs_value<T>(a, 1);
                     T p_face = 0.5 * (p_in + fs.p[valid] - rho_ref * sos * vc);
-                    T rho_face = a.fs[2] + (p_face - p_in) / sos / sos;
-                    T vxf = a.fs[4] - nxf * (p_in - p_face) / (rho_ref * sos);
-                    T vyf = a.fs[5] - nyf * (p_in - p_face) / (rho_ref * sos);
-                    T vzf = a.fs[6] - nzf * (p_in - p_face) / (rho_ref * sos);
+                    T rho_face = fs_value<T>(a, 2) + (p_face - p_in) / sos / sos;
+                    T vxf = fvx - nxf * (p_in - p_face) / (rho_ref * sos);
+                    T vyf = fvy - nyf * (p_in - p_face) / (rho_ref * sos);
+                    T vzf = fvz - nzf * (p_in - p_face) / (rho_ref * sos);
                     fs.p[ghost] = 2 * p_face - fs.p[valid];
                     fs.rho[ghost] = 2 * rho_face - fs.rho[valid];
                     fs.temp[ghost] = fs.p[ghost] / (fs.rho[ghost] * gas.R);
@@ -1012,16 +1013,17 @@ void FiniteVolume<T>::compute_dudt(FlowStates<T>& fs, const Grid<T>& g, Conserve
             if (a.kind != ActionKind::ConstantFlux) continue;
             for (size_t f : bc_faces[i]) {
                 T nxf = g.nx[f], nyf = g.ny[f], nzf = g.nz[f];
-                T u = gm.Cv * T(a.fs[0]);
-                T rvx = a.fs[4] - 0.0, rvy = a.fs[5] - 0.0, rvz = a.fs[6] - 0.0;
-                T mass = a.fs[2] * (rvx * nxf + rvy * nyf + rvz * nzf);
-                T p = a.fs[1];
+                const T fvx = fs_value<T>(a, 4), fvy = fs_value<T>(a, 5), fvz = fs_value<T>(a, 6);
+                T u = gm.Cv * fs_value<T>(a, 0);
+                T rvx = fvx - 0.0, rvy = fvy - 0.0, rvz = fvz - 0.0;
+                T mass = fs_value<T>(a, 2) * (rvx * nxf + rvy * nyf + rvz * nzf);
+                T p = fs_value<T>(a, 1);
                 flux.mass(f) = mass;
-                flux.mx(f) = p * nxf + a.fs[4] * mass;
-                flux.my(f) = p * nyf + a.fs[5] * mass;
-                if (dim == 3) flux.mz(f) = p * nzf + a.fs[6] * mass;
-                flux.energy(f) = mass * (u + 0.5 * (a.fs[4] * a.fs[4] + a.fs[5] * a.fs[5] + a.fs[6] * a.fs[6])) +
-                                 p * (a.fs[4] * nxf + a.fs[5] * nxf + a.fs[6] * nzf);
+                flux.mx(f) = p * nxf + fvx * mass;
+                flux.my(f) = p * nyf + fvy * mass;
+                if (dim == 3) flux.mz(f) = p * nzf + fvz * mass;
+                flux.energy(f) = mass * (u + 0.5 * (fvx * fvx + fvy * fvy + fvz * fvz)) +
+                                 p * (fvx * nxf + fvy * nxf + fvz * nzf);
             }
         }
     }

@@ -310,12 +310,21 @@ struct Action {
     ActionKind kind;
     // flow_state_copy / subsonic_inflow / constant_flux: T, p, rho, energy, vx, vy, vz
     double fs[7] = {0, 0, 0, 0, 0, 0, 0};
+    // the dual parts of fs in the Dual build (a directional derivative with
+    // respect to the flow state; zero otherwise, and unread by the real build)
+    double fs_du[7] = {0, 0, 0, 0, 0, 0, 0};
     double value = 0.0;  // fix_temperature temperature / subsonic_outflow pressure / profile pressure
     CubicSpline spline_v, spline_T;  // boundary_layer_profile: vx(y) and T(y)
 };
 struct BoundaryCondition {
     std::vector<Action> pre_reconstruction, post_convective_flux, pre_viscous_grad;
 };
+// Entry k of an action's flow state in the arithmetic T (with its dual part in
+// the Dual build).
+template <typename T>
+inline T fs_value(const Action& a, int k) { return T(a.fs[k]); }
+template <>
+inline Dual fs_value<Dual>(const Action& a, int k) { return Dual(a.fs[k], a.fs_du[k]); }
 
 enum class FluxKind { Hanel, Ausmdv, Ldfss2, Rusanov };
 enum class Thermo { rho_p, rho_T, rho_u, p_T };
