@@ -79,7 +79,21 @@ struct StateBufs {
     DBuf lsqw_lo, lsqd_lo, grad_lo, vgrad_lo, vghost_lo;
     bool geometry = false;
     bool prims_current = false;
+    bool lsq_shared = false;  // lsqw / lsqd (and their lo parts) hold one row per slot, the same for every cell
 };
+
+// Whether every column c of the rows x N array a (row-major [rows][N]) is
+// bitwise equal to column 0, and if so its first column.
+template <class T>
+bool shared_column(const std::vector<T>& a, int64_t rows, int64_t N, std::vector<T>& col) {
+    if (N < 1 || (int64_t)a.size() != rows * N) return false;
+    for (int64_t r = 0; r < rows; r++)
+        for (int64_t c = 1; c < N; c++)
+            if (std::memcmp(&a[r * N + c], &a[r * N], sizeof(T)) != 0) return false;
+    col.resize(rows);
+    for (int64_t r = 0; r < rows; r++) col[r] = a[r * N];
+    return true;
+}
 
 ActionKind parse_action_kind(const std::string& t) {
     if (t == "flow_state_copy") return aFlowStateCopy;
@@ -304,6 +318,13 @@ struct ibisgb_ctx {
                 else if (r == "none") renumber_mode = 2;
                 else throw ConfigError("grid.renumber must be auto, rcm or none");
             }
+            lsq_shared_mode = 0;
+            if (grid.contains("lsq_tables")) {  // not a reference key: the layout of the least-squares tables
+                const std::string t = grid.at("lsq_tables").as_string();
+                if (t == "auto") lsq_shared_mode = 0;
+                else if (t == "per_cell") lsq_shared_mode = 1;
+                else throw ConfigError("grid.lsq_tables must be auto or per_cell");
+            }
             prm.fR = (float)prm.R; prm.fCv = (float)prm.Cv; prm.fCp = (float)prm.Cp;
             prm.fgamma = (float)prm.gamma; prm.fgR = prm.fgamma * prm.fR; prm.feps = (float)prm.eps;
             prm.fdelta = (float)prm.delta; prm.fmu0 = (float)prm.mu0; prm.fT0 = (float)prm.T0;
@@ -476,6 +497,9 @@ struct ibisgb_ctx {
     // reference's numbering (grid.h:113-133).  Per-cell and per-face arithmetic and
     // summation orders are unchanged, so the results are the same bits.
     int renumber_mode = 0;  // 0 auto, 1 rcm, 2 none
+    // 0 auto: least-squares weights and face offsets stored once per slot when every
+    // cell's are bitwise the same (a uniform lattice); 1: always per cell
+    int lsq_shared_mode = 0;
     MeshNumbering num;
     int64_t bandwidth_ref = 0, bandwidth_internal = 0;
     DBuf d_cell_to_new, d_cell_to_ref, map_a, map_b;
@@ -804,11 +828,6 @@ struct ibisgb_ctx {
             s.grad_lo.alloc(sizeof(float) * 16 * mesh.N);
             s.vgrad_lo.alloc(sizeof(float) * 12 * mesh.N);
             s.vghost_lo.alloc(sizeof(float) * 5 * std::max<int64_t>(mesh.G, 1));
-            if (!mesh.lsqw.empty()) {
-                std::vector<float> wl(mesh.lsqw.size());
-                for (size_t q = 0; q < wl.size(); q++) wl[q] = lo(mesh.lsqw[q]);
-                upload(s.lsqw_lo, wl, stream);
-            }
         }
         const int64_t N = mesh.N, NT = mesh.NT(), F = mesh.F;
         std::vector<Gm> cc(3 * NT), r(6 * N, Gm(0)), fc(13 * F);
@@ -821,29 +840,47 @@ struct ibisgb_ctx {
         for (int q = 0; q < 13; q++)
             for (int64_t f = 0; f < F; f++) fc[q * F + f] = (Gm)(*fa[q])[f];
         upload(s.cc, cc, stream); upload(s.r, r, stream); upload(s.face, fc, stream);
+        // least-squares weights per neighbour slot and, for the float builds, the
+        // limiter's face offsets per face slot: coalesced instead of gathered
+        const int64_t MF = mesh.MF, rows = 3 * MF;
+        auto lo = [](double d) { return (float)(d - (double)(float)d); };
+        std::vector<Gm> w, d;
+        std::vector<float> wl, dl;
         if (!mesh.lsqw.empty()) {
-            std::vector<Gm> w(mesh.lsqw.begin(), mesh.lsqw.end());
-            upload(s.lsqw, w, stream);
+            w.assign(mesh.lsqw.begin(), mesh.lsqw.end());
+            if (with_lo) {
+                wl.resize(mesh.lsqw.size());
+                for (size_t q = 0; q < wl.size(); q++) wl[q] = lo(mesh.lsqw[q]);
+            }
         }
         if (sizeof(Gm) == sizeof(float) && prm.order == 2) {
-            // the limiter's face offsets, per face slot: coalesced instead of gathered
-            const int64_t MF = mesh.MF;
-            std::vector<Gm> d(3 * MF * N, Gm(0));
+            d.assign(rows * N, Gm(0));
             const std::vector<double>* fcs[3] = {&mesh.fcx, &mesh.fcy, &mesh.fcz};
             const std::vector<double>* ccs[3] = {&mesh.ccx, &mesh.ccy, &mesh.ccz};
-            std::vector<float> dl(with_lo ? 3 * MF * N : 0, 0.f);
+            dl.assign(with_lo ? rows * N : 0, 0.f);
             for (int64_t c = 0; c < N; c++)
                 for (int64_t k = 0; k < mesh.nfaces[c]; k++) {
                     const int64_t f = mesh.cell_face[c * MF + k];
                     for (int a = 0; a < 3; a++) {
                         const double x = (*fcs[a])[f] - (*ccs[a])[c];
                         d[(a * MF + k) * N + c] = (Gm)x;
-                        if (with_lo) dl[(a * MF + k) * N + c] = (float)(x - (double)(float)x);
+                        if (with_lo) dl[(a * MF + k) * N + c] = lo(x);
                     }
                 }
-            upload(s.lsqd, d, stream);
-            if (with_lo) upload(s.lsqd_lo, dl, stream);
         }
+        // On a uniform lattice every cell's tables are bitwise the same: keep one
+        // row per slot, read by every thread at the same address.  The values, and
+        // so the results, do not change.
+        std::vector<Gm> w1, d1;
+        std::vector<float> wl1, dl1;
+        s.lsq_shared = lsq_shared_mode == 0 && !w.empty() && shared_column(w, rows, N, w1) &&
+                       (d.empty() || shared_column(d, rows, N, d1)) &&
+                       (wl.empty() || shared_column(wl, rows, N, wl1)) &&
+                       (dl.empty() || shared_column(dl, rows, N, dl1));
+        if (!w.empty()) upload(s.lsqw, s.lsq_shared ? w1 : w, stream);
+        if (!d.empty()) upload(s.lsqd, s.lsq_shared ? d1 : d, stream);
+        if (!wl.empty()) upload(s.lsqw_lo, s.lsq_shared ? wl1 : wl, stream);
+        if (!dl.empty()) upload(s.lsqd_lo, s.lsq_shared ? dl1 : dl, stream);
         size_t P = sizeof(Gm);
         s.prim.alloc(P * 7 * NT);
         s.vghost.alloc(P * 5 * std::max<int64_t>(mesh.G, 1));
@@ -883,6 +920,7 @@ struct ibisgb_ctx {
         v.cc = s.cc.p; v.r = s.r.p; v.face = s.face.p; v.vol = vol.as<double>();
         v.inv_vol = inv_vol.as<double>(); v.inv_vol2 = inv_vol2.as<float2>(); v.lsqw = s.lsqw.p;
         v.lsqd = s.lsqd.p;
+        v.lsq_shared = s.lsq_shared ? 1 : 0;
         v.prim = (is_mixed(prec) && prim_cur) ? prim_alt.p : s.prim.p;
         v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
@@ -898,13 +936,17 @@ struct ibisgb_ctx {
         return v;
     }
 
+    void ensure_geometry(int prec) {
+        ensure_device();
+        if (is_mixed(prec)) upload_geometry<float>(s32);
+        else if (is_ff(prec)) upload_geometry<float>(sff, true);
+        else upload_geometry<double>(s64);
+    }
     // Make the primitives (and ghosts) of arithmetic `prec` reflect the current state.
     void ensure_prims(int prec) {
         ensure_device();
         if (!have_state) throw StateError("no initial condition: call ibisgb_set_primitives first");
-        if (is_mixed(prec)) upload_geometry<float>(s32);
-        else if (is_ff(prec)) upload_geometry<float>(sff, true);
-        else upload_geometry<double>(s64);
+        ensure_geometry(prec);
         StateBufs& s = bufs(prec);
         if (s.prims_current) return;
         DevView v = view(prec);
@@ -2777,6 +2819,14 @@ int ibisgb_vjp_flow_state(ibisgb_ctx* ctx, const double* w, double* out, int32_t
             CUDA_OK(cudaMemcpyAsync(out, ctx->geo_out_face.p, sizeof(double) * nb, cudaMemcpyDeviceToHost,
                                     ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ibisgb_lsq_shared(ibisgb_ctx* ctx, int32_t precision, int32_t* shared) {
+    if (!ctx || !shared || precision < 0 || precision > IBISGB_MIXED_FF) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_geometry(precision);
+        *shared = ctx->bufs(precision).lsq_shared ? 1 : 0;
     });
 }
 

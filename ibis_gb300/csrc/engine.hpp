@@ -116,6 +116,7 @@ struct DevView {
     const float2* inv_vol2; // N, 1/volume as a float pair (hi, lo) (mixed build)
     const void* lsqw;       // [3][MF][N] least-squares weights per neighbour slot (type Gm, fast paths)
     const void* lsqd;       // [3][MF][N] face centre minus cell centroid per face slot (float build), or null
+    int lsq_shared;         // 1: lsqw, lsqd and their lo parts are [3][MF], the same for every cell
     // state (type P)
     void* prim;    // [7][NT]: rho, p, T, e, vx, vy, vz
     void* vghost;  // [5][G]: p, T, vx, vy, vz after the pre-viscous-gradient actions

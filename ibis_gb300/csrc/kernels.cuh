@@ -418,17 +418,19 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
     const int nf = v.nfaces[i];
     const Gm* W = (const Gm*)v.lsqw;
     const int MF = v.MF;
+    // the weight and offset tables: per cell, or one row per slot shared by every cell
+    const int sN = v.lsq_shared ? 1 : N, si = v.lsq_shared ? 0 : i;
     auto slot = [&](int s, int nb) {
         R w1, w2, w3;
         if constexpr (FFG) {
             const float* Wl = v.lsqw_lo;
-            w1 = FF((float)W[s * N + i], Wl[s * N + i]);
-            w2 = FF((float)W[(MF + s) * N + i], Wl[(MF + s) * N + i]);
-            w3 = DIM == 3 ? FF((float)W[(2 * MF + s) * N + i], Wl[(2 * MF + s) * N + i]) : FF(0.f);
+            w1 = FF((float)W[s * sN + si], Wl[s * sN + si]);
+            w2 = FF((float)W[(MF + s) * sN + si], Wl[(MF + s) * sN + si]);
+            w3 = DIM == 3 ? FF((float)W[(2 * MF + s) * sN + si], Wl[(2 * MF + s) * sN + si]) : FF(0.f);
         } else if (!EXACT) {  // weights precomputed on the host from the same formulas
-            w1 = (R)W[s * N + i];
-            w2 = (R)W[(MF + s) * N + i];
-            w3 = DIM == 3 ? (R)W[(2 * MF + s) * N + i] : R(0.0);
+            w1 = (R)W[s * sN + si];
+            w2 = (R)W[(MF + s) * sN + si];
+            w3 = DIM == 3 ? (R)W[(2 * MF + s) * sN + si] : R(0.0);
         } else {
             R dx = (R)cc[nb] - xi, dy = (R)cc[NT + nb] - yi;
             R dz = DIM == 3 ? (R)cc[2 * NT + nb] - zi : R(0.0);
@@ -499,12 +501,12 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                     if (!EXACT && D) {
                         if constexpr (FFG) {
                             const float* Dl = v.lsqd_lo;
-                            dx = FF((float)D[s * N + i], Dl[s * N + i]);
-                            dy = FF((float)D[(MF + s) * N + i], Dl[(MF + s) * N + i]);
-                            dz = DIM == 3 ? FF((float)D[(2 * MF + s) * N + i], Dl[(2 * MF + s) * N + i]) : FF(0.f);
+                            dx = FF((float)D[s * sN + si], Dl[s * sN + si]);
+                            dy = FF((float)D[(MF + s) * sN + si], Dl[(MF + s) * sN + si]);
+                            dz = DIM == 3 ? FF((float)D[(2 * MF + s) * sN + si], Dl[(2 * MF + s) * sN + si]) : FF(0.f);
                         } else {
-                            dx = (R)D[s * N + i]; dy = (R)D[(MF + s) * N + i];
-                            dz = DIM == 3 ? (R)D[(2 * MF + s) * N + i] : R(0.0);
+                            dx = (R)D[s * sN + si]; dy = (R)D[(MF + s) * sN + si];
+                            dz = DIM == 3 ? (R)D[(2 * MF + s) * sN + si] : R(0.0);
                         }
                     } else if constexpr (REL) {
                         dx = (R)((double)fcen[f] - xid); dy = (R)((double)fcen[F + f] - yid);
@@ -536,12 +538,12 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
                     if (D) {  // face offsets stored per slot
                         if constexpr (FFG) {
                             const float* Dl = v.lsqd_lo;
-                            dx = FF((float)D[s * N + i], Dl[s * N + i]);
-                            dy = FF((float)D[(MF + s) * N + i], Dl[(MF + s) * N + i]);
-                            dz = DIM == 3 ? FF((float)D[(2 * MF + s) * N + i], Dl[(2 * MF + s) * N + i]) : FF(0.f);
+                            dx = FF((float)D[s * sN + si], Dl[s * sN + si]);
+                            dy = FF((float)D[(MF + s) * sN + si], Dl[(MF + s) * sN + si]);
+                            dz = DIM == 3 ? FF((float)D[(2 * MF + s) * sN + si], Dl[(2 * MF + s) * sN + si]) : FF(0.f);
                         } else {
-                            dx = (R)D[s * N + i]; dy = (R)D[(MF + s) * N + i];
-                            dz = DIM == 3 ? (R)D[(2 * MF + s) * N + i] : R(0.0);
+                            dx = (R)D[s * sN + si]; dy = (R)D[(MF + s) * sN + si];
+                            dz = DIM == 3 ? (R)D[(2 * MF + s) * sN + si] : R(0.0);
                         }
                     } else {
                         const int f = v.cell_face[s * N + i];

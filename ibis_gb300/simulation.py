@@ -314,6 +314,13 @@ class Simulation:
             raise ValueError("face must be (13, F) and cell (4, N+G)")
         self._call("ibisgb_set_geometry", _ptr(f), _ptr(c))
 
+    def lsq_shared(self, precision: str = "mixed") -> bool:
+        """Whether the least-squares weights and face offsets of `precision` are kept
+        once per face slot (every cell's bitwise the same: a uniform lattice)."""
+        out = C.c_int32()
+        self._call("ibisgb_lsq_shared", PRECISION[precision], C.byref(out))
+        return bool(out.value)
+
     _FS_KEYS = ("T", "p", "rho", "energy", "vx", "vy", "vz")
 
     def boundary_tags(self) -> list:

@@ -227,6 +227,18 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
  * the reference (its GridBlock is built once from the SU2 file). */
 int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell);
 
+/* Whether the least-squares weights and the limiter's face offsets of arithmetic
+ * `precision` are stored once per face slot (*shared = 1) rather than per cell
+ * (0).  They are when every cell's are bitwise the same in that arithmetic's
+ * storage type -- a uniform lattice, such as the benchmark's periodic box -- and
+ * the config's grid.lsq_tables is "auto" (the default; "per_cell" keeps them per
+ * cell).  The reconstruction then reads one row per slot that every thread shares
+ * instead of 24 values per cell; the values, and so the results, are the same.
+ * Uploads the geometry of that arithmetic if it is not on the device yet.  No
+ * counterpart in the reference (WLSGradient keeps per-cell factors,
+ * gradient.h:89-162). */
+int ibisgb_lsq_shared(ibisgb_ctx* ctx, int32_t precision, int32_t* shared);
+
 /* Replaces the flow state (7 doubles: T, p, rho, energy, vx, vy, vz -- the
  * "flow_state" object of the config) of boundary `tag`: every action of it that
  * carries one takes fs, as if the config had given it (FlowStateCopy and
