@@ -86,7 +86,7 @@ def load(build_if_missing: bool = True):
     L.ibisgb_get_dump.argtypes = [_P, C.c_int32, _P, C.c_int64]
     L.ibisgb_set_geometry.argtypes = [_P, _P, _P]
     L.ibisgb_set_flow_state.argtypes = [_P, C.c_char_p, _P]
-    L.ibisgb_lsq_shared.argtypes = [_P, C.c_int32, C.POINTER(C.c_int32)]
+    L.ibisgb_shared_tables.argtypes = [_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.ibisgb_get_flow_state.argtypes = [_P, C.c_char_p, _P]
     L.ibisgb_vjp_flow_state.argtypes = [_P, _P, _P, C.c_int32]
     L.ibisgb_vjp_flow_state_device.argtypes = [_P, _P, _P, C.c_int32, _P]

@@ -8,6 +8,8 @@
 #include <cstring>
 #include <functional>
 #include <limits>
+#include <map>
+#include <array>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -80,6 +82,8 @@ struct StateBufs {
     bool geometry = false;
     bool prims_current = false;
     bool lsq_shared = false;  // lsqw / lsqd (and their lo parts) hold one row per slot, the same for every cell
+    DBuf face_class, face_class_tab;  // float build: class of each face, and each class's row (kFaceClassRow)
+    int n_face_classes = 0;           // 0: the face kernels read the per-face arrays
 };
 
 // Whether every column c of the rows x N array a (row-major [rows][N]) is
@@ -93,6 +97,45 @@ bool shared_column(const std::vector<T>& a, int64_t rows, int64_t N, std::vector
     col.resize(rows);
     for (int64_t r = 0; r < rows; r++) col[r] = a[r * N];
     return true;
+}
+
+// The faces of a uniform lattice fall into a few classes whose geometry, as the
+// float face kernel reads it, is bitwise the same: the normal, the 2-D tangents
+// (t1 x, t1 y, t2 z; the 3-D kernel forms its frame from n) and each valid side's
+// reconstruction offset (face centre - centroid, the float subtraction the kernel
+// does).  On success cls holds each face's class and tab one kFaceClassRow row per
+// class; false when the faces have more than kMaxFaceClasses distinct rows.
+bool face_classes(const std::vector<float>& fc, const std::vector<float>& cc, const Mesh& mesh,
+                  std::vector<uint8_t>& cls, std::vector<float>& tab) {
+    const int64_t F = mesh.F, N = mesh.N, NT = mesh.NT();
+    const bool three = mesh.dim == 3;
+    std::map<std::array<uint32_t, kFaceClassRow>, int> index;
+    cls.assign(F, 0);
+    tab.clear();
+    for (int64_t f = 0; f < F; f++) {
+        float row[kFaceClassRow] = {};
+        for (int k = 0; k < 3; k++) row[k] = fc[k * F + f];
+        if (!three) { row[3] = fc[3 * F + f]; row[4] = fc[4 * F + f]; row[5] = fc[8 * F + f]; }
+        const int64_t side[2] = {mesh.left[f], mesh.right[f]};
+        for (int sd = 0; sd < 2; sd++) {
+            const int64_t c = side[sd];
+            if (c >= N) continue;
+            for (int k = 0; k < 3; k++) {
+                const float a = fc[(9 + k) * F + f], b = cc[k * NT + c];
+                row[6 + 3 * sd + k] = a - b;
+            }
+        }
+        std::array<uint32_t, kFaceClassRow> key;
+        std::memcpy(key.data(), row, sizeof(row));
+        auto it = index.find(key);
+        if (it == index.end()) {
+            if ((int)index.size() == kMaxFaceClasses) return false;
+            it = index.emplace(key, (int)index.size()).first;
+            tab.insert(tab.end(), row, row + kFaceClassRow);
+        }
+        cls[f] = (uint8_t)it->second;
+    }
+    return F > 0;
 }
 
 ActionKind parse_action_kind(const std::string& t) {
@@ -318,12 +361,12 @@ struct ibisgb_ctx {
                 else if (r == "none") renumber_mode = 2;
                 else throw ConfigError("grid.renumber must be auto, rcm or none");
             }
-            lsq_shared_mode = 0;
-            if (grid.contains("lsq_tables")) {  // not a reference key: the layout of the least-squares tables
-                const std::string t = grid.at("lsq_tables").as_string();
-                if (t == "auto") lsq_shared_mode = 0;
-                else if (t == "per_cell") lsq_shared_mode = 1;
-                else throw ConfigError("grid.lsq_tables must be auto or per_cell");
+            shared_tables_mode = 0;
+            if (grid.contains("geometry_tables")) {  // not a reference key: the layout of the geometry tables
+                const std::string t = grid.at("geometry_tables").as_string();
+                if (t == "auto") shared_tables_mode = 0;
+                else if (t == "per_element") shared_tables_mode = 1;
+                else throw ConfigError("grid.geometry_tables must be auto or per_element");
             }
             prm.fR = (float)prm.R; prm.fCv = (float)prm.Cv; prm.fCp = (float)prm.Cp;
             prm.fgamma = (float)prm.gamma; prm.fgR = prm.fgamma * prm.fR; prm.feps = (float)prm.eps;
@@ -497,9 +540,11 @@ struct ibisgb_ctx {
     // reference's numbering (grid.h:113-133).  Per-cell and per-face arithmetic and
     // summation orders are unchanged, so the results are the same bits.
     int renumber_mode = 0;  // 0 auto, 1 rcm, 2 none
-    // 0 auto: least-squares weights and face offsets stored once per slot when every
-    // cell's are bitwise the same (a uniform lattice); 1: always per cell
-    int lsq_shared_mode = 0;
+    // 0 auto: on a uniform lattice, the least-squares weights and face offsets stored
+    // once per slot (every cell's bitwise the same) and, for the float build, each
+    // face's normal and side offsets as a class index into a small table; 1: always
+    // per cell and per face
+    int shared_tables_mode = 0;
     MeshNumbering num;
     int64_t bandwidth_ref = 0, bandwidth_internal = 0;
     DBuf d_cell_to_new, d_cell_to_ref, map_a, map_b;
@@ -873,7 +918,7 @@ struct ibisgb_ctx {
         // so the results, do not change.
         std::vector<Gm> w1, d1;
         std::vector<float> wl1, dl1;
-        s.lsq_shared = lsq_shared_mode == 0 && !w.empty() && shared_column(w, rows, N, w1) &&
+        s.lsq_shared = shared_tables_mode == 0 && !w.empty() && shared_column(w, rows, N, w1) &&
                        (d.empty() || shared_column(d, rows, N, d1)) &&
                        (wl.empty() || shared_column(wl, rows, N, wl1)) &&
                        (dl.empty() || shared_column(dl, rows, N, dl1));
@@ -881,6 +926,16 @@ struct ibisgb_ctx {
         if (!d.empty()) upload(s.lsqd, s.lsq_shared ? d1 : d, stream);
         if (!wl.empty()) upload(s.lsqw_lo, s.lsq_shared ? wl1 : wl, stream);
         if (!dl.empty()) upload(s.lsqd_lo, s.lsq_shared ? dl1 : dl, stream);
+        if constexpr (sizeof(Gm) == sizeof(float)) {
+            s.n_face_classes = 0;
+            std::vector<uint8_t> fcls;
+            std::vector<float> ftab;
+            if (shared_tables_mode == 0 && !with_lo && face_classes(fc, cc, mesh, fcls, ftab)) {
+                upload(s.face_class, fcls, stream);
+                upload(s.face_class_tab, ftab, stream);
+                s.n_face_classes = (int)(ftab.size() / kFaceClassRow);
+            }
+        }
         size_t P = sizeof(Gm);
         s.prim.alloc(P * 7 * NT);
         s.vghost.alloc(P * 5 * std::max<int64_t>(mesh.G, 1));
@@ -921,6 +976,8 @@ struct ibisgb_ctx {
         v.inv_vol = inv_vol.as<double>(); v.inv_vol2 = inv_vol2.as<float2>(); v.lsqw = s.lsqw.p;
         v.lsqd = s.lsqd.p;
         v.lsq_shared = s.lsq_shared ? 1 : 0;
+        v.face_class = s.n_face_classes ? s.face_class.as<uint8_t>() : nullptr;
+        v.face_class_tab = s.n_face_classes ? s.face_class_tab.as<float>() : nullptr;
         v.prim = (is_mixed(prec) && prim_cur) ? prim_alt.p : s.prim.p;
         v.vghost = s.vghost.p; v.grad = s.grad.p; v.phi = s.phi.p;
         v.vgrad = s.vgrad.p; v.flux = s.flux.p; v.vsig = vsig.as<double>();
@@ -2822,11 +2879,12 @@ int ibisgb_vjp_flow_state(ibisgb_ctx* ctx, const double* w, double* out, int32_t
     });
 }
 
-int ibisgb_lsq_shared(ibisgb_ctx* ctx, int32_t precision, int32_t* shared) {
-    if (!ctx || !shared || precision < 0 || precision > IBISGB_MIXED_FF) return IBISGB_ERR_ARG;
+int ibisgb_shared_tables(ibisgb_ctx* ctx, int32_t precision, int32_t* lsq_shared, int32_t* face_classes) {
+    if (!ctx || precision < 0 || precision > IBISGB_MIXED_FF) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] {
         ctx->ensure_geometry(precision);
-        *shared = ctx->bufs(precision).lsq_shared ? 1 : 0;
+        if (lsq_shared) *lsq_shared = ctx->bufs(precision).lsq_shared ? 1 : 0;
+        if (face_classes) *face_classes = ctx->bufs(precision).n_face_classes;
     });
 }
 

@@ -815,7 +815,13 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
         if constexpr (FFR) return FF((float)pr[k * NT + c], v.prim_lo[k * NT + c]);
         else return (R)pr[k * NT + c];
     };
-    const R nx = geo(0), ny = geo(1), nz = DIM == 3 ? geo(2) : R(0.0);
+    // a uniform lattice's face class (float build): the normal, the 2-D tangents and
+    // the sides' offsets from the class's row, the same values the arrays hold
+    const float* ct = nullptr;
+    if constexpr (!FFR && !EXACT && sizeof(R) == sizeof(float) && sizeof(Gm) == sizeof(float))
+        if (v.face_class) ct = v.face_class_tab + kFaceClassRow * v.face_class[f];
+    const R nx = ct ? (R)ct[0] : geo(0), ny = ct ? (R)ct[1] : geo(1);
+    const R nz = DIM == 3 ? (ct ? (R)ct[2] : geo(2)) : R(0.0);
     R t1x, t1y, t1z, t2x, t2y, t2z;
     if constexpr (!EXACT && sizeof(R) == sizeof(float) && DIM == 3) {
         // The float build rotates into a frame built from n (any orthonormal
@@ -832,11 +838,12 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
         t2y = nz * t1x - nx * t1z;
         t2z = nx * t1y - ny * t1x;
     } else {
-        t1x = geo(3); t1y = geo(4); t1z = DIM == 3 ? geo(5) : R(0.0);
+        t1x = ct ? (R)ct[3] : geo(3); t1y = ct ? (R)ct[4] : geo(4); t1z = DIM == 3 ? geo(5) : R(0.0);
         t2x = DIM == 3 ? geo(6) : R(0.0); t2y = DIM == 3 ? geo(7) : R(0.0);
-        t2z = geo(8);
+        t2z = ct ? (R)ct[5] : geo(8);
     }
-    const R fx = geo(9), fy = geo(10), fz = DIM == 3 ? geo(11) : R(0.0);
+    const R fx = ct ? R(0.0) : geo(9), fy = ct ? R(0.0) : geo(10);
+    const R fz = DIM == 3 && !ct ? geo(11) : R(0.0);
     int ia, ib;
     thermo_vars(prm.thermo, ia, ib);
     const int cells[2] = {v.left[f], v.right[f]};
@@ -852,7 +859,12 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
             q[k] = (DIM == 2 && k == 6) || (reconstruct && k < 4 && k != ia && k != ib) ? R(0.0)
                                                                                     : prim(k, c);
         if (reconstruct && c < N) {
-            R dx = fx - cen(0, c), dy = fy - cen(1, c), dz = DIM == 3 ? fz - cen(2, c) : R(0.0);
+            R dx, dy, dz;
+            if (ct) {
+                dx = (R)ct[6 + 3 * side]; dy = (R)ct[7 + 3 * side]; dz = DIM == 3 ? (R)ct[8 + 3 * side] : R(0.0);
+            } else {
+                dx = fx - cen(0, c); dy = fy - cen(1, c); dz = DIM == 3 ? fz - cen(2, c) : R(0.0);
+            }
             if constexpr (prescaled_gradients<P, EXACT>()) {
                 // packed limiter-scaled gradients: q_f = q + (phi grad) . d
                 const float4* src = (const float4*)v.grad + (size_t)c * (kPackedGrad / 4);

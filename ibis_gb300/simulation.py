@@ -314,12 +314,14 @@ class Simulation:
             raise ValueError("face must be (13, F) and cell (4, N+G)")
         self._call("ibisgb_set_geometry", _ptr(f), _ptr(c))
 
-    def lsq_shared(self, precision: str = "mixed") -> bool:
-        """Whether the least-squares weights and face offsets of `precision` are kept
-        once per face slot (every cell's bitwise the same: a uniform lattice)."""
-        out = C.c_int32()
-        self._call("ibisgb_lsq_shared", PRECISION[precision], C.byref(out))
-        return bool(out.value)
+    def shared_tables(self, precision: str = "mixed") -> dict:
+        """The geometry-table layout of `precision` (ibisgb_shared_tables): lsq_shared,
+        whether the least-squares weights and face offsets are kept once per face slot
+        (a uniform lattice), and face_classes, the number of shared face-geometry rows
+        (0: per face)."""
+        a, b = C.c_int32(), C.c_int32()
+        self._call("ibisgb_shared_tables", PRECISION[precision], C.byref(a), C.byref(b))
+        return {"lsq_shared": bool(a.value), "face_classes": int(b.value)}
 
     _FS_KEYS = ("T", "p", "rho", "energy", "vx", "vy", "vz")
 

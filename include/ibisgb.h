@@ -227,17 +227,25 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
  * the reference (its GridBlock is built once from the SU2 file). */
 int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell);
 
-/* Whether the least-squares weights and the limiter's face offsets of arithmetic
- * `precision` are stored once per face slot (*shared = 1) rather than per cell
- * (0).  They are when every cell's are bitwise the same in that arithmetic's
- * storage type -- a uniform lattice, such as the benchmark's periodic box -- and
- * the config's grid.lsq_tables is "auto" (the default; "per_cell" keeps them per
- * cell).  The reconstruction then reads one row per slot that every thread shares
- * instead of 24 values per cell; the values, and so the results, are the same.
- * Uploads the geometry of that arithmetic if it is not on the device yet.  No
- * counterpart in the reference (WLSGradient keeps per-cell factors,
- * gradient.h:89-162). */
-int ibisgb_lsq_shared(ibisgb_ctx* ctx, int32_t precision, int32_t* shared);
+/* The geometry-table layout of arithmetic `precision` on this grid.  On a
+ * uniform lattice -- the benchmark's periodic box -- and with the config's
+ * grid.geometry_tables "auto" (the default; "per_element" keeps every table per
+ * cell and per face):
+ *  - *lsq_shared = 1 when the least-squares weights and the limiter's face
+ *    offsets are stored once per face slot, every cell's being bitwise the same
+ *    in that arithmetic's storage type; the reconstruction then reads one row per
+ *    slot that every thread shares instead of 24 values per cell;
+ *  - *face_classes = the number of face classes (MIXED only, else 0): faces whose
+ *    normal, 2-D tangents and side offsets (face centre - centroid, as the float
+ *    face kernel forms them) are bitwise the same share a row, and each face
+ *    keeps a one-byte class instead of its normal and centre and the gathers of
+ *    its cells' centroids; 0 when there are more than 64 distinct rows.
+ * The values, and so the results, are the same as with the per-element tables.
+ * Uploads the geometry of that arithmetic if it is not on the device yet.  Either
+ * pointer may be NULL.  No counterpart in the reference (WLSGradient and the
+ * interfaces keep per-cell and per-face geometry, gradient.h:89-162,
+ * interface.h:180-251). */
+int ibisgb_shared_tables(ibisgb_ctx* ctx, int32_t precision, int32_t* lsq_shared, int32_t* face_classes);
 
 /* Replaces the flow state (7 doubles: T, p, rho, energy, vx, vy, vz -- the
  * "flow_state" object of the config) of boundary `tag`: every action of it that

@@ -1,8 +1,10 @@
-"""Least-squares tables stored once per face slot on uniform lattices
-(grid.lsq_tables "auto"): the same bits as the per-cell tables ("per_cell") in
-every arithmetic -- residual, limiter values and branches, Runge-Kutta steps --
-on the periodic box and a 2-D channel whose cells are all alike, and the
-per-cell tables kept wherever the cells differ."""
+"""Shared geometry tables on uniform lattices (grid.geometry_tables "auto"):
+least-squares weights and face offsets stored once per face slot, and the float
+build's face classes (one-byte class per face into shared rows of normal and
+side offsets).  The same bits as the per-element tables ("per_element") in every
+arithmetic -- residual, limiter values and branches, Runge-Kutta steps -- on
+the periodic box and a 2-D channel whose cells are all alike, and per-element
+tables wherever the cells differ."""
 import copy
 
 import numpy as np
@@ -28,9 +30,9 @@ def uniform_channel():
 
 def pair(g, c, st):
     out = []
-    for mode in ("auto", "per_cell"):
+    for mode in ("auto", "per_element"):
         cc = copy.deepcopy(c)
-        cc["grid"]["lsq_tables"] = mode
+        cc["grid"]["geometry_tables"] = mode
         sim = Simulation(cc, g)
         sim.set_primitives(*st)
         out.append(sim)
@@ -48,7 +50,9 @@ def test_shared_tables_give_the_same_bits(which):
             random_state(g.num_cells, 1.0, 1.0, 0.3, 3, seed=13, amp=0.05)
     a, b = pair(g, c, st)
     for prec in ("mixed", "mixed_ff", "f64"):
-        assert a.lsq_shared(prec) and not b.lsq_shared(prec), prec
+        ta, tb = a.shared_tables(prec), b.shared_tables(prec)
+        assert ta["lsq_shared"] and not tb["lsq_shared"] and tb["face_classes"] == 0, prec
+        assert (0 < ta["face_classes"] <= 64) == (prec == "mixed"), (prec, ta)
         assert np.array_equal(a.compute_dudt(prec), b.compute_dudt(prec)), prec
     a.compute_dudt("mixed")
     b.compute_dudt("mixed")
@@ -63,8 +67,12 @@ def test_shared_tables_give_the_same_bits(which):
 
 @pytest.mark.parametrize("name", ["ramp", "tet", "plate"])
 def test_cells_that_differ_keep_per_cell_tables(name):
+    """Cells that differ keep per-cell least-squares tables; faces keep classes only
+    where at most 64 distinct rows exist, and either way the bits do not change."""
     g, c, st = case(name)
-    sim = Simulation(c, g)
-    sim.set_primitives(*st)
+    a, b = pair(g, c, st)
     for prec in ("mixed", "mixed_ff", "f64"):
-        assert not sim.lsq_shared(prec), prec
+        assert not a.shared_tables(prec)["lsq_shared"], prec
+        assert np.array_equal(a.compute_dudt(prec), b.compute_dudt(prec)), prec
+    if name == "ramp":
+        assert a.shared_tables("mixed")["face_classes"] == 0
