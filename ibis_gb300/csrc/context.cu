@@ -8,8 +8,6 @@
 #include <cstring>
 #include <functional>
 #include <limits>
-#include <map>
-#include <array>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -109,7 +107,7 @@ bool face_classes(const std::vector<float>& fc, const std::vector<float>& cc, co
                   std::vector<uint8_t>& cls, std::vector<float>& tab) {
     const int64_t F = mesh.F, N = mesh.N, NT = mesh.NT();
     const bool three = mesh.dim == 3;
-    std::map<std::array<uint32_t, kFaceClassRow>, int> index;
+    int n = 0, last = 0;  // classes so far; the last face's (neighbouring faces mostly share one)
     cls.assign(F, 0);
     tab.clear();
     for (int64_t f = 0; f < F; f++) {
@@ -125,15 +123,17 @@ bool face_classes(const std::vector<float>& fc, const std::vector<float>& cc, co
                 row[6 + 3 * sd + k] = a - b;
             }
         }
-        std::array<uint32_t, kFaceClassRow> key;
-        std::memcpy(key.data(), row, sizeof(row));
-        auto it = index.find(key);
-        if (it == index.end()) {
-            if ((int)index.size() == kMaxFaceClasses) return false;
-            it = index.emplace(key, (int)index.size()).first;
+        auto same = [&](int k) { return std::memcmp(&tab[(size_t)k * kFaceClassRow], row, sizeof(row)) == 0; };
+        int k = n > 0 && same(last) ? last : -1;
+        for (int j = 0; k < 0 && j < n; j++)
+            if (same(j)) k = j;
+        if (k < 0) {
+            if (n == kMaxFaceClasses) return false;
             tab.insert(tab.end(), row, row + kFaceClassRow);
+            k = n++;
         }
-        cls[f] = (uint8_t)it->second;
+        cls[f] = (uint8_t)k;
+        last = k;
     }
     return F > 0;
 }

@@ -479,7 +479,14 @@ __global__ void __launch_bounds__(BS, MINB) k_recon(DevView v, FvParams prm, int
             }
         }
     };
-    for (int s = 0; s < nf; s++) slot(s, v.cell_nbr[s * N + i]);
+    // each slot's neighbour id is loaded while the previous slot's values are in
+    // flight, so that the gathers do not wait for the id load in turn
+    int nb_next = nf > 0 ? v.cell_nbr[i] : 0;
+    for (int s = 0; s < nf; s++) {
+        const int nb = nb_next;
+        if (s + 1 < nf) nb_next = v.cell_nbr[(s + 1) * N + i];
+        slot(s, nb);
+    }
 
     if (reconstruct) {
         P* gout = (P*)v.grad;
