@@ -95,5 +95,6 @@ def test_roofline_block_follows_the_stage_path_in_use():
     t3, tm = bench.stage_traffic(s3, 256), bench.stage_traffic(sm, 256)
     assert t3 == 8 * bench.stage_traffic(s3, 128) and tm == 8 * bench.stage_traffic(sm, 128)
     n = 256 ** 3
-    assert 700 < t3 / n < 900 and 250 < tm / n < 320  # B per cell-update: three kernels vs one marching kernel
+    # B per cell-update: three kernels (shared geometry tables on the uniform box) vs one marching kernel
+    assert 450 < t3 / n < 700 and 250 < tm / n < 320
     assert bench.stage_traffic(s3, 64) is None and bench.stage_traffic(None, 256) is None
