@@ -90,6 +90,8 @@ def load(build_if_missing: bool = True):
     L.ibisgb_get_flow_state.argtypes = [_P, C.c_char_p, _P]
     L.ibisgb_vjp_flow_state.argtypes = [_P, _P, _P, C.c_int32]
     L.ibisgb_vjp_flow_state_device.argtypes = [_P, _P, _P, C.c_int32, _P]
+    L.ibisgb_jvp_flow_state.argtypes = [_P, _P, _P, C.c_int32]
+    L.ibisgb_jvp_flow_state_device.argtypes = [_P, _P, _P, C.c_int32, _P]
     L.ibisgb_numbering.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.ibisgb_synchronize.argtypes = [_P]
     L.ibisgb_set_conserved.argtypes = [_P, _P]

@@ -138,7 +138,8 @@ class ResidualFlowState(torch.autograd.Function):
     installs the flow state on every action of the boundary that carries one
     (ibisgb_set_flow_state); the backward pass is the state adjoint and the
     flow-state adjoint (ibisgb_vjp / ibisgb_vjp_flow_state) chained through
-    rho = p / (R T), energy = Cv T."""
+    rho = p / (R T), energy = Cv T, forward mode the two tangents (ibisgb_jvp /
+    ibisgb_jvp_flow_state)."""
 
     @staticmethod
     def forward(ctx, U, theta, sim, tag):
@@ -153,6 +154,7 @@ class ResidualFlowState(torch.autograd.Function):
         _py.residual(sim, _F64_EXACT, out)
         ctx.sim, ctx.tag = sim, tag
         ctx.save_for_backward(U, theta)
+        ctx.save_for_forward(U, theta)
         return out
 
     @staticmethod
@@ -174,6 +176,31 @@ class ResidualFlowState(torch.autograd.Function):
         gT = g[0] - g[2] * p / (R * T * T) + g[3] * gas["Cv"]
         gp = g[1] + g[2] / (R * T)
         return gU, torch.stack([gT, gp, g[4], g[5], g[6]]).reshape(theta.shape), None, None
+
+    @staticmethod
+    def jvp(ctx, dU, dtheta, _sim, _tag):
+        U, theta = ctx.saved_tensors
+        sim = ctx.sim
+        _py.set_flow_state(sim, ctx.tag, _flow_state_values(sim, theta))
+        _py.set_conserved(sim, U)
+        out = torch.zeros_like(U)
+        if dU is not None:
+            _py.jvp(sim, dU.contiguous(), out, 0.0)
+            out = -out  # the product is inv_dt v - J v
+        if dtheta is not None:
+            # the direction of the 7 flow-state entries: rho = p / (R T), energy = Cv T
+            gas = sim.config["gas_model"]
+            T, p = (float(x) for x in theta.detach().cpu()[:2])
+            dT, dp, dvx, dvy, dvz = (float(x) for x in dtheta.detach().cpu().reshape(5))
+            R = gas["R"]
+            row = [dT, dp, dp / (R * T) - p * dT / (R * T * T), gas["Cv"] * dT, dvx, dvy, dvz]
+            tags = sorted(sim.config["grid"]["boundaries"].keys())
+            d = torch.zeros((len(tags), 7), dtype=torch.float64, device=U.device)
+            d[tags.index(ctx.tag)] = torch.tensor(row, dtype=torch.float64, device=U.device)
+            g = torch.empty_like(U)
+            _py.jvp_flow_state(sim, d, g)
+            out = out + g
+        return out
 
 
 def residual_flow_state(sim, U, theta, tag: str = "inflow"):

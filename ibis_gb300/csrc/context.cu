@@ -1731,6 +1731,25 @@ struct ibisgb_ctx {
                               stream);
         CUDA_OK(cudaGetLastError());
     }
+    // out (N x nc rows, internal numbering) = dR/dfs . dfs for a direction dfs of
+    // every boundary's flow state (num_boundaries x 7, device), the actions of a
+    // boundary that carry a flow state moving together
+    void jvp_flow_state(const double* dfs_dev, double* out_dev, bool reconstruct) {
+        if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
+        if (n_cases > 1) throw StateError("a batch's boundary states belong to its cases");
+        DevView v = tangent_view();
+        v.fs_tan = dfs_dev;
+        launch_tangent(v, prm, nullptr, 0.0, reconstruct && prm.order == 2, out_dev, stream);  // -dR/dfs . dfs
+        RowScale neg{{-1.0, -1.0, -1.0, -1.0, -1.0}};
+        launch_scale_rows(out_dev, out_dev, (long long)nvars(), nc(), neg, stream);
+        CUDA_OK(cudaGetLastError());
+    }
+    void jvp_flow_state_rows(const double* dfs_dev, double* out_rows, bool reconstruct) {
+        if (!renumbered()) return jvp_flow_state(dfs_dev, out_rows, reconstruct);
+        map_b.alloc(sizeof(double) * nvars());
+        jvp_flow_state(dfs_dev, map_b.as<double>(), reconstruct);
+        map_rows_device(map_b.as<double>(), out_rows, nc(), false);
+    }
     void vjp_flow_state_rows(const double* w, double* out_dev, bool reconstruct) {
         if (!renumbered()) return vjp_flow_state(w, out_dev, reconstruct);
         map_a.alloc(sizeof(double) * nvars());
@@ -2860,6 +2879,43 @@ int ibisgb_vjp_flow_state_device(ibisgb_ctx* ctx, const double* w_device, double
             CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
             CUDA_OK(cudaEventDestroy(ev));
         }
+    });
+}
+
+int ibisgb_jvp_flow_state_device(ibisgb_ctx* ctx, const double* dfs_device, double* out_device,
+                                 int32_t allow_reconstruction, void* stream) {
+    if (!ctx || !dfs_device || !out_device) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        ctx->ensure_device();
+        if (user && user != ctx->stream) {
+            CUDA_OK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CUDA_OK(cudaEventRecord(ev, user));
+            CUDA_OK(cudaStreamWaitEvent(ctx->stream, ev, 0));
+        }
+        ctx->jvp_flow_state_rows(dfs_device, out_device, allow_reconstruction != 0);
+        if (ev) {
+            CUDA_OK(cudaEventRecord(ev, ctx->stream));
+            CUDA_OK(cudaStreamWaitEvent(user, ev, 0));
+            CUDA_OK(cudaEventDestroy(ev));
+        }
+    });
+}
+
+int ibisgb_jvp_flow_state(ibisgb_ctx* ctx, const double* dfs, double* out, int32_t allow_reconstruction) {
+    if (!ctx || !dfs || !out) return IBISGB_ERR_ARG;
+    return guarded(ctx, [&] {
+        ctx->ensure_device();
+        const size_t n = ctx->nvars(), nb = 7 * ctx->mesh.bounds.size();
+        ctx->ensure_krylov(1);
+        ctx->geo_out_face.alloc(sizeof(double) * std::max(nb, (size_t)1));
+        if (nb)
+            CUDA_OK(cudaMemcpyAsync(ctx->geo_out_face.p, dfs, sizeof(double) * nb, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+        ctx->jvp_flow_state_rows(ctx->geo_out_face.as<double>(), ctx->kw.as<double>(), allow_reconstruction != 0);
+        CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
 }
 

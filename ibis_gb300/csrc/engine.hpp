@@ -125,6 +125,10 @@ struct DevView {
     // classes' rows (n; 2-D t1 x, t1 y, t2 z; left and right offsets face centre - centroid)
     const unsigned char* face_class;  // [F]
     const float* face_class_tab;      // [classes][kFaceClassRow]
+    // flow-state tangent only, else null: a tangent direction of each boundary's
+    // flow state (T, p, rho, energy, vx, vy, vz), seeded by the dual ghost fill and
+    // the dual constant-flux faces
+    const double* fs_tan;  // [bounds][7]
     // state (type P)
     void* prim;    // [7][NT]: rho, p, T, e, vx, vy, vz
     void* vghost;  // [5][G]: p, T, vx, vy, vz after the pre-viscous-gradient actions

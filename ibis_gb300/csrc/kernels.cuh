@@ -251,7 +251,10 @@ __device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const S
     const Gm* face = (const Gm*)v.face;
     int f = v.ghost_face[g];
     StateT<S> gh = src;
-    apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm, v.gfix, v.G, g, v.face_lo);
+    const double* fs_dir = nullptr;  // the flow-state tangent's direction for this boundary
+    if constexpr (kIsDual<S>)
+        if (v.fs_tan) fs_dir = v.fs_tan + 7 * (size_t)v.ghost_bound[g];
+    apply_actions<S, Gm>(B.pre, B.n_pre, gh, src, face, v.F, f, prm, v.gfix, v.G, g, v.face_lo, fs_dir);
     P* pr = (P*)v.prim;
     const int NT = v.NT, id = v.N + g;
     if constexpr (kFFBuild && sizeof(P) == sizeof(float) && !kIsDual<S>) {
@@ -268,7 +271,7 @@ __device__ void fill_ghost(const DevView& v, const FvParams& prm, int g, const S
         pr[5 * NT + id] = to_storage<P>(gh.vy); pr[6 * NT + id] = to_storage<P>(gh.vz);
     }
     if (prm.viscous) {
-        apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm, v.gfix, v.G, g, v.face_lo);
+        apply_actions<S, Gm>(B.visc, B.n_visc, gh, src, face, v.F, f, prm, v.gfix, v.G, g, v.face_lo, fs_dir);
         P* vg = (P*)v.vghost;
         if constexpr (kFFBuild && sizeof(P) == sizeof(float) && !kIsDual<S>) {
             const double w[5] = {gh.p, gh.T, gh.vx, gh.vy, gh.vz};
@@ -927,8 +930,19 @@ __device__ __forceinline__ void face_convective(const DevView& v, const FvParams
     }
     convective_flux<R, DIM, EXACT>(prm, gm, S[0], S[1], nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z, Fg);
     if (prm.cflux) {  // apply_post_convective_flux_bc (finite_volume.cpp:71, 197-209)
-        if (const BoundDev* B = constant_flux_bound(v, cells[0], cells[1]))
-            constant_flux<R, DIM>(B->cfs, prm.Cv, nx, ny, nz, Fg);
+        if (const BoundDev* B = constant_flux_bound(v, cells[0], cells[1])) {
+            bool seeded = false;
+            if constexpr (kIsDual<R>)
+                if (v.fs_tan) {  // the flow-state tangent: the fixed state carries its direction
+                    const double* d = v.fs_tan + 7 * (size_t)(B - v.bounds);
+                    R fsd[7];
+#pragma unroll
+                    for (int k = 0; k < 7; k++) fsd[k] = R(B->cfs[k], d[k]);
+                    constant_flux<R, DIM>(fsd, prm.Cv, nx, ny, nz, Fg);
+                    seeded = true;
+                }
+            if (!seeded) constant_flux<R, DIM>(B->cfs, prm.Cv, nx, ny, nz, Fg);
+        }
     }
     nx_out = nx;
     ny_out = ny;

@@ -491,6 +491,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevView v, FvParams prm, in
     const int nf = v.nfaces[i];
     for (int s = 0; s < MF; s++)
         for (int m = 0; m < 7; m++) nba[((size_t)m * MF + s) * N + i] = 0.0;
+    if (a.geo_nbc)  // every slot and coordinate: pass 3 reads all three, a 2-D grid writes two
+        for (int s = 0; s < MF; s++)
+            for (int d = 0; d < 3; d++) a.geo_nbc[((size_t)d * MF + s) * N + i] = 0.0;
     const double* fg = (const double*)v.face;
     const double* cc = (const double*)v.cc;
     const double* rr = (const double*)v.r;

@@ -155,4 +155,15 @@ PYBIND11_MODULE(_ibisgb_py, m) {
         },
         py::arg("sim"), py::arg("w"), py::arg("out"), py::arg("allow_reconstruction") = true,
         "out (num_boundaries x 7, sorted tag order) = w^T dR/d(each boundary's flow state).");
+    m.def(
+        "jvp_flow_state",
+        [](py::object sim, py::object dfs, py::object out, bool allow_reconstruction) {
+            ibisgb_ctx* c = handle(sim);
+            const Sizes s = sizes(c);
+            const double* d = (const double*)device_ptr(dfs, "dfs", 7 * s.nb);
+            double* o = (double*)device_ptr(out, "out", s.n);
+            check(c, ibisgb_jvp_flow_state_device(c, d, o, allow_reconstruction ? 1 : 0, current_stream()));
+        },
+        py::arg("sim"), py::arg("dfs"), py::arg("out"), py::arg("allow_reconstruction") = true,
+        "out (N x n_conserved) = dR/dfs . dfs for dfs (num_boundaries x 7) a direction of every flow state.");
 }

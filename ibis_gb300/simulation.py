@@ -356,6 +356,17 @@ class Simulation:
         self._call("ibisgb_vjp_flow_state", _ptr(w), _ptr(out), int(allow_reconstruction))
         return {t: out[b].copy() for b, t in enumerate(tags)}
 
+    def flow_state_tangent(self, dfs: dict, allow_reconstruction: bool = True) -> np.ndarray:
+        """dR/dfs . dfs (ibisgb_jvp_flow_state) for {tag: direction of 7 (T, p, rho,
+        energy, vx, vy, vz)} (boundaries left out do not move); returns (N, n_conserved)."""
+        tags = self.boundary_tags()
+        d = np.zeros((max(len(tags), 1), 7))
+        for t, row in dfs.items():
+            d[tags.index(t)] = np.asarray(row, np.float64).reshape(7)
+        out = np.empty((self.num_cells, self.n_conserved))
+        self._call("ibisgb_jvp_flow_state", _ptr(d), _ptr(out), int(allow_reconstruction))
+        return out
+
     def geometry_tangent(self, dface, dcell, allow_reconstruction: bool = True) -> np.ndarray:
         """dR/dgeometry . (dface, dcell) (ibisgb_jvp_geometry) for dface (13, F) and
         dcell (4, N+G) in the layouts of the face / cell geometry dumps; returns

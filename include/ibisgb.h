@@ -281,6 +281,20 @@ int ibisgb_vjp_flow_state_device(ibisgb_ctx* ctx, const double* w_device, double
 /* As ibisgb_vjp_flow_state_device with host vectors. */
 int ibisgb_vjp_flow_state(ibisgb_ctx* ctx, const double* w, double* out, int32_t allow_reconstruction);
 
+/* out = dR/dfs . dfs: the tangent of the residual (N x n_conserved rows) along a
+ * direction dfs of every boundary's flow state (num_boundaries x 7, the layout of
+ * ibisgb_vjp_flow_state's output; rows of boundaries without a flow state are not
+ * read).  The dual ghost fill and the dual constant-flux faces carry the direction
+ * (every action of a boundary that carries a flow state moves together), on a
+ * state of zero tangent; ibisgb_vjp_flow_state is its transpose.  dfs_device and
+ * out_device are device memory, on `stream` (NULL: the context stream).  No
+ * counterpart in the reference. */
+int ibisgb_jvp_flow_state_device(ibisgb_ctx* ctx, const double* dfs_device, double* out_device,
+                                 int32_t allow_reconstruction, void* stream);
+
+/* As ibisgb_jvp_flow_state_device with host vectors. */
+int ibisgb_jvp_flow_state(ibisgb_ctx* ctx, const double* dfs, double* out, int32_t allow_reconstruction);
+
 /* The device arrays' cell and face order.  The grid's optional "renumber" key
  * ("auto" when absent, "rcm", "none"; not a reference key) selects it: "rcm"
  * orders the valid cells by reverse Cuthill-McKee over the interior-face graph

@@ -6,9 +6,10 @@ along a random flow-state perturbation (<w, dR/dfs . d> = <J_fs^T w, d> to
 1e-12; LDFSS2 against central differences) -- supersonic, subsonic and
 constant-flux inflows, the flow state
 copied before the viscous gradients, first and second order, 2-D and 3-D,
-every element type, the grid renumbered or not -- and the torch.autograd
-Function over the inflow parameters (T, p, vx, vy, vz) against central
-differences of the residual."""
+every element type, the grid renumbered or not -- the flow-state tangent
+ibisgb_jvp_flow_state equal to that dual derivative, and the torch.autograd
+Function over the inflow parameters (T, p, vx, vy, vz), reverse and forward
+mode, against central differences of the residual."""
 import copy
 
 import numpy as np
@@ -134,7 +135,30 @@ def test_flow_state_adjoint_matches_central_differences(flux):
     assert abs(fd - pred) <= 1e-5 * abs(pred), (fd, pred)
 
 
-def test_flow_state_adjoint_is_independent_of_the_numbering():
+@pytest.mark.parametrize("name,kw,tag", CASES, ids=IDS)
+def test_flow_state_tangent_equals_the_oracle_dual_derivative(name, kw, tag):
+    """ibisgb_jvp_flow_state: the dual ghost fill and constant-flux faces seeded with
+    a flow-state direction give the oracle's dual derivative to 1e-12."""
+    g, c, st = make_case(name, kw)
+    tag = first_tag(g, c, tag)
+    sim = Simulation(c, g)
+    sim.set_primitives(*st)
+    cs = copy.deepcopy(c)
+    cs["solver"] = grids.steady_state()
+    o = Oracle(cs, g, kind="dual")
+    o.set_initial_condition(*st)
+    o.steady_initialise()
+    fs0 = flow_states(c, tag)[0]
+    d = np.random.default_rng(29).standard_normal(7) * np.array([abs(fs0[k]) + 1.0 for k in KEYS])
+    if sim.dim == 2:
+        d[6] = 0.0
+    jd = o.flow_state_jvp(tag, d)
+    jt = sim.flow_state_tangent({tag: d})
+    assert np.abs(jd).max() > 0
+    assert np.abs(jt - jd).max() <= 1e-12 * np.abs(jd).max(), np.abs(jt - jd).max() / np.abs(jd).max()
+
+
+def test_flow_state_derivatives_are_independent_of_the_numbering():
     g, c, st = case("tet")
     tag = next(iter(g.markers))
     out = []
@@ -146,8 +170,10 @@ def test_flow_state_adjoint_is_independent_of_the_numbering():
         assert sim.numbering()["renumbered"] == (mode == "rcm")
         U = sim.conserved()
         w = np.random.default_rng(2).standard_normal(U.shape) / np.abs(U).mean(axis=0)
-        out.append(sim.flow_state_adjoint(w)[tag])
-    assert np.allclose(out[0], out[1], rtol=1e-12, atol=1e-12 * np.abs(out[0]).max())
+        d = np.random.default_rng(6).standard_normal(7) * 100.0
+        out.append((sim.flow_state_adjoint(w)[tag], sim.flow_state_tangent({tag: d})))
+    for a, b in zip(out[0], out[1]):
+        assert np.allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(a).max())
 
 
 @pytest.mark.parametrize("name,tag", [("subsonic", "west"), ("cflux_ramp", "inflow")])
@@ -171,5 +197,15 @@ def test_torch_autograd_through_the_inflow_parameters(name, tag):
     xt = (th0 / st_).clone().requires_grad_(True)
     f = lambda a, b: residual_flow_state(sim, a * su, b * st_, tag) / rs  # noqa: E731
     assert torch.autograd.gradcheck(f, (xu, xt), eps=1e-6, atol=1e-5, rtol=1e-4, nondet_tol=0.0, fast_mode=True)
+    # forward mode: the state and flow-state tangents together, against central differences
+    from torch.autograd.forward_ad import dual_level, make_dual, unpack_dual
+    du, dth = torch.randn_like(U0) * su, torch.randn_like(th0) * st_
+    with dual_level():
+        out = residual_flow_state(sim, make_dual(U0, du), make_dual(th0, dth), tag)
+        jt = unpack_dual(out).tangent
+    h = 1e-7
+    fd = (residual_flow_state(sim, U0 + h * du, th0 + h * dth, tag)
+          - residual_flow_state(sim, U0 - h * du, th0 - h * dth, tag)) / (2 * h)
+    assert torch.allclose(jt, fd, rtol=1e-5, atol=1e-5 * fd.abs().max().item())
     # the engine is left holding the last flow state it was given
     assert sim.flow_state(tag)["T"] == pytest.approx(fs["T"], rel=1e-5)
