@@ -91,6 +91,7 @@ def load(build_if_missing: bool = True):
     L.ibisgb_vjp_flow_state.argtypes = [_P, _P, _P, C.c_int32]
     L.ibisgb_vjp_flow_state_device.argtypes = [_P, _P, _P, C.c_int32, _P]
     L.ibisgb_jvp_flow_state.argtypes = [_P, _P, _P, C.c_int32]
+    L.ibisgb_set_scratch_poison.argtypes = [_P, C.c_int32]
     L.ibisgb_jvp_flow_state_device.argtypes = [_P, _P, _P, C.c_int32, _P]
     L.ibisgb_numbering.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.ibisgb_synchronize.argtypes = [_P]

@@ -1501,6 +1501,22 @@ struct ibisgb_ctx {
     }
 
     // ----- tangent (SteadyStateLinearisation::matrix_vector_product) ---------
+    // Scratch poisoning (ibisgb_set_scratch_poison): every buffer the derivative
+    // kernels use as scratch is filled with NaN before each call, so that a read of
+    // an entry the call did not write shows in its result.
+    bool scratch_poison = false;
+    void poison(DBuf& b) {
+        if (scratch_poison && b.p) CUDA_OK(cudaMemsetAsync(b.p, 0xFF, b.bytes, stream));
+    }
+    void poison_tangent() {
+        if (!scratch_poison) return;
+        for (DBuf* b : {&sdual.prim, &sdual.vghost, &sdual.grad, &sdual.phi, &sdual.vgrad, &sdual.flux}) poison(*b);
+    }
+    void poison_adjoint() {
+        if (!scratch_poison) return;
+        poison_tangent();
+        for (DBuf* b : {&adj_qf, &adj_self, &adj_nba, &adj_ga, &adj_qv, &adj_qg, &adj_gav}) poison(*b);
+    }
     DevView tangent_view() {
         ensure_device();
         upload_geometry<double>(s64);
@@ -1525,6 +1541,7 @@ struct ibisgb_ctx {
     void jvp(const double* v_dev, double* out_dev, double inv_dt, bool reconstruct) {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
         DevView v = tangent_view();
+        poison_tangent();
         launch_tangent(v, prm, v_dev, inv_dt, reconstruct && prm.order == 2, out_dev, stream);
         CUDA_OK(cudaGetLastError());
     }
@@ -1564,6 +1581,7 @@ struct ibisgb_ctx {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
         DevView v = tangent_view();
         ensure_adjoint();
+        poison_adjoint();
         AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
                      adj_back.as<signed char>(), adj_qv.as<double>(), adj_qg.as<double>(), adj_gav.as<double>()};
         launch_adjoint(v, prm, w_dev, reconstruct && prm.order == 2, a, out_dev, ghost_out_dev, stream);
@@ -1582,6 +1600,8 @@ struct ibisgb_ctx {
         geo_vb.alloc(sizeof(double) * 2 * F);
         geo_nbc.alloc(sizeof(double) * 3 * MF * std::max<int64_t>(N, 1));
         geo_ceb.alloc(sizeof(double) * 3 * F);
+        poison_adjoint();
+        for (DBuf* b : {&geo_fcb, &geo_vb, &geo_nbc, &geo_ceb}) poison(*b);
         AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
                      adj_back.as<signed char>(), adj_qv.as<double>(), adj_qg.as<double>(), adj_gav.as<double>()};
         a.geo_face = face_out;
@@ -1604,6 +1624,8 @@ struct ibisgb_ctx {
         gt_cc.alloc(D * 3 * NT);
         gt_vol.alloc(D * std::max<int64_t>(N, 1));
         gt_r.alloc(D * 6 * std::max<int64_t>(N, 1));
+        poison_tangent();
+        for (DBuf* b : {&gt_face, &gt_cc, &gt_vol, &gt_r}) poison(*b);
         GeoTangent g{gt_face.p, gt_cc.p, gt_vol.p, gt_r.p};
         launch_tangent_geometry(v, prm, dface, dcell, reconstruct && prm.order == 2, g, out, stream);
         CUDA_OK(cudaGetLastError());
@@ -1722,6 +1744,7 @@ struct ibisgb_ctx {
         ensure_adjoint();
         const int64_t G = mesh.G;
         fs_ghost.alloc(sizeof(double) * 7 * std::max<int64_t>(G, 1));
+        poison_adjoint();
         CUDA_OK(cudaMemsetAsync(fs_ghost.p, 0, sizeof(double) * 7 * std::max<int64_t>(G, 1), stream));
         AdjScratch a{adj_qf.as<double>(), adj_self.as<double>(), adj_nba.as<double>(), adj_ga.as<double>(),
                      adj_back.as<signed char>(), adj_qv.as<double>(), adj_qg.as<double>(), adj_gav.as<double>()};
@@ -1738,6 +1761,7 @@ struct ibisgb_ctx {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
         if (n_cases > 1) throw StateError("a batch's boundary states belong to its cases");
         DevView v = tangent_view();
+        poison_tangent();
         v.fs_tan = dfs_dev;
         launch_tangent(v, prm, nullptr, 0.0, reconstruct && prm.order == 2, out_dev, stream);  // -dR/dfs . dfs
         RowScale neg{{-1.0, -1.0, -1.0, -1.0, -1.0}};
@@ -2849,6 +2873,12 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes) {
 int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell) {
     if (!ctx || !face || !cell) return IBISGB_ERR_ARG;
     return guarded(ctx, [&] { ctx->set_geometry(face, cell); });
+}
+
+int ibisgb_set_scratch_poison(ibisgb_ctx* ctx, int32_t on) {
+    if (!ctx) return IBISGB_ERR_ARG;
+    ctx->scratch_poison = on != 0;
+    return IBISGB_OK;
 }
 
 int ibisgb_set_flow_state(ibisgb_ctx* ctx, const char* tag, const double* fs) {

@@ -356,6 +356,12 @@ class Simulation:
         self._call("ibisgb_vjp_flow_state", _ptr(w), _ptr(out), int(allow_reconstruction))
         return {t: out[b].copy() for b, t in enumerate(tags)}
 
+    def set_scratch_poison(self, on: bool) -> None:
+        """Fill the derivative kernels' scratch buffers with NaN before each tangent /
+        adjoint call (ibisgb_set_scratch_poison): a check that no call reads an entry it
+        did not write."""
+        self._call("ibisgb_set_scratch_poison", int(bool(on)))
+
     def flow_state_tangent(self, dfs: dict, allow_reconstruction: bool = True) -> np.ndarray:
         """dR/dfs . dfs (ibisgb_jvp_flow_state) for {tag: direction of 7 (T, p, rho,
         energy, vx, vy, vz)} (boundaries left out do not move); returns (N, n_conserved)."""
