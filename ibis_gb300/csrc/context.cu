@@ -1094,6 +1094,11 @@ struct ibisgb_ctx {
 
     void residual(int prec, double* out_device, bool record_branches) {
         ensure_prims(prec);
+        if (scratch_poison) {  // the stage's intermediates: each is written before it is read
+            StateBufs& sb = bufs(prec);
+            for (DBuf* b : {&sb.grad, &sb.phi, &sb.vgrad, &sb.flux, &sb.grad_lo, &sb.vgrad_lo, &sb.flux_lo, &vsig})
+                poison(*b);
+        }
         DevView v = view(prec);
         KernelOps o = ops(prec);
         // compute_dudt applies the pre-reconstruction actions first (finite_volume.cpp:62)

@@ -228,13 +228,15 @@ int ibisgb_get_dump(ibisgb_ctx* ctx, int32_t which, void* buf, int64_t bytes);
 int ibisgb_set_geometry(ibisgb_ctx* ctx, const double* face, const double* cell);
 
 /* A check for the tangent and adjoint calls (ibisgb_jvp*, ibisgb_vjp*,
- * ibisgb_adjoint_step's products): with on != 0, every device buffer those
- * kernels use as scratch (dual primitives, gradients, limiters and fluxes, the
- * adjoint's per-face and per-slot partials, the geometry and flow-state
- * scratch) is filled with NaN before each call, so that a read of an entry the
- * call did not write shows in its result.  Results are the same bits with it on
- * or off; it costs one memset per buffer per call.  No counterpart in the
- * reference. */
+ * ibisgb_adjoint_step's products) and the residual (ibisgb_residual*): with
+ * on != 0, every device buffer those kernels use as scratch (dual primitives,
+ * gradients, limiters and fluxes, the adjoint's per-face and per-slot partials,
+ * the geometry and flow-state scratch; the residual's gradients, limiters, face
+ * fluxes and viscous time-step signal) is filled with NaN before each call, so
+ * that a read of an entry the call did not write shows in its result.  Results
+ * are the same bits with it on or off; it costs one memset per buffer per call.
+ * The limiter dump of a 2-D grid then shows NaN in its unused fifth row.  No
+ * counterpart in the reference. */
 int ibisgb_set_scratch_poison(ibisgb_ctx* ctx, int32_t on);
 
 /* The geometry-table layout of arithmetic `precision` on this grid.  On a

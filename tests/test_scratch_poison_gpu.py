@@ -1,8 +1,9 @@
-"""No derivative call reads scratch it did not write: with every scratch buffer of
-the tangent and adjoint kernels filled with NaN before each call
-(ibisgb_set_scratch_poison), the state, geometry and flow-state tangents and
-adjoints are finite and the same bits as without -- 2-D and 3-D, first and second
-order, viscous, constant-flux, boundary-layer, periodic and renumbered grids."""
+"""No residual or derivative call reads scratch it did not write: with every
+scratch buffer of the residual, tangent and adjoint kernels filled with NaN before
+each call (ibisgb_set_scratch_poison), the residual in every precision and the
+state, geometry and flow-state tangents and adjoints are finite and the same bits
+as without -- 2-D and 3-D, first and second order, viscous, constant-flux,
+boundary-layer, periodic and renumbered grids."""
 import copy
 
 import numpy as np
@@ -32,7 +33,8 @@ def products(sim, c):
     dc[3, sim.num_cells:] = 0.0
     dfs = {t: rng.standard_normal(7) * 10.0 for t in sim.boundary_tags() if flow_states(c, t)}
     jtw, gadj = sim.vector_jacobian_product(w, ghosts=True)
-    out = [sim.matrix_vector_product(v), jtw, gadj, *sim.geometry_adjoint(w), sim.geometry_tangent(df, dc)]
+    out = [sim.compute_dudt(p) for p in ("f64_exact", "f64", "mixed", "mixed_grad", "mixed_ff")]
+    out += [sim.matrix_vector_product(v), jtw, gadj, *sim.geometry_adjoint(w), sim.geometry_tangent(df, dc)]
     if dfs:
         out += list(sim.flow_state_adjoint(w).values()) + [sim.flow_state_tangent(dfs)]
     return out
