@@ -22,7 +22,8 @@ def states(sim, n, seed):
 
 @pytest.mark.parametrize("name,prec,pinned", [("ramp", "mixed", True), ("ramp", "f64_exact", False),
                                               ("tet", "mixed_ff", True), ("box", "f64", True),
-                                              ("plate", "mixed", True)])
+                                              ("box", "mixed", True), ("box", "mixed_ff", True),
+                                              ("plate", "mixed", True), ("subsonic", "f64", True)])
 def test_pipelined_runs_equal_the_calls_one_by_one(name, prec, pinned):
     torch = pytest.importorskip("torch")
     g, c, st = case(name)
