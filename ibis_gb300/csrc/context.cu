@@ -98,10 +98,10 @@ bool shared_column(const std::vector<T>& a, int64_t rows, int64_t N, std::vector
 }
 
 // The faces of a uniform lattice fall into a few classes whose geometry, as the
-// float face kernel reads it, is bitwise the same: the normal, the 2-D tangents
-// (t1 x, t1 y, t2 z; the 3-D kernel forms its frame from n) and each valid side's
-// reconstruction offset (face centre - centroid, the float subtraction the kernel
-// does).  On success cls holds each face's class and tab one kFaceClassRow row per
+// float kernels read it, is bitwise the same: the normal, the 2-D tangents (t1 x,
+// t1 y, t2 z; the 3-D face kernel forms its frame from n), each valid side's
+// reconstruction offset (face centre - centroid, the float subtraction the face
+// kernel does) and the area (the local time step's).  On success cls holds each face's class and tab one kFaceClassRow row per
 // class; false when the faces have more than kMaxFaceClasses distinct rows.
 bool face_classes(const std::vector<float>& fc, const std::vector<float>& cc, const Mesh& mesh,
                   std::vector<uint8_t>& cls, std::vector<float>& tab) {
@@ -114,6 +114,7 @@ bool face_classes(const std::vector<float>& fc, const std::vector<float>& cc, co
         float row[kFaceClassRow] = {};
         for (int k = 0; k < 3; k++) row[k] = fc[k * F + f];
         if (!three) { row[3] = fc[3 * F + f]; row[4] = fc[4 * F + f]; row[5] = fc[8 * F + f]; }
+        row[12] = fc[12 * F + f];
         const int64_t side[2] = {mesh.left[f], mesh.right[f]};
         for (int sd = 0; sd < 2; sd++) {
             const int64_t c = side[sd];

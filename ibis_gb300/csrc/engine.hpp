@@ -29,8 +29,8 @@ enum ActionKind : int {
 constexpr int kMaxActions = 4;
 constexpr int kMaxStages = 8;
 // Face classes of a uniform lattice: n (3); 2-D t1 x, t1 y, t2 z (3); the left and
-// right sides' face centre - centroid (3 + 3, zero for a ghost side).
-constexpr int kFaceClassRow = 12;
+// right sides' face centre - centroid (3 + 3, zero for a ghost side); the area; 3 pads.
+constexpr int kFaceClassRow = 16;
 constexpr int kMaxFaceClasses = 64;
 
 struct Action {
@@ -122,7 +122,7 @@ struct DevView {
     const void* lsqd;       // [3][MF][N] face centre minus cell centroid per face slot (float build), or null
     int lsq_shared;         // 1: lsqw, lsqd and their lo parts are [3][MF], the same for every cell
     // float build on a uniform lattice, else null: each face's class and the
-    // classes' rows (n; 2-D t1 x, t1 y, t2 z; left and right offsets face centre - centroid)
+    // classes' rows (n; 2-D t1 x, t1 y, t2 z; left and right offsets face centre - centroid; area)
     const unsigned char* face_class;  // [F]
     const float* face_class_tab;      // [classes][kFaceClassRow]
     // flow-state tangent only, else null: a tangent direction of each boundary's

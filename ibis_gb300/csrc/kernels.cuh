@@ -1265,9 +1265,11 @@ __device__ double cell_local_dt(const DevView& v, const FvParams& prm, int i, P 
         float sf = 0.f;
         for (int s = 0; s < nf; s++) {
             const int f = v.cell_face[s * N + i];
-            const float A = (float)fg[12 * F + f];
-            float dot = vx * (float)fg[f] + vy * (float)fg[F + f];
-            if (DIM == 3) dot += vz * (float)fg[2 * F + f];
+            // a uniform lattice's face class holds the same normal and area
+            const float* ct = v.face_class ? v.face_class_tab + kFaceClassRow * v.face_class[f] : nullptr;
+            const float A = ct ? ct[12] : (float)fg[12 * F + f];
+            float dot = vx * (ct ? ct[0] : (float)fg[f]) + vy * (ct ? ct[1] : (float)fg[F + f]);
+            if (DIM == 3) dot += vz * (ct ? ct[2] : (float)fg[2 * F + f]);
             sf += (fabsf(dot) + a) * A;
             if (prm.viscous) srv += v.vsig[f] * (double)A * (double)A / vol;
         }

@@ -249,9 +249,10 @@ int ibisgb_set_scratch_poison(ibisgb_ctx* ctx, int32_t on);
  *    slot that every thread shares instead of 24 values per cell;
  *  - *face_classes = the number of face classes (MIXED only, else 0): faces whose
  *    normal, 2-D tangents and side offsets (face centre - centroid, as the float
- *    face kernel forms them) are bitwise the same share a row, and each face
- *    keeps a one-byte class instead of its normal and centre and the gathers of
- *    its cells' centroids; 0 when there are more than 64 distinct rows.
+ *    face kernel forms them) and area are bitwise the same share a row, and each
+ *    face keeps a one-byte class instead of its normal, centre and area and the
+ *    gathers of its cells' centroids (the face kernel and the local time step
+ *    read the class's row); 0 when there are more than 64 distinct rows.
  * The values, and so the results, are the same as with the per-element tables.
  * Uploads the geometry of that arithmetic if it is not on the device yet.  Either
  * pointer may be NULL.  No counterpart in the reference (WLSGradient and the
