@@ -1742,7 +1742,7 @@ struct ibisgb_ctx {
     // out (num_boundaries x 7, sorted tag order) = w^T dR/d(flow state of each
     // boundary), the derivative taken with every action of the boundary that
     // carries a flow state moving together (set_flow_state's semantics)
-    DBuf fs_ghost;
+    DBuf fs_ghost, fs_io;  // per-ghost partials; the host calls' flow-state rows (num_boundaries x 7)
     void vjp_flow_state(const double* w_dev, double* out_dev, bool reconstruct) {
         if (!have_state) throw StateError("no state: call ibisgb_set_primitives first");
         if (n_cases > 1) throw StateError("a batch's boundary states belong to its cases");
@@ -2945,11 +2945,9 @@ int ibisgb_jvp_flow_state(ibisgb_ctx* ctx, const double* dfs, double* out, int32
         ctx->ensure_device();
         const size_t n = ctx->nvars(), nb = 7 * ctx->mesh.bounds.size();
         ctx->ensure_krylov(1);
-        ctx->geo_out_face.alloc(sizeof(double) * std::max(nb, (size_t)1));
-        if (nb)
-            CUDA_OK(cudaMemcpyAsync(ctx->geo_out_face.p, dfs, sizeof(double) * nb, cudaMemcpyHostToDevice,
-                                    ctx->stream));
-        ctx->jvp_flow_state_rows(ctx->geo_out_face.as<double>(), ctx->kw.as<double>(), allow_reconstruction != 0);
+        ctx->fs_io.alloc(sizeof(double) * std::max(nb, (size_t)1));
+        if (nb) CUDA_OK(cudaMemcpyAsync(ctx->fs_io.p, dfs, sizeof(double) * nb, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->jvp_flow_state_rows(ctx->fs_io.as<double>(), ctx->kw.as<double>(), allow_reconstruction != 0);
         CUDA_OK(cudaMemcpyAsync(out, ctx->kw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
@@ -2961,12 +2959,11 @@ int ibisgb_vjp_flow_state(ibisgb_ctx* ctx, const double* w, double* out, int32_t
         ctx->ensure_device();
         const size_t n = ctx->nvars(), nb = 7 * ctx->mesh.bounds.size();
         ctx->ensure_krylov(1);
-        ctx->geo_out_face.alloc(sizeof(double) * std::max(nb, (size_t)1));
+        ctx->fs_io.alloc(sizeof(double) * std::max(nb, (size_t)1));
         CUDA_OK(cudaMemcpyAsync(ctx->kr0.p, w, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-        ctx->vjp_flow_state_rows(ctx->kr0.as<double>(), ctx->geo_out_face.as<double>(), allow_reconstruction != 0);
+        ctx->vjp_flow_state_rows(ctx->kr0.as<double>(), ctx->fs_io.as<double>(), allow_reconstruction != 0);
         if (nb)
-            CUDA_OK(cudaMemcpyAsync(out, ctx->geo_out_face.p, sizeof(double) * nb, cudaMemcpyDeviceToHost,
-                                    ctx->stream));
+            CUDA_OK(cudaMemcpyAsync(out, ctx->fs_io.p, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));
     });
 }
