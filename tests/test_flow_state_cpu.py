@@ -74,3 +74,27 @@ def test_oracle_flow_state_derivative_matches_central_differences(name, kw, tag)
     fd = (residual(h) - residual(-h)) / (2 * h)
     assert np.abs(jd).max() > 0
     assert np.abs(jd - fd).max() <= 1e-7 * np.abs(jd).max()
+
+
+def test_set_flow_state_on_the_host():
+    """ibisgb_set_flow_state / ibisgb_get_flow_state before the device is used: every
+    action of the boundary that carries a flow state takes the new one (the pre-
+    reconstruction copy and the constant flux of the same boundary), and bad calls
+    are refused with the C ABI's error codes and leave the state unchanged."""
+    from ibis_gb300 import Batch, Simulation
+    from ibis_gb300._lib import IbisgbError
+    g, c, _ = case("cflux_ramp")
+    sim = Simulation(c, g)
+    fs = sim.flow_state("inflow")
+    assert fs == {k: float(c["grid"]["boundaries"]["inflow"]["pre_reconstruction"][0]["flow_state"][k])
+                  for k in KEYS}
+    new = grids.flow_state(c["gas_model"], 310.0, 0.9e5, 650.0, 20.0)
+    sim.set_flow_state("inflow", new)
+    assert sim.flow_state("inflow") == {k: float(new[k]) for k in KEYS}
+    for tag, state in (("nowhere", new), ("outflow", new), ("inflow", dict(new, T=float("inf")))):
+        with pytest.raises(IbisgbError, match="ARG"):
+            sim.set_flow_state(tag, state)
+    assert sim.flow_state("inflow") == {k: float(new[k]) for k in KEYS}
+    b = Batch([Simulation(c, g), Simulation(c, g)])
+    with pytest.raises(IbisgbError, match="STATE"):
+        b.set_flow_state("inflow", new)
